@@ -1,0 +1,212 @@
+"""GB300-native differentiable Gaussian rasterizer, a drop-in for FasterGS's
+``diff_gaussian_rasterization_faster`` backend.
+
+Same public names and behaviour as FB's
+gs_submodules/diff-gaussian-rasterization_faster/diff_gaussian_rasterization_faster/__init__.py:
+``GaussianRasterizationSettings``, ``GaussianRasterizer``, ``rasterize_gaussians``,
+the ``_RasterizeGaussians`` autograd Function, the persistent ``Buffer`` and
+``SparseGaussianAdam``.  Every op runs on hand-written sm_103a kernels behind
+the C ABI in include/fgs.h; there is no CPU or PyTorch fallback.
+
+Differences that only show where FB would fail:
+  * the key-capacity overflow raises ``RuntimeError("Too many k-v pairs!")``
+    (FB raises a bare string, itself a TypeError) and nothing is written past
+    the capacity;
+  * ``Buffer`` is allocated on first use, not at import, so importing the
+    package does not need a GPU;
+  * ``cov3D_precomp`` raises NotImplementedError (FB accepts it, ignores it
+    and reads the absent scales).
+"""
+from __future__ import annotations
+
+from typing import NamedTuple
+
+import torch
+import torch.nn as nn
+
+from . import _C
+
+__all__ = ["GaussianRasterizationSettings", "GaussianRasterizer", "rasterize_gaussians", "Buffer",
+           "SparseGaussianAdam", "_RasterizeGaussians", "_C"]
+
+
+class Buffer:
+    """Persistent device buffers shared by all calls (FB __init__.py:21-38)."""
+
+    def __init__(self, device="cuda", MAX_NUM_RENDERED=2**24, MAX_NUM_TILES=2**20, **kwargs):
+        i64, i32 = torch.int64, torch.int32
+        self.gaussian_keys_unsorted = torch.zeros(MAX_NUM_RENDERED, device=device, dtype=i64)
+        self.gaussian_values_unsorted = torch.zeros(MAX_NUM_RENDERED, device=device, dtype=i32)
+        self.gaussian_keys_sorted = torch.zeros(MAX_NUM_RENDERED, device=device, dtype=i64)
+        self.gaussian_values_sorted = torch.zeros(MAX_NUM_RENDERED, device=device, dtype=i32)
+        self.MAX_NUM_RENDERED = MAX_NUM_RENDERED
+        self.MAX_NUM_TILES = MAX_NUM_TILES
+        self.SORT_BUFFER_SIZE = _C.ops.get_sort_buffer_size(MAX_NUM_RENDERED)
+        self.list_sorting_space = torch.zeros(self.SORT_BUFFER_SIZE, device=device, dtype=torch.int8)
+        self.ranges = torch.zeros((MAX_NUM_TILES, 2), device=device, dtype=i32)
+        self.curr_offset = torch.zeros(1, device=device, dtype=i32)
+        self.splat_buffer = torch.zeros([MAX_NUM_RENDERED, 32], device=device, dtype=torch.float32)
+        self.device = device
+
+
+class _LazyBuffer:
+    """Class attribute that allocates the shared Buffer on first access."""
+
+    def __init__(self):
+        self._buf = None
+
+    def __get__(self, obj, owner):
+        if self._buf is None:
+            self._buf = Buffer()
+        return self._buf
+
+    def __set__(self, obj, value):  # pragma: no cover - instances never set it
+        self._buf = value
+
+
+def rasterize_gaussians(means3D, dc, shs, colors_precomp, opacities, scales, rotations, cov3Ds_precomp,
+                        raster_settings, culling, xyz_gradient_accum, xyz_gradient_accum_abs, max_radii, denom):
+    return _RasterizeGaussians.apply(means3D, dc, shs, colors_precomp, opacities, scales, rotations,
+                                     cov3Ds_precomp, raster_settings, culling, xyz_gradient_accum,
+                                     xyz_gradient_accum_abs, max_radii, denom)
+
+
+class _RasterizeGaussians(torch.autograd.Function):
+    """FB __init__.py:76-187: preprocess -> sort -> render_16x16, backward through _C.ops.backward."""
+
+    buffer = _LazyBuffer()
+
+    @staticmethod
+    def forward(ctx, means3D, dc, shs, colors_precomp, opacities, scales, rotations, cov3Ds_precomp,
+                raster_settings, culling, xyz_gradient_accum, xyz_gradient_accum_abs, max_radii, denom):
+        buffer = _RasterizeGaussians.buffer
+        splat_buffer = buffer.splat_buffer
+        zFar, zNear = 100.0, 0.01
+        N = means3D.shape[0]
+        buffer.curr_offset.fill_(0)
+        radii = _C.ops.preprocess(
+            raster_settings.sh_degree, means3D, colors_precomp, dc, shs, opacities, scales, rotations,
+            raster_settings.scale_modifier, raster_settings.image_width, raster_settings.image_height, 16, 16,
+            raster_settings.campos, raster_settings.viewmatrix, raster_settings.projmatrix,
+            raster_settings.tanfovx, raster_settings.tanfovy, zFar, zNear,
+            buffer.gaussian_keys_unsorted, buffer.gaussian_values_unsorted, buffer.gaussian_values_sorted,
+            buffer.curr_offset, raster_settings.mult, splat_buffer, culling)
+        num_rendered = int(buffer.curr_offset.cpu()[0])
+        if num_rendered >= buffer.MAX_NUM_RENDERED:
+            raise RuntimeError("Too many k-v pairs!")
+        if _C.device_errors(means3D.device):
+            raise RuntimeError("preprocess overflowed a device queue (too many large Gaussians)")
+        _C.ops.sort_gaussian(num_rendered, raster_settings.image_width, raster_settings.image_height, 16, 16,
+                             buffer.list_sorting_space, buffer.gaussian_keys_unsorted,
+                             buffer.gaussian_values_unsorted, buffer.gaussian_keys_sorted,
+                             buffer.gaussian_values_sorted)
+        H, W = raster_settings.image_height, raster_settings.image_width
+        last_contributor = torch.zeros((H, W, 1), device=means3D.device, dtype=torch.int)
+        Ts_final = torch.zeros((H, W, 1), device=means3D.device, dtype=torch.float)
+        bucket_sum, out_color, img_buffer, smp_buffer = _C.ops.render_16x16(
+            N, num_rendered, W, H, splat_buffer, buffer.gaussian_keys_sorted, buffer.gaussian_values_sorted,
+            buffer.ranges, raster_settings.bg, last_contributor, Ts_final)
+        ctx.raster_settings = raster_settings
+        ctx.num_rendered = num_rendered
+        ctx.buffer = buffer
+        ctx.bucket_sum = bucket_sum
+        ctx.save_for_backward(means3D, scales, rotations, dc, shs, opacities, out_color, last_contributor,
+                              Ts_final, radii, splat_buffer, img_buffer, smp_buffer, xyz_gradient_accum,
+                              xyz_gradient_accum_abs, max_radii, denom)
+        return out_color, radii
+
+    @staticmethod
+    def backward(ctx, grad_out_color, _):
+        rs = ctx.raster_settings
+        buffer = ctx.buffer
+        zFar, zNear = 100.0, 0.01
+        (means3D, scales, rotations, dc, shs, opacities, out_color, last_contributor, Ts_final, radii,
+         splat_buffer, img_buffer, smp_buffer, xyz_gradient_accum, xyz_gradient_accum_abs, max_radii,
+         denom) = ctx.saved_tensors
+        (grad_mean2D, grad_color, grad_opacity, grad_mean3D, grad_cov3D, grad_dc, grad_shs, grad_scales,
+         grad_rotations) = _C.ops.backward(
+            rs.sh_degree, ctx.bucket_sum, means3D, radii, dc, shs, opacities, scales, rotations,
+            rs.scale_modifier, rs.image_width, rs.image_height, 16, 16, rs.tanfovx, rs.tanfovy, zFar, zNear,
+            rs.campos, rs.viewmatrix, rs.projmatrix, img_buffer, smp_buffer, splat_buffer,
+            buffer.gaussian_values_sorted, buffer.ranges, rs.bg, last_contributor, Ts_final,
+            grad_out_color.contiguous(), xyz_gradient_accum, xyz_gradient_accum_abs, max_radii, denom)
+        return (grad_mean3D, grad_dc, grad_shs, grad_color, grad_opacity, grad_scales, grad_rotations, grad_cov3D,
+                None, None, None, None, None, None)
+
+
+class GaussianRasterizationSettings(NamedTuple):
+    """FB __init__.py:191-204."""
+    image_height: int
+    image_width: int
+    tanfovx: float
+    tanfovy: float
+    bg: torch.Tensor
+    scale_modifier: float
+    viewmatrix: torch.Tensor
+    projmatrix: torch.Tensor
+    sh_degree: int
+    campos: torch.Tensor
+    mult: float
+    prefiltered: bool
+    debug: bool
+
+
+class GaussianRasterizer(nn.Module):
+    """FB __init__.py:207-264."""
+
+    def __init__(self, raster_settings, **kwargs):
+        super().__init__()
+        self.raster_settings = raster_settings
+
+    def forward(self, means3D, opacities, dc=None, shs=None, colors_precomp=None, scales=None, rotations=None,
+                cov3D_precomp=None, culling=None, xyz_gradient_accum=None, xyz_gradient_accum_abs=None,
+                max_radii=None, denom=None):
+        if (shs is None and colors_precomp is None) or (shs is not None and colors_precomp is not None):
+            raise Exception('Please provide excatly one of either SHs or precomputed colors!')
+        if ((scales is None or rotations is None) and cov3D_precomp is None) or \
+                ((scales is not None or rotations is not None) and cov3D_precomp is not None):
+            raise Exception('Please provide exactly one of either scale/rotation pair or precomputed 3D covariance!')
+        empty = torch.tensor([])
+        dc = empty if dc is None else dc
+        shs = empty if shs is None else shs
+        culling = torch.tensor([], dtype=torch.bool) if culling is None else culling
+        colors_precomp = empty if colors_precomp is None else colors_precomp
+        scales = empty if scales is None else scales
+        rotations = empty if rotations is None else rotations
+        cov3D_precomp = empty if cov3D_precomp is None else cov3D_precomp
+        xyz_gradient_accum = empty if xyz_gradient_accum is None else xyz_gradient_accum
+        xyz_gradient_accum_abs = empty if xyz_gradient_accum_abs is None else xyz_gradient_accum_abs
+        max_radii = empty if max_radii is None else max_radii
+        denom = empty if denom is None else denom
+        return rasterize_gaussians(means3D, dc, shs, colors_precomp, opacities, scales, rotations, cov3D_precomp,
+                                   self.raster_settings, culling, xyz_gradient_accum, xyz_gradient_accum_abs,
+                                   max_radii, denom)
+
+
+class SparseGaussianAdam(torch.optim.Adam):
+    """Adam that only steps the rows of visible Gaussians (FB __init__.py:267-298)."""
+
+    def __init__(self, params, lr, eps):
+        super().__init__(params=params, lr=lr, eps=eps)
+
+    @torch.no_grad()
+    def step(self, visibility, N):
+        for group in self.param_groups:
+            lr = group["lr"]
+            eps = group["eps"]
+            assert len(group["params"]) == 1, "more than one tensor in group"
+            param = group["params"][0]
+            if param.grad is None or param.grad.numel() == 0:
+                continue
+            state = self.state[param]
+            if len(state) == 0:
+                state['step'] = torch.tensor(0.0, dtype=torch.float32)
+                state['exp_avg'] = torch.zeros_like(param, memory_format=torch.preserve_format)
+                state['exp_avg_sq'] = torch.zeros_like(param, memory_format=torch.preserve_format)
+            exp_avg = state["exp_avg"]
+            exp_avg_sq = state["exp_avg_sq"]
+            state['step'] += 1
+            step = state['step']
+            M = param.numel() // N
+            _C.ops.adamUpdate(param, param.grad, exp_avg, exp_avg_sq, visibility,
+                              lr * (1 - 0.999 ** step) ** 0.5 / (1 - 0.9 ** step), 0.9, 0.999, eps, N, M)

@@ -1,0 +1,89 @@
+"""ctypes binding of libfgs.so (the C ABI declared in include/fgs.h).
+
+The library is the product: there is no CPU or PyTorch fallback.  Loading
+fails loudly when libfgs.so is missing; ``fastergs_gb300.build.build()``
+compiles it for sm_103a.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import threading
+from pathlib import Path
+
+from . import build as _build
+
+_LIB = None
+_LOCK = threading.Lock()
+
+vp, i32, i64, f32, sz = C.c_void_p, C.c_int, C.c_int64, C.c_float, C.c_size_t
+u32p = C.POINTER(C.c_uint32)
+
+# name: (restype, argtypes) -- mirrors include/fgs.h
+SIGNATURES = {
+    "fgs_status_string": (C.c_char_p, [i32]),
+    "fgs_version": (C.c_char_p, []),
+    "fgs_device_errors": (i32, [C.POINTER(C.c_int), i32, vp]),
+    "fgs_preprocess": (i32, [i32, i32, i32, vp, vp, vp, vp, vp, vp, vp, f32, i32, i32, i32, i32, vp, vp, vp,
+                             f32, f32, f32, f32, f32, vp, vp, i64, vp, vp, i64, vp, i64, vp, vp, vp, vp]),
+    "fgs_sort_temp_bytes": (sz, [i64]),
+    "fgs_sort": (i32, [i64, i32, i32, i32, i32, vp, sz, vp, vp, vp, vp, vp]),
+    "fgs_tile_ranges": (i32, [i64, i32, vp, vp, vp]),
+    "fgs_max_buckets": (i64, [i64, i32, i32, i32, i32, i32]),
+    "fgs_state_bytes": (i32, [i32, i32, i32, i32, i64, C.POINTER(C.c_size_t), C.POINTER(C.c_size_t)]),
+    "fgs_render_fwd": (i32, [i32, i64, i32, i32, i32, i32, i32, vp, vp, vp, vp, vp, vp, vp, vp, vp, sz, vp, sz,
+                             i64, u32p, vp]),
+    "fgs_render_bwd": (i32, [i32, i32, i32, i32, i32, i32, vp, vp, vp, vp, vp, vp, vp, vp, i64, vp, vp, vp]),
+    "fgs_preprocess_bwd": (i32, [i32, i32, i32, vp, vp, vp, vp, vp, vp, vp, f32, vp, vp, i32, i32, f32, f32, vp,
+                                 vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp]),
+    "fgs_densify_stats": (i32, [i32, vp, vp, vp, vp, vp, vp, vp]),
+    "fgs_adam_update": (i32, [vp, vp, vp, vp, vp, f32, f32, f32, f32, C.c_uint32, C.c_uint32, vp]),
+}
+
+OPTIONAL = {
+    # batched multi-view entry points (present when batched.cu is built)
+    "fgs_batched_plan_bytes": None,
+}
+
+
+class FgsError(RuntimeError):
+    """A C-ABI call returned a non-OK fgs_status."""
+
+    def __init__(self, fn: str, status: int, msg: str):
+        super().__init__(f"{fn} failed: {msg} (status {status})")
+        self.status = status
+
+
+def lib_path() -> Path:
+    return _build.LIB
+
+
+def load() -> C.CDLL:
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    with _LOCK:
+        if _LIB is None:
+            p = lib_path()
+            if not p.exists():
+                raise ImportError(
+                    f"{p} is missing: build the CUDA library first (python -m fastergs_gb300.build); "
+                    "this package has no CPU fallback")
+            lib = C.CDLL(str(p))
+            for name, (res, args) in SIGNATURES.items():
+                fn = getattr(lib, name)
+                fn.restype = res
+                fn.argtypes = args
+            _LIB = lib
+    return _LIB
+
+
+def check(fn: str, status: int) -> None:
+    if status != 0:
+        msg = load().fgs_status_string(status).decode()
+        raise FgsError(fn, status, msg)
+
+
+def call(name: str, *args):
+    st = getattr(load(), name)(*args)
+    check(name, st)
+    return st

@@ -1,0 +1,519 @@
+// Backward pass, sm_103a: bucket-parallel composite backward and the fused
+// per-Gaussian backward of projection, EWA covariance, SH and scale/rotation.
+//
+// Restates FB csrc/cuda_rasterizer/backward.cu with these GB300 changes:
+//   * a bucket is walked front to back from the merge's prefix (C, T) before
+//     the bucket, so transmittance is recomputed by multiplication instead of
+//     FB's repeated division T / (1 - alpha) walking back to front; the colour
+//     behind a Gaussian is C_final - prefix, exactly FB's res_ar;
+//   * a pixel/Gaussian pair with alpha = 0 contributes nothing and is skipped;
+//   * the eleven per-Gaussian partial sums of a warp are reduced with a
+//     transpose-reduce (16 shuffles instead of 55) and land with one 12-lane
+//     reduction store into an interleaved 48-byte gradient record, instead of
+//     eleven scalar atomics from one lane;
+//   * the preprocess backward is one kernel (FB launches two) that also
+//     scatters the record into FB's output tensors and accumulates the
+//     densification statistics.
+#include "render_common.cuh"
+
+namespace fgs {
+namespace {
+
+constexpr int kBwdWarps = 4;
+
+struct BwdArgs {
+  const float* splat;
+  const uint32_t* vals;
+  const uint32_t* ranges;
+  const uint32_t* bucket_tile;
+  const uint32_t* bucket_off;
+  const uint32_t* bucket_sum;
+  const uint32_t* max_contrib;
+  const float4* samples;
+  const float* pix_color;
+  const float* Ts_final;
+  const int* last_contrib;
+  const float* dL;
+  const float* bg;
+  float* grad;
+  int W, H, bx, by, gx, bs;
+};
+
+// Sum 16 per-lane values over the warp.  On return lane l holds the total of
+// value (l >> 1) & 15 (lanes 2j and 2j+1 both hold value j).
+__device__ __forceinline__ float warp_transpose_reduce16(float (&v)[16], int lane) {
+#pragma unroll
+  for (int j = 0; j < 8; ++j) {
+    const bool hi = lane & 16;
+    const float send = hi ? v[j] : v[j + 8];
+    const float keep = hi ? v[j + 8] : v[j];
+    v[j] = keep + __shfl_xor_sync(0xffffffffu, send, 16);
+  }
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    const bool hi = lane & 8;
+    const float send = hi ? v[j] : v[j + 4];
+    const float keep = hi ? v[j + 4] : v[j];
+    v[j] = keep + __shfl_xor_sync(0xffffffffu, send, 8);
+  }
+#pragma unroll
+  for (int j = 0; j < 2; ++j) {
+    const bool hi = lane & 4;
+    const float send = hi ? v[j] : v[j + 2];
+    const float keep = hi ? v[j + 2] : v[j];
+    v[j] = keep + __shfl_xor_sync(0xffffffffu, send, 4);
+  }
+  {
+    const bool hi = lane & 2;
+    const float send = hi ? v[0] : v[1];
+    const float keep = hi ? v[1] : v[0];
+    v[0] = keep + __shfl_xor_sync(0xffffffffu, send, 2);
+  }
+  return v[0] + __shfl_xor_sync(0xffffffffu, v[0], 1);
+}
+
+__global__ void __launch_bounds__(kBwdWarps * kWarp) k_render_bwd(const BwdArgs a) {
+  __shared__ BucketStage s_stage[kBwdWarps];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  BucketStage& st = s_stage[warp];
+  const int B = (int)a.bucket_sum[0];
+  const int lx = lane % a.bx, ly0 = lane / a.bx;
+  const int rows = kWarp / a.bx;
+  const float ystep = (float)rows;
+  const int HW = a.W * a.H;
+  const float hx = 0.5f * (float)a.W, hy = 0.5f * (float)a.H;
+  const float bgr = a.bg[0], bgg = a.bg[1], bgb = a.bg[2];
+  // Scale applied after the reduction to the value a lane ends up holding:
+  // mean2D x/|x| need ln2 * W/2, y/|y| ln2 * H/2, conic -0.5 (ln2 * -0.5 log2e),
+  // colour 1, opacity ln2 * log2e / o = 1 / o (applied per Gaussian).
+  const int vid = (lane >> 1) & 15;
+  const float vscale = (vid == 0 || vid == 2)   ? kLn2 * hx
+                       : (vid == 1 || vid == 3) ? kLn2 * hy
+                       : (vid >= 4 && vid <= 7) ? -0.5f
+                                                : 1.0f;
+
+  for (int b = blockIdx.x * kBwdWarps + warp; b < B; b += gridDim.x * kBwdWarps) {
+    const BucketInfo bi = bucket_info(b, a.bucket_tile, a.bucket_off, a.ranges, a.bs);
+    const uint32_t thres = (uint32_t)(bi.local * a.bs);
+    if (thres >= a.max_contrib[bi.tile]) continue;  // no pixel of the tile reaches this bucket
+    stage_bucket(st, a.splat, a.vals + bi.start, bi.n, lane);
+    const int tx0 = (bi.tile % a.gx) * a.bx, ty0 = (bi.tile / a.gx) * a.by;
+    const float px = (float)(tx0 + lx), py0 = (float)(ty0 + ly0);
+
+    float T[kPxPerThread], Pd[kPxPerThread], Lr[kPxPerThread], Lg[kPxPerThread], Lb[kPxPerThread],
+        K[kPxPerThread];
+    uint32_t alive = 0;
+#pragma unroll
+    for (int k = 0; k < kPxPerThread; ++k) {
+      const int gxp = tx0 + lx, gyp = ty0 + ly0 + k * rows;
+      T[k] = 0.f; Pd[k] = 0.f; Lr[k] = 0.f; Lg[k] = 0.f; Lb[k] = 0.f; K[k] = 0.f;
+      if (gxp < a.W && gyp < a.H) {
+        const int pix = gyp * a.W + gxp;
+        if ((uint32_t)a.last_contrib[pix] > thres) {
+          alive |= 1u << k;
+          const float4 prev = bi.local > 0 ? a.samples[(size_t)(b - 1) * kTilePixels + lane + k * kWarp]
+                                           : make_float4(0.f, 0.f, 0.f, 1.f);
+          Lr[k] = a.dL[pix];
+          Lg[k] = a.dL[HW + pix];
+          Lb[k] = a.dL[2 * HW + pix];
+          T[k] = prev.w;
+          Pd[k] = prev.x * Lr[k] + prev.y * Lg[k] + prev.z * Lb[k];
+          // K = C_final . dL + T_final * (bg . dL): everything behind a
+          // Gaussian is K - (prefix up to and including it) . dL.
+          K[k] = a.pix_color[pix] * Lr[k] + a.pix_color[HW + pix] * Lg[k] + a.pix_color[2 * HW + pix] * Lb[k] +
+                 a.Ts_final[pix] * (bgr * Lr[k] + bgg * Lg[k] + bgb * Lb[k]);
+        }
+      }
+    }
+    if (__any_sync(0xffffffffu, alive) == 0) {
+      __syncwarp();
+      continue;
+    }
+
+    for (int g = 0; g < bi.n; ++g) {
+      const float2 xy = st.xy[g];
+      const float4 co = st.co[g];
+      const float4 c = st.rgb[g];
+      const float dx = xy.x - px;
+      const float A = fmaf(co.x * dx, dx, co.w);
+      const float Bx = co.y * dx;
+      const float gx0 = 2.f * co.x * dx;
+      float dy = xy.y - py0;
+      float v[16];
+#pragma unroll
+      for (int j = 0; j < 16; ++j) v[j] = 0.f;
+      bool any = false;
+#pragma unroll
+      for (int k = 0; k < kPxPerThread; ++k) {
+        const float e = fmaf(dy, fmaf(co.z, dy, Bx), A);
+        const float al = fminf(kAlphaMax, ex2_approx(e));
+        if (((alive >> k) & 1u) && al >= kAlphaCut) {
+          any = true;
+          const float w = al * T[k];
+          const float cd = c.x * Lr[k] + c.y * Lg[k] + c.z * Lb[k];
+          Pd[k] = fmaf(w, cd, Pd[k]);
+          const float inv = __frcp_rn(1.f - al);
+          const float dLda = T[k] * cd - inv * (K[k] - Pd[k]);
+          T[k] -= w;
+          v[8] = fmaf(w, Lr[k], v[8]);
+          v[9] = fmaf(w, Lg[k], v[9]);
+          v[10] = fmaf(w, Lb[k], v[10]);
+          const float dp = dLda * al;  // dL/dpower / ln2
+          const float tx = dp * fmaf(co.y, dy, gx0);
+          const float ty = dp * fmaf(2.f * co.z, dy, Bx);
+          v[0] += tx;
+          v[1] += ty;
+          v[2] += fabsf(tx);
+          v[3] += fabsf(ty);
+          v[4] = fmaf(dp, dx * dx, v[4]);
+          v[5] = fmaf(dp * dx, dy, v[5]);
+          v[7] = fmaf(dp * dy, dy, v[7]);
+          v[11] += dp;
+        }
+        dy -= ystep;
+      }
+      if (__any_sync(0xffffffffu, any)) {
+        const float tot = warp_transpose_reduce16(v, lane);
+        if (!(lane & 1) && vid < FGS_GRAD_STRIDE && vid != 6) {
+          const float s = (vid == 11) ? 1.0f / ex2_approx(co.w) : vscale;
+          atomicAdd(a.grad + (size_t)__float_as_uint(c.w) * FGS_GRAD_STRIDE + vid, tot * s);
+        }
+      }
+    }
+    __syncwarp();
+  }
+}
+
+struct PbwdArgs {
+  int P, D, M;
+  const float* means;
+  const int* radii;
+  const float* dc;
+  const float* shs;
+  const float* splat;
+  const float* scales;
+  const float* rots;
+  float smod;
+  const float* view;
+  const float* proj;
+  float fx, fy, tanx, tany;
+  const float* campos;
+  const float* grad;
+  float* dmean2D;
+  float* dconic;
+  float* dopac;
+  float* dcolor;
+  float* dmean3D;
+  float* dcov3D;
+  float* ddc;
+  float* dsh;
+  float* dscale;
+  float* drot;
+  float* accum;
+  float* accum_abs;
+  float* max_radii;
+  float* denom;
+};
+
+__device__ __forceinline__ void sh_term(float B, float bx, float by, float bz, const float* co, float* out,
+                                        float3 drgb, float3& ddir) {
+  out[0] = B * drgb.x;
+  out[1] = B * drgb.y;
+  out[2] = B * drgb.z;
+  const float dot = co[0] * drgb.x + co[1] * drgb.y + co[2] * drgb.z;
+  ddir.x = fmaf(bx, dot, ddir.x);
+  ddir.y = fmaf(by, dot, ddir.y);
+  ddir.z = fmaf(bz, dot, ddir.z);
+}
+
+__global__ void __launch_bounds__(256) k_preprocess_bwd(const PbwdArgs a) {
+  const int i = blockIdx.x * 256 + threadIdx.x;
+  if (i >= a.P) return;
+  const float4* gr = reinterpret_cast<const float4*>(a.grad + (size_t)i * FGS_GRAD_STRIDE);
+  const float4 gm2 = gr[0], gcn = gr[1], gco = gr[2];
+  reinterpret_cast<float4*>(a.dmean2D)[i] = gm2;
+  reinterpret_cast<float4*>(a.dconic)[i] = make_float4(gcn.x, gcn.y, 0.f, gcn.w);
+  a.dcolor[3 * (size_t)i] = gco.x;
+  a.dcolor[3 * (size_t)i + 1] = gco.y;
+  a.dcolor[3 * (size_t)i + 2] = gco.z;
+  a.dopac[i] = gco.w;
+  float* gm = a.dmean3D + 3 * (size_t)i;
+  float* gc = a.dcov3D + 6 * (size_t)i;
+  float* gdc = a.ddc + 3 * (size_t)i;
+  float* gsh = a.dsh ? a.dsh + (size_t)i * a.M * 3 : nullptr;
+  float* gs = a.dscale + 3 * (size_t)i;
+  const int radius = a.radii[i];
+  if (!(radius > 0)) {
+    gm[0] = gm[1] = gm[2] = 0.f;
+    for (int k = 0; k < 6; ++k) gc[k] = 0.f;
+    gdc[0] = gdc[1] = gdc[2] = 0.f;
+    if (gsh) for (int k = 0; k < 3 * a.M; ++k) gsh[k] = 0.f;
+    gs[0] = gs[1] = gs[2] = 0.f;
+    reinterpret_cast<float4*>(a.drot)[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    return;
+  }
+  const float3 p = make_float3(a.means[3 * (size_t)i], a.means[3 * (size_t)i + 1], a.means[3 * (size_t)i + 2]);
+  // --- rotation / covariance (raw quaternion, FB backward.cu:407-430)
+  const float4 q = reinterpret_cast<const float4*>(a.rots)[i];
+  const float qr = q.x, qx = q.y, qy = q.z, qz = q.w;
+  float R[3][3];
+  R[0][0] = 1.f - 2.f * (qy * qy + qz * qz); R[0][1] = 2.f * (qx * qy - qr * qz); R[0][2] = 2.f * (qx * qz + qr * qy);
+  R[1][0] = 2.f * (qx * qy + qr * qz); R[1][1] = 1.f - 2.f * (qx * qx + qz * qz); R[1][2] = 2.f * (qy * qz - qr * qx);
+  R[2][0] = 2.f * (qx * qz - qr * qy); R[2][1] = 2.f * (qy * qz + qr * qx); R[2][2] = 1.f - 2.f * (qx * qx + qy * qy);
+  const float sv[3] = {a.smod * a.scales[3 * (size_t)i], a.smod * a.scales[3 * (size_t)i + 1],
+                       a.smod * a.scales[3 * (size_t)i + 2]};
+  const float s2[3] = {sv[0] * sv[0], sv[1] * sv[1], sv[2] * sv[2]};
+  float S[3][3];
+#pragma unroll
+  for (int r = 0; r < 3; ++r)
+#pragma unroll
+    for (int c = 0; c < 3; ++c) S[r][c] = R[r][0] * s2[0] * R[c][0] + R[r][1] * s2[1] * R[c][1] + R[r][2] * s2[2] * R[c][2];
+  // --- conic -> cov2D -> cov3D / mean (FB backward.cu:250-403)
+  const float3 t = xform_point3(a.view, p);
+  const float limx = 1.3f * a.tanx, limy = 1.3f * a.tany;
+  const float txtz = t.x / t.z, tytz = t.y / t.z;
+  const float tx = fminf(limx, fmaxf(-limx, txtz)) * t.z;
+  const float ty = fminf(limy, fmaxf(-limy, tytz)) * t.z;
+  const float xm = (txtz < -limx || txtz > limx) ? 0.f : 1.f;
+  const float ym = (tytz < -limy || tytz > limy) ? 0.f : 1.f;
+  const float iz = 1.f / t.z, iz2 = iz * iz, iz3 = iz2 * iz;
+  const float j00 = a.fx * iz, j02 = -a.fx * tx * iz2, j11 = a.fy * iz, j12 = -a.fy * ty * iz2;
+  const float* V = a.view;
+  float M0[3], M1[3];
+#pragma unroll
+  for (int b = 0; b < 3; ++b) {
+    M0[b] = j00 * V[b * 4 + 0] + j02 * V[b * 4 + 2];
+    M1[b] = j11 * V[b * 4 + 1] + j12 * V[b * 4 + 2];
+  }
+  float SM0[3], SM1[3];
+#pragma unroll
+  for (int b = 0; b < 3; ++b) {
+    SM0[b] = S[b][0] * M0[0] + S[b][1] * M0[1] + S[b][2] * M0[2];
+    SM1[b] = S[b][0] * M1[0] + S[b][1] * M1[1] + S[b][2] * M1[2];
+  }
+  const float ca = M0[0] * SM0[0] + M0[1] * SM0[1] + M0[2] * SM0[2] + 0.3f;
+  const float cb = M0[0] * SM1[0] + M0[1] * SM1[1] + M0[2] * SM1[2];
+  const float cc = M1[0] * SM1[0] + M1[1] * SM1[1] + M1[2] * SM1[2] + 0.3f;
+  const float gx = gcn.x, gy = gcn.y, gz = gcn.w;
+  const float den = ca * cc - cb * cb;
+  const float d2 = 1.f / (den * den + 0.0000001f);
+  const float dLa = d2 * (-cc * cc * gx + 2.f * cb * cc * gy + (den - ca * cc) * gz);
+  const float dLc = d2 * (-ca * ca * gz + 2.f * ca * cb * gy + (den - ca * cc) * gx);
+  const float dLb = d2 * 2.f * (cb * cc * gx - (den + 2.f * cb * cb) * gy + ca * cb * gz);
+  float G[3][3];
+#pragma unroll
+  for (int r = 0; r < 3; ++r)
+#pragma unroll
+    for (int c = 0; c < 3; ++c)
+      G[r][c] = M0[r] * M0[c] * dLa + 0.5f * (M0[r] * M1[c] + M0[c] * M1[r]) * dLb + M1[r] * M1[c] * dLc;
+  gc[0] = G[0][0]; gc[1] = 2.f * G[0][1]; gc[2] = 2.f * G[0][2];
+  gc[3] = G[1][1]; gc[4] = 2.f * G[1][2]; gc[5] = G[2][2];
+  float dM0[3], dM1[3];
+#pragma unroll
+  for (int b = 0; b < 3; ++b) {
+    dM0[b] = 2.f * dLa * SM0[b] + dLb * SM1[b];
+    dM1[b] = 2.f * dLc * SM1[b] + dLb * SM0[b];
+  }
+  // dL/dJ[a][k] = sum_b dM[a][b] * Rw[k][b], Rw[k][b] = V[b*4 + k]
+  const float dJ00 = dM0[0] * V[0] + dM0[1] * V[4] + dM0[2] * V[8];
+  const float dJ02 = dM0[0] * V[2] + dM0[1] * V[6] + dM0[2] * V[10];
+  const float dJ11 = dM1[0] * V[1] + dM1[1] * V[5] + dM1[2] * V[9];
+  const float dJ12 = dM1[0] * V[2] + dM1[1] * V[6] + dM1[2] * V[10];
+  const float dtx = xm * -a.fx * iz2 * dJ02;
+  const float dty = ym * -a.fy * iz2 * dJ12;
+  const float dtz = -a.fx * iz2 * dJ00 - a.fy * iz2 * dJ11 + 2.f * a.fx * tx * iz3 * dJ02 + 2.f * a.fy * ty * iz3 * dJ12;
+  float m3[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) m3[k] = V[k * 4 + 0] * dtx + V[k * 4 + 1] * dty + V[k * 4 + 2] * dtz;
+  // --- screen-space mean (FB backward.cu:504-526)
+  const float4 hp = xform_point4(a.proj, p);
+  const float mw = 1.f / (hp.w + 0.0000001f);
+  const float* Pm = a.proj;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const float jx = Pm[4 * k] * mw - Pm[4 * k + 3] * hp.x * mw * mw;
+    const float jy = Pm[4 * k + 1] * mw - Pm[4 * k + 3] * hp.y * mw * mw;
+    m3[k] += jx * gm2.x + jy * gm2.y;
+  }
+  // --- SH (FB backward.cu:121-245), only when SH coefficients were given
+  if (a.shs) {
+    const float* rec = a.splat + (size_t)i * 32;
+    const float3 drgb = make_float3(gco.x * (1.f - rec[F_CLAMP]), gco.y * (1.f - rec[F_CLAMP + 1]),
+                                    gco.z * (1.f - rec[F_CLAMP + 2]));
+    const float vx = p.x - a.campos[0], vy = p.y - a.campos[1], vz = p.z - a.campos[2];
+    const float n2 = vx * vx + vy * vy + vz * vz, inv_n = rsqrtf(n2);
+    const float x = vx * inv_n, y = vy * inv_n, z = vz * inv_n;
+    const float c0 = 0.28209479177387814f;
+    gdc[0] = c0 * drgb.x; gdc[1] = c0 * drgb.y; gdc[2] = c0 * drgb.z;
+    const float* co = a.shs + (size_t)i * a.M * 3;
+    float3 dd = make_float3(0.f, 0.f, 0.f);
+    const int used = (a.D + 1) * (a.D + 1) - 1;
+    if (a.D > 0) {
+      const float c1 = 0.4886025119029199f;
+      sh_term(-c1 * y, 0.f, -c1, 0.f, co + 0, gsh + 0, drgb, dd);
+      sh_term(c1 * z, 0.f, 0.f, c1, co + 3, gsh + 3, drgb, dd);
+      sh_term(-c1 * x, -c1, 0.f, 0.f, co + 6, gsh + 6, drgb, dd);
+      if (a.D > 1) {
+        const float k2a = 1.0925484305920792f, k2b = 0.31539156525252005f, k2c = 0.5462742152960396f;
+        const float xx = x * x, yy = y * y, zz = z * z;
+        sh_term(k2a * x * y, k2a * y, k2a * x, 0.f, co + 9, gsh + 9, drgb, dd);
+        sh_term(-k2a * y * z, 0.f, -k2a * z, -k2a * y, co + 12, gsh + 12, drgb, dd);
+        sh_term(k2b * (2.f * zz - xx - yy), -2.f * k2b * x, -2.f * k2b * y, 4.f * k2b * z, co + 15, gsh + 15, drgb, dd);
+        sh_term(-k2a * x * z, -k2a * z, 0.f, -k2a * x, co + 18, gsh + 18, drgb, dd);
+        sh_term(k2c * (xx - yy), 2.f * k2c * x, -2.f * k2c * y, 0.f, co + 21, gsh + 21, drgb, dd);
+        if (a.D > 2) {
+          const float ka = 0.5900435899266435f, kb = 2.890611442640554f, kc = 0.4570457994644658f,
+                      kd = 0.3731763325901154f, ke = 1.445305721320277f;
+          sh_term(-ka * y * (3.f * xx - yy), -ka * 6.f * x * y, -ka * (3.f * xx - 3.f * yy), 0.f, co + 24, gsh + 24,
+                  drgb, dd);
+          sh_term(kb * x * y * z, kb * y * z, kb * x * z, kb * x * y, co + 27, gsh + 27, drgb, dd);
+          sh_term(-kc * y * (4.f * zz - xx - yy), kc * 2.f * x * y, -kc * (4.f * zz - xx - 3.f * yy),
+                  -kc * 8.f * y * z, co + 30, gsh + 30, drgb, dd);
+          sh_term(kd * z * (2.f * zz - 3.f * xx - 3.f * yy), -kd * 6.f * x * z, -kd * 6.f * y * z,
+                  kd * (6.f * zz - 3.f * xx - 3.f * yy), co + 33, gsh + 33, drgb, dd);
+          sh_term(-kc * x * (4.f * zz - xx - yy), -kc * (4.f * zz - 3.f * xx - yy), kc * 2.f * x * y,
+                  -kc * 8.f * x * z, co + 36, gsh + 36, drgb, dd);
+          sh_term(ke * z * (xx - yy), ke * 2.f * x * z, -ke * 2.f * y * z, ke * (xx - yy), co + 39, gsh + 39, drgb,
+                  dd);
+          sh_term(-ka * x * (xx - 3.f * yy), -ka * (3.f * xx - 3.f * yy), ka * 6.f * x * y, 0.f, co + 42, gsh + 42,
+                  drgb, dd);
+        }
+      }
+    }
+    for (int k = 3 * used; k < 3 * a.M; ++k) gsh[k] = 0.f;
+    // d(v / |v|)/dv applied to the direction gradient
+    const float vd = vx * dd.x + vy * dd.y + vz * dd.z;
+    const float inv3 = inv_n * inv_n * inv_n;
+    m3[0] += (dd.x * n2 - vx * vd) * inv3;
+    m3[1] += (dd.y * n2 - vy * vd) * inv3;
+    m3[2] += (dd.z * n2 - vz * vd) * inv3;
+  } else {
+    gdc[0] = gdc[1] = gdc[2] = 0.f;
+    if (gsh) for (int k = 0; k < 3 * a.M; ++k) gsh[k] = 0.f;
+  }
+  gm[0] = m3[0]; gm[1] = m3[1]; gm[2] = m3[2];
+  // --- scale / rotation: Sigma = R diag(s^2) R^T (FB backward.cu:407-483)
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    float acc = 0.f;
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+#pragma unroll
+      for (int c = 0; c < 3; ++c) acc += G[r][c] * R[r][k] * R[c][k];
+    gs[k] = 2.f * sv[k] * acc;  // w.r.t. the modified scale, as FB returns it
+  }
+  float dR[3][3];  // 2 G R diag(s^2)
+#pragma unroll
+  for (int r = 0; r < 3; ++r)
+#pragma unroll
+    for (int c = 0; c < 3; ++c) dR[r][c] = 2.f * (G[r][0] * R[0][c] + G[r][1] * R[1][c] + G[r][2] * R[2][c]) * s2[c];
+  const float dqr = 2.f * qz * (dR[1][0] - dR[0][1]) + 2.f * qy * (dR[0][2] - dR[2][0]) + 2.f * qx * (dR[2][1] - dR[1][2]);
+  const float dqx = 2.f * qy * (dR[0][1] + dR[1][0]) + 2.f * qz * (dR[0][2] + dR[2][0]) +
+                    2.f * qr * (dR[2][1] - dR[1][2]) - 4.f * qx * (dR[1][1] + dR[2][2]);
+  const float dqy = 2.f * qx * (dR[0][1] + dR[1][0]) + 2.f * qr * (dR[0][2] - dR[2][0]) +
+                    2.f * qz * (dR[1][2] + dR[2][1]) - 4.f * qy * (dR[0][0] + dR[2][2]);
+  const float dqz = 2.f * qr * (dR[1][0] - dR[0][1]) + 2.f * qx * (dR[0][2] + dR[2][0]) +
+                    2.f * qy * (dR[1][2] + dR[2][1]) - 4.f * qz * (dR[0][0] + dR[1][1]);
+  reinterpret_cast<float4*>(a.drot)[i] = make_float4(dqr, dqx, dqy, dqz);
+  // --- densification statistics (FB backward.cu:892-918)
+  if (a.accum) {
+    if (a.denom) a.denom[i] += 1.f;
+    if (a.max_radii) a.max_radii[i] = fmaxf(a.max_radii[i], (float)radius);
+    a.accum[i] += sqrt_approx(gm2.x * gm2.x + gm2.y * gm2.y);
+    if (a.accum_abs) a.accum_abs[i] += sqrt_approx(gm2.z * gm2.z + gm2.w * gm2.w);
+  }
+}
+
+__global__ void __launch_bounds__(256) k_densify(int P, const int* radii, const float4* dm2, float* accum,
+                                                 float* accum_abs, float* max_radii, float* denom) {
+  const int i = blockIdx.x * 256 + threadIdx.x;
+  if (i >= P || !(radii[i] > 0)) return;
+  const float4 g = dm2[i];
+  if (denom) denom[i] += 1.f;
+  if (max_radii) max_radii[i] = fmaxf(max_radii[i], (float)radii[i]);
+  if (accum) accum[i] += sqrt_approx(g.x * g.x + g.y * g.y);
+  if (accum_abs) accum_abs[i] += sqrt_approx(g.z * g.z + g.w * g.w);
+}
+
+bool tile_shape_ok(int bx, int by) { return bx * by == kTilePixels && (bx == 8 || bx == 16 || bx == 32); }
+
+}  // namespace
+}  // namespace fgs
+
+FGS_DEFINE_ERROR_ACCESSOR(backward)
+
+using namespace fgs;
+
+extern "C" fgs_status fgs_render_bwd(int P, int width, int height, int block_x, int block_y, int bucket_size,
+                                     const uint32_t* values_sorted, const uint32_t* ranges, const float* bg,
+                                     const float* splat_buffer, const float* Ts_final,
+                                     const int32_t* last_contributor, const void* image_state,
+                                     const void* sample_state, int64_t max_buckets, const float* dL_dpixels,
+                                     float* grad_record, void* stream) {
+  if (P < 0 || width <= 0 || height <= 0 || !tile_shape_ok(block_x, block_y) || bucket_size < 1 ||
+      bucket_size > kMaxBucket || max_buckets < 0)
+    return FGS_ERR_BAD_ARG;
+  if (P == 0) return FGS_OK;
+  if (!ranges || !bg || !splat_buffer || !Ts_final || !last_contributor || !image_state || !sample_state ||
+      !dL_dpixels || !grad_record || !values_sorted)
+    return FGS_ERR_BAD_ARG;
+  if (((uintptr_t)grad_record & 15) || ((uintptr_t)splat_buffer & 15)) return FGS_ERR_BAD_ARG;
+  const int gx = (width + block_x - 1) / block_x, gy = (height + block_y - 1) / block_y, T = gx * gy;
+  const ImageState im = carve_image(const_cast<void*>(image_state), width, height, T);
+  const SampleState sm = carve_sample(const_cast<void*>(sample_state), max_buckets > 0 ? max_buckets : 1);
+  cudaStream_t s = (cudaStream_t)stream;
+  FGS_TRY(cudaMemsetAsync(grad_record, 0, sizeof(float) * FGS_GRAD_STRIDE * (size_t)P, s));
+  BwdArgs a{splat_buffer, values_sorted, ranges, sm.bucket_tile, im.bucket_off, im.bucket_sum, im.max_contrib,
+            sm.samples, im.pix_color, Ts_final, last_contributor, dL_dpixels, bg, grad_record,
+            width, height, block_x, block_y, gx, bucket_size};
+  k_render_bwd<<<num_sms() * 8, kBwdWarps * kWarp, 0, s>>>(a);
+  FGS_LAUNCH_CHECK();
+  return FGS_OK;
+}
+
+extern "C" fgs_status fgs_preprocess_bwd(
+    int P, int D, int M, const float* means3D, const int32_t* radii, const float* dc, const float* shs,
+    const float* splat_buffer, const float* scales, const float* rotations, float scale_modifier,
+    const float* viewmatrix, const float* projmatrix, int width, int height, float tan_fovx, float tan_fovy,
+    const float* campos, const float* grad_record, float* dL_dmean2D, float* dL_dconic, float* dL_dopacity,
+    float* dL_dcolor, float* dL_dmean3D, float* dL_dcov3D, float* dL_ddc, float* dL_dsh, float* dL_dscale,
+    float* dL_drot, float* xyz_gradient_accum, float* xyz_gradient_accum_abs, float* max_radii, float* denom,
+    void* stream) {
+  if (P < 0 || D < 0 || D > 3 || M < 0 || width <= 0 || height <= 0) return FGS_ERR_BAD_ARG;
+  if (P == 0) return FGS_OK;
+  if (!means3D || !radii || !splat_buffer || !scales || !rotations || !viewmatrix || !projmatrix || !grad_record ||
+      !dL_dmean2D || !dL_dconic || !dL_dopacity || !dL_dcolor || !dL_dmean3D || !dL_dcov3D || !dL_ddc ||
+      !dL_dscale || !dL_drot)
+    return FGS_ERR_BAD_ARG;
+  if (shs && (!dc || !campos || (D > 0 && M < (D + 1) * (D + 1) - 1) || !dL_dsh)) return FGS_ERR_BAD_ARG;
+  if (((uintptr_t)grad_record & 15) || ((uintptr_t)dL_dmean2D & 15) || ((uintptr_t)dL_dconic & 15) ||
+      ((uintptr_t)rotations & 15) || ((uintptr_t)dL_drot & 15))
+    return FGS_ERR_BAD_ARG;
+  PbwdArgs a;
+  a.P = P; a.D = D; a.M = M;
+  a.means = means3D; a.radii = radii; a.dc = dc; a.shs = shs; a.splat = splat_buffer;
+  a.scales = scales; a.rots = rotations; a.smod = scale_modifier;
+  a.view = viewmatrix; a.proj = projmatrix;
+  a.fx = width / (2.0f * tan_fovx); a.fy = height / (2.0f * tan_fovy); a.tanx = tan_fovx; a.tany = tan_fovy;
+  a.campos = campos; a.grad = grad_record;
+  a.dmean2D = dL_dmean2D; a.dconic = dL_dconic; a.dopac = dL_dopacity; a.dcolor = dL_dcolor;
+  a.dmean3D = dL_dmean3D; a.dcov3D = dL_dcov3D; a.ddc = dL_ddc; a.dsh = shs ? dL_dsh : (M > 0 ? dL_dsh : nullptr);
+  a.dscale = dL_dscale; a.drot = dL_drot;
+  a.accum = xyz_gradient_accum; a.accum_abs = xyz_gradient_accum_abs; a.max_radii = max_radii; a.denom = denom;
+  k_preprocess_bwd<<<(P + 255) / 256, 256, 0, (cudaStream_t)stream>>>(a);
+  FGS_LAUNCH_CHECK();
+  return FGS_OK;
+}
+
+extern "C" fgs_status fgs_densify_stats(int P, const int32_t* radii, const float* dL_dmean2D,
+                                        float* xyz_gradient_accum, float* xyz_gradient_accum_abs,
+                                        float* max_radii, float* denom, void* stream) {
+  if (P < 0) return FGS_ERR_BAD_ARG;
+  if (P == 0) return FGS_OK;
+  if (!radii || !dL_dmean2D || ((uintptr_t)dL_dmean2D & 15)) return FGS_ERR_BAD_ARG;
+  k_densify<<<(P + 255) / 256, 256, 0, (cudaStream_t)stream>>>(P, radii, reinterpret_cast<const float4*>(dL_dmean2D),
+                                                              xyz_gradient_accum, xyz_gradient_accum_abs, max_radii,
+                                                              denom);
+  FGS_LAUNCH_CHECK();
+  return FGS_OK;
+}

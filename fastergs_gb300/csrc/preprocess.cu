@@ -1,0 +1,425 @@
+// Per-Gaussian preprocess and (tile | depth, Gaussian) key emission, sm_103a.
+//
+// Restates FB csrc/cuda_rasterizer/preprocess.cu (projection, EWA covariance,
+// SH colour, tile rectangle, ellipse/tile test, lane-packed emission of small
+// Gaussians, 128-tile sub-tasks for large ones) with a GB300 layout:
+//   * one CTA of 8 warps handles 256 consecutive Gaussians, one per thread;
+//   * the warp's small Gaussians are flattened into one candidate list
+//     (exclusive scan of rect areas) and 32 candidates are tested per step, so
+//     every lane does useful work whatever the footprint mix;
+//   * hits are staged per warp in shared memory and flushed with one atomic
+//     per ~100 pairs instead of one per 32 candidates;
+//   * large Gaussians queue (id, first tile) sub-tasks that a persistent
+//     second kernel drains; the task count never travels to the host.
+#include "fgs_common.cuh"
+
+namespace fgs {
+namespace {
+
+constexpr int kPreThreads = 256;
+constexpr int kPreWarps = kPreThreads / kWarp;
+constexpr int kStage = 128;  // staged pairs per warp before a flush
+
+struct PreArgs {
+  int P, D, M;
+  const float* means;
+  const float* colors;
+  const float* dc;
+  const float* shs;
+  const float* opac;
+  const float* scales;
+  const float* rots;
+  float smod;
+  int W, H, bx, by, gx, gy;
+  const float* campos;
+  const float* view;
+  const float* proj;
+  float tanx, tany, fx, fy, mult;
+  const uint8_t* culling;
+  float* splat;
+  unsigned long long* keys;
+  uint32_t* vals;
+  long long cap;
+  uint32_t* tasks;
+  long long task_cap;  // in tasks (2 words each)
+  unsigned int* curr;
+  int* counters;
+  int* radii;
+};
+
+// Ellipse chord test along one tile edge (FB preprocess.cu:168-177): does the
+// quadratic A u^2 + B u + C = 0 have a root interval meeting [l - d, r - d]?
+__device__ __forceinline__ bool chord_hits(float A, float B, float C, float d, float l, float r) {
+  const float disc = B * B - 4.0f * A * C;
+  const float t1 = (l - d) * (2.0f * A) + B;
+  const float t2 = (r - d) * (2.0f * A) + B;
+  return disc >= 0.0f && (t1 <= 0.0f || t1 * t1 <= disc) && (t2 >= 0.0f || t2 * t2 <= disc);
+}
+
+// Does the level set conic(d) = 2*power touch the pixel block whose top-left
+// pixel centre is (px0, py0)?  Centre-inside test plus a chord test against
+// the nearest vertical and nearest horizontal edge (FB preprocess.cu:179-218).
+__device__ __forceinline__ bool tile_hit(int px0, int py0, int bx, int by, float2 c, float4 cp) {
+  const float x0 = (float)px0, x1 = (float)(px0 + bx - 1);
+  const float y0 = (float)py0, y1 = (float)(py0 + by - 1);
+  if (c.x >= x0 && c.x <= x1 && c.y >= y0 && c.y <= y1) return true;
+  const float w = 2.0f * cp.w;
+  const float dx = c.x - ((c.x * 2.0f < x0 + x1) ? x0 : x1);
+  if (chord_hits(cp.z, -2.0f * cp.y * dx, cp.x * dx * dx - w, c.y, y0, y1)) return true;
+  const float dy = c.y - ((c.y * 2.0f < y0 + y1) ? y0 : y1);
+  return chord_hits(cp.x, -2.0f * cp.y * dy, cp.z * dy * dy - w, c.x, x0, x1);
+}
+
+struct WarpStage {
+  unsigned long long* key;
+  uint32_t* val;
+  int n;
+};
+
+__device__ __forceinline__ void stage_flush(WarpStage& st, const PreArgs& a, int lane) {
+  __syncwarp();
+  if (st.n == 0) return;
+  unsigned int base = 0;
+  if (lane == 0) base = atomicAdd(a.curr, (unsigned int)st.n);
+  base = __shfl_sync(0xffffffffu, base, 0);
+  bool over = false;
+  for (int j = lane; j < st.n; j += kWarp) {
+    const long long dst = (long long)base + j;
+    if (dst < a.cap) {
+      a.keys[dst] = st.key[j];
+      a.vals[dst] = st.val[j];
+    } else {
+      over = true;
+    }
+  }
+  if (__any_sync(0xffffffffu, over) && lane == 0) raise_error(kErrCapacity);
+  st.n = 0;
+  __syncwarp();
+}
+
+__device__ __forceinline__ void stage_push(WarpStage& st, const PreArgs& a, int lane, bool hit,
+                                           unsigned long long key, uint32_t id) {
+  const uint32_t m = __ballot_sync(0xffffffffu, hit);
+  if (m == 0) return;
+  const int cnt = __popc(m);
+  if (st.n + cnt > kStage) stage_flush(st, a, lane);
+  if (hit) {
+    const int pos = st.n + __popc(m & lanemask_lt());
+    st.key[pos] = key;
+    st.val[pos] = id;
+  }
+  st.n += cnt;
+}
+
+__device__ __forceinline__ float3 f3(float x, float y, float z) { return make_float3(x, y, z); }
+__device__ __forceinline__ float3 operator+(float3 a, float3 b) { return f3(a.x + b.x, a.y + b.y, a.z + b.z); }
+__device__ __forceinline__ float3 operator*(float s, float3 a) { return f3(s * a.x, s * a.y, s * a.z); }
+__device__ __forceinline__ float3 ld3(const float* p) { return f3(p[0], p[1], p[2]); }
+
+// SH colour at the unit view direction (FB preprocess.cu:119-166).
+__device__ __forceinline__ float3 sh_colour(int D, float x, float y, float z, const float* dc, const float* sh,
+                                            float* clamp) {
+  float3 r = 0.28209479177387814f * ld3(dc);
+  if (D > 0) {
+    const float c1 = 0.4886025119029199f;
+    r = r + (-c1 * y) * ld3(sh + 0) + (c1 * z) * ld3(sh + 3) + (-c1 * x) * ld3(sh + 6);
+    if (D > 1) {
+      const float xx = x * x, yy = y * y, zz = z * z, xy = x * y, yz = y * z, xz = x * z;
+      r = r + (1.0925484305920792f * xy) * ld3(sh + 9) + (-1.0925484305920792f * yz) * ld3(sh + 12) +
+          (0.31539156525252005f * (2.0f * zz - xx - yy)) * ld3(sh + 15) +
+          (-1.0925484305920792f * xz) * ld3(sh + 18) + (0.5462742152960396f * (xx - yy)) * ld3(sh + 21);
+      if (D > 2) {
+        r = r + (-0.5900435899266435f * y * (3.0f * xx - yy)) * ld3(sh + 24) +
+            (2.890611442640554f * xy * z) * ld3(sh + 27) +
+            (-0.4570457994644658f * y * (4.0f * zz - xx - yy)) * ld3(sh + 30) +
+            (0.3731763325901154f * z * (2.0f * zz - 3.0f * xx - 3.0f * yy)) * ld3(sh + 33) +
+            (-0.4570457994644658f * x * (4.0f * zz - xx - yy)) * ld3(sh + 36) +
+            (1.445305721320277f * z * (xx - yy)) * ld3(sh + 39) +
+            (-0.5900435899266435f * x * (xx - 3.0f * yy)) * ld3(sh + 42);
+      }
+    }
+  }
+  r = r + f3(0.5f, 0.5f, 0.5f);
+  clamp[0] = r.x < 0.0f ? 1.0f : 0.0f;
+  clamp[1] = r.y < 0.0f ? 1.0f : 0.0f;
+  clamp[2] = r.z < 0.0f ? 1.0f : 0.0f;
+  return f3(fmaxf(r.x, 0.0f), fmaxf(r.y, 0.0f), fmaxf(r.z, 0.0f));
+}
+
+__global__ void __launch_bounds__(kPreThreads) k_preprocess(const PreArgs a) {
+  __shared__ float2 s_xy[kPreWarps][kWarp];
+  __shared__ float4 s_cp[kPreWarps][kWarp];    // conic a, b, c, power
+  __shared__ int4 s_geo[kPreWarps][kWarp];     // rect min x, min y, width, candidate start
+  __shared__ uint32_t s_depth[kPreWarps][kWarp];
+  __shared__ unsigned long long s_key[kPreWarps][kStage];
+  __shared__ uint32_t s_val[kPreWarps][kStage];
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int i = blockIdx.x * kPreThreads + threadIdx.x;
+
+  bool valid = false;
+  int area = 0, tw = 0;
+  int2 rmin = make_int2(0, 0), rmax = make_int2(0, 0);
+  float2 xy = make_float2(0.f, 0.f);
+  float4 cp = make_float4(0.f, 0.f, 0.f, 0.f);
+  float depth = 0.f;
+
+  if (i < a.P) {
+    float radius = 0.0f;
+    float rec[32];
+#pragma unroll
+    for (int k = 0; k < 32; ++k) rec[k] = 0.0f;
+    do {
+      if (a.culling && a.culling[i]) break;
+      const float3 p = ld3(a.means + 3 * (size_t)i);
+      const float3 t = xform_point3(a.view, p);
+      if (t.z <= 0.2f) break;                        // near cull (FB preprocess.cu:456)
+      const float o = a.opac[i];
+      if (255.0f * o < 1.0f) break;                  // opacity cull (FB preprocess.cu:459)
+      const float4 hp = xform_point4(a.proj, p);
+      const float pw = 1.0f / (hp.w + 0.0000001f);
+      const float ndcx = hp.x * pw, ndcy = hp.y * pw;
+
+      // 3D covariance R diag(s^2) R^T from the raw quaternion (FB preprocess.cu:364-400).
+      const float4 q = *reinterpret_cast<const float4*>(a.rots + 4 * (size_t)i);
+      const float qr = q.x, qx = q.y, qy = q.z, qz = q.w;
+      float R[3][3];
+      R[0][0] = 1.f - 2.f * (qy * qy + qz * qz); R[0][1] = 2.f * (qx * qy - qr * qz); R[0][2] = 2.f * (qx * qz + qr * qy);
+      R[1][0] = 2.f * (qx * qy + qr * qz); R[1][1] = 1.f - 2.f * (qx * qx + qz * qz); R[1][2] = 2.f * (qy * qz - qr * qx);
+      R[2][0] = 2.f * (qx * qz - qr * qy); R[2][1] = 2.f * (qy * qz + qr * qx); R[2][2] = 1.f - 2.f * (qx * qx + qy * qy);
+      const float sx = a.smod * a.scales[3 * (size_t)i], sy = a.smod * a.scales[3 * (size_t)i + 1],
+                  sz = a.smod * a.scales[3 * (size_t)i + 2];
+      const float s2[3] = {sx * sx, sy * sy, sz * sz};
+      float S[6];
+      {
+        int k = 0;
+#pragma unroll
+        for (int r = 0; r < 3; ++r)
+#pragma unroll
+          for (int c = r; c < 3; ++c) S[k++] = R[r][0] * s2[0] * R[c][0] + R[r][1] * s2[1] * R[c][1] + R[r][2] * s2[2] * R[c][2];
+      }
+      // EWA screen covariance (FB preprocess.cu:79-117).
+      const float limx = 1.3f * a.tanx, limy = 1.3f * a.tany;
+      const float tx = fminf(limx, fmaxf(-limx, t.x / t.z)) * t.z;
+      const float ty = fminf(limy, fmaxf(-limy, t.y / t.z)) * t.z;
+      const float j00 = a.fx / t.z, j02 = -(a.fx * tx) / (t.z * t.z);
+      const float j11 = a.fy / t.z, j12 = -(a.fy * ty) / (t.z * t.z);
+      const float* V = a.view;
+      // M = J * Rw, Rw[k][b] = V[b*4 + k]
+      float M0[3], M1[3];
+#pragma unroll
+      for (int b = 0; b < 3; ++b) {
+        M0[b] = j00 * V[b * 4 + 0] + j02 * V[b * 4 + 2];
+        M1[b] = j11 * V[b * 4 + 1] + j12 * V[b * 4 + 2];
+      }
+      const float SM0[3] = {S[0] * M0[0] + S[1] * M0[1] + S[2] * M0[2], S[1] * M0[0] + S[3] * M0[1] + S[4] * M0[2],
+                            S[2] * M0[0] + S[4] * M0[1] + S[5] * M0[2]};
+      const float SM1[3] = {S[0] * M1[0] + S[1] * M1[1] + S[2] * M1[2], S[1] * M1[0] + S[3] * M1[1] + S[4] * M1[2],
+                            S[2] * M1[0] + S[4] * M1[1] + S[5] * M1[2]};
+      const float ca = M0[0] * SM0[0] + M0[1] * SM0[1] + M0[2] * SM0[2] + 0.3f;
+      const float cb = M0[0] * SM1[0] + M0[1] * SM1[1] + M0[2] * SM1[2];
+      const float cc = M1[0] * SM1[0] + M1[1] * SM1[1] + M1[2] * SM1[2] + 0.3f;
+      const float det = ca * cc - cb * cb;
+      const float det_inv = 1.0f / det;
+      const float3 conic = f3(cc * det_inv, -cb * det_inv, ca * det_inv);
+      // Reported radius (FB preprocess.cu:480-485; the 3.33 bound is a double there).
+      const float mid = 0.5f * (ca + cc);
+      const double extent = fmin(3.33, (double)sqrtf(2.0f * logf(o * 255.0f)));
+      const float lambda = mid + sqrtf(fmaxf(0.01f, mid * mid - det));
+      radius = (float)ceil(extent * (double)sqrtf(lambda));
+      // Tile rectangle of the 1/256 level set (FB preprocess.cu:488-497).
+      const float log2o = lg2_approx(o);
+      const float power = (kLn2 * 8.0f + kLn2 * log2o) * a.mult;
+      const int wpx = (int)(1.414214f * sqrt_approx(ca * power) + 1.0f);
+      const int hpx = (int)(1.414214f * sqrt_approx(cc * power) + 1.0f);
+      // ndc -> pixel in double, as FB's ndc2Pix promotes it (preprocess.cu:42-44).
+      xy.x = (float)((((double)ndcx + 1.0) * a.W - 1.0) * 0.5);
+      xy.y = (float)((((double)ndcy + 1.0) * a.H - 1.0) * 0.5);
+      rmin.x = min(a.gx, max(0, (int)((xy.x - wpx) / (float)a.bx)));
+      rmin.y = min(a.gy, max(0, (int)((xy.y - hpx) / (float)a.by)));
+      rmax.x = min(a.gx, max(0, (int)((xy.x + wpx) / (float)a.bx) + 1));
+      rmax.y = min(a.gy, max(0, (int)((xy.y + hpx) / (float)a.by) + 1));
+      tw = rmax.x - rmin.x;
+      area = tw * (rmax.y - rmin.y);
+      if (area <= 0) break;
+      valid = true;
+      cp = make_float4(conic.x, conic.y, conic.z, power);
+      depth = t.z;
+
+      float3 rgb;
+      if (a.colors) {
+        rgb = ld3(a.colors + 3 * (size_t)i);
+      } else {
+        const float3 cpos = ld3(a.campos);
+        float dxv = p.x - cpos.x, dyv = p.y - cpos.y, dzv = p.z - cpos.z;
+        const float inv = 1.0f / sqrtf(dxv * dxv + dyv * dyv + dzv * dzv);
+        rgb = sh_colour(a.D, dxv * inv, dyv * inv, dzv * inv, a.dc + 3 * (size_t)i,
+                        a.shs ? a.shs + (size_t)i * a.M * 3 : nullptr, rec + F_CLAMP);
+      }
+      rec[F_XY] = xy.x; rec[F_XY + 1] = xy.y;
+      rec[F_RGBD] = rgb.x; rec[F_RGBD + 1] = rgb.y; rec[F_RGBD + 2] = rgb.z; rec[F_RGBD + 3] = t.z;
+      rec[F_CONO] = (-0.5f * kLog2e) * conic.x;
+      rec[F_CONO + 1] = -kLog2e * conic.y;
+      rec[F_CONO + 2] = (-0.5f * kLog2e) * conic.z;
+      rec[F_CONO + 3] = log2o;
+      rec[F_RMIN] = __int_as_float(rmin.x); rec[F_RMIN + 1] = __int_as_float(rmin.y);
+      rec[F_RMAX] = __int_as_float(rmax.x); rec[F_RMAX + 1] = __int_as_float(rmax.y);
+      rec[F_CONIC] = conic.x; rec[F_CONIC + 1] = conic.y; rec[F_CONIC + 2] = conic.z;
+      rec[F_PVIEW] = t.x; rec[F_PVIEW + 1] = t.y; rec[F_PVIEW + 2] = t.z;
+      rec[F_POWER] = power;
+#pragma unroll
+      for (int k = 0; k < 6; ++k) rec[F_COV3D + k] = S[k];
+    } while (false);
+    a.radii[i] = valid ? (int)radius : 0;
+    if (valid) {
+      float4* dst = reinterpret_cast<float4*>(a.splat + (size_t)i * 32);
+#pragma unroll
+      for (int k = 0; k < 8; ++k) dst[k] = make_float4(rec[4 * k], rec[4 * k + 1], rec[4 * k + 2], rec[4 * k + 3]);
+    }
+  }
+
+  // Large footprints: queue 128-tile sub-tasks (FB preprocess.cu:723-745).
+  const bool small = valid && area < kLargeTiles;
+  if (valid && !small) {
+    const int n = (area + kLargeTiles - 1) / kLargeTiles;
+    const int base = atomicAdd(&a.counters[0], n);
+    for (int j = 0; j < n; ++j) {
+      const long long t = (long long)base + j;
+      if (t < a.task_cap) {
+        a.tasks[2 * t] = (uint32_t)i;
+        a.tasks[2 * t + 1] = (uint32_t)(j * kLargeTiles);
+      } else {
+        raise_error(kErrCapacity);
+      }
+    }
+  }
+
+  // Small footprints: flatten the warp's (Gaussian, tile) candidates and test
+  // 32 at a time (the lane packing of FB preprocess.cu:536-696).
+  const int cnt = small ? area : 0;
+  int incl = cnt;
+#pragma unroll
+  for (int o = 1; o < kWarp; o <<= 1) {
+    const int v = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += v;
+  }
+  const int total = __shfl_sync(0xffffffffu, incl, 31);
+  s_xy[warp][lane] = xy;
+  s_cp[warp][lane] = cp;
+  s_geo[warp][lane] = make_int4(rmin.x, rmin.y, tw, incl - cnt);
+  s_depth[warp][lane] = __float_as_uint(depth);
+  __syncwarp();
+
+  WarpStage st{s_key[warp], s_val[warp], 0};
+  const int warp_first = blockIdx.x * kPreThreads + warp * kWarp;
+  for (int base = 0; base < total; base += kWarp) {
+    const int c = base + lane;
+    bool hit = false;
+    unsigned long long key = 0;
+    uint32_t gid = 0;
+    if (c < total) {
+      // Owner = last lane whose candidate start is <= c (steps sum to 31, so
+      // lo + step never leaves the warp).
+      int lo = 0;
+#pragma unroll
+      for (int step = 16; step > 0; step >>= 1)
+        if (s_geo[warp][lo + step].w <= c) lo += step;
+      const int4 g = s_geo[warp][lo];
+      const int local = c - g.w;
+      const int ty = local / g.z, tx = local - ty * g.z;
+      const int x = g.x + tx, y = g.y + ty;
+      hit = tile_hit(x * a.bx, y * a.by, a.bx, a.by, s_xy[warp][lo], s_cp[warp][lo]);
+      key = ((unsigned long long)(uint32_t)(y * a.gx + x) << 32) | s_depth[warp][lo];
+      gid = (uint32_t)(warp_first + lo);
+    }
+    stage_push(st, a, lane, hit, key, gid);
+  }
+  stage_flush(st, a, lane);
+}
+
+// Drains the large-Gaussian sub-task queue: one warp per 128-tile sub-task,
+// persistent grid (FB preprocess.cu:749-895 uses a work-stealing cursor and a
+// host read of the task count; here the count stays on the device).
+__global__ void __launch_bounds__(kPreThreads) k_preprocess_large(const PreArgs a) {
+  __shared__ unsigned long long s_key[kPreWarps][kStage];
+  __shared__ uint32_t s_val[kPreWarps][kStage];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const long long ntask = min((long long)a.counters[0], a.task_cap);
+  const int gw = blockIdx.x * kPreWarps + warp, nw = gridDim.x * kPreWarps;
+  WarpStage st{s_key[warp], s_val[warp], 0};
+  for (long long t = gw; t < ntask; t += nw) {
+    const uint32_t id = a.tasks[2 * t], off = a.tasks[2 * t + 1];
+    const float* r = a.splat + (size_t)id * 32;
+    const float2 xy = make_float2(r[F_XY], r[F_XY + 1]);
+    const uint32_t depth = __float_as_uint(r[F_RGBD + 3]);
+    const int rx0 = __float_as_int(r[F_RMIN]), ry0 = __float_as_int(r[F_RMIN + 1]);
+    const int rx1 = __float_as_int(r[F_RMAX]), ry1 = __float_as_int(r[F_RMAX + 1]);
+    const float4 cp = make_float4(r[F_CONIC], r[F_CONIC + 1], r[F_CONIC + 2], r[F_POWER]);
+    const int w = rx1 - rx0, area = w * (ry1 - ry0);
+    const int end = min((int)off + kLargeTiles, area);
+#pragma unroll 1
+    for (int k = 0; k < kLargeTiles / kWarp; ++k) {
+      const int c = (int)off + k * kWarp + lane;
+      bool hit = false;
+      unsigned long long key = 0;
+      if (c < end) {
+        const int ty = c / w, tx = c - ty * w;
+        const int x = rx0 + tx, y = ry0 + ty;
+        hit = tile_hit(x * a.bx, y * a.by, a.bx, a.by, xy, cp);
+        key = ((unsigned long long)(uint32_t)(y * a.gx + x) << 32) | depth;
+      }
+      stage_push(st, a, lane, hit, key, id);
+    }
+  }
+  stage_flush(st, a, lane);
+}
+
+}  // namespace
+}  // namespace fgs
+
+FGS_DEFINE_ERROR_ACCESSOR(preprocess)
+
+extern "C" fgs_status fgs_preprocess(
+    int P, int D, int M, const float* means3D, const float* colors_precomp, const float* dc, const float* shs,
+    const float* opacities, const float* scales, const float* rotations, float scale_modifier, int width,
+    int height, int block_x, int block_y, const float* campos, const float* viewmatrix, const float* projmatrix,
+    float tan_fovx, float tan_fovy, float zfar, float znear, float mult, const uint8_t* culling,
+    float* splat_buffer, int64_t splat_rows, uint64_t* keys_unsorted, uint32_t* values_unsorted,
+    int64_t pair_capacity, uint32_t* task_scratch, int64_t task_scratch_words, int32_t* curr_offset,
+    int32_t* counters, int32_t* radii, void* stream) {
+  (void)zfar;
+  (void)znear;
+  using namespace fgs;
+  if (P < 0 || D < 0 || D > 3 || width <= 0 || height <= 0 || block_x <= 0 || block_y <= 0) return FGS_ERR_BAD_ARG;
+  if (P == 0) return FGS_OK;
+  if (!means3D || !opacities || !scales || !rotations || !viewmatrix || !projmatrix || !splat_buffer ||
+      !keys_unsorted || !values_unsorted || !curr_offset || !counters || !radii || !task_scratch)
+    return FGS_ERR_BAD_ARG;
+  if (!colors_precomp) {
+    if (!dc || !campos) return FGS_ERR_BAD_ARG;
+    if (D > 0 && (!shs || M < (D + 1) * (D + 1) - 1)) return FGS_ERR_BAD_ARG;
+  }
+  if (((uintptr_t)rotations & 15) || ((uintptr_t)splat_buffer & 15) || ((uintptr_t)keys_unsorted & 7))
+    return FGS_ERR_BAD_ARG;
+  if ((int64_t)P > splat_rows) return FGS_ERR_CAPACITY;
+  cudaStream_t s = (cudaStream_t)stream;
+  PreArgs a;
+  a.P = P; a.D = D; a.M = M;
+  a.means = means3D; a.colors = colors_precomp; a.dc = dc; a.shs = shs; a.opac = opacities;
+  a.scales = scales; a.rots = rotations; a.smod = scale_modifier;
+  a.W = width; a.H = height; a.bx = block_x; a.by = block_y;
+  a.gx = (width + block_x - 1) / block_x; a.gy = (height + block_y - 1) / block_y;
+  a.campos = campos; a.view = viewmatrix; a.proj = projmatrix;
+  a.tanx = tan_fovx; a.tany = tan_fovy;
+  a.fx = width / (2.0f * tan_fovx); a.fy = height / (2.0f * tan_fovy);
+  a.mult = mult; a.culling = culling; a.splat = splat_buffer;
+  a.keys = reinterpret_cast<unsigned long long*>(keys_unsorted); a.vals = values_unsorted;
+  a.cap = pair_capacity; a.tasks = task_scratch; a.task_cap = task_scratch_words / 2;
+  a.curr = reinterpret_cast<unsigned int*>(curr_offset); a.counters = counters; a.radii = radii;
+  FGS_TRY(cudaMemsetAsync(counters, 0, FGS_COUNTER_WORDS * sizeof(int32_t), s));
+  k_preprocess<<<(P + kPreThreads - 1) / kPreThreads, kPreThreads, 0, s>>>(a);
+  FGS_LAUNCH_CHECK();
+  k_preprocess_large<<<num_sms() * 4, kPreThreads, 0, s>>>(a);
+  FGS_LAUNCH_CHECK();
+  return FGS_OK;
+}

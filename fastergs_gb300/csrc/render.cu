@@ -1,0 +1,280 @@
+// Forward composite, sm_103a: tile ranges, bucket bookkeeping, bucket-parallel
+// alpha compositing and the associative (colour, transmittance) merge.
+//
+// Restates FB csrc/cuda_rasterizer/render.cu: a tile's depth-sorted list is
+// cut into fixed-size buckets, every bucket is composited independently from
+// T = 1, C = 0, and a per-pixel merge folds the buckets front to back with
+// C += T * C_b, T *= T_b, stopping after the bucket that drops T below 1e-4.
+// GB300 changes:
+//   * bucket bookkeeping never leaves the device (FB copies the bucket total
+//     to the host mid-frame); the composite kernel is persistent and reads the
+//     total from device memory;
+//   * a bucket's records are staged once into shared memory (coalesced
+//     per-lane loads, structure-of-arrays) and broadcast from there;
+//   * each lane owns a column strip of 8 pixels, so a Gaussian's row terms are
+//     shared and every sample store is a contiguous 512-byte warp store;
+//   * the sample state is 16 bytes per pixel and bucket, updated in place by
+//     the merge (FB keeps 40).
+#include <algorithm>
+
+#include "render_common.cuh"
+
+namespace fgs {
+namespace {
+
+constexpr int kFwdWarps = 4;
+
+__global__ void __launch_bounds__(256) k_tile_ranges(const unsigned long long* __restrict__ keys, long long n,
+                                                     uint32_t* __restrict__ ranges) {
+  const long long i = blockIdx.x * 256ll + threadIdx.x;
+  if (i >= n) return;
+  const uint32_t t = (uint32_t)(keys[i] >> 32);
+  if (i == 0) {
+    ranges[2 * t] = 0;
+  } else {
+    const uint32_t pt = (uint32_t)(keys[i - 1] >> 32);
+    if (pt != t) {
+      ranges[2 * pt + 1] = (uint32_t)i;
+      ranges[2 * t] = (uint32_t)i;
+    }
+  }
+  if (i == n - 1) ranges[2 * t + 1] = (uint32_t)n;
+}
+
+// One CTA: bucket counts per tile, inclusive scan, bucket -> tile map.
+// FB does this with perTileBucketCount + cub::DeviceScan + a host copy of the
+// total + perBucketRange (render.cu:13-49, 418-434).
+__global__ void __launch_bounds__(1024) k_bucket_setup(int T, const uint32_t* __restrict__ ranges, int bs,
+                                                       long long max_buckets, uint32_t* __restrict__ bucket_off,
+                                                       uint32_t* __restrict__ bucket_tile, uint32_t* bucket_sum) {
+  __shared__ uint32_t s_warp[32];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int chunk = (T + 1023) / 1024;
+  const int t0 = min(T, tid * chunk), t1 = min(T, t0 + chunk);
+  uint32_t local = 0;
+  for (int t = t0; t < t1; ++t) local += (ranges[2 * t + 1] - ranges[2 * t] + bs - 1) / bs;
+  uint32_t incl = local;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t u = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += u;
+  }
+  if (lane == 31) s_warp[warp] = incl;
+  __syncthreads();
+  uint32_t wbase = 0, total = 0;
+  for (int w = 0; w < 32; ++w) {
+    const uint32_t x = s_warp[w];
+    if (w < warp) wbase += x;
+    total += x;
+  }
+  uint32_t run = wbase + incl - local;
+  for (int t = t0; t < t1; ++t) {
+    const uint32_t nb = (ranges[2 * t + 1] - ranges[2 * t] + bs - 1) / bs;
+    for (uint32_t j = 0; j < nb; ++j)
+      if ((long long)(run + j) < max_buckets) bucket_tile[run + j] = (uint32_t)t;
+    run += nb;
+    bucket_off[t] = run;
+  }
+  if (tid == 0) {
+    bucket_sum[0] = (uint32_t)min((long long)total, max_buckets);
+    bucket_sum[1] = total;
+    if ((long long)total > max_buckets) raise_error(kErrCapacity);
+  }
+}
+
+struct FwdArgs {
+  const float* splat;
+  const uint32_t* vals;
+  const uint32_t* ranges;
+  const uint32_t* bucket_tile;
+  const uint32_t* bucket_off;
+  const uint32_t* bucket_sum;
+  float4* samples;
+  int W, H, bx, by, gx, bs;
+};
+
+__global__ void __launch_bounds__(kFwdWarps * kWarp) k_render_fwd(const FwdArgs a) {
+  __shared__ BucketStage s_stage[kFwdWarps];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  BucketStage& st = s_stage[warp];
+  const int B = (int)a.bucket_sum[0];
+  const int lx = lane % a.bx, ly0 = lane / a.bx;
+  const float ystep = (float)(kWarp / a.bx);
+  for (int b = blockIdx.x * kFwdWarps + warp; b < B; b += gridDim.x * kFwdWarps) {
+    const BucketInfo bi = bucket_info(b, a.bucket_tile, a.bucket_off, a.ranges, a.bs);
+    stage_bucket(st, a.splat, a.vals + bi.start, bi.n, lane);
+    const float px = (float)((bi.tile % a.gx) * a.bx + lx);
+    const float py0 = (float)((bi.tile / a.gx) * a.by + ly0);
+    float T[kPxPerThread], Cr[kPxPerThread], Cg[kPxPerThread], Cb[kPxPerThread];
+#pragma unroll
+    for (int k = 0; k < kPxPerThread; ++k) { T[k] = 1.f; Cr[k] = 0.f; Cg[k] = 0.f; Cb[k] = 0.f; }
+    for (int g = 0; g < bi.n; ++g) {
+      const float2 xy = st.xy[g];
+      const float4 co = st.co[g];
+      const float4 c = st.rgb[g];
+      const float dx = xy.x - px;
+      const float A = fmaf(co.x * dx, dx, co.w);
+      const float Bx = co.y * dx;
+      float dy = xy.y - py0;
+#pragma unroll
+      for (int k = 0; k < kPxPerThread; ++k) {
+        // alpha = o * exp(-q/2) evaluated as 2^(con_o . [1, dx^2, dxdy, dy^2])
+        const float e = fmaf(dy, fmaf(co.z, dy, Bx), A);
+        float al = fminf(kAlphaMax, ex2_approx(e));
+        al = al < kAlphaCut ? 0.f : al;
+        const float w = al * T[k];
+        Cr[k] = fmaf(c.x, w, Cr[k]);
+        Cg[k] = fmaf(c.y, w, Cg[k]);
+        Cb[k] = fmaf(c.z, w, Cb[k]);
+        T[k] -= w;
+        dy -= ystep;
+      }
+    }
+    __syncwarp();
+    float4* out = a.samples + (size_t)b * kTilePixels + lane;
+#pragma unroll
+    for (int k = 0; k < kPxPerThread; ++k) out[k * kWarp] = make_float4(Cr[k], Cg[k], Cb[k], T[k]);
+  }
+}
+
+struct MergeArgs {
+  const uint32_t* ranges;
+  const uint32_t* bucket_off;
+  float4* samples;
+  const float* bg;
+  float* out_color;
+  float* pix_color;
+  int* last_contrib;
+  float* Ts_final;
+  uint32_t* max_contrib;
+  int W, H, bx, by, gx, bs;
+};
+
+// Per pixel: fold the tile's buckets front to back, storing the running
+// prefix in place (FB mergeResults, render.cu:285-391).
+__global__ void __launch_bounds__(kTilePixels) k_merge(const MergeArgs a) {
+  __shared__ uint32_t s_max[kTilePixels / kWarp];
+  const int tile = blockIdx.x, p = threadIdx.x;
+  const int px = (tile % a.gx) * a.bx + p % a.bx, py = (tile / a.gx) * a.by + p / a.bx;
+  const bool in = px < a.W && py < a.H;
+  const int first = tile ? (int)a.bucket_off[tile - 1] : 0, last = (int)a.bucket_off[tile];
+  const int rs = (int)a.ranges[2 * tile], re = (int)a.ranges[2 * tile + 1];
+  float T = 1.f, Cr = 0.f, Cg = 0.f, Cb = 0.f;
+  uint32_t contrib = 0;
+  if (in) {
+    float4* s = a.samples + (size_t)first * kTilePixels + p;
+    float4 cur = first < last ? s[0] : make_float4(0.f, 0.f, 0.f, 1.f);
+    for (int b = first; b < last; ++b) {
+      const float4 nxt = (b + 1 < last) ? s[kTilePixels] : cur;
+      Cr = fmaf(T, cur.x, Cr);
+      Cg = fmaf(T, cur.y, Cg);
+      Cb = fmaf(T, cur.z, Cb);
+      T *= cur.w;
+      *s = make_float4(Cr, Cg, Cb, T);
+      contrib += (uint32_t)min(a.bs, re - (rs + (b - first) * a.bs));
+      if (T < kTMin) break;
+      cur = nxt;
+      s += kTilePixels;
+    }
+    const int pix = py * a.W + px, HW = a.W * a.H;
+    a.last_contrib[pix] = (int)contrib;
+    a.Ts_final[pix] = T;
+    a.out_color[pix] = Cr + T * a.bg[0];
+    a.out_color[HW + pix] = Cg + T * a.bg[1];
+    a.out_color[2 * HW + pix] = Cb + T * a.bg[2];
+    a.pix_color[pix] = Cr;
+    a.pix_color[HW + pix] = Cg;
+    a.pix_color[2 * HW + pix] = Cb;
+  }
+  const uint32_t m = __reduce_max_sync(0xffffffffu, contrib);
+  if ((p & 31) == 0) s_max[p >> 5] = m;
+  __syncthreads();
+  if (p == 0) {
+    uint32_t mm = 0;
+    for (int w = 0; w < kTilePixels / kWarp; ++w) mm = max(mm, s_max[w]);
+    a.max_contrib[tile] = mm;
+  }
+}
+
+bool tile_shape_ok(int bx, int by) { return bx * by == kTilePixels && (bx == 8 || bx == 16 || bx == 32); }
+
+}  // namespace
+}  // namespace fgs
+
+FGS_DEFINE_ERROR_ACCESSOR(render)
+
+using namespace fgs;
+
+extern "C" fgs_status fgs_tile_ranges(int64_t num_rendered, int num_tiles, const uint64_t* keys_sorted,
+                                      uint32_t* ranges, void* stream) {
+  if (num_rendered < 0 || num_tiles <= 0 || !ranges || (num_rendered > 0 && !keys_sorted)) return FGS_ERR_BAD_ARG;
+  cudaStream_t s = (cudaStream_t)stream;
+  FGS_TRY(cudaMemsetAsync(ranges, 0, sizeof(uint32_t) * 2 * (size_t)num_tiles, s));
+  if (num_rendered > 0) {
+    k_tile_ranges<<<(unsigned)((num_rendered + 255) / 256), 256, 0, s>>>(
+        reinterpret_cast<const unsigned long long*>(keys_sorted), num_rendered, ranges);
+    FGS_LAUNCH_CHECK();
+  }
+  return FGS_OK;
+}
+
+extern "C" int64_t fgs_max_buckets(int64_t num_rendered, int width, int height, int block_x, int block_y,
+                                   int bucket_size) {
+  if (width <= 0 || height <= 0 || block_x <= 0 || block_y <= 0 || bucket_size <= 0 || num_rendered < 0) return -1;
+  const int64_t T = (int64_t)((width + block_x - 1) / block_x) * ((height + block_y - 1) / block_y);
+  // Every tile wastes at most one partially filled bucket.
+  return (num_rendered + bucket_size - 1) / bucket_size + std::min<int64_t>(T, num_rendered);
+}
+
+extern "C" fgs_status fgs_state_bytes(int width, int height, int block_x, int block_y, int64_t max_buckets,
+                                      size_t* image_bytes, size_t* sample_bytes) {
+  if (width <= 0 || height <= 0 || block_x <= 0 || block_y <= 0 || max_buckets < 0) return FGS_ERR_BAD_ARG;
+  const int T = ((width + block_x - 1) / block_x) * ((height + block_y - 1) / block_y);
+  if (image_bytes) *image_bytes = carve_image(nullptr, width, height, T).bytes;
+  if (sample_bytes) *sample_bytes = carve_sample(nullptr, std::max<int64_t>(max_buckets, 1)).bytes;
+  return FGS_OK;
+}
+
+extern "C" fgs_status fgs_render_fwd(int P, int64_t num_rendered, int width, int height, int block_x, int block_y,
+                                     int bucket_size, const float* splat_buffer, const uint64_t* keys_sorted,
+                                     const uint32_t* values_sorted, uint32_t* ranges, const float* bg,
+                                     float* out_color, int32_t* last_contributor, float* Ts_final,
+                                     void* image_state, size_t image_bytes, void* sample_state,
+                                     size_t sample_bytes, int64_t max_buckets, uint32_t* bucket_sum_host,
+                                     void* stream) {
+  (void)P;
+  if (width <= 0 || height <= 0 || !tile_shape_ok(block_x, block_y) || bucket_size < 1 ||
+      bucket_size > kMaxBucket || num_rendered < 0 || max_buckets < 0)
+    return FGS_ERR_BAD_ARG;
+  if (!splat_buffer || !ranges || !bg || !out_color || !last_contributor || !Ts_final || !image_state ||
+      !sample_state || (num_rendered > 0 && (!keys_sorted || !values_sorted)))
+    return FGS_ERR_BAD_ARG;
+  if (((uintptr_t)splat_buffer & 15) || ((uintptr_t)image_state & 255) || ((uintptr_t)sample_state & 255))
+    return FGS_ERR_BAD_ARG;
+  const int gx = (width + block_x - 1) / block_x, gy = (height + block_y - 1) / block_y, T = gx * gy;
+  const ImageState im = carve_image(image_state, width, height, T);
+  const SampleState sm = carve_sample(sample_state, std::max<int64_t>(max_buckets, 1));
+  if (image_bytes < im.bytes || sample_bytes < sm.bytes) return FGS_ERR_CAPACITY;
+  cudaStream_t s = (cudaStream_t)stream;
+  fgs_status st = fgs_tile_ranges(num_rendered, T, keys_sorted, ranges, stream);
+  if (st != FGS_OK) return st;
+  k_bucket_setup<<<1, 1024, 0, s>>>(T, ranges, bucket_size, max_buckets, im.bucket_off, sm.bucket_tile,
+                                    im.bucket_sum);
+  FGS_LAUNCH_CHECK();
+  FwdArgs fa{splat_buffer, values_sorted, ranges, sm.bucket_tile, im.bucket_off, im.bucket_sum, sm.samples,
+             width, height, block_x, block_y, gx, bucket_size};
+  k_render_fwd<<<num_sms() * 8, kFwdWarps * kWarp, 0, s>>>(fa);
+  FGS_LAUNCH_CHECK();
+  MergeArgs ma{ranges, im.bucket_off, sm.samples, bg, out_color, im.pix_color, last_contributor, Ts_final,
+               im.max_contrib, width, height, block_x, block_y, gx, bucket_size};
+  k_merge<<<T, kTilePixels, 0, s>>>(ma);
+  FGS_LAUNCH_CHECK();
+  if (bucket_sum_host) {
+    uint32_t hs[2] = {0, 0};
+    FGS_TRY(cudaMemcpyAsync(hs, im.bucket_sum, sizeof(hs), cudaMemcpyDeviceToHost, s));
+    FGS_TRY(cudaStreamSynchronize(s));
+    *bucket_sum_host = hs[1];
+    if ((int64_t)hs[1] > max_buckets) return FGS_ERR_CAPACITY;
+  }
+  return FGS_OK;
+}

@@ -1,0 +1,98 @@
+// State layout shared by the forward and backward composite kernels.
+#pragma once
+#include "fgs_common.cuh"
+
+namespace fgs {
+
+constexpr int kTilePixels = 256;   // block_x * block_y must equal this
+constexpr int kPxPerThread = 8;    // pixels per lane: one warp covers a tile
+constexpr int kMaxBucket = 128;    // largest supported bucket size
+
+// Per-image state (FB ImageState, rasterizer_imp.h:76-88), carved from one
+// caller buffer:  pixel colour planes (3, H*W) without background,
+// per-tile max contributor count, per-tile inclusive bucket offsets, and a
+// 16-byte header holding the bucket total.
+struct ImageState {
+  float* pix_color;         // 3 * HW
+  uint32_t* max_contrib;    // T
+  uint32_t* bucket_off;     // T (inclusive scan of bucket counts)
+  uint32_t* bucket_sum;     // 1
+  size_t bytes;
+};
+
+// Per-bucket state (FB SampleState, rasterizer_imp.h:91-102): the owning tile
+// of each bucket and, per (bucket, pixel), a float4 (C.rgb, T).  The forward
+// composite writes the bucket-local values; the merge overwrites them in place
+// with the running prefix after the bucket, which is all the backward needs
+// (16 bytes per pixel and bucket instead of FB's 40).
+struct SampleState {
+  uint32_t* bucket_tile;    // max_buckets
+  float4* samples;          // max_buckets * 256
+  size_t bytes;
+};
+
+inline size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
+
+inline ImageState carve_image(void* base, int W, int H, int T) {
+  char* p = static_cast<char*>(base);
+  ImageState s;
+  size_t off = 0;
+  s.bucket_sum = reinterpret_cast<uint32_t*>(p + off);  off = align_up(off + 16, 256);
+  s.pix_color = reinterpret_cast<float*>(p + off);      off = align_up(off + sizeof(float) * 3 * (size_t)W * H, 256);
+  s.max_contrib = reinterpret_cast<uint32_t*>(p + off); off = align_up(off + sizeof(uint32_t) * (size_t)T, 256);
+  s.bucket_off = reinterpret_cast<uint32_t*>(p + off);  off = align_up(off + sizeof(uint32_t) * (size_t)T, 256);
+  s.bytes = off;
+  return s;
+}
+
+inline SampleState carve_sample(void* base, int64_t max_buckets) {
+  char* p = static_cast<char*>(base);
+  SampleState s;
+  size_t off = 0;
+  s.bucket_tile = reinterpret_cast<uint32_t*>(p + off); off = align_up(off + sizeof(uint32_t) * (size_t)max_buckets, 256);
+  s.samples = reinterpret_cast<float4*>(p + off);       off = align_up(off + sizeof(float4) * kTilePixels * (size_t)max_buckets, 256);
+  s.bytes = off;
+  return s;
+}
+
+// Records of one bucket staged in shared memory, structure-of-arrays.
+struct BucketStage {
+  float2 xy[kMaxBucket];
+  float4 co[kMaxBucket];    // con_o: (-0.5 log2e a, -log2e b, -0.5 log2e c, log2 o)
+  float4 rgb[kMaxBucket];   // r, g, b, (backward: Gaussian id bits)
+};
+
+// Load the render fields (floats 0..9) of n records whose ids start at ids.
+__device__ __forceinline__ void stage_bucket(BucketStage& st, const float* __restrict__ splat,
+                                             const uint32_t* __restrict__ ids, int n, int lane) {
+  for (int j = lane; j < n; j += kWarp) {
+    const uint32_t id = ids[j];
+    const float4* r = reinterpret_cast<const float4*>(splat + (size_t)id * 32);
+    const float4 a = __ldg(r);        // x, y, r, g
+    const float4 b = __ldg(r + 1);    // b, depth, co.x, co.y
+    const float2 c = __ldg(reinterpret_cast<const float2*>(splat + (size_t)id * 32 + 8));  // co.z, co.w
+    st.xy[j] = make_float2(a.x, a.y);
+    st.co[j] = make_float4(b.z, b.w, c.x, c.y);
+    st.rgb[j] = make_float4(a.z, a.w, b.x, __uint_as_float(id));
+  }
+  __syncwarp();
+}
+
+// Bucket b -> (tile, first pair, pair count, index of the bucket in its tile).
+struct BucketInfo {
+  int tile, start, n, local;
+};
+__device__ __forceinline__ BucketInfo bucket_info(int b, const uint32_t* __restrict__ bucket_tile,
+                                                  const uint32_t* __restrict__ bucket_off,
+                                                  const uint32_t* __restrict__ ranges, int bs) {
+  BucketInfo bi;
+  bi.tile = (int)bucket_tile[b];
+  const int first = bi.tile ? (int)bucket_off[bi.tile - 1] : 0;
+  bi.local = b - first;
+  const int rs = (int)ranges[2 * bi.tile], re = (int)ranges[2 * bi.tile + 1];
+  bi.start = rs + bi.local * bs;
+  bi.n = min(bs, re - bi.start);
+  return bi;
+}
+
+}  // namespace fgs

@@ -1,0 +1,276 @@
+// Stable LSD radix sort of (u64 key, u32 value) pairs, sm_103a.
+//
+// Replaces the cub::DeviceRadixSort::SortPairs call of FB
+// (csrc/cuda_rasterizer/sort.cu:28-44) with a single-pass-per-digit
+// ("onesweep") sort written for this GPU:
+//   * one upfront kernel builds the 8-bit digit histograms of every pass in a
+//     single read of the keys;
+//   * each pass is one kernel: a CTA ranks a 4096-key tile in shared memory
+//     (warp match + per-warp digit counters, so ranks are stable), publishes its
+//     per-digit counts, obtains the exclusive prefix of all earlier tiles by a
+//     decoupled look-back, and scatters through shared memory so that global
+//     writes form contiguous runs per digit;
+//   * only the key bits that can differ are sorted: 32 depth bits plus
+//     ceil(log2(tiles)) tile bits, i.e. 5-6 passes for 256..32768 tiles.
+// Every look-back wait is bounded (kSpinLimit polls); on expiry the kernel
+// records kErrTimeout in the error word and continues, so it never hangs.
+#include <algorithm>
+
+#include "fgs_common.cuh"
+
+namespace fgs {
+namespace {
+
+constexpr int kSortThreads = 256;
+constexpr int kSortWarps = kSortThreads / kWarp;
+constexpr int kSortItems = 16;
+constexpr int kSortTile = kSortThreads * kSortItems;   // 4096 keys
+constexpr int kRadix = 256;
+constexpr int kMaxPasses = 8;
+constexpr uint32_t kFlagAgg = 1u << 30;
+constexpr uint32_t kFlagInc = 2u << 30;
+constexpr uint32_t kValueMask = (1u << 30) - 1;
+constexpr int kSortDynSmem = (int)((sizeof(unsigned long long) + sizeof(uint32_t)) * kSortTile);
+
+struct SortLayout {
+  size_t hist, counters, lookback, alt_keys, alt_vals, total;
+  int64_t tiles;
+};
+
+SortLayout layout_for(int64_t n) {
+  auto up = [](size_t v) { return (v + 255) & ~(size_t)255; };
+  SortLayout L;
+  L.tiles = (n + kSortTile - 1) / kSortTile;
+  size_t off = 0;
+  L.hist = off;      off = up(off + sizeof(uint32_t) * kMaxPasses * kRadix);
+  L.counters = off;  off = up(off + sizeof(uint32_t) * kMaxPasses);
+  L.lookback = off;  off = up(off + sizeof(uint32_t) * kMaxPasses * (size_t)L.tiles * kRadix);
+  L.alt_keys = off;  off = up(off + sizeof(uint64_t) * (size_t)n);
+  L.alt_vals = off;  off = up(off + sizeof(uint32_t) * (size_t)n);
+  L.total = off;
+  return L;
+}
+
+// All pass histograms in one read of the keys.
+__global__ void __launch_bounds__(kSortThreads) k_histogram(const unsigned long long* keys, long long n,
+                                                            int passes, uint32_t* hist) {
+  __shared__ uint32_t s_h[kMaxPasses][kRadix];
+  for (int j = threadIdx.x; j < kMaxPasses * kRadix; j += kSortThreads) (&s_h[0][0])[j] = 0;
+  __syncthreads();
+  for (long long k = blockIdx.x * (long long)kSortThreads + threadIdx.x; k < n;
+       k += (long long)gridDim.x * kSortThreads) {
+    const unsigned long long key = keys[k];
+    for (int p = 0; p < passes; ++p) atomicAdd(&s_h[p][(key >> (8 * p)) & 0xff], 1u);
+  }
+  __syncthreads();
+  for (int j = threadIdx.x; j < passes * kRadix; j += kSortThreads) {
+    const uint32_t v = (&s_h[0][0])[j];
+    if (v) atomicAdd(&hist[j], v);
+  }
+}
+
+// Exclusive scan of 256 values held one per thread; returns the exclusive
+// prefix, *total receives the sum.  Uses s_tmp[kSortWarps].
+__device__ __forceinline__ uint32_t block_excl_scan_256(uint32_t v, uint32_t* s_tmp, uint32_t* total) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint32_t incl = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t u = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += u;
+  }
+  if (lane == 31) s_tmp[warp] = incl;
+  __syncthreads();
+  uint32_t wbase = 0, tot = 0;
+#pragma unroll
+  for (int w = 0; w < kSortWarps; ++w) {
+    const uint32_t x = s_tmp[w];
+    if (w < warp) wbase += x;
+    tot += x;
+  }
+  __syncthreads();
+  *total = tot;
+  return wbase + incl - v;
+}
+
+__global__ void __launch_bounds__(kSortThreads) k_onesweep(
+    const unsigned long long* __restrict__ keys_in, const uint32_t* __restrict__ vals_in,
+    unsigned long long* __restrict__ keys_out, uint32_t* __restrict__ vals_out, long long n, int shift,
+    const uint32_t* __restrict__ hist, uint32_t* lookback, uint32_t* tile_counter) {
+  extern __shared__ __align__(16) unsigned char s_dyn[];  // kSortDynSmem bytes
+  unsigned long long* s_keys = reinterpret_cast<unsigned long long*>(s_dyn);
+  uint32_t* s_vals = reinterpret_cast<uint32_t*>(s_dyn + sizeof(unsigned long long) * kSortTile);
+  __shared__ uint32_t s_whist[kSortWarps][kRadix];
+  __shared__ uint32_t s_dst[kRadix];
+  __shared__ uint32_t s_toff[kRadix];
+  __shared__ uint32_t s_tmp[kSortWarps];
+  __shared__ uint32_t s_tile;
+
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  if (tid == 0) s_tile = atomicAdd(tile_counter, 1u);
+  for (int j = tid; j < kSortWarps * kRadix; j += kSortThreads) (&s_whist[0][0])[j] = 0;
+  __syncthreads();
+  const uint32_t tile = s_tile;
+  const long long tile_base = (long long)tile * kSortTile;
+
+  // Load: warp w owns keys [tile_base + w*512, +512), 32 consecutive per step,
+  // so (warp, step, lane) is the input order and the ranks below are stable.
+  unsigned long long k[kSortItems];
+  uint32_t v[kSortItems];
+  uint32_t rank[kSortItems];
+  int n_invalid = 0;
+#pragma unroll
+  for (int r = 0; r < kSortItems; ++r) {
+    const long long idx = tile_base + warp * (kWarp * kSortItems) + r * kWarp + lane;
+    if (idx < n) {
+      k[r] = keys_in[idx];
+      v[r] = vals_in[idx];
+    } else {
+      k[r] = ~0ull;  // digit 255, ranked after every real key of the tile
+      v[r] = 0;
+      ++n_invalid;
+    }
+  }
+#pragma unroll
+  for (int r = 0; r < kSortItems; ++r) {
+    const uint32_t d = (uint32_t)(k[r] >> shift) & 0xff;
+    const uint32_t peers = __match_any_sync(0xffffffffu, d);
+    const uint32_t before = s_whist[warp][d];
+    __syncwarp();
+    if ((peers & lanemask_lt()) == 0) s_whist[warp][d] = before + __popc(peers);
+    __syncwarp();
+    rank[r] = before + __popc(peers & lanemask_lt());
+  }
+  __syncthreads();
+
+  // Per digit (one thread each): warp offsets, tile count, look-back.
+  const uint32_t d = tid;
+  uint32_t cnt = 0;
+#pragma unroll
+  for (int w = 0; w < kSortWarps; ++w) {
+    const uint32_t x = s_whist[w][d];
+    s_whist[w][d] = cnt;
+    cnt += x;
+  }
+  // Padding keys only exist in the last tile and all sit in digit 255.
+  int pad = n_invalid;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) pad += __shfl_xor_sync(0xffffffffu, pad, o);
+  if (lane == 0) s_tmp[warp] = (uint32_t)pad;
+  __syncthreads();
+  uint32_t pad_total = 0;
+#pragma unroll
+  for (int w = 0; w < kSortWarps; ++w) pad_total += s_tmp[w];
+  __syncthreads();
+  const uint32_t real = (d == 255) ? cnt - pad_total : cnt;
+
+  uint32_t* lb = lookback + (size_t)tile * kRadix;
+  uint32_t excl = 0;
+  if (tile == 0) {
+    st_volatile_u32(lb + d, kFlagInc | real);
+  } else {
+    st_volatile_u32(lb + d, kFlagAgg | real);
+    long long pred = (long long)tile - 1;
+    int polls = 0;
+    while (pred >= 0) {
+      const uint32_t w = ld_volatile_u32(lookback + (size_t)pred * kRadix + d);
+      const uint32_t flag = w & ~kValueMask;
+      if (flag == 0) {
+        if (++polls > kSpinLimit) {
+          raise_error(kErrTimeout);
+          break;
+        }
+        __nanosleep(64);
+        continue;
+      }
+      excl += w & kValueMask;
+      if (flag == kFlagInc) break;
+      --pred;
+    }
+    st_volatile_u32(lb + d, kFlagInc | (excl + real));
+  }
+
+  // Global digit base of this pass, tile-local digit offsets.
+  uint32_t gtot, ttot;
+  const uint32_t gbase = block_excl_scan_256(hist[d], s_tmp, &gtot);
+  const uint32_t toff = block_excl_scan_256(cnt, s_tmp, &ttot);
+  s_toff[d] = toff;
+  s_dst[d] = gbase + excl - toff;  // global position of shared slot i = s_dst[digit] + i
+  __syncthreads();
+
+#pragma unroll
+  for (int r = 0; r < kSortItems; ++r) {
+    const uint32_t dd = (uint32_t)(k[r] >> shift) & 0xff;
+    const uint32_t slot = s_toff[dd] + s_whist[warp][dd] + rank[r];
+    s_keys[slot] = k[r];
+    s_vals[slot] = v[r];
+  }
+  __syncthreads();
+  const int valid = (int)min((long long)kSortTile, n - tile_base);
+  for (int j = tid; j < valid; j += kSortThreads) {
+    const unsigned long long kk = s_keys[j];
+    const uint32_t pos = s_dst[(uint32_t)(kk >> shift) & 0xff] + (uint32_t)j;
+    keys_out[pos] = kk;
+    vals_out[pos] = s_vals[j];
+  }
+}
+
+}  // namespace
+}  // namespace fgs
+
+FGS_DEFINE_ERROR_ACCESSOR(sort)
+
+extern "C" size_t fgs_sort_temp_bytes(int64_t num_rendered) {
+  if (num_rendered < 1) num_rendered = 1;
+  return fgs::layout_for(num_rendered).total;
+}
+
+extern "C" fgs_status fgs_sort(int64_t num_rendered, int width, int height, int block_x, int block_y, void* temp,
+                               size_t temp_bytes, const uint64_t* keys_in, const uint32_t* values_in,
+                               uint64_t* keys_out, uint32_t* values_out, void* stream) {
+  using namespace fgs;
+  if (num_rendered < 0 || width <= 0 || height <= 0 || block_x <= 0 || block_y <= 0) return FGS_ERR_BAD_ARG;
+  if (num_rendered == 0) return FGS_OK;
+  if (num_rendered >= (int64_t)kValueMask) return FGS_ERR_CAPACITY;
+  if (!temp || !keys_in || !values_in || !keys_out || !values_out) return FGS_ERR_BAD_ARG;
+  if (((uintptr_t)temp & 255) || ((uintptr_t)keys_in & 7) || ((uintptr_t)keys_out & 7)) return FGS_ERR_BAD_ARG;
+  const SortLayout L = layout_for(num_rendered);
+  if (temp_bytes < L.total) return FGS_ERR_CAPACITY;
+  const uint32_t tiles = (uint32_t)(((width + block_x - 1) / block_x) * ((height + block_y - 1) / block_y));
+  const int bits = 32 + tile_bits(tiles);
+  const int passes = (bits + 7) / 8;
+  cudaStream_t s = (cudaStream_t)stream;
+  char* base = static_cast<char*>(temp);
+  uint32_t* hist = reinterpret_cast<uint32_t*>(base + L.hist);
+  uint32_t* counters = reinterpret_cast<uint32_t*>(base + L.counters);
+  uint32_t* lookback = reinterpret_cast<uint32_t*>(base + L.lookback);
+  auto* alt_k = reinterpret_cast<unsigned long long*>(base + L.alt_keys);
+  auto* alt_v = reinterpret_cast<uint32_t*>(base + L.alt_vals);
+  // hist, counters and the look-back words of every pass start at zero.
+  FGS_TRY(cudaMemsetAsync(base, 0, L.alt_keys, s));
+  const int hist_blocks = (int)std::min<int64_t>((num_rendered + kSortThreads * 8 - 1) / (kSortThreads * 8),
+                                                 (int64_t)num_sms() * 8);
+  k_histogram<<<hist_blocks, kSortThreads, 0, s>>>(reinterpret_cast<const unsigned long long*>(keys_in),
+                                                   num_rendered, passes, hist);
+  FGS_LAUNCH_CHECK();
+  static bool smem_set = false;  // per process; the attribute is per function, not per device
+  if (!smem_set) {
+    FGS_TRY(cudaFuncSetAttribute(k_onesweep, cudaFuncAttributeMaxDynamicSharedMemorySize, kSortDynSmem));
+    smem_set = true;
+  }
+  const unsigned long long* src_k = reinterpret_cast<const unsigned long long*>(keys_in);
+  const uint32_t* src_v = values_in;
+  for (int p = 0; p < passes; ++p) {
+    // Ping-pong so that the last pass lands in the output buffers.
+    const bool to_out = ((passes - 1 - p) % 2) == 0;
+    unsigned long long* dk = to_out ? reinterpret_cast<unsigned long long*>(keys_out) : alt_k;
+    uint32_t* dv = to_out ? values_out : alt_v;
+    k_onesweep<<<(unsigned)L.tiles, kSortThreads, kSortDynSmem, s>>>(src_k, src_v, dk, dv, num_rendered, 8 * p,
+                                                          hist + p * kRadix,
+                                                          lookback + (size_t)p * L.tiles * kRadix, counters + p);
+    FGS_LAUNCH_CHECK();
+    src_k = dk;
+    src_v = dv;
+  }
+  return FGS_OK;
+}

@@ -1,0 +1,169 @@
+/*
+ * fgs.h - C ABI of the GB300 (sm_103a) Gaussian-splatting rasterizer.
+ *
+ * Drop-in for the CUDA backend of FasterGS
+ * (gs_submodules/diff-gaussian-rasterization_faster, "FB" below).  Every entry
+ * point takes plain device pointers, sizes and a cudaStream_t passed as void*,
+ * launches its kernels on that stream, never allocates, and returns an
+ * fgs_status.  Nothing here synchronises the stream unless a parameter asks
+ * for a host-side value (documented per function).
+ *
+ * Tensor layouts are FB's: means (P,3), opacities (P,1), scales (P,3),
+ * rotations (P,4) raw quaternions (r,x,y,z), dc (P,1,3), shs (P,M,3),
+ * column-major 4x4 view / full-projection matrices, images (3,H,W),
+ * per-pixel buffers (H,W,1), 64-bit keys (tile << 32 | float bits of depth).
+ */
+#ifndef FGS_H_
+#define FGS_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  FGS_OK = 0,
+  FGS_ERR_BAD_ARG = 1,        /* null / misaligned pointer, bad size or shape */
+  FGS_ERR_CAPACITY = 2,       /* a caller-provided buffer is too small */
+  FGS_ERR_CUDA = 3,           /* a CUDA runtime call or launch failed */
+  FGS_ERR_TIMEOUT = 4,        /* a bounded device-side wait gave up */
+  FGS_ERR_UNSUPPORTED = 5     /* valid call that this build does not implement */
+} fgs_status;
+
+/* Number of int32 words of the device counter block used by fgs_preprocess. */
+#define FGS_COUNTER_WORDS 16
+/* Floats per Gaussian of the interleaved gradient record written by
+ * fgs_render_bwd: [dmean2D.xyzw | dconic.xyzw | dcolor.rgb, dopacity]. */
+#define FGS_GRAD_STRIDE 12
+/* Floats per Gaussian of the splat record (FB rasterizer_imp.h:27-38). */
+#define FGS_SPLAT_STRIDE 32
+
+const char* fgs_status_string(int status);
+/* Build identification, e.g. "fgs 0.1 sm_103a". */
+const char* fgs_version(void);
+
+/* Reads and optionally clears the device error word that kernels set when a
+ * bounded wait gives up (bit 0) or a capacity check skips writes (bit 1).
+ * Synchronises the stream.  *flags receives the word. */
+fgs_status fgs_device_errors(int* flags, int clear, void* stream);
+
+/*
+ * Per-Gaussian preprocess and (tile, Gaussian) key emission.
+ * Replaces faster::preprocess (FB csrc/ops.h:71-85, body
+ * csrc/cuda_rasterizer/preprocess.cu:928-971).
+ *
+ * Small-footprint Gaussians (rect < 128 tiles) are packed across warp lanes;
+ * large ones are split into 128-tile sub-tasks queued in task_scratch
+ * (FB keeps the same queue in gaussian_values_sorted) and drained by a second
+ * kernel without a host round trip.  Appends K pairs at *curr_offset, which
+ * the caller zeroes beforehand, exactly like FB.  Writes past pair_capacity
+ * are skipped while *curr_offset keeps counting, so the caller detects
+ * overflow by comparing K with the capacity.  counters: device int32
+ * [FGS_COUNTER_WORDS], zeroed here.  radii (P) is fully written.
+ */
+fgs_status fgs_preprocess(
+    int P, int D, int M,
+    const float* means3D, const float* colors_precomp, const float* dc, const float* shs,
+    const float* opacities, const float* scales, const float* rotations, float scale_modifier,
+    int width, int height, int block_x, int block_y,
+    const float* campos, const float* viewmatrix, const float* projmatrix,
+    float tan_fovx, float tan_fovy, float zfar, float znear, float mult, const uint8_t* culling,
+    float* splat_buffer, int64_t splat_rows,
+    uint64_t* keys_unsorted, uint32_t* values_unsorted, int64_t pair_capacity,
+    uint32_t* task_scratch, int64_t task_scratch_words,
+    int32_t* curr_offset, int32_t* counters, int32_t* radii, void* stream);
+
+/* Temporary bytes fgs_sort needs for up to num_rendered pairs.
+ * Replaces faster::get_sort_buffer_size (FB csrc/ops.h:94, sort.cu:46-54). */
+size_t fgs_sort_temp_bytes(int64_t num_rendered);
+
+/*
+ * Stable ascending LSD radix sort of (key, value) pairs on the low
+ * 32 + ceil(log2(tiles)) key bits, tiles = ceil(W/bx)*ceil(H/by).
+ * Replaces faster::sort_gaussian (FB csrc/ops.h:87-92, sort.cu:28-44), which
+ * calls cub::DeviceRadixSort::SortPairs.  Inputs are not modified.
+ */
+fgs_status fgs_sort(int64_t num_rendered, int width, int height, int block_x, int block_y,
+                    void* temp, size_t temp_bytes,
+                    const uint64_t* keys_in, const uint32_t* values_in,
+                    uint64_t* keys_out, uint32_t* values_out, void* stream);
+
+/* [start, end) of every tile in a sorted key list; ranges is (tiles, 2) u32
+ * and is zeroed first.  Replaces identifyTileRanges and its launch
+ * (FB render.cu:54-79, :406-412). */
+fgs_status fgs_tile_ranges(int64_t num_rendered, int num_tiles, const uint64_t* keys_sorted,
+                           uint32_t* ranges, void* stream);
+
+/* Upper bound on the bucket count of a frame with num_rendered pairs. */
+int64_t fgs_max_buckets(int64_t num_rendered, int width, int height, int block_x, int block_y,
+                        int bucket_size);
+
+/* Bytes of the per-image state and per-bucket sample state that fgs_render_fwd
+ * fills and fgs_render_bwd consumes (FB ImageState / SampleState,
+ * rasterizer_imp.h:76-102, rasterizer_imp.cu:7-48). */
+fgs_status fgs_state_bytes(int width, int height, int block_x, int block_y, int64_t max_buckets,
+                           size_t* image_bytes, size_t* sample_bytes);
+
+/*
+ * Forward composite: tile ranges, bucket bookkeeping, parallel per-bucket
+ * compositing and the associative (colour, transmittance) merge.
+ * Replaces faster::render_16x16 (FB csrc/ops.h:96-106, render.cu:393-470).
+ * out_color (3,H,W), last_contributor (H,W), Ts_final (H,W) are written.
+ * If bucket_sum_host is non-NULL the stream is synchronised at the end and
+ * the bucket count is stored there (FB returns it to Python).
+ */
+fgs_status fgs_render_fwd(int P, int64_t num_rendered, int width, int height, int block_x, int block_y,
+                          int bucket_size, const float* splat_buffer, const uint64_t* keys_sorted,
+                          const uint32_t* values_sorted, uint32_t* ranges, const float* bg,
+                          float* out_color, int32_t* last_contributor, float* Ts_final,
+                          void* image_state, size_t image_bytes, void* sample_state, size_t sample_bytes,
+                          int64_t max_buckets, uint32_t* bucket_sum_host, void* stream);
+
+/*
+ * Backward composite, bucket-parallel, front-to-back inside each bucket.
+ * Replaces faster::render_backward (FB csrc/ops.h:123-135,
+ * backward.cu:956-977).  grad_record (P, FGS_GRAD_STRIDE) is zeroed here and
+ * accumulated with vector reductions.
+ */
+fgs_status fgs_render_bwd(int P, int width, int height, int block_x, int block_y, int bucket_size,
+                          const uint32_t* values_sorted, const uint32_t* ranges, const float* bg,
+                          const float* splat_buffer, const float* Ts_final, const int32_t* last_contributor,
+                          const void* image_state, const void* sample_state, int64_t max_buckets,
+                          const float* dL_dpixels, float* grad_record, void* stream);
+
+/*
+ * Per-Gaussian backward of projection, EWA covariance, SH and 3D covariance;
+ * scatters the render gradients into FB's output tensors and, when
+ * xyz_gradient_accum is non-NULL, accumulates densification statistics.
+ * Replaces faster::preprocess_backward + add_densification_stats
+ * (FB csrc/ops.h:108-121,137-145; backward.cu:922-954,980-999) and the
+ * output allocation of backward_torch (FB csrc/pybind.cpp:258-267).
+ * All outputs are fully written (zeros where FB leaves zeros).
+ */
+fgs_status fgs_preprocess_bwd(
+    int P, int D, int M, const float* means3D, const int32_t* radii, const float* dc, const float* shs,
+    const float* splat_buffer, const float* scales, const float* rotations, float scale_modifier,
+    const float* viewmatrix, const float* projmatrix, int width, int height, float tan_fovx, float tan_fovy,
+    const float* campos, const float* grad_record,
+    float* dL_dmean2D, float* dL_dconic, float* dL_dopacity, float* dL_dcolor,
+    float* dL_dmean3D, float* dL_dcov3D, float* dL_ddc, float* dL_dsh, float* dL_dscale, float* dL_drot,
+    float* xyz_gradient_accum, float* xyz_gradient_accum_abs, float* max_radii, float* denom,
+    void* stream);
+
+/* Densification statistics alone (FB backward.cu:892-918).  Each output is
+ * optional; dL_dmean2D is (P,4). */
+fgs_status fgs_densify_stats(int P, const int32_t* radii, const float* dL_dmean2D, float* xyz_gradient_accum,
+                             float* xyz_gradient_accum_abs, float* max_radii, float* denom, void* stream);
+
+/* Masked Adam step over N rows of M floats; rows with visible[i]==0 are left
+ * untouched.  Replaces ADAM::adamUpdate (FB adam.h, adam.cu:9-66). */
+fgs_status fgs_adam_update(float* param, const float* grad, float* exp_avg, float* exp_avg_sq,
+                           const uint8_t* visible, float lr, float b1, float b2, float eps,
+                           uint32_t N, uint32_t M, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FGS_H_ */

@@ -1,0 +1,230 @@
+"""FP64 CPU oracle of the FasterGS rasterizer -- TEST INFRASTRUCTURE ONLY.
+
+Only tests/, ``__graft_entry__.smoke()`` and the CPU-baseline leg of
+``bench.py`` import this package, and only as the checker or the timed CPU
+baseline.  The product (``fastergs_gb300``) never calls it.
+
+Parity status: pinned against the reference's own Python code for SH
+evaluation, scale/rotation covariance and camera matrices (fixtures under
+tests/golden/); the rasterizer core is a restatement of the reference CUDA
+source (see oracle.cpp for the file:line map) and is otherwise unpinned,
+because the reference ships no tests or golden vectors and its CUDA build
+cannot run where the fixtures are generated.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import shutil
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+SRC = HERE / "oracle.cpp"
+LIB = HERE / "liboracle.so"
+
+_lib = None
+
+
+def build(force: bool = False) -> Path:
+    """g++ -O2 -fopenmp -shared; skipped when the library is newer than the source."""
+    if not force and LIB.exists() and LIB.stat().st_mtime >= SRC.stat().st_mtime:
+        return LIB
+    cxx = os.environ.get("CXX") or shutil.which("g++") or "g++"
+    tmp = LIB.with_suffix(".so.tmp")
+    cmd = [cxx, "-O2", "-std=c++17", "-fopenmp", "-shared", "-fPIC", str(SRC), "-o", str(tmp)]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"oracle build failed:\n{r.stderr}")
+    os.replace(tmp, LIB)
+    return LIB
+
+
+def load():
+    global _lib
+    if _lib is None:
+        build()
+        lib = C.CDLL(str(LIB))
+        vp, i32, i64, f64 = C.c_void_p, C.c_int, C.c_int64, C.c_double
+        sig = {
+            "orc_new": (vp, []),
+            "orc_free": (None, [vp]),
+            "orc_set_scene": (i32, [vp, i32, i32, i32, vp, vp, vp, vp, vp, vp, vp, vp, f64, i32, i32, i32, i32, vp,
+                                    vp, vp, f64, f64, f64]),
+            "orc_preprocess": (None, [vp]),
+            "orc_set_records": (None, [vp, vp, vp, vp]),
+            "orc_emit_sort": (i64, [vp, f64]),
+            "orc_set_lists": (None, [vp, i64, vp, vp]),
+            "orc_render": (None, [vp, vp, i32, f64, f64]),
+            "orc_num_pairs": (i64, [vp]),
+            "orc_num_buckets": (i64, [vp]),
+            "orc_get_preprocess": (None, [vp, vp, vp, vp, vp, vp]),
+            "orc_get_pairs": (None, [vp, vp, vp, vp, vp]),
+            "orc_get_image": (None, [vp, vp, vp, vp, vp, vp, vp]),
+            "orc_backward": (None, [vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp]),
+            "orc_densify": (None, [vp, vp, vp, vp, vp, vp]),
+            "orc_num_threads": (i32, []),
+            "orc_set_threads": (None, [i32]),
+            "orc_eval_sh": (None, [i32, i32, vp, vp, vp]),
+            "orc_get_decisions": (None, [vp, vp, vp]),
+            "orc_cov3d": (None, [i32, vp, vp, f64, vp]),
+        }
+        for name, (res, args) in sig.items():
+            fn = getattr(lib, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = lib
+    return _lib
+
+
+def _d(a):
+    """float64 C-contiguous copy (or None)."""
+    if a is None:
+        return None
+    return np.ascontiguousarray(np.asarray(a, dtype=np.float64))
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+class Oracle:
+    """One scene + camera.  Typical use: set_scene -> preprocess -> emit_sort -> render -> backward."""
+
+    def __init__(self):
+        self.lib = load()
+        self.h = self.lib.orc_new()
+        self._keep = []
+
+    def __del__(self):
+        if getattr(self, "h", None) and self.lib is not None:
+            self.lib.orc_free(self.h)
+            self.h = None
+
+    def set_scene(self, means, opacities, scales, rotations, camera, dc=None, shs=None, colors=None, sh_degree=0,
+                  culling=None, scale_modifier=1.0, mult=1.0, block=(16, 16)):
+        P = means.shape[0]
+        self.P, self.W, self.H = P, camera.width, camera.height
+        self.bx, self.by = block
+        self.gx = (self.W + self.bx - 1) // self.bx
+        self.gy = (self.H + self.by - 1) // self.by
+        self.M = 0 if shs is None else shs.shape[1]
+        arrs = [_d(means), _d(colors), _d(dc), _d(shs), _d(opacities).reshape(-1), _d(scales), _d(rotations)]
+        cull = None if culling is None else np.ascontiguousarray(np.asarray(culling, dtype=np.uint8))
+        view = _d(np.asarray(camera.viewmatrix).reshape(-1))
+        proj = _d(np.asarray(camera.projmatrix).reshape(-1))
+        cpos = _d(camera.campos)
+        self._keep = arrs + [cull, view, proj, cpos]
+        st = self.lib.orc_set_scene(self.h, P, int(sh_degree), self.M, *[_p(a) for a in arrs], _p(cull),
+                                    float(scale_modifier), self.W, self.H, self.bx, self.by, _p(view), _p(proj),
+                                    _p(cpos), float(camera.tanfovx), float(camera.tanfovy), float(mult))
+        if st != 0:
+            raise ValueError("oracle rejected the scene (missing scales/rotations or colour inputs)")
+        return self
+
+    def preprocess(self):
+        self.lib.orc_preprocess(self.h)
+        return self
+
+    def records(self):
+        rec = np.empty((self.P, 32), np.float64)
+        radii = np.empty(self.P, np.int32)
+        valid = np.empty(self.P, np.uint8)
+        amb = np.empty(self.P, np.uint8)
+        area = np.empty(self.P, np.int32)
+        self.lib.orc_get_preprocess(self.h, _p(rec), _p(radii), _p(valid), _p(amb), _p(area))
+        return dict(rec=rec, radii=radii, valid=valid.astype(bool), ambiguous=amb.astype(bool), rect_area=area)
+
+    def set_records(self, rec, radii, valid):
+        rec = _d(rec)
+        radii = np.ascontiguousarray(radii, dtype=np.int32)
+        valid = np.ascontiguousarray(valid, dtype=np.uint8)
+        self._keep_rec = (rec, radii, valid)
+        self.lib.orc_set_records(self.h, _p(rec), _p(radii), _p(valid))
+        return self
+
+    def emit_sort(self, eps_pair: float = 1e-5) -> int:
+        return int(self.lib.orc_emit_sort(self.h, float(eps_pair)))
+
+    def pairs(self):
+        K = int(self.lib.orc_num_pairs(self.h))
+        keys = np.empty(K, np.uint64)
+        ids = np.empty(K, np.int32)
+        amb = np.empty(K, np.uint8)
+        ranges = np.empty((self.gx * self.gy, 2), np.int32)
+        self.lib.orc_get_pairs(self.h, _p(keys), _p(ids), _p(amb), _p(ranges))
+        return dict(keys=keys, ids=ids, ambiguous=amb.astype(bool), ranges=ranges)
+
+    def set_lists(self, ids, ranges):
+        ids = np.ascontiguousarray(ids, dtype=np.int32)
+        ranges = np.ascontiguousarray(ranges, dtype=np.int32).reshape(-1)
+        self._keep_lists = (ids, ranges)
+        self.lib.orc_set_lists(self.h, int(ids.size), _p(ids), _p(ranges))
+        return self
+
+    def render(self, bg=(0.0, 0.0, 0.0), bucket_size: int = 128, eps_alpha: float = 1e-5, eps_T: float = 1e-5):
+        bgd = _d(np.asarray(bg).reshape(3))
+        self.lib.orc_render(self.h, _p(bgd), int(bucket_size), float(eps_alpha), float(eps_T))
+        return self
+
+    def image(self):
+        HW = self.W * self.H
+        out = np.empty((3, self.H, self.W), np.float64)
+        pc = np.empty((self.H, self.W, 3), np.float64)
+        lc = np.empty((self.H, self.W), np.int32)
+        tf = np.empty((self.H, self.W), np.float64)
+        amb = np.empty((self.H, self.W), np.uint8)
+        mc = np.empty(self.gx * self.gy, np.int32)
+        self.lib.orc_get_image(self.h, _p(out), _p(pc), _p(lc), _p(tf), _p(amb), _p(mc))
+        return dict(out_color=out, pixel_colors=pc, last_contributor=lc, Ts_final=tf, ambiguous=amb.astype(bool),
+                    max_contrib=mc, num_buckets=int(self.lib.orc_num_buckets(self.h)))
+
+    def decisions(self):
+        """(#evaluations with alpha >= 1/255, #clamped at 0.99), per-Gaussian clamp flags."""
+        counts = np.zeros(2, np.int64)
+        cl = np.zeros(self.P, np.uint8)
+        self.lib.orc_get_decisions(self.h, _p(counts), _p(cl))
+        return (int(counts[0]), int(counts[1])), cl.astype(bool)
+
+    def backward(self, dL_dout):
+        P, M = self.P, self.M
+        dL = _d(dL_dout)
+        out = dict(dmean2D=np.empty((P, 4)), dconic=np.empty((P, 4)), dopacity=np.empty(P),
+                   dcolor=np.empty((P, 3)), dmean3D=np.empty((P, 3)), dcov3D=np.empty((P, 6)),
+                   ddc=np.empty((P, 1, 3)), dsh=np.empty((P, max(M, 0), 3)), dscale=np.empty((P, 3)),
+                   drot=np.empty((P, 4)))
+        self.lib.orc_backward(self.h, _p(dL), *[_p(out[k]) for k in ("dmean2D", "dconic", "dopacity", "dcolor",
+                                                                     "dmean3D", "dcov3D", "ddc", "dsh", "dscale",
+                                                                     "drot")])
+        return out
+
+    def densify(self, dmean2D, grad_accum=None, grad_accum_abs=None, max_radii=None, denom=None):
+        arrs = [_d(dmean2D), _d(grad_accum), _d(grad_accum_abs), _d(max_radii), _d(denom)]
+        self.lib.orc_densify(self.h, *[_p(a) for a in arrs])
+        return arrs[1:]
+
+
+def num_threads() -> int:
+    return int(load().orc_num_threads())
+
+
+def set_threads(n: int) -> None:
+    load().orc_set_threads(int(n))
+
+
+def eval_sh(deg: int, dirs, coeffs):
+    """SH colour without offset/clamp; coeffs (n, 16, 3), coefficient 0 = DC."""
+    dirs, coeffs = _d(dirs), _d(coeffs)
+    out = np.empty((dirs.shape[0], 3))
+    load().orc_eval_sh(dirs.shape[0], int(deg), _p(dirs), _p(coeffs), _p(out))
+    return out
+
+
+def cov3d(scales, quats, scale_modifier: float = 1.0):
+    """Upper triangle (xx, xy, xz, yy, yz, zz) of R diag(s^2) R^T, raw quaternions."""
+    scales, quats = _d(scales), _d(quats)
+    out = np.empty((scales.shape[0], 6))
+    load().orc_cov3d(scales.shape[0], _p(scales), _p(quats), float(scale_modifier), _p(out))
+    return out

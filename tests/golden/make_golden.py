@@ -1,0 +1,112 @@
+"""Generates the golden fixtures that pin the CPU oracle against the reference.
+
+Runs the reference's own Python code, imported from a FasterGS checkout
+(default /root/reference, override with FASTERGS_REF), on seeded inputs and
+stores inputs and outputs in tests/golden/*.npz:
+
+  sh_golden.npz       3DGS/utils/sh_utils.py eval_sh, degrees 0..3
+  cov_golden.npz      3DGS/utils/general_utils.py build_scaling_rotation ->
+                      L L^T -> strip_symmetric (the 3DGS covariance path)
+  camera_golden.npz   3DGS/utils/graphics_utils.py getWorld2View2 /
+                      getProjectionMatrix composed as 3DGS/scene/cameras.py:54-57
+
+build_rotation / build_scaling_rotation allocate with device='cuda'; the
+script runs them on CPU by handing the module a torch proxy whose zeros()
+drops the device argument.  Nothing else of the reference is changed.
+
+Usage:  python tests/golden/make_golden.py
+"""
+from __future__ import annotations
+
+import importlib.util
+import math
+import os
+import sys
+import types
+from pathlib import Path
+
+import numpy as np
+import torch
+
+HERE = Path(__file__).resolve().parent
+REF = Path(os.environ.get("FASTERGS_REF", "/root/reference"))
+
+
+def _load(rel: str, name: str):
+    spec = importlib.util.spec_from_file_location(name, REF / rel)
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod
+
+
+def _cpu_torch_proxy():
+    proxy = types.SimpleNamespace(**{k: getattr(torch, k) for k in dir(torch) if not k.startswith("__")})
+
+    def zeros(*args, **kwargs):
+        kwargs.pop("device", None)
+        return torch.zeros(*args, **kwargs)
+
+    proxy.zeros = zeros
+    return proxy
+
+
+def make_sh(rng):
+    sh_utils = _load("3DGS/utils/sh_utils.py", "ref_sh_utils")
+    n = 512
+    dirs = rng.normal(size=(n, 3))
+    dirs /= np.linalg.norm(dirs, axis=1, keepdims=True)
+    coeffs = rng.normal(size=(n, 16, 3))  # (n, k, channel)
+    out = {}
+    for deg in range(4):
+        sh = torch.tensor(coeffs, dtype=torch.float64).transpose(1, 2)  # (n, 3, 16) as eval_sh wants
+        out[f"deg{deg}"] = sh_utils.eval_sh(deg, sh, torch.tensor(dirs, dtype=torch.float64)).numpy()
+    np.savez_compressed(HERE / "sh_golden.npz", dirs=dirs, coeffs=coeffs, **out)
+
+
+def make_cov(rng):
+    gu = _load("3DGS/utils/general_utils.py", "ref_general_utils")
+    gu.torch = _cpu_torch_proxy()
+    n = 512
+    scales = np.exp(rng.normal(-2.0, 1.0, size=(n, 3)))
+    quats = rng.normal(size=(n, 4))
+    quats /= np.linalg.norm(quats, axis=1, keepdims=True)
+    L = gu.build_scaling_rotation(torch.tensor(scales, dtype=torch.float32), torch.tensor(quats, dtype=torch.float32))
+    cov = gu.strip_symmetric(L @ L.transpose(1, 2))
+    np.savez_compressed(HERE / "cov_golden.npz", scales=scales, quats=quats, cov=cov.numpy().astype(np.float64))
+
+
+def make_cameras(rng):
+    gr = _load("3DGS/utils/graphics_utils.py", "ref_graphics_utils")
+    cases = []
+    for k in range(6):
+        q = rng.normal(size=4)
+        q /= np.linalg.norm(q)
+        r, x, y, z = q
+        R = np.array([[1 - 2 * (y * y + z * z), 2 * (x * y - r * z), 2 * (x * z + r * y)],
+                      [2 * (x * y + r * z), 1 - 2 * (x * x + z * z), 2 * (y * z - r * x)],
+                      [2 * (x * z - r * y), 2 * (y * z + r * x), 1 - 2 * (x * x + y * y)]])
+        T = rng.normal(size=3) * 3
+        fovx = math.radians(float(rng.uniform(40, 80)))
+        fovy = math.radians(float(rng.uniform(30, 70)))
+        wv = torch.tensor(gr.getWorld2View2(R, T)).transpose(0, 1)
+        pm = gr.getProjectionMatrix(znear=0.01, zfar=100.0, fovX=fovx, fovY=fovy).transpose(0, 1)
+        full = wv.unsqueeze(0).bmm(pm.unsqueeze(0)).squeeze(0)
+        center = wv.inverse()[3, :3]
+        cases.append((R, T, fovx, fovy, wv.numpy(), pm.numpy(), full.numpy(), center.numpy()))
+    arr = lambda i: np.stack([c[i] for c in cases])
+    np.savez_compressed(HERE / "camera_golden.npz", R=arr(0), T=arr(1), fovx=arr(2), fovy=arr(3),
+                        world_view=arr(4), proj=arr(5), full_proj=arr(6), center=arr(7))
+
+
+def main():
+    if not REF.exists():
+        sys.exit(f"reference checkout not found at {REF}")
+    rng = np.random.default_rng(20240611)
+    make_sh(rng)
+    make_cov(rng)
+    make_cameras(rng)
+    print("wrote", sorted(p.name for p in HERE.glob("*.npz")))
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,123 @@
+"""Helpers shared by the GPU parity tests: run the plain path through the
+C-ABI (``fastergs_gb300._C.ops``) and set up the oracle on the same inputs."""
+from __future__ import annotations
+
+import numpy as np
+import torch
+
+import oracle
+from fastergs_gb300 import Buffer, _C
+
+
+def tensors(scene, dev):
+    m, sc, rot, op, dc, shs = scene.activated()
+    t = lambda a: torch.tensor(np.ascontiguousarray(a), device=dev)
+    return dict(means=t(m), scales=t(sc), rotations=t(rot), opacities=t(op), dc=t(dc), shs=t(shs))
+
+
+_BUFFERS = {}
+
+
+def buffer(dev, cap=2**21):
+    key = (str(dev), cap)
+    if key not in _BUFFERS:
+        _BUFFERS.clear()
+        torch.cuda.empty_cache()
+        _BUFFERS[key] = Buffer(device=dev, MAX_NUM_RENDERED=cap)
+    return _BUFFERS[key]
+
+
+def run_forward(scene, dev, bg=(0.0, 0.0, 0.0), culling=None, colors=None, mult=1.0, smod=1.0, cap=2**21,
+                shs_override="keep"):
+    cam = scene.camera
+    T = tensors(scene, dev)
+    buf = buffer(dev, cap)
+    f = lambda a: torch.tensor(np.asarray(a, np.float32), device=dev)
+    empty = torch.tensor([])
+    shs = T["shs"] if shs_override == "keep" else shs_override
+    cull = empty.bool() if culling is None else torch.tensor(culling, device=dev)
+    col = empty if colors is None else f(colors)
+    buf.curr_offset.fill_(0)
+    radii = _C.ops.preprocess(scene.sh_degree, T["means"], col, T["dc"] if colors is None else empty,
+                              shs if colors is None else empty, T["opacities"], T["scales"], T["rotations"], smod,
+                              cam.width, cam.height, 16, 16, f(cam.campos), f(cam.viewmatrix), f(cam.projmatrix),
+                              cam.tanfovx, cam.tanfovy, 100.0, 0.01, buf.gaussian_keys_unsorted,
+                              buf.gaussian_values_unsorted, buf.gaussian_values_sorted, buf.curr_offset, mult,
+                              buf.splat_buffer, cull)
+    K = int(buf.curr_offset.cpu()[0])
+    assert K < buf.MAX_NUM_RENDERED
+    assert _C.device_errors(dev) == 0
+    keys_u = buf.gaussian_keys_unsorted[:K].clone()
+    vals_u = buf.gaussian_values_unsorted[:K].clone()
+    _C.ops.sort_gaussian(K, cam.width, cam.height, 16, 16, buf.list_sorting_space, buf.gaussian_keys_unsorted,
+                         buf.gaussian_values_unsorted, buf.gaussian_keys_sorted, buf.gaussian_values_sorted)
+    H, W = cam.height, cam.width
+    lc = torch.zeros((H, W, 1), device=dev, dtype=torch.int32)
+    Tf = torch.zeros((H, W, 1), device=dev, dtype=torch.float32)
+    bsum, out, img_buf, smp_buf = _C.ops.render_16x16(scene.P, K, W, H, buf.splat_buffer,
+                                                      buf.gaussian_keys_sorted, buf.gaussian_values_sorted,
+                                                      buf.ranges, f(bg), lc, Tf)
+    torch.cuda.synchronize()
+    assert _C.device_errors(dev) == 0
+    P = scene.P
+    return dict(
+        K=K, bucket_sum=bsum, radii=radii, out_color=out, last_contrib=lc, Ts_final=Tf, img_buf=img_buf,
+        smp_buf=smp_buf, keys_unsorted=keys_u.cpu().numpy(), vals_unsorted=vals_u.cpu().numpy(),
+        keys_sorted=buf.gaussian_keys_sorted[:K].cpu().numpy(), vals_sorted=buf.gaussian_values_sorted[:K].cpu().numpy(),
+        ranges=buf.ranges[: ((W + 15) // 16) * ((H + 15) // 16)].cpu().numpy(),
+        rec=buf.splat_buffer[:P].cpu().numpy(), T=T, buf=buf, bg=f(bg), culling=cull, colors=col, shs=shs,
+        mult=mult, smod=smod)
+
+
+def run_backward(scene, fw, dL, dev, stats=False):
+    cam = scene.camera
+    T = fw["T"]
+    buf = fw["buf"]
+    f = lambda a: torch.tensor(np.asarray(a, np.float32), device=dev)
+    empty = torch.tensor([])
+    P = scene.P
+    accum = [torch.zeros((P, 1), device=dev) for _ in range(4)] if stats else [empty] * 4
+    colors = fw["colors"].numel() > 0
+    res = _C.ops.backward(scene.sh_degree, fw["bucket_sum"], T["means"], fw["radii"],
+                          T["dc"] if not colors else empty, fw["shs"] if not colors else empty, T["opacities"],
+                          T["scales"], T["rotations"], fw["smod"], cam.width, cam.height, 16, 16, cam.tanfovx,
+                          cam.tanfovy, 100.0, 0.01, f(cam.campos), f(cam.viewmatrix), f(cam.projmatrix),
+                          fw["img_buf"], fw["smp_buf"], buf.splat_buffer, buf.gaussian_values_sorted, buf.ranges,
+                          fw["bg"], fw["last_contrib"], fw["Ts_final"], f(dL), *accum)
+    torch.cuda.synchronize()
+    names = ["dmean2D", "dcolor", "dopacity", "dmean3D", "dcov3D", "ddc", "dsh", "dscale", "drot"]
+    out = {k: v.cpu().numpy().astype(np.float64) for k, v in zip(names, res)}
+    if stats:
+        out["stats"] = [a.cpu().numpy()[:, 0].astype(np.float64) for a in accum]
+    return out
+
+
+def oracle_scene(scene, culling=None, colors=None, mult=1.0, smod=1.0, with_shs=True):
+    m, sc, rot, op, dc, shs = [np.asarray(a, np.float64) for a in scene.activated()]
+    o = oracle.Oracle()
+    o.set_scene(m, op, sc, rot, scene.camera, dc=None if colors is not None else dc,
+                shs=(shs if with_shs else None) if colors is None else None, colors=colors,
+                sh_degree=scene.sh_degree, culling=culling, scale_modifier=smod, mult=mult)
+    return o
+
+
+def gpu_records_as_oracle(fw):
+    """The device's float32 records as float64, rect ints decoded."""
+    rec = fw["rec"].astype(np.float64)
+    raw = fw["rec"].view(np.int32)
+    rec[:, 10:14] = raw[:, 10:14]
+    radii = fw["radii"].cpu().numpy()
+    valid = np.zeros(rec.shape[0], bool)
+    valid[np.unique(fw["vals_sorted"])] = True
+    return rec, radii, valid
+
+
+def replay_oracle(scene, fw, bg=(0.0, 0.0, 0.0), eps_alpha=1e-5, eps_T=1e-5, **kw):
+    """Oracle compositing on the device's own records and sorted lists."""
+    o = oracle_scene(scene, **kw)
+    rec, radii, _ = gpu_records_as_oracle(fw)
+    valid = (radii > 0) | np.isin(np.arange(scene.P), fw["vals_sorted"])
+    o.set_records(rec, radii, valid)
+    o.set_lists(fw["vals_sorted"], fw["ranges"])
+    o.render(bg=bg, eps_alpha=eps_alpha, eps_T=eps_T)
+    return o

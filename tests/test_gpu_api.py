@@ -1,0 +1,163 @@
+"""GPU tests of the drop-in Python API: GaussianRasterizer / autograd,
+capacity errors, SparseGaussianAdam, and finite differences through the whole
+chain (activations + rasterizer) against the FP64 oracle."""
+import numpy as np
+import pytest
+import torch
+
+import oracle
+from fastergs_gb300 import (Buffer, GaussianRasterizationSettings, GaussianRasterizer, SparseGaussianAdam,
+                            _RasterizeGaussians, scenes)
+
+pytestmark = pytest.mark.gpu
+
+
+def settings_for(cam, dev, deg, bg=(0.0, 0.0, 0.0)):
+    t = lambda a: torch.tensor(np.asarray(a, np.float32), device=dev)
+    return GaussianRasterizationSettings(
+        image_height=cam.height, image_width=cam.width, tanfovx=cam.tanfovx, tanfovy=cam.tanfovy, bg=t(bg),
+        scale_modifier=1.0, viewmatrix=t(cam.viewmatrix), projmatrix=t(cam.projmatrix), sh_degree=deg,
+        campos=t(cam.campos), mult=1.0, prefiltered=False, debug=False)
+
+
+def raw_params(scene, dev):
+    t = lambda a: torch.tensor(np.asarray(a, np.float32), device=dev, requires_grad=True)
+    return dict(means=t(scene.means), log_scales=t(scene.log_scales), quats=t(scene.quats),
+                logits=t(scene.opacity_logits), dc=t(scene.dc), shs=t(scene.shs))
+
+
+def render(scene, p, dev):
+    rast = GaussianRasterizer(settings_for(scene.camera, dev, scene.sh_degree))
+    q = p["quats"] / p["quats"].norm(dim=1, keepdim=True)
+    return rast(means3D=p["means"], opacities=torch.sigmoid(p["logits"]), dc=p["dc"], shs=p["shs"],
+                scales=torch.exp(p["log_scales"]), rotations=q)
+
+
+def test_autograd_roundtrip_and_radii(cuda_device):
+    s = scenes.scene_c1()
+    p = raw_params(s, cuda_device)
+    img, radii = render(s, p, cuda_device)
+    assert img.shape == (3, 256, 256) and radii.dtype == torch.int32
+    (img * torch.tensor(scenes.upstream_grad(0, 256, 256), device=cuda_device)).sum().backward()
+    for k, v in p.items():
+        assert v.grad is not None and torch.isfinite(v.grad).all(), k
+
+
+def test_argument_validation_mirrors_reference(cuda_device):
+    s = scenes.scene_c1(P=100)
+    rast = GaussianRasterizer(settings_for(s.camera, cuda_device, 0))
+    m = torch.zeros((100, 3), device=cuda_device)
+    with pytest.raises(Exception, match="one of either SHs"):
+        rast(means3D=m, opacities=m[:, :1])
+    with pytest.raises(Exception, match="scale/rotation pair"):
+        rast(means3D=m, opacities=m[:, :1], shs=torch.zeros((100, 15, 3), device=cuda_device))
+
+
+def test_capacity_overflow_raises(cuda_device):
+    s = scenes.scene_c1()
+    slot = _RasterizeGaussians.__dict__["buffer"]  # the lazily allocated shared Buffer
+    old = slot._buf
+    try:
+        slot._buf = Buffer(device=cuda_device, MAX_NUM_RENDERED=1024)
+        with pytest.raises(RuntimeError, match="Too many k-v pairs"):
+            render(s, raw_params(s, cuda_device), cuda_device)
+    finally:
+        slot._buf = old
+    img, _ = render(s, raw_params(s, cuda_device), cuda_device)
+    assert torch.isfinite(img).all()
+
+
+def test_sparse_adam_matches_masked_adam(cuda_device):
+    torch.manual_seed(0)
+    N, M = 1000, 3
+    param = torch.randn(N, M, device=cuda_device, requires_grad=True)
+    ref = param.detach().clone()
+    opt = SparseGaussianAdam([param], lr=0.01, eps=1e-15)
+    m1 = torch.zeros_like(ref)
+    m2 = torch.zeros_like(ref)
+    for step in range(1, 4):
+        g = torch.randn(N, M, device=cuda_device)
+        vis = torch.rand(N, device=cuda_device) < 0.5
+        param.grad = g.clone()
+        opt.step(vis, N)
+        lr = 0.01 * (1 - 0.999 ** step) ** 0.5 / (1 - 0.9 ** step)
+        m1n = 0.9 * m1 + 0.1 * g
+        m2n = 0.999 * m2 + 0.001 * g * g
+        upd = ref - lr * m1n / (m2n.sqrt() + 1e-15)
+        v = vis[:, None]
+        ref = torch.where(v, upd, ref)
+        m1 = torch.where(v, m1n, m1)
+        m2 = torch.where(v, m2n, m2)
+        torch.testing.assert_close(param.detach(), ref, rtol=1e-5, atol=1e-6)
+
+
+def _oracle_loss(scene, raw, dL):
+    means, ls, q, lg, dc, shs = raw
+    qn = q / np.linalg.norm(q, axis=1, keepdims=True)
+    o = oracle.Oracle().set_scene(means, 1 / (1 + np.exp(-lg)), np.exp(ls), qn, scene.camera, dc=dc, shs=shs,
+                                  sh_degree=scene.sh_degree)
+    o.preprocess()
+    K = o.emit_sort()
+    o.render()
+    im = o.image()
+    (non, ncl), cl = o.decisions()
+    sig = (K, non, ncl, int(im["last_contributor"].sum()))
+    return float((im["out_color"] * dL).sum()), sig, cl
+
+
+def test_gradients_match_fp64_finite_differences(cuda_device):
+    """C5a: 2,000 Gaussians, 128x128, SH degree 1; FP64 central differences
+    (relative step 1e-4) on 200 seeded entries over means, log-scales,
+    quaternions, opacity logits and SH; entries whose +/- evaluations change a
+    discrete decision (pair list, alpha cut-off, merge break) or touch an
+    alpha clamped at 0.99 (where FB's analytic gradient is not the derivative)
+    are skipped and counted.  Tolerance per entry:
+    |device - fd| <= 1e-4 * |fd| + 1e-4 * max |fd| of the parameter group."""
+    s = scenes.scene_c5a()
+    dL = scenes.upstream_grad(0, s.camera.height, s.camera.width).astype(np.float64)
+    p = raw_params(s, cuda_device)
+    img, _ = render(s, p, cuda_device)
+    (img * torch.tensor(dL, dtype=torch.float32, device=cuda_device)).sum().backward()
+    grads = [p[k].grad.cpu().numpy().astype(np.float64) for k in ("means", "log_scales", "quats", "logits", "dc",
+                                                                   "shs")]
+    raw = [np.asarray(a, np.float64) for a in (s.means, s.log_scales, s.quats, s.opacity_logits, s.dc, s.shs)]
+    _, sig0, clamped = _oracle_loss(s, raw, dL)
+    rng = np.random.default_rng(123)
+    groups = [0, 1, 2, 3, 4, 5]
+    checked, skipped = 0, 0
+    per_group = {g: [] for g in groups}
+    for n in range(200):
+        gi = groups[n % len(groups)]
+        arr = raw[gi]
+        if gi == 5:  # SH degree 1 uses the first three rest coefficients
+            i = int(rng.integers(s.P))
+            flat = np.ravel_multi_index((i, int(rng.integers(3)), int(rng.integers(3))), arr.shape)
+        else:
+            flat = int(rng.integers(arr.size))
+        gauss = np.unravel_index(flat, arr.shape)[0]
+        if clamped[gauss]:
+            skipped += 1
+            continue
+        h = 1e-4 * max(abs(arr.reshape(-1)[flat]), 1e-2)
+        vals = []
+        sigs = []
+        for sgn in (1, -1):
+            r2 = [a.copy() for a in raw]
+            r2[gi].reshape(-1)[flat] += sgn * h
+            L, sig, _ = _oracle_loss(s, r2, dL)
+            vals.append(L)
+            sigs.append(sig)
+        if sigs[0] != sig0 or sigs[1] != sig0:
+            skipped += 1
+            continue
+        fd = (vals[0] - vals[1]) / (2 * h)
+        per_group[gi].append((fd, grads[gi].reshape(-1)[flat]))
+        checked += 1
+    assert checked >= 120, (checked, skipped)
+    for gi, pairs in per_group.items():
+        if not pairs:
+            continue
+        fd = np.array([a for a, _ in pairs])
+        an = np.array([b for _, b in pairs])
+        tol = 1e-4 * np.abs(fd) + 1e-4 * np.abs(fd).max()
+        assert np.all(np.abs(an - fd) <= tol), (gi, np.max(np.abs(an - fd) / (np.abs(fd) + 1e-12)))
