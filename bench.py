@@ -1,0 +1,357 @@
+"""Benchmark: fwd+bwd ms/step and render FPS of the rasterizer at 1M Gaussians.
+
+Workload (default): 1,000,000 seeded synthetic Gaussians in a 10x10x10 box
+2-12 units ahead, heavy-tailed log-scales N(-4, 1), SH degree 3, one
+1297x840 view (FoV 50 deg), dL/dimage ~ N(0, 1) -- the configuration the
+reference's headline metric is quoted on, with synthetic data standing in for
+Mip-NeRF 360.  One step = forward + backward through the drop-in API
+(GaussianRasterizer + autograd).  Per-step inputs (~0.5 GB of parameters,
+records, pair lists and sample state) exceed the 129 MB L2.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+N > 1 runs one independent replica per GPU (the path does not shard on one
+view); rank 0 prints one JSON line with the whole-job numbers.
+"--impl reference" times the FP64 CPU restatement of the reference algorithm
+(the reference has no CPU path of its own, and its CUDA build cannot run on
+this box) on all host cores, on a bounded sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "fwd+bwd ms/step & render FPS (1M Gaussians) batched vs plain, same GB300"
+WORKLOAD = "c2: 1M Gaussians, 1297x840, SH degree 3, single view, fwd+bwd"
+CPU_SAMPLE_DIV = 16     # CPU baseline renders 1/16 of the Gaussians at full resolution
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--gaussians", type=int, default=1_000_000)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    return ap.parse_args()
+
+
+# --------------------------------------------------------------------------- distributed plumbing
+def dist_setup(n_gpus: int, backend: str):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group(backend=backend)
+    return rank, local, world
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(x: float, world: int, device=None) -> float:
+    """Max of a per-rank scalar (the slowest replica defines the job time)."""
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+# --------------------------------------------------------------------------- clocks
+class ClockSampler:
+    """nvidia-smi samples every 200 ms while the timed region runs."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.path = Path(tempfile.mkstemp(suffix=".csv")[1])
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits", "-i",
+                 str(self.index), "-lms", "200"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        rows = []
+        for line in self.path.read_text().splitlines():
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                rows.append(parts)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        smax = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == "active"})
+        under_load = [v for v in sm if smax and v > 0.5 * max(smax)] or sm
+        return {"sm_mhz": statistics.median(under_load) if under_load else None,
+                "sm_max_mhz": max(smax) if smax else None, "reasons": reasons, "samples": len(rows)}
+
+
+# --------------------------------------------------------------------------- CPU baseline (oracle port)
+def cpu_baseline(steps: int, warmup: int, n_gauss: int):
+    """FP64 restatement of the reference on all host cores, on 1/16 of the
+    Gaussians at full resolution; the per-step time is scaled by 16 (pair
+    count and compositing work grow linearly with the Gaussian count)."""
+    import oracle
+    from fastergs_gb300 import scenes
+    P = max(n_gauss // CPU_SAMPLE_DIV, 1)
+    s = scenes.scene_c2(seed=0, P=P)
+    m, sc, rot, op, dc, shs = [np.asarray(a, np.float64) for a in s.activated()]
+    dL = scenes.upstream_grad(0, s.camera.height, s.camera.width).astype(np.float64)
+    times = []
+    for it in range(warmup + steps):
+        t0 = time.perf_counter()
+        o = oracle.Oracle().set_scene(m, op, sc, rot, s.camera, dc=dc, shs=shs, sh_degree=s.sh_degree)
+        o.preprocess()
+        o.emit_sort()
+        o.render()
+        o.backward(dL)
+        dt = time.perf_counter() - t0
+        if it >= warmup:
+            times.append(dt)
+    scale = n_gauss / P
+    return {"value": statistics.median(times) * 1000.0 * scale, "unit": "ms/step", "cores": oracle.num_threads(),
+            "kind": "port",
+            "sample": f"{P} of {n_gauss} Gaussians (same distribution), full 1297x840 fwd+bwd, "
+                      f"median of {steps} steps x{scale:g}"}
+
+
+# --------------------------------------------------------------------------- GPU path
+def gpu_bench(args, rank, local, world):
+    import torch
+    import fastergs_gb300 as fgs
+    from fastergs_gb300 import _C, _lib, scenes
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    s = scenes.scene_c2(seed=0, P=args.gaussians)
+    cam = s.camera
+    m, sc, rot, op, dc, shs = s.activated()
+    host = {k: torch.from_numpy(np.ascontiguousarray(v)).pin_memory()
+            for k, v in dict(means=m, scales=sc, rotations=rot, opacities=op, dc=dc, shs=shs).items()}
+    dL_host = torch.from_numpy(scenes.upstream_grad(0, cam.height, cam.width)).pin_memory()
+    dev_in = {k: v.to(dev) for k, v in host.items()}
+    dL = dL_host.to(dev)
+    t = lambda a: torch.tensor(np.asarray(a, np.float32), device=dev)
+    settings = fgs.GaussianRasterizationSettings(
+        image_height=cam.height, image_width=cam.width, tanfovx=cam.tanfovx, tanfovy=cam.tanfovy,
+        bg=torch.zeros(3, device=dev), scale_modifier=1.0, viewmatrix=t(cam.viewmatrix),
+        projmatrix=t(cam.projmatrix), sh_degree=s.sh_degree, campos=t(cam.campos), mult=1.0, prefiltered=False,
+        debug=False)
+    rast = fgs.GaussianRasterizer(settings)
+    # Size the shared buffer for this workload (FB's Buffer takes MAX_NUM_RENDERED).
+    slot = fgs._RasterizeGaussians.__dict__["buffer"]
+    slot._buf = fgs.Buffer(device=dev, MAX_NUM_RENDERED=1 << 26)
+    stream = torch.cuda.current_stream(dev)
+
+    def step(params, backward=True):
+        leaves = {k: v.detach().requires_grad_(backward) for k, v in params.items()}
+        img, radii = rast(means3D=leaves["means"], opacities=leaves["opacities"], dc=leaves["dc"],
+                          shs=leaves["shs"], scales=leaves["scales"], rotations=leaves["rotations"])
+        if backward:
+            torch.autograd.backward(img, grad_tensors=dL)
+        return img, leaves
+
+    # warm-up (also discovers K for the roofline)
+    for _ in range(args.warmup):
+        step(dev_in)
+    torch.cuda.synchronize()
+    K = int(slot._buf.curr_offset.item())
+
+    # timed region: device-resident inputs
+    barrier(world)
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        ev0.record(stream)
+        for _ in range(args.steps):
+            step(dev_in)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+    barrier(world)
+    ms_step = ev0.elapsed_time(ev1) / args.steps
+    ms_step_job = max_over_ranks(ms_step, world, dev)
+    clocks = clk.summary()
+
+    # render-only FPS (forward under no_grad)
+    with torch.no_grad():
+        for _ in range(max(args.warmup, 3)):
+            step(dev_in, backward=False)
+        torch.cuda.synchronize()
+        ev0.record(stream)
+        for _ in range(args.steps):
+            step(dev_in, backward=False)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+    fwd_ms = max_over_ranks(ev0.elapsed_time(ev1) / args.steps, world, dev)
+
+    # per-kernel device time, live, on the launch stream
+    _lib.kernel_timers(True)
+    _lib.read_kernel_timers()
+    for _ in range(args.steps):
+        step(dev_in)
+    torch.cuda.synchronize()
+    ktimes = _lib.read_kernel_timers()
+    _lib.kernel_timers(False)
+    launches_per_step = sum(c for _, c in ktimes.values()) / args.steps
+    bucket_sum = None
+
+    # end to end through the public API with host buffers
+    e2e = None
+    if not args.no_e2e:
+        in_bytes = sum(v.numel() * v.element_size() for v in host.values()) + dL_host.numel() * 4
+        out_img = torch.empty((3, cam.height, cam.width), dtype=torch.float32).pin_memory()
+        out_grads = {k: torch.empty_like(v).pin_memory() for k, v in host.items()}
+        out_bytes = out_img.numel() * 4 + sum(v.numel() * v.element_size() for v in out_grads.values())
+
+        def e2e_step():
+            d = {k: v.to(dev, non_blocking=True) for k, v in host.items()}
+            dL.copy_(dL_host, non_blocking=True)
+            img, leaves = step(d)
+            out_img.copy_(img.detach(), non_blocking=True)
+            for k, v in leaves.items():
+                out_grads[k].copy_(v.grad, non_blocking=True)
+        for _ in range(2):
+            e2e_step()
+        torch.cuda.synchronize()
+        barrier(world)
+        t0 = time.perf_counter()
+        ev0.record(stream)
+        for _ in range(args.steps):
+            e2e_step()
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        e2e_ms = max_over_ranks(ev0.elapsed_time(ev1) / args.steps, world, dev)
+        e2e = {"value": e2e_ms / world, "unit": "ms/step", "h2d_bytes_per_step": int(in_bytes),
+               "d2h_bytes_per_step": int(out_bytes), "wall_ms_per_step": (time.perf_counter() - t0) * 1e3 / args.steps}
+    return dict(ms_step=ms_step_job, fwd_ms=fwd_ms, clocks=clocks, ktimes=ktimes, K=K,
+                launches_per_step=launches_per_step, e2e=e2e, P=s.P, W=cam.width, H=cam.height)
+
+
+def roofline(res, peaks):
+    """Roofline objects for the dominant kernel (by device time)."""
+    P, K = res["P"], res["K"]
+    steps_ms = {k: v[0] for k, v in res["ktimes"].items()}
+    launches = {k: v[1] for k, v in res["ktimes"].items()}
+    sh_floats = 45
+    # algorithmic bytes per launch
+    algo = {
+        "preprocess": P * (56 + 4 * sh_floats) + P * 44 + 12 * K,
+        "sort_pass": 24 * K,
+        "sort_hist": 8 * K,
+        "render_fwd": 40 * K + 16 * 256 * math.ceil(K / 128),
+        "render_bwd": 40 * K + 16 * 256 * math.ceil(K / 128) + 48 * K,
+        "preprocess_bwd": P * (56 + 4 * sh_floats + 48) + P * (56 + 4 * sh_floats),
+        "merge": 32 * 256 * math.ceil(K / 128),
+        "tile_ranges": 8 * K,
+    }
+    dom = max(steps_ms, key=lambda k: steps_ms[k])
+    hbm = peaks.get("hbm_gbs", 6800.0)
+    per_launch_ms = steps_ms[dom] / max(launches[dom], 1)
+    b = algo.get(dom, 0)
+    achieved = b / (per_launch_ms * 1e-3) / 1e9 if per_launch_ms > 0 else 0.0
+    roof = {"kernel": dom, "bound": "hbm", "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
+            "frac": round(achieved / hbm, 4), "traffic": None,
+            "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if "hbm_gbs" in peaks else "fallback 6.8 TB/s",
+            "ms_per_launch": round(per_launch_ms, 4), "algorithmic_bytes": int(b)}
+    table = {}
+    for k in steps_ms:
+        if launches[k]:
+            pl = steps_ms[k] / launches[k]
+            entry = {"ms_per_launch": round(pl, 4), "launches": launches[k]}
+            if k in algo and pl > 0:
+                entry["hbm_frac"] = round(algo[k] / (pl * 1e-3) / 1e9 / hbm, 4)
+            table[k] = entry
+    return roof, table
+
+
+def main():
+    args = parse()
+    backend = "gloo" if args.impl == "reference" else "nccl"
+    rank, local, world = dist_setup(args.gpus, backend)
+    peaks = {}
+    pk = ROOT / "MEASURED_PEAKS.json"
+    if pk.exists():
+        peaks = json.loads(pk.read_text())
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        cb = cpu_baseline(args.steps, args.warmup, args.gaussians)
+        line = {"impl": "reference", "metric": METRIC, "value": round(cb["value"], 3), "unit": "ms/step",
+                "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(cb["value"], 3),
+                "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                "data": "synthetic", "config": {"workload": WORKLOAD, "parallelism": "cpu"},
+                "cpu_baseline": cb,
+                "e2e": {"value": round(cb["value"], 3), "unit": "ms/step", "h2d_bytes_per_step": 0,
+                        "d2h_bytes_per_step": 0}}
+        print(json.dumps(line), flush=True)
+        return
+
+    import __graft_entry__
+    __graft_entry__.build()
+    res = gpu_bench(args, rank, local, world)
+    if rank != 0:
+        barrier(world)
+        return
+    roof, table = roofline(res, peaks)
+    cb = None if args.no_cpu_baseline else cpu_baseline(1, 0, args.gaussians)
+    ms_job = res["ms_step"] / world
+    line = {
+        "metric": METRIC, "value": round(ms_job, 4), "unit": "ms/step", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(res["ms_step"], 4), "higher_is_better": False,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "gaussians": res["P"], "width": res["W"], "height": res["H"],
+                   "pairs_K": res["K"], "parallelism": f"replicas{world}", "l2": "per-step inputs exceed L2"},
+        "render_fps": round(1000.0 / res["fwd_ms"] * world, 2),
+        "render_ms": round(res["fwd_ms"], 4),
+        "e2e": res["e2e"], "gpu_launches": int(round(res["launches_per_step"] * args.steps)),
+        "clocks": res["clocks"], "roofline": roof, "kernels": table, "cpu_baseline": cb,
+    }
+    print(json.dumps(line), flush=True)
+    barrier(world)
+
+
+if __name__ == "__main__":
+    main()

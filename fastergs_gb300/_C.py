@@ -139,6 +139,7 @@ def render_16x16(P, num_rendered, width, height, splat_buffer, gaussian_keys_sor
     if bg.numel() != 3:
         raise ValueError("bg must hold 3 values")
     mb, ib, sb = state_sizes(num_rendered, width, height, TILE, TILE, bucket_size)
+    mb = max(mb, 1)
     rows = mb + 1
     if rows * _SAMPLE_ROW < sb:
         raise RuntimeError("sample-state row sizing is inconsistent with the library")
@@ -185,6 +186,11 @@ def backward(degree, bucket_sum, means3D, radii, dc, sh, opacities, scales, rota
     ro = _f32("rotations", rotations, dev)
     dL = _f32("dL_dout_color", dL_dout_color, dev)
     bg = _f32("background", background, dev)
+    campos = _f32("campos", campos, dev)
+    viewmatrix = _f32("viewmatrix", viewmatrix, dev)
+    projmatrix = _f32("projmatrix", projmatrix, dev)
+    if dL.numel() != 3 * int(width) * int(height):
+        raise ValueError("dL_dout_color must be (3, H, W)")
     mb = smp_func.size(0) - 1
     s = _stream(dev)
     _lib.call("fgs_render_bwd", int(P), int(width), int(height), int(block_x), int(block_y), int(bucket_size),

@@ -37,12 +37,13 @@ SIGNATURES = {
                                  vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp]),
     "fgs_densify_stats": (i32, [i32, vp, vp, vp, vp, vp, vp, vp]),
     "fgs_adam_update": (i32, [vp, vp, vp, vp, vp, f32, f32, f32, f32, C.c_uint32, C.c_uint32, vp]),
+    "fgs_kernel_timer": (i32, [i32, i32]),
+    "fgs_kernel_timer_read": (i32, [i32, C.POINTER(C.c_double), C.POINTER(C.c_int)]),
 }
 
-OPTIONAL = {
-    # batched multi-view entry points (present when batched.cu is built)
-    "fgs_batched_plan_bytes": None,
-}
+# Kernel ids of fgs_kernel_timer (include/fgs.h).
+KERNELS = {"preprocess": 0, "preprocess_large": 1, "sort_hist": 2, "sort_pass": 3, "tile_ranges": 4,
+           "bucket_setup": 5, "render_fwd": 6, "merge": 7, "render_bwd": 8, "preprocess_bwd": 9}
 
 
 class FgsError(RuntimeError):
@@ -87,3 +88,19 @@ def call(name: str, *args):
     st = getattr(load(), name)(*args)
     check(name, st)
     return st
+
+
+def kernel_timers(enable: bool, names=None) -> None:
+    """Turn per-kernel event timing on or off (all kernels by default)."""
+    for n in names or KERNELS:
+        call("fgs_kernel_timer", KERNELS[n], int(enable))
+
+
+def read_kernel_timers(names=None) -> dict:
+    """{name: (total_ms, launches)} since the previous read; synchronises."""
+    out = {}
+    for n in names or KERNELS:
+        ms, cnt = C.c_double(0.0), C.c_int(0)
+        call("fgs_kernel_timer_read", KERNELS[n], C.byref(ms), C.byref(cnt))
+        out[n] = (float(ms.value), int(cnt.value))
+    return out

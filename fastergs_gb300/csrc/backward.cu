@@ -154,7 +154,7 @@ __global__ void __launch_bounds__(kBwdWarps * kWarp) k_render_bwd(const BwdArgs 
           Pd[k] = fmaf(w, cd, Pd[k]);
           const float inv = __frcp_rn(1.f - al);
           const float dLda = T[k] * cd - inv * (K[k] - Pd[k]);
-          T[k] -= w;
+          T[k] = fmaf(-al, T[k], T[k]);  // T (1 - alpha), rounded once
           v[8] = fmaf(w, Lr[k], v[8]);
           v[9] = fmaf(w, Lg[k], v[9]);
           v[10] = fmaf(w, Lb[k], v[10]);
@@ -263,11 +263,6 @@ __global__ void __launch_bounds__(256) k_preprocess_bwd(const PbwdArgs a) {
   const float sv[3] = {a.smod * a.scales[3 * (size_t)i], a.smod * a.scales[3 * (size_t)i + 1],
                        a.smod * a.scales[3 * (size_t)i + 2]};
   const float s2[3] = {sv[0] * sv[0], sv[1] * sv[1], sv[2] * sv[2]};
-  float S[3][3];
-#pragma unroll
-  for (int r = 0; r < 3; ++r)
-#pragma unroll
-    for (int c = 0; c < 3; ++c) S[r][c] = R[r][0] * s2[0] * R[c][0] + R[r][1] * s2[1] * R[c][1] + R[r][2] * s2[2] * R[c][2];
   // --- conic -> cov2D -> cov3D / mean (FB backward.cu:250-403)
   const float3 t = xform_point3(a.view, p);
   const float limx = 1.3f * a.tanx, limy = 1.3f * a.tany;
@@ -285,21 +280,15 @@ __global__ void __launch_bounds__(256) k_preprocess_bwd(const PbwdArgs a) {
     M0[b] = j00 * V[b * 4 + 0] + j02 * V[b * 4 + 2];
     M1[b] = j11 * V[b * 4 + 1] + j12 * V[b * 4 + 2];
   }
-  float SM0[3], SM1[3];
-#pragma unroll
-  for (int b = 0; b < 3; ++b) {
-    SM0[b] = S[b][0] * M0[0] + S[b][1] * M0[1] + S[b][2] * M0[2];
-    SM1[b] = S[b][0] * M1[0] + S[b][1] * M1[1] + S[b][2] * M1[2];
-  }
-  const float ca = M0[0] * SM0[0] + M0[1] * SM0[1] + M0[2] * SM0[2] + 0.3f;
-  const float cb = M0[0] * SM1[0] + M0[1] * SM1[1] + M0[2] * SM1[2];
-  const float cc = M1[0] * SM1[0] + M1[1] * SM1[1] + M1[2] * SM1[2] + 0.3f;
+  const ScreenCov sc2 = screen_cov(M0, M1, R, s2);
+  const float ca = sc2.a, cb = sc2.b, cc = sc2.c, den = sc2.det;
   const float gx = gcn.x, gy = gcn.y, gz = gcn.w;
-  const float den = ca * cc - cb * cb;
+  // dL/d(a, b, c) of the conic (c, -b, a) / den, with den - a c = -b^2.
   const float d2 = 1.f / (den * den + 0.0000001f);
-  const float dLa = d2 * (-cc * cc * gx + 2.f * cb * cc * gy + (den - ca * cc) * gz);
-  const float dLc = d2 * (-ca * ca * gz + 2.f * ca * cb * gy + (den - ca * cc) * gx);
+  const float dLa = d2 * (-cc * cc * gx + 2.f * cb * cc * gy - cb * cb * gz);
+  const float dLc = d2 * (-ca * ca * gz + 2.f * ca * cb * gy - cb * cb * gx);
   const float dLb = d2 * 2.f * (cb * cc * gx - (den + 2.f * cb * cb) * gy + ca * cb * gz);
+  // dL/dSigma (3D), symmetric: M0^T M0 dLa + sym(M0^T M1) dLb + M1^T M1 dLc
   float G[3][3];
 #pragma unroll
   for (int r = 0; r < 3; ++r)
@@ -308,6 +297,13 @@ __global__ void __launch_bounds__(256) k_preprocess_bwd(const PbwdArgs a) {
       G[r][c] = M0[r] * M0[c] * dLa + 0.5f * (M0[r] * M1[c] + M0[c] * M1[r]) * dLb + M1[r] * M1[c] * dLc;
   gc[0] = G[0][0]; gc[1] = 2.f * G[0][1]; gc[2] = 2.f * G[0][2];
   gc[3] = G[1][1]; gc[4] = 2.f * G[1][2]; gc[5] = G[2][2];
+  // Sigma M_a^T = R diag(s2) N_a^T
+  float SM0[3], SM1[3];
+#pragma unroll
+  for (int b = 0; b < 3; ++b) {
+    SM0[b] = R[b][0] * s2[0] * sc2.N0[0] + R[b][1] * s2[1] * sc2.N0[1] + R[b][2] * s2[2] * sc2.N0[2];
+    SM1[b] = R[b][0] * s2[0] * sc2.N1[0] + R[b][1] * s2[1] * sc2.N1[1] + R[b][2] * s2[2] * sc2.N1[2];
+  }
   float dM0[3], dM1[3];
 #pragma unroll
   for (int b = 0; b < 3; ++b) {
@@ -392,21 +388,20 @@ __global__ void __launch_bounds__(256) k_preprocess_bwd(const PbwdArgs a) {
     if (gsh) for (int k = 0; k < 3 * a.M; ++k) gsh[k] = 0.f;
   }
   gm[0] = m3[0]; gm[1] = m3[1]; gm[2] = m3[2];
-  // --- scale / rotation: Sigma = R diag(s^2) R^T (FB backward.cu:407-483)
+  // --- scale / rotation: Sigma = R diag(s^2) R^T (FB backward.cu:407-483).
+  // R_k^T G R_k = N0k^2 dLa + N0k N1k dLb + N1k^2 dLc with N = M R.
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
-    float acc = 0.f;
-#pragma unroll
-    for (int r = 0; r < 3; ++r)
-#pragma unroll
-      for (int c = 0; c < 3; ++c) acc += G[r][c] * R[r][k] * R[c][k];
-    gs[k] = 2.f * sv[k] * acc;  // w.r.t. the modified scale, as FB returns it
+    const float n0 = sc2.N0[k], n1 = sc2.N1[k];
+    gs[k] = 2.f * sv[k] * (n0 * n0 * dLa + n0 * n1 * dLb + n1 * n1 * dLc);  // w.r.t. the modified scale
   }
-  float dR[3][3];  // 2 G R diag(s^2)
+  float dR[3][3];  // 2 G R diag(s^2), (G R)[r][k] = M0r N0k dLa + sym dLb + M1r N1k dLc
 #pragma unroll
   for (int r = 0; r < 3; ++r)
 #pragma unroll
-    for (int c = 0; c < 3; ++c) dR[r][c] = 2.f * (G[r][0] * R[0][c] + G[r][1] * R[1][c] + G[r][2] * R[2][c]) * s2[c];
+    for (int k = 0; k < 3; ++k)
+      dR[r][k] = 2.f * s2[k] *
+                 (M0[r] * sc2.N0[k] * dLa + 0.5f * (M0[r] * sc2.N1[k] + M1[r] * sc2.N0[k]) * dLb + M1[r] * sc2.N1[k] * dLc);
   const float dqr = 2.f * qz * (dR[1][0] - dR[0][1]) + 2.f * qy * (dR[0][2] - dR[2][0]) + 2.f * qx * (dR[2][1] - dR[1][2]);
   const float dqx = 2.f * qy * (dR[0][1] + dR[1][0]) + 2.f * qz * (dR[0][2] + dR[2][0]) +
                     2.f * qr * (dR[2][1] - dR[1][2]) - 4.f * qx * (dR[1][1] + dR[2][2]);
@@ -466,7 +461,11 @@ extern "C" fgs_status fgs_render_bwd(int P, int width, int height, int block_x, 
   BwdArgs a{splat_buffer, values_sorted, ranges, sm.bucket_tile, im.bucket_off, im.bucket_sum, im.max_contrib,
             sm.samples, im.pix_color, Ts_final, last_contributor, dL_dpixels, bg, grad_record,
             width, height, block_x, block_y, gx, bucket_size};
-  k_render_bwd<<<num_sms() * 8, kBwdWarps * kWarp, 0, s>>>(a);
+  {
+    KernelTimer kt__(FGS_K_RENDER_BWD, s);
+    k_render_bwd<<<num_sms() * 8, kBwdWarps * kWarp, 0, s>>>(a);
+    kt__.stop();
+  }
   FGS_LAUNCH_CHECK();
   return FGS_OK;
 }
@@ -500,7 +499,11 @@ extern "C" fgs_status fgs_preprocess_bwd(
   a.dmean3D = dL_dmean3D; a.dcov3D = dL_dcov3D; a.ddc = dL_ddc; a.dsh = shs ? dL_dsh : (M > 0 ? dL_dsh : nullptr);
   a.dscale = dL_dscale; a.drot = dL_drot;
   a.accum = xyz_gradient_accum; a.accum_abs = xyz_gradient_accum_abs; a.max_radii = max_radii; a.denom = denom;
-  k_preprocess_bwd<<<(P + 255) / 256, 256, 0, (cudaStream_t)stream>>>(a);
+  {
+    KernelTimer kt__(FGS_K_PREPROCESS_BWD, (cudaStream_t)stream);
+    k_preprocess_bwd<<<(P + 255) / 256, 256, 0, (cudaStream_t)stream>>>(a);
+    kt__.stop();
+  }
   FGS_LAUNCH_CHECK();
   return FGS_OK;
 }

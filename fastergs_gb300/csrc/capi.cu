@@ -1,6 +1,8 @@
 // Library-wide C entry points: status strings, device error word, SM count
 // cache, and the masked Adam step.
 #include <mutex>
+#include <utility>
+#include <vector>
 
 #include "fgs_common.cuh"
 
@@ -17,6 +19,41 @@ int num_sms() {
     cache[dev] = n;
   }
   return cache[dev];
+}
+
+namespace {
+struct TimerSlot {
+  std::mutex mu;
+  bool enabled = false;
+  std::vector<std::pair<cudaEvent_t, cudaEvent_t>> pairs;  // recorded since the last read
+  cudaEvent_t open = nullptr;
+};
+TimerSlot g_timers[FGS_K_COUNT];
+
+}  // namespace
+
+void timer_begin(int id, cudaStream_t s) {
+  if (id < 0 || id >= FGS_K_COUNT) return;
+  TimerSlot& t = g_timers[id];
+  if (!t.enabled) return;
+  std::lock_guard<std::mutex> lk(t.mu);
+  cudaEvent_t e = nullptr;
+  cudaEventCreate(&e);
+  cudaEventRecord(e, s);
+  t.open = e;
+}
+
+void timer_end(int id, cudaStream_t s) {
+  if (id < 0 || id >= FGS_K_COUNT) return;
+  TimerSlot& t = g_timers[id];
+  if (!t.enabled) return;
+  std::lock_guard<std::mutex> lk(t.mu);
+  if (!t.open) return;
+  cudaEvent_t e = nullptr;
+  cudaEventCreate(&e);
+  cudaEventRecord(e, s);
+  t.pairs.emplace_back(t.open, e);
+  t.open = nullptr;
 }
 
 namespace {
@@ -76,5 +113,30 @@ extern "C" fgs_status fgs_adam_update(float* param, const float* grad, float* ex
   fgs::k_adam<<<(unsigned)((cnt + 255) / 256), 256, 0, (cudaStream_t)stream>>>(param, grad, exp_avg, exp_avg_sq,
                                                                                visible, lr, b1, b2, eps, N, M);
   FGS_LAUNCH_CHECK();
+  return FGS_OK;
+}
+
+extern "C" fgs_status fgs_kernel_timer(int kernel_id, int enable) {
+  if (kernel_id < 0 || kernel_id >= FGS_K_COUNT) return FGS_ERR_BAD_ARG;
+  fgs::g_timers[kernel_id].enabled = enable != 0;
+  return FGS_OK;
+}
+
+extern "C" fgs_status fgs_kernel_timer_read(int kernel_id, double* total_ms, int* launches) {
+  if (kernel_id < 0 || kernel_id >= FGS_K_COUNT || !total_ms || !launches) return FGS_ERR_BAD_ARG;
+  auto& t = fgs::g_timers[kernel_id];
+  std::lock_guard<std::mutex> lk(t.mu);
+  double sum = 0.0;
+  for (auto& pr : t.pairs) {
+    float ms = 0.f;
+    if (cudaEventSynchronize(pr.second) != cudaSuccess) return FGS_ERR_CUDA;
+    if (cudaEventElapsedTime(&ms, pr.first, pr.second) != cudaSuccess) return FGS_ERR_CUDA;
+    sum += ms;
+    cudaEventDestroy(pr.first);
+    cudaEventDestroy(pr.second);
+  }
+  *total_ms = sum;
+  *launches = (int)t.pairs.size();
+  t.pairs.clear();
   return FGS_OK;
 }

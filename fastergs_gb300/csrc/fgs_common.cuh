@@ -85,6 +85,45 @@ __device__ __forceinline__ float4 xform_point4(const float* m, float3 p) {
                      m[2] * p.x + m[6] * p.y + m[10] * p.z + m[14], m[3] * p.x + m[7] * p.y + m[11] * p.z + m[15]);
 }
 
+// Kahan's 2x2 determinant a*d - b*c with one rounding of the cancelling part.
+__device__ __forceinline__ float det2_kahan(float a, float b, float c, float d) {
+  const float w = b * c;
+  const float e = fmaf(-b, c, w);
+  const float f = fmaf(a, d, -w);
+  return f + e;
+}
+
+// Screen covariance of a 3D Gaussian Sigma = R diag(s2) R^T seen through the
+// 2x3 EWA Jacobian M:  Sigma2 = N diag(s2) N^T + 0.3 I with N = M R.  The
+// determinant is the Cauchy-Binet sum of squared 2x2 minors plus the
+// low-pass terms, all non-negative, so it keeps full FP32 accuracy for thin,
+// elongated footprints where a*c - b*b cancels (the relative error of the
+// latter grows with the footprint's condition number).
+struct ScreenCov {
+  float a, b, c, det;   // a, c include the 0.3 low-pass
+  float N0[3], N1[3];   // rows of M R
+};
+__device__ __forceinline__ ScreenCov screen_cov(const float M0[3], const float M1[3], const float R[3][3],
+                                                const float s2[3]) {
+  ScreenCov r;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    r.N0[k] = M0[0] * R[0][k] + M0[1] * R[1][k] + M0[2] * R[2][k];
+    r.N1[k] = M1[0] * R[0][k] + M1[1] * R[1][k] + M1[2] * R[2][k];
+  }
+  const float ap = s2[0] * r.N0[0] * r.N0[0] + s2[1] * r.N0[1] * r.N0[1] + s2[2] * r.N0[2] * r.N0[2];
+  const float cp = s2[0] * r.N1[0] * r.N1[0] + s2[1] * r.N1[1] * r.N1[1] + s2[2] * r.N1[2] * r.N1[2];
+  r.b = s2[0] * r.N0[0] * r.N1[0] + s2[1] * r.N0[1] * r.N1[1] + s2[2] * r.N0[2] * r.N1[2];
+  const float m01 = det2_kahan(r.N0[0], r.N0[1], r.N1[0], r.N1[1]);
+  const float m02 = det2_kahan(r.N0[0], r.N0[2], r.N1[0], r.N1[2]);
+  const float m12 = det2_kahan(r.N0[1], r.N0[2], r.N1[1], r.N1[2]);
+  const float detp = s2[0] * s2[1] * m01 * m01 + s2[0] * s2[2] * m02 * m02 + s2[1] * s2[2] * m12 * m12;
+  r.a = ap + 0.3f;
+  r.c = cp + 0.3f;
+  r.det = detp + 0.3f * (ap + cp) + 0.09f;
+  return r;
+}
+
 // Device error word; one per translation unit (no relocatable device code),
 // each unit exposes it through FGS_DEFINE_ERROR_ACCESSOR.
 static __device__ int g_error_word;
@@ -96,6 +135,16 @@ cudaError_t errors_preprocess(int* out, bool clear, cudaStream_t s);
 cudaError_t errors_sort(int* out, bool clear, cudaStream_t s);
 cudaError_t errors_render(int* out, bool clear, cudaStream_t s);
 cudaError_t errors_backward(int* out, bool clear, cudaStream_t s);
+// Optional per-kernel event timing (fgs_kernel_timer).  Usage around a launch:
+//   KernelTimer kt(FGS_K_RENDER_FWD, stream); launch...; kt.stop();
+void timer_begin(int id, cudaStream_t s);
+void timer_end(int id, cudaStream_t s);
+struct KernelTimer {
+  int id;
+  cudaStream_t s;
+  KernelTimer(int id_, cudaStream_t s_) : id(id_), s(s_) { timer_begin(id, s); }
+  void stop() { timer_end(id, s); }
+};
 inline int tile_bits(uint32_t tiles) {
   int b = 0;
   while (b < 32 && (1u << b) < tiles) ++b;

@@ -212,20 +212,16 @@ __global__ void __launch_bounds__(kPreThreads) k_preprocess(const PreArgs a) {
         M0[b] = j00 * V[b * 4 + 0] + j02 * V[b * 4 + 2];
         M1[b] = j11 * V[b * 4 + 1] + j12 * V[b * 4 + 2];
       }
-      const float SM0[3] = {S[0] * M0[0] + S[1] * M0[1] + S[2] * M0[2], S[1] * M0[0] + S[3] * M0[1] + S[4] * M0[2],
-                            S[2] * M0[0] + S[4] * M0[1] + S[5] * M0[2]};
-      const float SM1[3] = {S[0] * M1[0] + S[1] * M1[1] + S[2] * M1[2], S[1] * M1[0] + S[3] * M1[1] + S[4] * M1[2],
-                            S[2] * M1[0] + S[4] * M1[1] + S[5] * M1[2]};
-      const float ca = M0[0] * SM0[0] + M0[1] * SM0[1] + M0[2] * SM0[2] + 0.3f;
-      const float cb = M0[0] * SM1[0] + M0[1] * SM1[1] + M0[2] * SM1[2];
-      const float cc = M1[0] * SM1[0] + M1[1] * SM1[1] + M1[2] * SM1[2] + 0.3f;
-      const float det = ca * cc - cb * cb;
+      const ScreenCov sc2 = screen_cov(M0, M1, R, s2);
+      const float ca = sc2.a, cb = sc2.b, cc = sc2.c, det = sc2.det;
       const float det_inv = 1.0f / det;
       const float3 conic = f3(cc * det_inv, -cb * det_inv, ca * det_inv);
       // Reported radius (FB preprocess.cu:480-485; the 3.33 bound is a double there).
       const float mid = 0.5f * (ca + cc);
       const double extent = fmin(3.33, (double)sqrtf(2.0f * logf(o * 255.0f)));
-      const float lambda = mid + sqrtf(fmaxf(0.01f, mid * mid - det));
+      // mid^2 - det written as ((a - c)/2)^2 + b^2, which does not cancel
+      const float hd = 0.5f * (ca - cc);
+      const float lambda = mid + sqrtf(fmaxf(0.01f, hd * hd + cb * cb));
       radius = (float)ceil(extent * (double)sqrtf(lambda));
       // Tile rectangle of the 1/256 level set (FB preprocess.cu:488-497).
       const float log2o = lg2_approx(o);
@@ -417,9 +413,17 @@ extern "C" fgs_status fgs_preprocess(
   a.cap = pair_capacity; a.tasks = task_scratch; a.task_cap = task_scratch_words / 2;
   a.curr = reinterpret_cast<unsigned int*>(curr_offset); a.counters = counters; a.radii = radii;
   FGS_TRY(cudaMemsetAsync(counters, 0, FGS_COUNTER_WORDS * sizeof(int32_t), s));
-  k_preprocess<<<(P + kPreThreads - 1) / kPreThreads, kPreThreads, 0, s>>>(a);
+  {
+    KernelTimer kt__(FGS_K_PREPROCESS, s);
+    k_preprocess<<<(P + kPreThreads - 1) / kPreThreads, kPreThreads, 0, s>>>(a);
+    kt__.stop();
+  }
   FGS_LAUNCH_CHECK();
-  k_preprocess_large<<<num_sms() * 4, kPreThreads, 0, s>>>(a);
+  {
+    KernelTimer kt__(FGS_K_PREPROCESS_LARGE, s);
+    k_preprocess_large<<<num_sms() * 4, kPreThreads, 0, s>>>(a);
+    kt__.stop();
+  }
   FGS_LAUNCH_CHECK();
   return FGS_OK;
 }

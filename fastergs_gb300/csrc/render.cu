@@ -25,15 +25,19 @@ namespace {
 constexpr int kFwdWarps = 4;
 
 __global__ void __launch_bounds__(256) k_tile_ranges(const unsigned long long* __restrict__ keys, long long n,
-                                                     uint32_t* __restrict__ ranges) {
+                                                     uint32_t num_tiles, uint32_t* __restrict__ ranges) {
   const long long i = blockIdx.x * 256ll + threadIdx.x;
   if (i >= n) return;
   const uint32_t t = (uint32_t)(keys[i] >> 32);
+  if (t >= num_tiles) {  // not a key of this frame
+    raise_error(kErrCapacity);
+    return;
+  }
   if (i == 0) {
     ranges[2 * t] = 0;
   } else {
     const uint32_t pt = (uint32_t)(keys[i - 1] >> 32);
-    if (pt != t) {
+    if (pt != t && pt < num_tiles) {
       ranges[2 * pt + 1] = (uint32_t)i;
       ranges[2 * t] = (uint32_t)i;
     }
@@ -126,7 +130,7 @@ __global__ void __launch_bounds__(kFwdWarps * kWarp) k_render_fwd(const FwdArgs 
         Cr[k] = fmaf(c.x, w, Cr[k]);
         Cg[k] = fmaf(c.y, w, Cg[k]);
         Cb[k] = fmaf(c.z, w, Cb[k]);
-        T[k] -= w;
+        T[k] = fmaf(-al, T[k], T[k]);  // T (1 - alpha), rounded once
         dy -= ystep;
       }
     }
@@ -140,6 +144,7 @@ __global__ void __launch_bounds__(kFwdWarps * kWarp) k_render_fwd(const FwdArgs 
 struct MergeArgs {
   const uint32_t* ranges;
   const uint32_t* bucket_off;
+  const uint32_t* bucket_sum;
   float4* samples;
   const float* bg;
   float* out_color;
@@ -157,7 +162,10 @@ __global__ void __launch_bounds__(kTilePixels) k_merge(const MergeArgs a) {
   const int tile = blockIdx.x, p = threadIdx.x;
   const int px = (tile % a.gx) * a.bx + p % a.bx, py = (tile / a.gx) * a.by + p / a.bx;
   const bool in = px < a.W && py < a.H;
-  const int first = tile ? (int)a.bucket_off[tile - 1] : 0, last = (int)a.bucket_off[tile];
+  // bucket_sum[0] is the bucket count clamped to the sample capacity.
+  const int cap = (int)a.bucket_sum[0];
+  const int first = min(cap, tile ? (int)a.bucket_off[tile - 1] : 0);
+  const int last = min(cap, (int)a.bucket_off[tile]);
   const int rs = (int)a.ranges[2 * tile], re = (int)a.ranges[2 * tile + 1];
   float T = 1.f, Cr = 0.f, Cg = 0.f, Cb = 0.f;
   uint32_t contrib = 0;
@@ -211,8 +219,10 @@ extern "C" fgs_status fgs_tile_ranges(int64_t num_rendered, int num_tiles, const
   cudaStream_t s = (cudaStream_t)stream;
   FGS_TRY(cudaMemsetAsync(ranges, 0, sizeof(uint32_t) * 2 * (size_t)num_tiles, s));
   if (num_rendered > 0) {
+    KernelTimer kt__(FGS_K_TILE_RANGES, s);
     k_tile_ranges<<<(unsigned)((num_rendered + 255) / 256), 256, 0, s>>>(
-        reinterpret_cast<const unsigned long long*>(keys_sorted), num_rendered, ranges);
+        reinterpret_cast<const unsigned long long*>(keys_sorted), num_rendered, (uint32_t)num_tiles, ranges);
+    kt__.stop();
     FGS_LAUNCH_CHECK();
   }
   return FGS_OK;
@@ -258,16 +268,28 @@ extern "C" fgs_status fgs_render_fwd(int P, int64_t num_rendered, int width, int
   cudaStream_t s = (cudaStream_t)stream;
   fgs_status st = fgs_tile_ranges(num_rendered, T, keys_sorted, ranges, stream);
   if (st != FGS_OK) return st;
-  k_bucket_setup<<<1, 1024, 0, s>>>(T, ranges, bucket_size, max_buckets, im.bucket_off, sm.bucket_tile,
+  {
+    KernelTimer kt__(FGS_K_BUCKET_SETUP, s);
+    k_bucket_setup<<<1, 1024, 0, s>>>(T, ranges, bucket_size, max_buckets, im.bucket_off, sm.bucket_tile,
                                     im.bucket_sum);
+    kt__.stop();
+  }
   FGS_LAUNCH_CHECK();
   FwdArgs fa{splat_buffer, values_sorted, ranges, sm.bucket_tile, im.bucket_off, im.bucket_sum, sm.samples,
              width, height, block_x, block_y, gx, bucket_size};
-  k_render_fwd<<<num_sms() * 8, kFwdWarps * kWarp, 0, s>>>(fa);
+  {
+    KernelTimer kt__(FGS_K_RENDER_FWD, s);
+    k_render_fwd<<<num_sms() * 8, kFwdWarps * kWarp, 0, s>>>(fa);
+    kt__.stop();
+  }
   FGS_LAUNCH_CHECK();
-  MergeArgs ma{ranges, im.bucket_off, sm.samples, bg, out_color, im.pix_color, last_contributor, Ts_final,
+  MergeArgs ma{ranges, im.bucket_off, im.bucket_sum, sm.samples, bg, out_color, im.pix_color, last_contributor, Ts_final,
                im.max_contrib, width, height, block_x, block_y, gx, bucket_size};
-  k_merge<<<T, kTilePixels, 0, s>>>(ma);
+  {
+    KernelTimer kt__(FGS_K_MERGE, s);
+    k_merge<<<T, kTilePixels, 0, s>>>(ma);
+    kt__.stop();
+  }
   FGS_LAUNCH_CHECK();
   if (bucket_sum_host) {
     uint32_t hs[2] = {0, 0};

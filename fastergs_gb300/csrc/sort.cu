@@ -210,8 +210,12 @@ __global__ void __launch_bounds__(kSortThreads) k_onesweep(
   for (int j = tid; j < valid; j += kSortThreads) {
     const unsigned long long kk = s_keys[j];
     const uint32_t pos = s_dst[(uint32_t)(kk >> shift) & 0xff] + (uint32_t)j;
-    keys_out[pos] = kk;
-    vals_out[pos] = s_vals[j];
+    if ((long long)pos < n) {
+      keys_out[pos] = kk;
+      vals_out[pos] = s_vals[j];
+    } else {
+      raise_error(kErrTimeout);  // only reachable after an expired look-back
+    }
   }
 }
 
@@ -250,8 +254,12 @@ extern "C" fgs_status fgs_sort(int64_t num_rendered, int width, int height, int 
   FGS_TRY(cudaMemsetAsync(base, 0, L.alt_keys, s));
   const int hist_blocks = (int)std::min<int64_t>((num_rendered + kSortThreads * 8 - 1) / (kSortThreads * 8),
                                                  (int64_t)num_sms() * 8);
-  k_histogram<<<hist_blocks, kSortThreads, 0, s>>>(reinterpret_cast<const unsigned long long*>(keys_in),
+  {
+    KernelTimer kt__(FGS_K_SORT_HIST, s);
+    k_histogram<<<hist_blocks, kSortThreads, 0, s>>>(reinterpret_cast<const unsigned long long*>(keys_in),
                                                    num_rendered, passes, hist);
+    kt__.stop();
+  }
   FGS_LAUNCH_CHECK();
   static bool smem_set = false;  // per process; the attribute is per function, not per device
   if (!smem_set) {
@@ -265,10 +273,14 @@ extern "C" fgs_status fgs_sort(int64_t num_rendered, int width, int height, int 
     const bool to_out = ((passes - 1 - p) % 2) == 0;
     unsigned long long* dk = to_out ? reinterpret_cast<unsigned long long*>(keys_out) : alt_k;
     uint32_t* dv = to_out ? values_out : alt_v;
-    k_onesweep<<<(unsigned)L.tiles, kSortThreads, kSortDynSmem, s>>>(src_k, src_v, dk, dv, num_rendered, 8 * p,
+    {
+      KernelTimer kt__(FGS_K_SORT_PASS, s);
+      k_onesweep<<<(unsigned)L.tiles, kSortThreads, kSortDynSmem, s>>>(src_k, src_v, dk, dv, num_rendered, 8 * p,
                                                           hist + p * kRadix,
                                                           lookback + (size_t)p * L.tiles * kRadix, counters + p);
-    FGS_LAUNCH_CHECK();
+      kt__.stop();
+    }
+  FGS_LAUNCH_CHECK();
     src_k = dk;
     src_v = dv;
   }

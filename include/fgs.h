@@ -163,6 +163,19 @@ fgs_status fgs_adam_update(float* param, const float* grad, float* exp_avg, floa
                            const uint8_t* visible, float lr, float b1, float b2, float eps,
                            uint32_t N, uint32_t M, void* stream);
 
+/* Kernel-level timing for benchmarks.  While enabled for a kernel id, the
+ * library records a CUDA event pair around every launch of that kernel on its
+ * launch stream; fgs_kernel_timer_read synchronises those events and returns
+ * the summed device time and launch count since the last read.  No
+ * counterpart in FB (its DEBUG_TIME macros are unused, ops.h:10-14). */
+enum {
+  FGS_K_PREPROCESS = 0, FGS_K_PREPROCESS_LARGE = 1, FGS_K_SORT_HIST = 2, FGS_K_SORT_PASS = 3,
+  FGS_K_TILE_RANGES = 4, FGS_K_BUCKET_SETUP = 5, FGS_K_RENDER_FWD = 6, FGS_K_MERGE = 7,
+  FGS_K_RENDER_BWD = 8, FGS_K_PREPROCESS_BWD = 9, FGS_K_COUNT = 10
+};
+fgs_status fgs_kernel_timer(int kernel_id, int enable);
+fgs_status fgs_kernel_timer_read(int kernel_id, double* total_ms, int* launches);
+
 #ifdef __cplusplus
 }
 #endif

@@ -58,7 +58,9 @@ def test_capacity_overflow_raises(cuda_device):
     slot = _RasterizeGaussians.__dict__["buffer"]  # the lazily allocated shared Buffer
     old = slot._buf
     try:
-        slot._buf = Buffer(device=cuda_device, MAX_NUM_RENDERED=1024)
+        small = Buffer(device=cuda_device, MAX_NUM_RENDERED=1024)
+        small.splat_buffer = torch.zeros((s.P, 32), device=cuda_device)  # room for every Gaussian's record
+        slot._buf = small
         with pytest.raises(RuntimeError, match="Too many k-v pairs"):
             render(s, raw_params(s, cuda_device), cuda_device)
     finally:
