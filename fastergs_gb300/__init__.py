@@ -92,9 +92,10 @@ class _RasterizeGaussians(torch.autograd.Function):
             buffer.gaussian_keys_unsorted, buffer.gaussian_values_unsorted, buffer.gaussian_values_sorted,
             buffer.curr_offset, raster_settings.mult, splat_buffer, culling)
         num_rendered = int(buffer.curr_offset.cpu()[0])
+        device_errors = _C.device_errors(means3D.device)  # read and cleared either way
         if num_rendered >= buffer.MAX_NUM_RENDERED:
             raise RuntimeError("Too many k-v pairs!")
-        if _C.device_errors(means3D.device):
+        if device_errors:
             raise RuntimeError("preprocess overflowed a device queue (too many large Gaussians)")
         _C.ops.sort_gaussian(num_rendered, raster_settings.image_width, raster_settings.image_height, 16, 16,
                              buffer.list_sorting_space, buffer.gaussian_keys_unsorted,

@@ -79,7 +79,6 @@ __global__ void __launch_bounds__(kBwdWarps * kWarp) k_render_bwd(const BwdArgs 
   const int B = (int)a.bucket_sum[0];
   const int lx = lane % a.bx, ly0 = lane / a.bx;
   const int rows = kWarp / a.bx;
-  const float ystep = (float)rows;
   const int HW = a.W * a.H;
   const float hx = 0.5f * (float)a.W, hy = 0.5f * (float)a.H;
   const float bgr = a.bg[0], bgg = a.bg[1], bgb = a.bg[2];
@@ -131,36 +130,38 @@ __global__ void __launch_bounds__(kBwdWarps * kWarp) k_render_bwd(const BwdArgs 
     }
 
     for (int g = 0; g < bi.n; ++g) {
-      const float2 xy = st.xy[g];
-      const float4 co = st.co[g];
+      const float4 pos = st.pos[g];
+      const float4 q = st.quad[g];   // A1, P, C1, log2 o
       const float4 c = st.rgb[g];
-      const float dx = xy.x - px;
-      const float A = fmaf(co.x * dx, dx, co.w);
-      const float Bx = co.y * dx;
-      const float gx0 = 2.f * co.x * dx;
-      float dy = xy.y - py0;
+      const float dx = centre_offset(pos.x, pos.z, px);
+      const float ry = pos.y - py0;  // exact: both are integers
+      const float A2 = 2.f * q.x, C2 = 2.f * q.z;
       float v[16];
 #pragma unroll
       for (int j = 0; j < 16; ++j) v[j] = 0.f;
       bool any = false;
 #pragma unroll
       for (int k = 0; k < kPxPerThread; ++k) {
-        const float e = fmaf(dy, fmaf(co.z, dy, Bx), A);
+        const float dy = (ry - (float)(k * rows)) + pos.w;
+        const float w = fmaf(q.y, dy, dx);
+        const float e = fmaf(q.x * w, w, fmaf(q.z * dy, dy, q.w));
         const float al = fminf(kAlphaMax, ex2_approx(e));
         if (((alive >> k) & 1u) && al >= kAlphaCut) {
           any = true;
-          const float w = al * T[k];
+          const float wt = al * T[k];
           const float cd = c.x * Lr[k] + c.y * Lg[k] + c.z * Lb[k];
-          Pd[k] = fmaf(w, cd, Pd[k]);
+          Pd[k] = fmaf(wt, cd, Pd[k]);
           const float inv = __frcp_rn(1.f - al);
           const float dLda = T[k] * cd - inv * (K[k] - Pd[k]);
-          T[k] = fmaf(-al, T[k], T[k]);  // T (1 - alpha), rounded once
-          v[8] = fmaf(w, Lr[k], v[8]);
-          v[9] = fmaf(w, Lg[k], v[9]);
-          v[10] = fmaf(w, Lb[k], v[10]);
-          const float dp = dLda * al;  // dL/dpower / ln2
-          const float tx = dp * fmaf(co.y, dy, gx0);
-          const float ty = dp * fmaf(2.f * co.z, dy, Bx);
+          T[k] = fmaf(-al, T[k], T[k]);
+          v[8] = fmaf(wt, Lr[k], v[8]);
+          v[9] = fmaf(wt, Lg[k], v[9]);
+          v[10] = fmaf(wt, Lb[k], v[10]);
+          const float dp = dLda * al;  // dL/dexponent / ln2
+          // d exponent / d(centre x) = 2 A1 w, d / d(centre y) = 2 A1 P w + 2 C1 dy
+          const float gw = A2 * w;
+          const float tx = dp * gw;
+          const float ty = dp * fmaf(gw, q.y, C2 * dy);
           v[0] += tx;
           v[1] += ty;
           v[2] += fabsf(tx);
@@ -170,12 +171,11 @@ __global__ void __launch_bounds__(kBwdWarps * kWarp) k_render_bwd(const BwdArgs 
           v[7] = fmaf(dp * dy, dy, v[7]);
           v[11] += dp;
         }
-        dy -= ystep;
       }
       if (__any_sync(0xffffffffu, any)) {
         const float tot = warp_transpose_reduce16(v, lane);
         if (!(lane & 1) && vid < FGS_GRAD_STRIDE && vid != 6) {
-          const float s = (vid == 11) ? 1.0f / ex2_approx(co.w) : vscale;
+          const float s = (vid == 11) ? 1.0f / ex2_approx(q.w) : vscale;
           atomicAdd(a.grad + (size_t)__float_as_uint(c.w) * FGS_GRAD_STRIDE + vid, tot * s);
         }
       }
@@ -281,34 +281,42 @@ __global__ void __launch_bounds__(256) k_preprocess_bwd(const PbwdArgs a) {
     M1[b] = j11 * V[b * 4 + 1] + j12 * V[b * 4 + 2];
   }
   const ScreenCov sc2 = screen_cov(M0, M1, R, s2);
-  const float ca = sc2.a, cb = sc2.b, cc = sc2.c, den = sc2.det;
-  const float gx = gcn.x, gy = gcn.y, gz = gcn.w;
-  // dL/d(a, b, c) of the conic (c, -b, a) / den, with den - a c = -b^2.
-  const float d2 = 1.f / (den * den + 0.0000001f);
-  const float dLa = d2 * (-cc * cc * gx + 2.f * cb * cc * gy - cb * cb * gz);
-  const float dLc = d2 * (-ca * ca * gz + 2.f * ca * cb * gy - cb * cb * gx);
-  const float dLb = d2 * 2.f * (cb * cc * gx - (den + 2.f * cb * cb) * gy + ca * cb * gz);
-  // dL/dSigma (3D), symmetric: M0^T M0 dLa + sym(M0^T M1) dLb + M1^T M1 dLc
-  float G[3][3];
+  const float idet = 1.f / sc2.det;
+  const float ia = sc2.c * idet, ib = -sc2.b * idet, ic = sc2.a * idet;  // C = Sigma2^-1 (the conic)
+  const float gx = gcn.x, gy = gcn.y, gz = gcn.w;  // dL/dconic, off-diagonal halved as FB stores it
+  // FB divides by den^2 + 1e-7 instead of den^2 (backward.cu:304); keep that factor.
+  const float rr = sc2.det * sc2.det / (sc2.det * sc2.det + 0.0000001f);
+  // dL/dSigma2 = rr * E with E = -C Gm C.  FB forms E and then projects it on
+  // each principal axis N_k (backward.cu:310-347, 445-454), which cancels with
+  // the square of the footprint's condition number; here every axis term is
+  // formed from v_k = C N_k instead: N_k^T E N_k = -v_k^T Gm v_k.
+  float dM0[3] = {0.f, 0.f, 0.f}, dM1[3] = {0.f, 0.f, 0.f};
+  float dR[3][3];  // dL/dR, R the rotation of the raw quaternion
 #pragma unroll
-  for (int r = 0; r < 3; ++r)
+  for (int k = 0; k < 3; ++k) {
+    const float v0 = ia * sc2.N0[k] + ib * sc2.N1[k];
+    const float v1 = ib * sc2.N0[k] + ic * sc2.N1[k];
+    const float g0 = gx * v0 + gy * v1, g1 = gy * v0 + gz * v1;
+    gs[k] = -2.f * sv[k] * rr * (v0 * g0 + v1 * g1);  // w.r.t. the modified scale, as FB returns it
+    const float y0 = ia * g0 + ib * g1, y1 = ib * g0 + ic * g1;
+    const float f = -2.f * s2[k] * rr;
 #pragma unroll
-    for (int c = 0; c < 3; ++c)
-      G[r][c] = M0[r] * M0[c] * dLa + 0.5f * (M0[r] * M1[c] + M0[c] * M1[r]) * dLb + M1[r] * M1[c] * dLc;
-  gc[0] = G[0][0]; gc[1] = 2.f * G[0][1]; gc[2] = 2.f * G[0][2];
-  gc[3] = G[1][1]; gc[4] = 2.f * G[1][2]; gc[5] = G[2][2];
-  // Sigma M_a^T = R diag(s2) N_a^T
-  float SM0[3], SM1[3];
-#pragma unroll
-  for (int b = 0; b < 3; ++b) {
-    SM0[b] = R[b][0] * s2[0] * sc2.N0[0] + R[b][1] * s2[1] * sc2.N0[1] + R[b][2] * s2[2] * sc2.N0[2];
-    SM1[b] = R[b][0] * s2[0] * sc2.N1[0] + R[b][1] * s2[1] * sc2.N1[1] + R[b][2] * s2[2] * sc2.N1[2];
+    for (int b = 0; b < 3; ++b) {
+      dR[b][k] = f * (M0[b] * y0 + M1[b] * y1);
+      dM0[b] = fmaf(f * y0, R[b][k], dM0[b]);
+      dM1[b] = fmaf(f * y1, R[b][k], dM1[b]);
+    }
   }
-  float dM0[3], dM1[3];
+  {  // dL/dcov3D in FB's storage (diagonal once, off-diagonal doubled)
+    const float c00 = ia * gx + ib * gy, c01 = ia * gy + ib * gz, c10 = ib * gx + ic * gy, c11 = ib * gy + ic * gz;
+    const float E00 = -rr * (c00 * ia + c01 * ib), E01 = -rr * (c00 * ib + c01 * ic), E11 = -rr * (c10 * ib + c11 * ic);
+    float G[3][3];
 #pragma unroll
-  for (int b = 0; b < 3; ++b) {
-    dM0[b] = 2.f * dLa * SM0[b] + dLb * SM1[b];
-    dM1[b] = 2.f * dLc * SM1[b] + dLb * SM0[b];
+    for (int r = 0; r < 3; ++r)
+#pragma unroll
+      for (int c = 0; c < 3; ++c) G[r][c] = M0[r] * M0[c] * E00 + (M0[r] * M1[c] + M1[r] * M0[c]) * E01 + M1[r] * M1[c] * E11;
+    gc[0] = G[0][0]; gc[1] = 2.f * G[0][1]; gc[2] = 2.f * G[0][2];
+    gc[3] = G[1][1]; gc[4] = 2.f * G[1][2]; gc[5] = G[2][2];
   }
   // dL/dJ[a][k] = sum_b dM[a][b] * Rw[k][b], Rw[k][b] = V[b*4 + k]
   const float dJ00 = dM0[0] * V[0] + dM0[1] * V[4] + dM0[2] * V[8];
@@ -388,20 +396,7 @@ __global__ void __launch_bounds__(256) k_preprocess_bwd(const PbwdArgs a) {
     if (gsh) for (int k = 0; k < 3 * a.M; ++k) gsh[k] = 0.f;
   }
   gm[0] = m3[0]; gm[1] = m3[1]; gm[2] = m3[2];
-  // --- scale / rotation: Sigma = R diag(s^2) R^T (FB backward.cu:407-483).
-  // R_k^T G R_k = N0k^2 dLa + N0k N1k dLb + N1k^2 dLc with N = M R.
-#pragma unroll
-  for (int k = 0; k < 3; ++k) {
-    const float n0 = sc2.N0[k], n1 = sc2.N1[k];
-    gs[k] = 2.f * sv[k] * (n0 * n0 * dLa + n0 * n1 * dLb + n1 * n1 * dLc);  // w.r.t. the modified scale
-  }
-  float dR[3][3];  // 2 G R diag(s^2), (G R)[r][k] = M0r N0k dLa + sym dLb + M1r N1k dLc
-#pragma unroll
-  for (int r = 0; r < 3; ++r)
-#pragma unroll
-    for (int k = 0; k < 3; ++k)
-      dR[r][k] = 2.f * s2[k] *
-                 (M0[r] * sc2.N0[k] * dLa + 0.5f * (M0[r] * sc2.N1[k] + M1[r] * sc2.N0[k]) * dLb + M1[r] * sc2.N1[k] * dLc);
+  // --- rotation (FB backward.cu:460-482): dL/dq from dL/dR of the raw quaternion
   const float dqr = 2.f * qz * (dR[1][0] - dR[0][1]) + 2.f * qy * (dR[0][2] - dR[2][0]) + 2.f * qx * (dR[2][1] - dR[1][2]);
   const float dqx = 2.f * qy * (dR[0][1] + dR[1][0]) + 2.f * qz * (dR[0][2] + dR[2][0]) +
                     2.f * qr * (dR[2][1] - dR[1][2]) - 4.f * qx * (dR[1][1] + dR[2][2]);

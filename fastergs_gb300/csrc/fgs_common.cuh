@@ -7,20 +7,30 @@
 
 namespace fgs {
 
-// Splat record field offsets: one 32-float (128-byte) record per Gaussian,
-// the same field map as FB (rasterizer_imp.h:27-38) so records are
-// interchangeable between the two implementations.
+// Splat record: 32 floats (128 bytes) per Gaussian.  It holds every field of
+// FB's record (rasterizer_imp.h:27-38) but orders them so the 12 floats the
+// compositing kernels read come first (three 16-byte loads, two sectors), and
+// it stores the footprint in a form that keeps full FP32 accuracy:
+//   * the exponent of alpha is log2(o) + A1 (dx + P dy)^2 + C1 dy^2, a sum of
+//     non-positive terms (FB's a dx^2 + 2b dx dy + c dy^2 cancels for thin,
+//     elongated footprints);
+//   * the pixel position is floor(x) + fx with fx taken from an FP64
+//     projection, so dx = (floor(x) - px) + fx is exact to ~1e-7 px (an FP32
+//     x near 1000 px is only good to 6e-5 px).
 enum : int {
-  F_XY = 0,       // pixel x, y
-  F_RGBD = 2,     // r, g, b, view depth
-  F_CONO = 6,     // (-0.5 log2e a, -log2e b, -0.5 log2e c, log2 opacity)
-  F_RMIN = 10,    // tile rect min (int bits)
-  F_RMAX = 12,    // tile rect max (int bits)
-  F_CONIC = 14,   // conic a, b, c
-  F_PVIEW = 17,   // view-space position
-  F_POWER = 20,   // ln(256 opacity) * mult
-  F_CLAMP = 22,   // SH clamp flags (1.0 = clamped)
-  F_COV3D = 25,   // upper triangle of the 3D covariance
+  F_XY = 0,       // pixel x, y (FP32, as FB stores them)
+  F_RGB = 2,      // r, g, b
+  F_DEPTH = 5,    // view depth (key source)
+  F_CHOL = 6,     // A1 = -0.5 log2e conic_a, P = conic_b / conic_a, C1 = -0.5 log2e / cov_c
+  F_LOG2O = 9,    // log2 opacity
+  F_FRAC = 10,    // x - floor(float(x)), y - floor(float(y)) from the FP64 projection
+  F_RMIN = 12,    // tile rect min (int bits)
+  F_RMAX = 14,    // tile rect max (int bits)
+  F_CONIC = 16,   // conic a, b, c
+  F_POWER = 19,   // ln(256 opacity) * mult
+  F_CLAMP = 20,   // SH clamp flags (1.0 = clamped)
+  F_COV3D = 23,   // upper triangle of the 3D covariance
+  F_PVIEW = 29,   // view-space position
 };
 
 constexpr int kWarp = 32;

@@ -176,9 +176,22 @@ __global__ void __launch_bounds__(kPreThreads) k_preprocess(const PreArgs a) {
       if (t.z <= 0.2f) break;                        // near cull (FB preprocess.cu:456)
       const float o = a.opac[i];
       if (255.0f * o < 1.0f) break;                  // opacity cull (FB preprocess.cu:459)
-      const float4 hp = xform_point4(a.proj, p);
-      const float pw = 1.0f / (hp.w + 0.0000001f);
-      const float ndcx = hp.x * pw, ndcy = hp.y * pw;
+      // Projection to pixels in FP64.  FB projects in FP32 and converts NDC to
+      // pixels in double (preprocess.cu:463-465, 494); an FP32 pixel position
+      // near 1000 px is only good to 6e-5 px, which would dominate the image
+      // error, so the position is formed here in FP64 and its fraction kept.
+      const float* Pm = a.proj;
+      const double px = p.x, py = p.y, pz = p.z;
+      auto row = [&](int r) {
+        return __fma_rn((double)Pm[r], px, __fma_rn((double)Pm[4 + r], py, __fma_rn((double)Pm[8 + r], pz, (double)Pm[12 + r])));
+      };
+      const double hx = row(0), hy = row(1), hw = row(3);
+      const double wden = hw + 1e-7;
+      // 1/wden: FP32 seed refined by one Newton step (relative error ~1e-14).
+      double rw = (double)(1.0f / (float)wden);
+      rw = rw * __fma_rn(-wden, rw, 2.0);
+      const double X = __fma_rn(hx * rw + 1.0, (double)a.W, -1.0) * 0.5;
+      const double Y = __fma_rn(hy * rw + 1.0, (double)a.H, -1.0) * 0.5;
 
       // 3D covariance R diag(s^2) R^T from the raw quaternion (FB preprocess.cu:364-400).
       const float4 q = *reinterpret_cast<const float4*>(a.rots + 4 * (size_t)i);
@@ -228,9 +241,7 @@ __global__ void __launch_bounds__(kPreThreads) k_preprocess(const PreArgs a) {
       const float power = (kLn2 * 8.0f + kLn2 * log2o) * a.mult;
       const int wpx = (int)(1.414214f * sqrt_approx(ca * power) + 1.0f);
       const int hpx = (int)(1.414214f * sqrt_approx(cc * power) + 1.0f);
-      // ndc -> pixel in double, as FB's ndc2Pix promotes it (preprocess.cu:42-44).
-      xy.x = (float)((((double)ndcx + 1.0) * a.W - 1.0) * 0.5);
-      xy.y = (float)((((double)ndcy + 1.0) * a.H - 1.0) * 0.5);
+      xy = make_float2((float)X, (float)Y);
       rmin.x = min(a.gx, max(0, (int)((xy.x - wpx) / (float)a.bx)));
       rmin.y = min(a.gy, max(0, (int)((xy.y - hpx) / (float)a.by)));
       rmax.x = min(a.gx, max(0, (int)((xy.x + wpx) / (float)a.bx) + 1));
@@ -253,16 +264,21 @@ __global__ void __launch_bounds__(kPreThreads) k_preprocess(const PreArgs a) {
                         a.shs ? a.shs + (size_t)i * a.M * 3 : nullptr, rec + F_CLAMP);
       }
       rec[F_XY] = xy.x; rec[F_XY + 1] = xy.y;
-      rec[F_RGBD] = rgb.x; rec[F_RGBD + 1] = rgb.y; rec[F_RGBD + 2] = rgb.z; rec[F_RGBD + 3] = t.z;
-      rec[F_CONO] = (-0.5f * kLog2e) * conic.x;
-      rec[F_CONO + 1] = -kLog2e * conic.y;
-      rec[F_CONO + 2] = (-0.5f * kLog2e) * conic.z;
-      rec[F_CONO + 3] = log2o;
+      rec[F_RGB] = rgb.x; rec[F_RGB + 1] = rgb.y; rec[F_RGB + 2] = rgb.z;
+      rec[F_DEPTH] = t.z;
+      // Exponent of alpha in the cancellation-free form
+      // log2 o + A1 (dx + P dy)^2 + C1 dy^2 (equal to FB's con_o form).
+      rec[F_CHOL] = (-0.5f * kLog2e) * conic.x;
+      rec[F_CHOL + 1] = -cb / cc;
+      rec[F_CHOL + 2] = (-0.5f * kLog2e) / cc;
+      rec[F_LOG2O] = log2o;
+      rec[F_FRAC] = (float)(X - (double)floorf(xy.x));
+      rec[F_FRAC + 1] = (float)(Y - (double)floorf(xy.y));
       rec[F_RMIN] = __int_as_float(rmin.x); rec[F_RMIN + 1] = __int_as_float(rmin.y);
       rec[F_RMAX] = __int_as_float(rmax.x); rec[F_RMAX + 1] = __int_as_float(rmax.y);
       rec[F_CONIC] = conic.x; rec[F_CONIC + 1] = conic.y; rec[F_CONIC + 2] = conic.z;
-      rec[F_PVIEW] = t.x; rec[F_PVIEW + 1] = t.y; rec[F_PVIEW + 2] = t.z;
       rec[F_POWER] = power;
+      rec[F_PVIEW] = t.x; rec[F_PVIEW + 1] = t.y; rec[F_PVIEW + 2] = t.z;
 #pragma unroll
       for (int k = 0; k < 6; ++k) rec[F_COV3D + k] = S[k];
     } while (false);
@@ -347,7 +363,7 @@ __global__ void __launch_bounds__(kPreThreads) k_preprocess_large(const PreArgs 
     const uint32_t id = a.tasks[2 * t], off = a.tasks[2 * t + 1];
     const float* r = a.splat + (size_t)id * 32;
     const float2 xy = make_float2(r[F_XY], r[F_XY + 1]);
-    const uint32_t depth = __float_as_uint(r[F_RGBD + 3]);
+    const uint32_t depth = __float_as_uint(r[F_DEPTH]);
     const int rx0 = __float_as_int(r[F_RMIN]), ry0 = __float_as_int(r[F_RMIN + 1]);
     const int rx1 = __float_as_int(r[F_RMAX]), ry1 = __float_as_int(r[F_RMAX + 1]);
     const float4 cp = make_float4(r[F_CONIC], r[F_CONIC + 1], r[F_CONIC + 2], r[F_POWER]);

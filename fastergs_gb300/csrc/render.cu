@@ -113,25 +113,24 @@ __global__ void __launch_bounds__(kFwdWarps * kWarp) k_render_fwd(const FwdArgs 
 #pragma unroll
     for (int k = 0; k < kPxPerThread; ++k) { T[k] = 1.f; Cr[k] = 0.f; Cg[k] = 0.f; Cb[k] = 0.f; }
     for (int g = 0; g < bi.n; ++g) {
-      const float2 xy = st.xy[g];
-      const float4 co = st.co[g];
+      const float4 pos = st.pos[g];
+      const float4 q = st.quad[g];   // A1, P, C1, log2 o
       const float4 c = st.rgb[g];
-      const float dx = xy.x - px;
-      const float A = fmaf(co.x * dx, dx, co.w);
-      const float Bx = co.y * dx;
-      float dy = xy.y - py0;
+      const float dx = centre_offset(pos.x, pos.z, px);
+      const float ry = pos.y - py0;  // exact: both are integers
 #pragma unroll
       for (int k = 0; k < kPxPerThread; ++k) {
-        // alpha = o * exp(-q/2) evaluated as 2^(con_o . [1, dx^2, dxdy, dy^2])
-        const float e = fmaf(dy, fmaf(co.z, dy, Bx), A);
+        const float dy = (ry - (float)k * ystep) + pos.w;
+        // alpha = o * exp(-q/2) = 2^(log2 o + A1 (dx + P dy)^2 + C1 dy^2)
+        const float w = fmaf(q.y, dy, dx);
+        const float e = fmaf(q.x * w, w, fmaf(q.z * dy, dy, q.w));
         float al = fminf(kAlphaMax, ex2_approx(e));
         al = al < kAlphaCut ? 0.f : al;
-        const float w = al * T[k];
-        Cr[k] = fmaf(c.x, w, Cr[k]);
-        Cg[k] = fmaf(c.y, w, Cg[k]);
-        Cb[k] = fmaf(c.z, w, Cb[k]);
+        const float wt = al * T[k];
+        Cr[k] = fmaf(c.x, wt, Cr[k]);
+        Cg[k] = fmaf(c.y, wt, Cg[k]);
+        Cb[k] = fmaf(c.z, wt, Cb[k]);
         T[k] = fmaf(-al, T[k], T[k]);  // T (1 - alpha), rounded once
-        dy -= ystep;
       }
     }
     __syncwarp();

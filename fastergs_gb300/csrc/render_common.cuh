@@ -57,25 +57,31 @@ inline SampleState carve_sample(void* base, int64_t max_buckets) {
 
 // Records of one bucket staged in shared memory, structure-of-arrays.
 struct BucketStage {
-  float2 xy[kMaxBucket];
-  float4 co[kMaxBucket];    // con_o: (-0.5 log2e a, -log2e b, -0.5 log2e c, log2 o)
-  float4 rgb[kMaxBucket];   // r, g, b, (backward: Gaussian id bits)
+  float4 pos[kMaxBucket];   // floor(x), floor(y), fraction x, fraction y
+  float4 quad[kMaxBucket];  // A1, P, C1, log2 opacity
+  float4 rgb[kMaxBucket];   // r, g, b, Gaussian id bits
 };
 
-// Load the render fields (floats 0..9) of n records whose ids start at ids.
+// Load the render fields (floats 0..11) of the n records whose ids start at ids.
 __device__ __forceinline__ void stage_bucket(BucketStage& st, const float* __restrict__ splat,
                                              const uint32_t* __restrict__ ids, int n, int lane) {
   for (int j = lane; j < n; j += kWarp) {
     const uint32_t id = ids[j];
     const float4* r = reinterpret_cast<const float4*>(splat + (size_t)id * 32);
     const float4 a = __ldg(r);        // x, y, r, g
-    const float4 b = __ldg(r + 1);    // b, depth, co.x, co.y
-    const float2 c = __ldg(reinterpret_cast<const float2*>(splat + (size_t)id * 32 + 8));  // co.z, co.w
-    st.xy[j] = make_float2(a.x, a.y);
-    st.co[j] = make_float4(b.z, b.w, c.x, c.y);
+    const float4 b = __ldg(r + 1);    // b, depth, A1, P
+    const float4 c = __ldg(r + 2);    // C1, log2 o, fraction x, fraction y
+    st.pos[j] = make_float4(floorf(a.x), floorf(a.y), c.z, c.w);
+    st.quad[j] = make_float4(b.z, b.w, c.x, c.y);
     st.rgb[j] = make_float4(a.z, a.w, b.x, __uint_as_float(id));
   }
   __syncwarp();
+}
+
+// Offsets from a pixel to a staged Gaussian's centre: the integer parts
+// subtract exactly, the fraction adds once.
+__device__ __forceinline__ float centre_offset(float whole, float frac, float pixel) {
+  return (whole - pixel) + frac;
 }
 
 // Bucket b -> (tile, first pair, pair count, index of the bucket in its tile).

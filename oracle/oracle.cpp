@@ -41,11 +41,14 @@
 
 namespace {
 
-// Record field offsets, one 32-float record per Gaussian
-// (FB/csrc/cuda_rasterizer/rasterizer_imp.h:27-38).
+// Record field offsets, one 32-float record per Gaussian.  Same fields as FB's
+// record (rasterizer_imp.h:27-38) in the device library's order; the alpha
+// exponent is stored as log2 o + A1 (dx + P dy)^2 + C1 dy^2 and the pixel
+// position as floor(float(x)) + fraction, which in exact arithmetic equals
+// FB's con_o form (preprocess.cu:709-710) and pixel position.
 enum : int {
-  F_XY = 0, F_RGBD = 2, F_CONO = 6, F_RMIN = 10, F_RMAX = 12, F_CONIC = 14,
-  F_PVIEW = 17, F_POWER = 20, F_CLAMP = 22, F_COV3D = 25, REC = 32
+  F_XY = 0, F_RGB = 2, F_DEPTH = 5, F_CHOL = 6, F_LOG2O = 9, F_FRAC = 10, F_RMIN = 12, F_RMAX = 14,
+  F_CONIC = 16, F_POWER = 19, F_CLAMP = 20, F_COV3D = 23, F_PVIEW = 29, REC = 32
 };
 
 constexpr double kLn2 = 0.693147180559945309417232121458;
@@ -268,15 +271,18 @@ void preprocess_one(Scene& s, int i) {
     }
   }
   r[F_XY + 0] = xy[0]; r[F_XY + 1] = xy[1];
-  r[F_RGBD + 0] = rgb[0]; r[F_RGBD + 1] = rgb[1]; r[F_RGBD + 2] = rgb[2]; r[F_RGBD + 3] = t[2];
-  r[F_CONO + 0] = -0.5 * kLog2e * conic[0];
-  r[F_CONO + 1] = -kLog2e * conic[1];
-  r[F_CONO + 2] = -0.5 * kLog2e * conic[2];
-  r[F_CONO + 3] = log2o;
+  r[F_RGB + 0] = rgb[0]; r[F_RGB + 1] = rgb[1]; r[F_RGB + 2] = rgb[2];
+  r[F_DEPTH] = t[2];
+  r[F_CHOL + 0] = -0.5 * kLog2e * conic[0];
+  r[F_CHOL + 1] = -cb / cc;
+  r[F_CHOL + 2] = -0.5 * kLog2e / cc;
+  r[F_LOG2O] = log2o;
+  r[F_FRAC + 0] = xy[0] - std::floor((double)(float)xy[0]);
+  r[F_FRAC + 1] = xy[1] - std::floor((double)(float)xy[1]);
   r[F_RMIN + 0] = rminx; r[F_RMIN + 1] = rminy; r[F_RMAX + 0] = rmaxx; r[F_RMAX + 1] = rmaxy;
   r[F_CONIC + 0] = conic[0]; r[F_CONIC + 1] = conic[1]; r[F_CONIC + 2] = conic[2];
-  r[F_PVIEW + 0] = t[0]; r[F_PVIEW + 1] = t[1]; r[F_PVIEW + 2] = t[2];
   r[F_POWER] = power;
+  r[F_PVIEW + 0] = t[0]; r[F_PVIEW + 1] = t[1]; r[F_PVIEW + 2] = t[2];
   s.radii[i] = (int)radius;
   s.valid[i] = 1;
   s.rect_area[i] = area;
@@ -315,7 +321,7 @@ void emit_and_sort(Scene& s, double eps_pair) {
     const double* r = &s.rec[(size_t)i * REC];
     const int x0 = (int)r[F_RMIN], y0 = (int)r[F_RMIN + 1], x1 = (int)r[F_RMAX], y1 = (int)r[F_RMAX + 1];
     const double cx = r[F_XY], cy = r[F_XY + 1], power = r[F_POWER];
-    const float depth_f = as_float(r[F_RGBD + 3]);
+    const float depth_f = as_float(r[F_DEPTH]);
     for (int ty = y0; ty < y1; ++ty)
       for (int tx = x0; tx < x1; ++tx) {
         const double px0 = tx * c.bx, px1 = px0 + c.bx - 1, py0 = ty * c.by, py1 = py0 + c.by - 1;
@@ -330,7 +336,7 @@ void emit_and_sort(Scene& s, double eps_pair) {
         if (hit || amb) {
           Pair p;
           p.key = ((uint64_t)(uint32_t)(ty * c.gx + tx) << 32) | float_bits(depth_f);
-          p.depth = r[F_RGBD + 3];
+          p.depth = r[F_DEPTH];
           p.id = i;
           p.amb = amb ? 1 : 0;
           if (!hit) p.amb |= 2;   // bit 1: pair present only as an ambiguous candidate
@@ -364,11 +370,21 @@ void build_ranges_from_pairs(Scene& s) {
   }
 }
 
-inline double alpha_of(const double* r, double px, double py, double* dx_out, double* dy_out) {
-  const double dx = r[F_XY] - px, dy = r[F_XY + 1] - py;
-  *dx_out = dx; *dy_out = dy;
-  const double pw = r[F_CONO + 3] + r[F_CONO] * dx * dx + r[F_CONO + 2] * dy * dy + r[F_CONO + 1] * dx * dy;
-  return std::exp2(pw);
+// Exponent of alpha for pixel (px, py) and its partial derivatives with
+// respect to the centre.  dx, dy = centre - pixel.
+struct AlphaEval {
+  double a, dx, dy, dedx, dedy;
+};
+inline AlphaEval alpha_of(const double* r, double px, double py) {
+  AlphaEval v;
+  v.dx = (std::floor((double)(float)r[F_XY]) - px) + r[F_FRAC];
+  v.dy = (std::floor((double)(float)r[F_XY + 1]) - py) + r[F_FRAC + 1];
+  const double A1 = r[F_CHOL], P = r[F_CHOL + 1], C1 = r[F_CHOL + 2];
+  const double w = v.dx + P * v.dy;
+  v.a = std::exp2(r[F_LOG2O] + A1 * w * w + C1 * v.dy * v.dy);
+  v.dedx = 2 * A1 * w;
+  v.dedy = 2 * A1 * P * w + 2 * C1 * v.dy;
+  return v;
 }
 
 // Bucketed compositing and merge (render.cu:99-123,130-275,285-391).
@@ -405,13 +421,12 @@ void composite(Scene& s) {
         const int g0 = start + b * bs, g1 = std::min(end, g0 + bs);
         for (int g = g0; g < g1; ++g) {
           const double* r = &s.rec[(size_t)s.ids[g] * REC];
-          double dx, dy;
-          double a = alpha_of(r, px, py, &dx, &dy);
+          double a = alpha_of(r, px, py).a;
           if (std::fabs(a - cut) <= s.eps_alpha * cut) amb = true;
           if (a > 0.99) { s.gauss_clamped[s.ids[g]] = 1; ++n_cl; }
           a = std::min(0.99, a);
           if (a < cut) a = 0; else ++n_on;
-          for (int ch = 0; ch < 3; ++ch) Cb[ch] += r[F_RGBD + ch] * a * Tb;
+          for (int ch = 0; ch < 3; ++ch) Cb[ch] += r[F_RGB + ch] * a * Tb;
           Tb -= a * Tb;
         }
         for (int ch = 0; ch < 3; ++ch) C[ch] += Tp * Cb[ch];
@@ -478,26 +493,27 @@ void composite_backward(const Scene& s, const double* dL, double* dm2, double* d
         const double bgd = s.bg[0] * d[0] + s.bg[1] * d[1] + s.bg[2] * d[2];
         for (int g = g1 - 1; g >= g0; --g) {
           const double* r = &s.rec[(size_t)s.ids[g] * REC];
-          double dx, dy;
-          double a = alpha_of(r, px, py, &dx, &dy);
-          a = std::min(0.99, a);
+          const AlphaEval ev = alpha_of(r, px, py);
+          const double dx = ev.dx, dy = ev.dy;
+          double a = std::min(0.99, ev.a);
           if (a < cut) a = 0;
           const double inv = 1.0 / (1.0 - a);
           Tc = std::min(Tc * inv, 1.0);
           const double w = a * Tc;
           double dLda = 0;
-          for (int ch = 0; ch < 3; ++ch) dLda += (Tc * r[F_RGBD + ch] - res[ch] * inv) * d[ch];
-          for (int ch = 0; ch < 3; ++ch) res[ch] += w * r[F_RGBD + ch];
+          for (int ch = 0; ch < 3; ++ch) dLda += (Tc * r[F_RGB + ch] - res[ch] * inv) * d[ch];
+          for (int ch = 0; ch < 3; ++ch) res[ch] += w * r[F_RGB + ch];
           dLda += -Tf * inv * bgd;
           const double dpw = dLda * a * kLn2;
           double* q = &acc[(size_t)(g - g0) * 12];
           for (int ch = 0; ch < 3; ++ch) q[8 + ch] += w * d[ch];
-          const double mx = dpw * (2 * r[F_CONO] * dx + r[F_CONO + 1] * dy) * hx;
-          const double my = dpw * (2 * r[F_CONO + 2] * dy + r[F_CONO + 1] * dx) * hy;
+          // dpower/dcentre (FB backward.cu:614-615), scaled by W/2, H/2 to NDC
+          const double mx = dpw * ev.dedx * hx;
+          const double my = dpw * ev.dedy * hy;
           q[0] += mx; q[1] += my; q[2] += std::fabs(mx); q[3] += std::fabs(my);
           const double k = -0.5 * kLog2e * dpw;
           q[4] += k * dx * dx; q[5] += k * dx * dy; q[7] += k * dy * dy;
-          q[11] += dpw * kLog2e / std::exp2(r[F_CONO + 3]);
+          q[11] += dpw * kLog2e / std::exp2(r[F_LOG2O]);
         }
       }
       for (int g = g0; g < g1; ++g) {

@@ -105,7 +105,7 @@ def gpu_records_as_oracle(fw):
     """The device's float32 records as float64, rect ints decoded."""
     rec = fw["rec"].astype(np.float64)
     raw = fw["rec"].view(np.int32)
-    rec[:, 10:14] = raw[:, 10:14]
+    rec[:, 12:16] = raw[:, 12:16]  # tile rect (int bits)
     radii = fw["radii"].cpu().numpy()
     valid = np.zeros(rec.shape[0], bool)
     valid[np.unique(fw["vals_sorted"])] = True

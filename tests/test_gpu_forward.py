@@ -9,7 +9,9 @@ Tolerances (FP32 device vs FP64 oracle):
     records and lists (replay), excluding pixels the oracle flags as
     ambiguous (an alpha within 1e-5 relative of the 1/255 cut-off or a
     bucket-end transmittance within 1e-5 relative of 1e-4);
-  * images end to end (independent FP64 preprocess): max-abs 1e-4.
+  * images against the oracle's own FP64 records (compositing the device's
+    pair lists, or fully independent lists for the small scenes): max-abs
+    1e-5.
 """
 import numpy as np
 import pytest
@@ -45,20 +47,27 @@ def test_preprocess_records_match_oracle(cuda_device, name):
     g = fw["rec"].astype(np.float64)
     gi = fw["rec"].view(np.int32)
     ref = r["rec"]
-    np.testing.assert_allclose(g[valid, 0:2], ref[valid, 0:2], atol=2e-3, rtol=0)        # pixel xy
-    np.testing.assert_allclose(g[valid, 2:5], ref[valid, 2:5], atol=1e-5, rtol=0)        # rgb
-    np.testing.assert_allclose(g[valid, 5], ref[valid, 5], rtol=1e-6)                    # depth
-    np.testing.assert_array_equal(gi[valid, 10:14], ref[valid, 10:14].astype(np.int32))  # tile rect
-    cn = np.linalg.norm(ref[valid, 14:17], axis=1, keepdims=True)
-    assert np.all(np.abs(g[valid, 14:17] - ref[valid, 14:17]) <= 2e-4 * cn)             # conic
-    assert np.all(np.abs(g[valid, 6:9] - ref[valid, 6:9]) <= 4e-4 * cn)                  # con_o quadratic part
-    np.testing.assert_allclose(g[valid, 9], ref[valid, 9], atol=2e-6)                    # log2 opacity
-    np.testing.assert_allclose(g[valid, 20], ref[valid, 20], rtol=2e-6, atol=2e-6)       # power
-    tr = (ref[valid, 25] + ref[valid, 28] + ref[valid, 30])[:, None]
-    assert np.all(np.abs(g[valid, 25:31] - ref[valid, 25:31]) <= 1e-6 * tr)              # cov3D
-    pre = ref[valid, 2:5]  # clamp flags are exact away from a zero crossing
-    sure = np.all(np.abs(pre) > 1e-5, axis=1) | (ref[valid, 22:25].sum(1) == 0)
-    np.testing.assert_array_equal(g[valid][sure, 22:25], ref[valid][sure, 22:25])
+    v = valid
+    np.testing.assert_allclose(g[v, 0:2], ref[v, 0:2], atol=1e-4, rtol=0)              # FP32 pixel xy
+    # full-precision position: floor(float x) + fraction (FP64 projection)
+    gpos = np.floor(g[v, 0:2]) + g[v, 10:12]
+    opos = np.floor(ref[v, 0:2].astype(np.float32).astype(np.float64)) + ref[v, 10:12]
+    np.testing.assert_allclose(gpos, opos, atol=1e-6, rtol=0)
+    np.testing.assert_allclose(g[v, 2:5], ref[v, 2:5], atol=1e-5, rtol=0)               # rgb
+    np.testing.assert_allclose(g[v, 5], ref[v, 5], rtol=1e-6)                           # depth
+    np.testing.assert_allclose(g[v, 6], ref[v, 6], rtol=2e-5)                           # A1
+    assert np.all(np.abs(g[v, 7] - ref[v, 7]) <= 2e-5 * (np.abs(ref[v, 7]) + 1))        # P
+    np.testing.assert_allclose(g[v, 8], ref[v, 8], rtol=2e-5)                           # C1
+    np.testing.assert_allclose(g[v, 9], ref[v, 9], atol=2e-6)                           # log2 opacity
+    np.testing.assert_array_equal(gi[v, 12:16], ref[v, 12:16].astype(np.int32))        # tile rect
+    cn = np.linalg.norm(ref[v, 16:19], axis=1, keepdims=True)
+    assert np.all(np.abs(g[v, 16:19] - ref[v, 16:19]) <= 2e-5 * cn)                    # conic
+    np.testing.assert_allclose(g[v, 19], ref[v, 19], rtol=2e-6, atol=2e-6)             # power
+    tr = (ref[v, 23] + ref[v, 26] + ref[v, 28])[:, None]
+    assert np.all(np.abs(g[v, 23:29] - ref[v, 23:29]) <= 1e-6 * tr)                     # cov3D
+    pre = ref[v, 2:5]  # clamp flags are exact away from a zero crossing
+    sure = np.all(np.abs(pre) > 1e-5, axis=1) | (ref[v, 20:23].sum(1) == 0)
+    np.testing.assert_array_equal(g[v][sure, 20:23], ref[v][sure, 20:23])
 
 
 @pytest.mark.parametrize("name", list(SCENES))
@@ -158,8 +167,25 @@ def test_render_matches_oracle_replay(cuda_device, name, bg):
     assert fw["bucket_sum"] == im["num_buckets"]
 
 
+@pytest.mark.parametrize("name", list(SCENES))
+def test_render_vs_fp64_records(cuda_device, name):
+    """Images against the oracle's own FP64 preprocess, compositing the
+    device's (tile, Gaussian) lists: 1e-5 max-abs."""
+    s = SCENES[name]()
+    fw = run_forward(s, cuda_device)
+    o = oracle_scene(s).preprocess()
+    o.set_lists(fw["vals_sorted"], fw["ranges"])
+    o.render(eps_alpha=1e-4, eps_T=1e-4)
+    im = o.image()
+    ok = ~im["ambiguous"]
+    assert ok.mean() > 0.99
+    gimg = fw["out_color"].cpu().numpy().astype(np.float64)
+    assert np.abs(gimg - im["out_color"])[:, ok].max() <= 1e-5
+
+
 @pytest.mark.parametrize("name", ["c1", "c5a"])
 def test_render_end_to_end_vs_fp64_oracle(cuda_device, name):
+    """Fully independent FP64 pipeline (own pair lists and sort)."""
     s = SCENES[name]()
     fw = run_forward(s, cuda_device)
     o = oracle_scene(s).preprocess()
@@ -168,7 +194,7 @@ def test_render_end_to_end_vs_fp64_oracle(cuda_device, name):
     im = o.image()
     ok = ~im["ambiguous"]
     gimg = fw["out_color"].cpu().numpy().astype(np.float64)
-    assert np.abs(gimg - im["out_color"])[:, ok].max() <= 1e-4
+    assert np.abs(gimg - im["out_color"])[:, ok].max() <= 1e-5
 
 
 def test_ragged_image_and_culling(cuda_device):
