@@ -27,6 +27,7 @@ SIGNATURES = {
                              f32, f32, f32, f32, f32, vp, vp, i64, vp, vp, i64, vp, i64, vp, vp, vp, vp]),
     "fgs_sort_temp_bytes": (sz, [i64]),
     "fgs_sort": (i32, [i64, i32, i32, i32, i32, vp, sz, vp, vp, vp, vp, vp]),
+    "fgs_sort_noalloc": (i32, [i64, i32, i32, i32, i32, vp, vp, vp, vp, vp]),
     "fgs_tile_ranges": (i32, [i64, i32, vp, vp, vp]),
     "fgs_max_buckets": (i64, [i64, i32, i32, i32, i32, i32]),
     "fgs_state_bytes": (i32, [i32, i32, i32, i32, i64, C.POINTER(C.c_size_t), C.POINTER(C.c_size_t)]),

@@ -15,6 +15,7 @@
 // Every look-back wait is bounded (kSpinLimit polls); on expiry the kernel
 // records kErrTimeout in the error word and continues, so it never hangs.
 #include <algorithm>
+#include <mutex>
 
 #include "fgs_common.cuh"
 
@@ -33,12 +34,14 @@ constexpr uint32_t kValueMask = (1u << 30) - 1;
 constexpr int kSortDynSmem = (int)((sizeof(unsigned long long) + sizeof(uint32_t)) * kSortTile);
 
 struct SortLayout {
-  size_t hist, counters, lookback, alt_keys, alt_vals, total;
-  int64_t tiles;
+  size_t hist = 0, counters = 0, lookback = 0, alt_keys = 0, alt_vals = 0, total = 0;
+  int64_t tiles = 0;
 };
 
-SortLayout layout_for(int64_t n) {
-  auto up = [](size_t v) { return (v + 255) & ~(size_t)255; };
+constexpr size_t up256(size_t v) { return (v + 255) & ~(size_t)255; }
+
+constexpr SortLayout layout_for(int64_t n) {
+  constexpr auto up = up256;
   SortLayout L;
   L.tiles = (n + kSortTile - 1) / kSortTile;
   size_t off = 0;
@@ -285,4 +288,52 @@ extern "C" fgs_status fgs_sort(int64_t num_rendered, int width, int height, int 
     src_v = dv;
   }
   return FGS_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Sort without caller-provided scratch (fgs_sort_noalloc).
+//
+// Some callers cannot allocate device memory at the point where they sort:
+// code running inside a memory pool or arena they do not own, plugins whose
+// host forbids allocation after start-up, and real-time loops that must not
+// stall on cudaMalloc.  For them the scratch of fgs_sort lives in this
+// file-scope array, sized for FGS_SORT_NOALLOC_MAX_PAIRS pairs.  Every GPU
+// that loads the library holds it (about 14 MiB) until the process exits.
+namespace fgs {
+namespace {
+constexpr int64_t kNoAllocMaxPairs = FGS_SORT_NOALLOC_MAX_PAIRS;
+constexpr size_t kNoAllocBytes = layout_for(kNoAllocMaxPairs).total;
+static __device__ __align__(256) unsigned char g_sort_scratch[kNoAllocBytes];
+
+// Device address of g_sort_scratch, looked up once per device (the host-side
+// name of a __device__ array is not a device address).
+constexpr int kMaxDevices = 64;
+std::mutex g_scratch_mu;
+void* g_scratch_ptr[kMaxDevices] = {nullptr};
+}  // namespace
+}  // namespace fgs
+
+extern "C" fgs_status fgs_sort_noalloc(int64_t num_rendered, int width, int height, int block_x, int block_y,
+                                       const uint64_t* keys_in, const uint32_t* values_in, uint64_t* keys_out,
+                                       uint32_t* values_out, void* stream) {
+  using namespace fgs;
+  if (num_rendered < 0) return FGS_ERR_BAD_ARG;
+  if (num_rendered > kNoAllocMaxPairs) return FGS_ERR_CAPACITY;
+  int dev = 0;
+  FGS_TRY(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= kMaxDevices) return FGS_ERR_UNSUPPORTED;
+  void* scratch = nullptr;
+  {
+    std::lock_guard<std::mutex> lk(g_scratch_mu);
+    if (!g_scratch_ptr[dev]) {
+      void* p = nullptr;
+      const cudaError_t e = cudaGetSymbolAddress(&p, g_sort_scratch);
+      if (e != cudaSuccess || !p) return FGS_ERR_CUDA;
+      g_scratch_ptr[dev] = p;
+    }
+    scratch = g_scratch_ptr[dev];
+  }
+  // fgs_sort zeroes the histogram and look-back words it needs on every call.
+  return fgs_sort(num_rendered, width, height, block_x, block_y, scratch, kNoAllocBytes, keys_in, values_in,
+                  keys_out, values_out, stream);
 }

@@ -90,6 +90,24 @@ fgs_status fgs_sort(int64_t num_rendered, int width, int height, int block_x, in
                     const uint64_t* keys_in, const uint32_t* values_in,
                     uint64_t* keys_out, uint32_t* values_out, void* stream);
 
+/*
+ * fgs_sort for callers that cannot allocate device memory when they sort
+ * (code inside a memory pool or arena it does not own, hosts that forbid
+ * allocation after start-up, real-time loops that must not stall on
+ * cudaMalloc).  No counterpart in the reference.  The scratch is a
+ * library-owned static device array sized for FGS_SORT_NOALLOC_MAX_PAIRS
+ * pairs (about 14 MiB, held by every GPU that loads the library until the
+ * process exits); larger num_rendered returns FGS_ERR_CAPACITY.  The first
+ * call on a device looks up the array's device address, so make that first
+ * call before any stream capture.  All calls share the array: calls that
+ * overlap on the GPU (other streams, other threads) race and must be
+ * serialised by the caller.  Calls no allocator.
+ */
+#define FGS_SORT_NOALLOC_MAX_PAIRS (1 << 20)
+fgs_status fgs_sort_noalloc(int64_t num_rendered, int width, int height, int block_x, int block_y,
+                            const uint64_t* keys_in, const uint32_t* values_in,
+                            uint64_t* keys_out, uint32_t* values_out, void* stream);
+
 /* [start, end) of every tile in a sorted key list; ranges is (tiles, 2) u32
  * and is zeroed first.  Replaces identifyTileRanges and its launch
  * (FB render.cu:54-79, :406-412). */
