@@ -180,10 +180,24 @@ def gpu_bench(args, rank, local, world):
         projmatrix=t(cam.projmatrix), sh_degree=s.sh_degree, campos=t(cam.campos), mult=1.0, prefiltered=False,
         debug=False)
     rast = fgs.GaussianRasterizer(settings)
-    # Size the shared buffer for this workload (FB's Buffer takes MAX_NUM_RENDERED).
+    # Size the shared buffer for this workload (FB's Buffer takes MAX_NUM_RENDERED):
+    # start at 2^22 pairs and double until a frame fits.
     slot = fgs._RasterizeGaussians.__dict__["buffer"]
-    slot._buf = fgs.Buffer(device=dev, MAX_NUM_RENDERED=1 << 26)
     stream = torch.cuda.current_stream(dev)
+    cap = 1 << 22
+    while True:
+        slot._buf = None
+        torch.cuda.empty_cache()
+        slot._buf = fgs.Buffer(device=dev, MAX_NUM_RENDERED=max(cap, s.P))
+        try:
+            with torch.no_grad():
+                rast(means3D=dev_in["means"], opacities=dev_in["opacities"], dc=dev_in["dc"], shs=dev_in["shs"],
+                     scales=dev_in["scales"], rotations=dev_in["rotations"])
+            break
+        except RuntimeError as e:
+            if "Too many k-v pairs" not in str(e):
+                raise
+            cap *= 2
 
     def step(params, backward=True):
         leaves = {k: v.detach().requires_grad_(backward) for k, v in params.items()}

@@ -102,8 +102,9 @@ class _RasterizeGaussians(torch.autograd.Function):
                              buffer.gaussian_values_unsorted, buffer.gaussian_keys_sorted,
                              buffer.gaussian_values_sorted)
         H, W = raster_settings.image_height, raster_settings.image_width
-        last_contributor = torch.zeros((H, W, 1), device=means3D.device, dtype=torch.int)
-        Ts_final = torch.zeros((H, W, 1), device=means3D.device, dtype=torch.float)
+        # every pixel is written by the merge, so no zero-fill is needed
+        last_contributor = torch.empty((H, W, 1), device=means3D.device, dtype=torch.int)
+        Ts_final = torch.empty((H, W, 1), device=means3D.device, dtype=torch.float)
         bucket_sum, out_color, img_buffer, smp_buffer = _C.ops.render_16x16(
             N, num_rendered, W, H, splat_buffer, buffer.gaussian_keys_sorted, buffer.gaussian_values_sorted,
             buffer.ranges, raster_settings.bg, last_contributor, Ts_final)

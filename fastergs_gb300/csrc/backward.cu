@@ -72,13 +72,14 @@ __device__ __forceinline__ float warp_transpose_reduce16(float (&v)[16], int lan
   return v[0] + __shfl_xor_sync(0xffffffffu, v[0], 1);
 }
 
+template <int BX>
 __global__ void __launch_bounds__(kBwdWarps * kWarp) k_render_bwd(const BwdArgs a) {
+  using M = TileMap<BX>;
+  constexpr int BY = kTilePixels / BX;
   __shared__ BucketStage s_stage[kBwdWarps];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   BucketStage& st = s_stage[warp];
   const int B = (int)a.bucket_sum[0];
-  const int lx = lane % a.bx, ly0 = lane / a.bx;
-  const int rows = kWarp / a.bx;
   const int HW = a.W * a.H;
   const float hx = 0.5f * (float)a.W, hy = 0.5f * (float)a.H;
   const float bgr = a.bg[0], bgg = a.bg[1], bgb = a.bg[2];
@@ -95,81 +96,101 @@ __global__ void __launch_bounds__(kBwdWarps * kWarp) k_render_bwd(const BwdArgs 
     const BucketInfo bi = bucket_info(b, a.bucket_tile, a.bucket_off, a.ranges, a.bs);
     const uint32_t thres = (uint32_t)(bi.local * a.bs);
     if (thres >= a.max_contrib[bi.tile]) continue;  // no pixel of the tile reaches this bucket
-    stage_bucket(st, a.splat, a.vals + bi.start, bi.n, lane);
-    const int tx0 = (bi.tile % a.gx) * a.bx, ty0 = (bi.tile / a.gx) * a.by;
-    const float px = (float)(tx0 + lx), py0 = (float)(ty0 + ly0);
+    const int tx0 = (bi.tile % a.gx) * BX, ty0 = (bi.tile / a.gx) * BY;
+    stage_bucket<BX>(st, a.splat, a.vals + bi.start, bi.n, lane, tx0, ty0);
+    float pxc[M::kCols], pyr[M::kRows];
+#pragma unroll
+    for (int c = 0; c < M::kCols; ++c) pxc[c] = (float)(tx0 + 8 * c + (lane & 7));
+#pragma unroll
+    for (int r = 0; r < M::kRows; ++r) pyr[r] = (float)(ty0 + 4 * r + (lane >> 3));
 
     float T[kPxPerThread], Pd[kPxPerThread], Lr[kPxPerThread], Lg[kPxPerThread], Lb[kPxPerThread],
         K[kPxPerThread];
     uint32_t alive = 0;
 #pragma unroll
-    for (int k = 0; k < kPxPerThread; ++k) {
-      const int gxp = tx0 + lx, gyp = ty0 + ly0 + k * rows;
-      T[k] = 0.f; Pd[k] = 0.f; Lr[k] = 0.f; Lg[k] = 0.f; Lb[k] = 0.f; K[k] = 0.f;
-      if (gxp < a.W && gyp < a.H) {
-        const int pix = gyp * a.W + gxp;
-        if ((uint32_t)a.last_contrib[pix] > thres) {
-          alive |= 1u << k;
-          const float4 prev = bi.local > 0 ? a.samples[(size_t)(b - 1) * kTilePixels + lane + k * kWarp]
-                                           : make_float4(0.f, 0.f, 0.f, 1.f);
-          Lr[k] = a.dL[pix];
-          Lg[k] = a.dL[HW + pix];
-          Lb[k] = a.dL[2 * HW + pix];
-          T[k] = prev.w;
-          Pd[k] = prev.x * Lr[k] + prev.y * Lg[k] + prev.z * Lb[k];
-          // K = C_final . dL + T_final * (bg . dL): everything behind a
-          // Gaussian is K - (prefix up to and including it) . dL.
-          K[k] = a.pix_color[pix] * Lr[k] + a.pix_color[HW + pix] * Lg[k] + a.pix_color[2 * HW + pix] * Lb[k] +
-                 a.Ts_final[pix] * (bgr * Lr[k] + bgg * Lg[k] + bgb * Lb[k]);
+    for (int r = 0; r < M::kRows; ++r)
+#pragma unroll
+      for (int cc = 0; cc < M::kCols; ++cc) {
+        const int k = r * M::kCols + cc;
+        const int gxp = (int)pxc[cc], gyp = (int)pyr[r];
+        T[k] = 0.f; Pd[k] = 0.f; Lr[k] = 0.f; Lg[k] = 0.f; Lb[k] = 0.f; K[k] = 0.f;
+        if (gxp < a.W && gyp < a.H) {
+          const int pix = gyp * a.W + gxp;
+          if ((uint32_t)a.last_contrib[pix] > thres) {
+            alive |= 1u << k;
+            const float4 prev = bi.local > 0 ? a.samples[(size_t)(b - 1) * kTilePixels + M::pix(r, cc, lane)]
+                                             : make_float4(0.f, 0.f, 0.f, 1.f);
+            Lr[k] = a.dL[pix];
+            Lg[k] = a.dL[HW + pix];
+            Lb[k] = a.dL[2 * HW + pix];
+            T[k] = prev.w;
+            Pd[k] = prev.x * Lr[k] + prev.y * Lg[k] + prev.z * Lb[k];
+            // K = C_final . dL + T_final * (bg . dL): everything behind a
+            // Gaussian is K - (prefix up to and including it) . dL.
+            K[k] = a.pix_color[pix] * Lr[k] + a.pix_color[HW + pix] * Lg[k] +
+                   a.pix_color[2 * HW + pix] * Lb[k] + a.Ts_final[pix] * (bgr * Lr[k] + bgg * Lg[k] + bgb * Lb[k]);
+          }
         }
       }
-    }
     if (__any_sync(0xffffffffu, alive) == 0) {
       __syncwarp();
       continue;
     }
 
     for (int g = 0; g < bi.n; ++g) {
+      const uint32_t mask = st.mask[g];
+      if (mask == 0) continue;  // alpha < 1/256 on the whole tile: no contribution
       const float4 pos = st.pos[g];
       const float4 q = st.quad[g];   // A1, P, C1, log2 o
       const float4 c = st.rgb[g];
-      const float dx = centre_offset(pos.x, pos.z, px);
-      const float ry = pos.y - py0;  // exact: both are integers
       const float A2 = 2.f * q.x, C2 = 2.f * q.z;
+      float dx[M::kCols];
+#pragma unroll
+      for (int cc = 0; cc < M::kCols; ++cc) dx[cc] = centre_offset(pos.x, pos.z, pxc[cc]);
       float v[16];
 #pragma unroll
       for (int j = 0; j < 16; ++j) v[j] = 0.f;
       bool any = false;
 #pragma unroll
-      for (int k = 0; k < kPxPerThread; ++k) {
-        const float dy = (ry - (float)(k * rows)) + pos.w;
-        const float w = fmaf(q.y, dy, dx);
-        const float e = fmaf(q.x * w, w, fmaf(q.z * dy, dy, q.w));
-        const float al = fminf(kAlphaMax, ex2_approx(e));
-        if (((alive >> k) & 1u) && al >= kAlphaCut) {
-          any = true;
-          const float wt = al * T[k];
-          const float cd = c.x * Lr[k] + c.y * Lg[k] + c.z * Lb[k];
-          Pd[k] = fmaf(wt, cd, Pd[k]);
-          const float inv = __frcp_rn(1.f - al);
-          const float dLda = T[k] * cd - inv * (K[k] - Pd[k]);
-          T[k] = fmaf(-al, T[k], T[k]);
-          v[8] = fmaf(wt, Lr[k], v[8]);
-          v[9] = fmaf(wt, Lg[k], v[9]);
-          v[10] = fmaf(wt, Lb[k], v[10]);
-          const float dp = dLda * al;  // dL/dexponent / ln2
-          // d exponent / d(centre x) = 2 A1 w, d / d(centre y) = 2 A1 P w + 2 C1 dy
-          const float gw = A2 * w;
-          const float tx = dp * gw;
-          const float ty = dp * fmaf(gw, q.y, C2 * dy);
-          v[0] += tx;
-          v[1] += ty;
-          v[2] += fabsf(tx);
-          v[3] += fabsf(ty);
-          v[4] = fmaf(dp, dx * dx, v[4]);
-          v[5] = fmaf(dp * dx, dy, v[5]);
-          v[7] = fmaf(dp * dy, dy, v[7]);
-          v[11] += dp;
+      for (int r = 0; r < M::kRows; ++r) {
+        const uint32_t rm = (mask >> (r * M::kCols)) & ((1u << M::kCols) - 1u);
+        if (rm == 0) continue;
+        const float dy = centre_offset(pos.y, pos.w, pyr[r]);
+        const float f = fmaf(q.z * dy, dy, q.w);
+        const float c2dy = C2 * dy;
+#pragma unroll
+        for (int cc = 0; cc < M::kCols; ++cc) {
+          if (!((rm >> cc) & 1u)) continue;
+          const int k = r * M::kCols + cc;
+          const float w = fmaf(q.y, dy, dx[cc]);
+          const float e = fmaf(q.x * w, w, f);
+          const float al = fminf(kAlphaMax, ex2_approx(e));
+          if (((alive >> k) & 1u) && al >= kAlphaCut) {
+            any = true;
+            const float wt = al * T[k];
+            const float cd = c.x * Lr[k] + c.y * Lg[k] + c.z * Lb[k];
+            Pd[k] = fmaf(wt, cd, Pd[k]);
+            const float inv = __frcp_rn(1.f - al);
+            const float dLda = T[k] * cd - inv * (K[k] - Pd[k]);
+            T[k] = fmaf(-al, T[k], T[k]);
+            v[8] = fmaf(wt, Lr[k], v[8]);
+            v[9] = fmaf(wt, Lg[k], v[9]);
+            v[10] = fmaf(wt, Lb[k], v[10]);
+            const float dp = dLda * al;  // dL/dexponent / ln2
+            // d exponent / d(centre x) = 2 A1 w, d / d(centre y) = 2 A1 P w + 2 C1 dy
+            const float gw = A2 * w;
+            const float tx = dp * gw;
+            const float ty = dp * fmaf(gw, q.y, c2dy);
+            const float ddx = dx[cc];
+            v[0] += tx;
+            v[1] += ty;
+            v[2] += fabsf(tx);
+            v[3] += fabsf(ty);
+            v[4] = fmaf(dp, ddx * ddx, v[4]);
+            v[5] = fmaf(dp * ddx, dy, v[5]);
+            v[7] = fmaf(dp * dy, dy, v[7]);
+            v[11] += dp;
+          }
         }
       }
       if (__any_sync(0xffffffffu, any)) {
@@ -458,7 +479,10 @@ extern "C" fgs_status fgs_render_bwd(int P, int width, int height, int block_x, 
             width, height, block_x, block_y, gx, bucket_size};
   {
     KernelTimer kt__(FGS_K_RENDER_BWD, s);
-    k_render_bwd<<<num_sms() * 8, kBwdWarps * kWarp, 0, s>>>(a);
+    const int grid = num_sms() * 8;
+    if (block_x == 8) k_render_bwd<8><<<grid, kBwdWarps * kWarp, 0, s>>>(a);
+    else if (block_x == 16) k_render_bwd<16><<<grid, kBwdWarps * kWarp, 0, s>>>(a);
+    else k_render_bwd<32><<<grid, kBwdWarps * kWarp, 0, s>>>(a);
     kt__.stop();
   }
   FGS_LAUNCH_CHECK();

@@ -97,46 +97,67 @@ struct FwdArgs {
   int W, H, bx, by, gx, bs;
 };
 
+template <int BX>
 __global__ void __launch_bounds__(kFwdWarps * kWarp) k_render_fwd(const FwdArgs a) {
+  using M = TileMap<BX>;
+  constexpr int BY = kTilePixels / BX;
   __shared__ BucketStage s_stage[kFwdWarps];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   BucketStage& st = s_stage[warp];
   const int B = (int)a.bucket_sum[0];
-  const int lx = lane % a.bx, ly0 = lane / a.bx;
-  const float ystep = (float)(kWarp / a.bx);
   for (int b = blockIdx.x * kFwdWarps + warp; b < B; b += gridDim.x * kFwdWarps) {
     const BucketInfo bi = bucket_info(b, a.bucket_tile, a.bucket_off, a.ranges, a.bs);
-    stage_bucket(st, a.splat, a.vals + bi.start, bi.n, lane);
-    const float px = (float)((bi.tile % a.gx) * a.bx + lx);
-    const float py0 = (float)((bi.tile / a.gx) * a.by + ly0);
+    const int tx0 = (bi.tile % a.gx) * BX, ty0 = (bi.tile / a.gx) * BY;
+    stage_bucket<BX>(st, a.splat, a.vals + bi.start, bi.n, lane, tx0, ty0);
+    float pxc[M::kCols], pyr[M::kRows];
+#pragma unroll
+    for (int c = 0; c < M::kCols; ++c) pxc[c] = (float)(tx0 + 8 * c + (lane & 7));
+#pragma unroll
+    for (int r = 0; r < M::kRows; ++r) pyr[r] = (float)(ty0 + 4 * r + (lane >> 3));
     float T[kPxPerThread], Cr[kPxPerThread], Cg[kPxPerThread], Cb[kPxPerThread];
 #pragma unroll
     for (int k = 0; k < kPxPerThread; ++k) { T[k] = 1.f; Cr[k] = 0.f; Cg[k] = 0.f; Cb[k] = 0.f; }
     for (int g = 0; g < bi.n; ++g) {
+      const uint32_t mask = st.mask[g];
+      if (mask == 0) continue;  // alpha < 1/256 on the whole tile
       const float4 pos = st.pos[g];
       const float4 q = st.quad[g];   // A1, P, C1, log2 o
       const float4 c = st.rgb[g];
-      const float dx = centre_offset(pos.x, pos.z, px);
-      const float ry = pos.y - py0;  // exact: both are integers
+      float dx[M::kCols];
 #pragma unroll
-      for (int k = 0; k < kPxPerThread; ++k) {
-        const float dy = (ry - (float)k * ystep) + pos.w;
-        // alpha = o * exp(-q/2) = 2^(log2 o + A1 (dx + P dy)^2 + C1 dy^2)
-        const float w = fmaf(q.y, dy, dx);
-        const float e = fmaf(q.x * w, w, fmaf(q.z * dy, dy, q.w));
-        float al = fminf(kAlphaMax, ex2_approx(e));
-        al = al < kAlphaCut ? 0.f : al;
-        const float wt = al * T[k];
-        Cr[k] = fmaf(c.x, wt, Cr[k]);
-        Cg[k] = fmaf(c.y, wt, Cg[k]);
-        Cb[k] = fmaf(c.z, wt, Cb[k]);
-        T[k] = fmaf(-al, T[k], T[k]);  // T (1 - alpha), rounded once
+      for (int cc = 0; cc < M::kCols; ++cc) dx[cc] = centre_offset(pos.x, pos.z, pxc[cc]);
+#pragma unroll
+      for (int r = 0; r < M::kRows; ++r) {
+        const uint32_t rm = (mask >> (r * M::kCols)) & ((1u << M::kCols) - 1u);
+        if (rm == 0) continue;
+        const float dy = centre_offset(pos.y, pos.w, pyr[r]);
+        const float f = fmaf(q.z * dy, dy, q.w);  // log2 o + C1 dy^2
+#pragma unroll
+        for (int cc = 0; cc < M::kCols; ++cc) {
+          if (!((rm >> cc) & 1u)) continue;
+          const int k = r * M::kCols + cc;
+          // alpha = o * exp(-q/2) = 2^(log2 o + A1 (dx + P dy)^2 + C1 dy^2)
+          const float w = fmaf(q.y, dy, dx[cc]);
+          const float e = fmaf(q.x * w, w, f);
+          float al = fminf(kAlphaMax, ex2_approx(e));
+          al = al < kAlphaCut ? 0.f : al;
+          const float wt = al * T[k];
+          Cr[k] = fmaf(c.x, wt, Cr[k]);
+          Cg[k] = fmaf(c.y, wt, Cg[k]);
+          Cb[k] = fmaf(c.z, wt, Cb[k]);
+          T[k] = fmaf(-al, T[k], T[k]);  // T (1 - alpha), rounded once
+        }
       }
     }
     __syncwarp();
-    float4* out = a.samples + (size_t)b * kTilePixels + lane;
+    float4* out = a.samples + (size_t)b * kTilePixels;
 #pragma unroll
-    for (int k = 0; k < kPxPerThread; ++k) out[k * kWarp] = make_float4(Cr[k], Cg[k], Cb[k], T[k]);
+    for (int r = 0; r < M::kRows; ++r)
+#pragma unroll
+      for (int cc = 0; cc < M::kCols; ++cc) {
+        const int k = r * M::kCols + cc;
+        out[M::pix(r, cc, lane)] = make_float4(Cr[k], Cg[k], Cb[k], T[k]);
+      }
   }
 }
 
@@ -278,7 +299,10 @@ extern "C" fgs_status fgs_render_fwd(int P, int64_t num_rendered, int width, int
              width, height, block_x, block_y, gx, bucket_size};
   {
     KernelTimer kt__(FGS_K_RENDER_FWD, s);
-    k_render_fwd<<<num_sms() * 8, kFwdWarps * kWarp, 0, s>>>(fa);
+    const int grid = num_sms() * 8;
+    if (block_x == 8) k_render_fwd<8><<<grid, kFwdWarps * kWarp, 0, s>>>(fa);
+    else if (block_x == 16) k_render_fwd<16><<<grid, kFwdWarps * kWarp, 0, s>>>(fa);
+    else k_render_fwd<32><<<grid, kFwdWarps * kWarp, 0, s>>>(fa);
     kt__.stop();
   }
   FGS_LAUNCH_CHECK();

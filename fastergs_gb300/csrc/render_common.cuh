@@ -55,25 +55,65 @@ inline SampleState carve_sample(void* base, int64_t max_buckets) {
   return s;
 }
 
-// Records of one bucket staged in shared memory, structure-of-arrays.
-struct BucketStage {
-  float4 pos[kMaxBucket];   // floor(x), floor(y), fraction x, fraction y
-  float4 quad[kMaxBucket];  // A1, P, C1, log2 opacity
-  float4 rgb[kMaxBucket];   // r, g, b, Gaussian id bits
+// Pixel mapping of the compositing kernels: a warp covers one tile as a grid
+// of 8 x 4 sub-blocks (2 x 4 of them for 16 x 16 tiles); lane l owns pixel
+// (l & 7, l >> 3) of every sub-block.  A Gaussian is evaluated only on the
+// sub-blocks its alpha >= 1/256 ellipse reaches, a warp-uniform decision.
+template <int BX>
+struct TileMap {
+  static constexpr int kCols = BX / 8;               // sub-blocks per row
+  static constexpr int kRows = kTilePixels / BX / 4;  // sub-block rows
+  static_assert(kCols * kRows == kPxPerThread, "one pixel per lane per sub-block");
+  // pixel index inside the tile (row-major, BX wide) of sub-block (r, c) for this lane
+  __device__ static int pix(int r, int c, int lane) { return (4 * r + (lane >> 3)) * BX + 8 * c + (lane & 7); }
 };
 
-// Load the render fields (floats 0..11) of the n records whose ids start at ids.
+// Records of one bucket staged in shared memory, structure-of-arrays.
+struct BucketStage {
+  float4 pos[kMaxBucket];     // floor(x), floor(y), fraction x, fraction y
+  float4 quad[kMaxBucket];    // A1, P, C1, log2 opacity
+  float4 rgb[kMaxBucket];     // r, g, b, Gaussian id bits
+  uint32_t mask[kMaxBucket];  // sub-blocks the Gaussian can reach (bit r * kCols + c)
+};
+
+// Stage the render fields (floats 0..11) of the n records whose ids start at
+// ids, and each Gaussian's sub-block mask for the tile at (tx0, ty0).
+template <int BX>
 __device__ __forceinline__ void stage_bucket(BucketStage& st, const float* __restrict__ splat,
-                                             const uint32_t* __restrict__ ids, int n, int lane) {
+                                             const uint32_t* __restrict__ ids, int n, int lane, int tx0, int ty0) {
+  using M = TileMap<BX>;
   for (int j = lane; j < n; j += kWarp) {
     const uint32_t id = ids[j];
     const float4* r = reinterpret_cast<const float4*>(splat + (size_t)id * 32);
     const float4 a = __ldg(r);        // x, y, r, g
     const float4 b = __ldg(r + 1);    // b, depth, A1, P
     const float4 c = __ldg(r + 2);    // C1, log2 o, fraction x, fraction y
-    st.pos[j] = make_float4(floorf(a.x), floorf(a.y), c.z, c.w);
+    const float X = floorf(a.x), Y = floorf(a.y);
+    st.pos[j] = make_float4(X, Y, c.z, c.w);
     st.quad[j] = make_float4(b.z, b.w, c.x, c.y);
     st.rgb[j] = make_float4(a.z, a.w, b.x, __uint_as_float(id));
+    // Half-extents of the ellipse alpha >= 1/256, i.e. q <= 2 ln(256 o):
+    // |dx| <= sqrt(Q cov_xx), |dy| <= sqrt(Q cov_yy) with cov_yy = -0.5 log2e / C1
+    // and cov_xx = P^2 cov_yy + 1 / conic_a, 1 / conic_a = -0.5 log2e / A1.
+    // Outside it alpha < 1/256 < 1/255 even after FP32 rounding, so skipping
+    // those pixels changes nothing.
+    const float Q = 2.0f * kLn2 * (c.y + 8.0f);
+    const float cyy = -0.5f * kLog2e / c.x;
+    const float cxx = b.w * b.w * cyy - 0.5f * kLog2e / b.z;
+    const float rx = sqrtf(fmaxf(Q * cxx, 0.f)) + 1e-3f, ry = sqrtf(fmaxf(Q * cyy, 0.f)) + 1e-3f;
+    const float cx = (X - (float)tx0) + c.z, cy = (Y - (float)ty0) + c.w;
+    uint32_t cols = 0, rows = 0;
+#pragma unroll
+    for (int k = 0; k < M::kCols; ++k)
+      if (cx + rx >= 8.f * k && cx - rx <= 8.f * k + 7.f) cols |= 1u << k;
+#pragma unroll
+    for (int k = 0; k < M::kRows; ++k)
+      if (cy + ry >= 4.f * k && cy - ry <= 4.f * k + 3.f) rows |= 1u << k;
+    uint32_t m = 0;
+#pragma unroll
+    for (int k = 0; k < M::kRows; ++k)
+      if ((rows >> k) & 1u) m |= cols << (k * M::kCols);
+    st.mask[j] = (Q > 0.f) ? m : 0u;
   }
   __syncwarp();
 }
