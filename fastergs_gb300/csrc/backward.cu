@@ -27,7 +27,7 @@ struct BwdArgs {
   const uint32_t* ranges;
   const uint32_t* bucket_tile;
   const uint32_t* bucket_off;
-  const uint32_t* bucket_sum;
+  uint32_t* bucket_sum;
   const uint32_t* max_contrib;
   const float4* samples;
   const float* pix_color;
@@ -73,7 +73,7 @@ __device__ __forceinline__ float warp_transpose_reduce16(float (&v)[16], int lan
 }
 
 template <int BX>
-__global__ void __launch_bounds__(kBwdWarps * kWarp) k_render_bwd(const BwdArgs a) {
+__global__ void __launch_bounds__(kBwdWarps * kWarp, 5) k_render_bwd(const BwdArgs a) {
   using M = TileMap<BX>;
   constexpr int BY = kTilePixels / BX;
   __shared__ BucketStage s_stage[kBwdWarps];
@@ -92,10 +92,14 @@ __global__ void __launch_bounds__(kBwdWarps * kWarp) k_render_bwd(const BwdArgs 
                        : (vid >= 4 && vid <= 7) ? -0.5f
                                                 : 1.0f;
 
-  for (int b = blockIdx.x * kBwdWarps + warp; b < B; b += gridDim.x * kBwdWarps) {
+  for (int b = next_bucket(a.bucket_sum + 3, lane); b < B;) {
+    const int b_next = next_bucket(a.bucket_sum + 3, lane);
     const BucketInfo bi = bucket_info(b, a.bucket_tile, a.bucket_off, a.ranges, a.bs);
     const uint32_t thres = (uint32_t)(bi.local * a.bs);
-    if (thres >= a.max_contrib[bi.tile]) continue;  // no pixel of the tile reaches this bucket
+    if (thres >= a.max_contrib[bi.tile]) {  // no pixel of the tile reaches this bucket
+      b = b_next;
+      continue;
+    }
     const int tx0 = (bi.tile % a.gx) * BX, ty0 = (bi.tile / a.gx) * BY;
     stage_bucket<BX>(st, a.splat, a.vals + bi.start, bi.n, lane, tx0, ty0);
     float pxc[M::kCols], pyr[M::kRows];
@@ -134,6 +138,7 @@ __global__ void __launch_bounds__(kBwdWarps * kWarp) k_render_bwd(const BwdArgs 
       }
     if (__any_sync(0xffffffffu, alive) == 0) {
       __syncwarp();
+      b = b_next;
       continue;
     }
 
@@ -202,6 +207,7 @@ __global__ void __launch_bounds__(kBwdWarps * kWarp) k_render_bwd(const BwdArgs 
       }
     }
     __syncwarp();
+    b = b_next;
   }
 }
 
@@ -474,15 +480,17 @@ extern "C" fgs_status fgs_render_bwd(int P, int width, int height, int block_x, 
   const SampleState sm = carve_sample(const_cast<void*>(sample_state), max_buckets > 0 ? max_buckets : 1);
   cudaStream_t s = (cudaStream_t)stream;
   FGS_TRY(cudaMemsetAsync(grad_record, 0, sizeof(float) * FGS_GRAD_STRIDE * (size_t)P, s));
+  // backward work cursor (word 3 of the image-state header); reset on every call
+  FGS_TRY(cudaMemsetAsync(im.bucket_sum + 3, 0, sizeof(uint32_t), s));
   BwdArgs a{splat_buffer, values_sorted, ranges, sm.bucket_tile, im.bucket_off, im.bucket_sum, im.max_contrib,
             sm.samples, im.pix_color, Ts_final, last_contributor, dL_dpixels, bg, grad_record,
             width, height, block_x, block_y, gx, bucket_size};
   {
     KernelTimer kt__(FGS_K_RENDER_BWD, s);
-    const int grid = num_sms() * 8;
-    if (block_x == 8) k_render_bwd<8><<<grid, kBwdWarps * kWarp, 0, s>>>(a);
-    else if (block_x == 16) k_render_bwd<16><<<grid, kBwdWarps * kWarp, 0, s>>>(a);
-    else k_render_bwd<32><<<grid, kBwdWarps * kWarp, 0, s>>>(a);
+    const int nt = kBwdWarps * kWarp;
+    if (block_x == 8) k_render_bwd<8><<<num_sms() * resident_blocks(k_render_bwd<8>, nt, 0), nt, 0, s>>>(a);
+    else if (block_x == 16) k_render_bwd<16><<<num_sms() * resident_blocks(k_render_bwd<16>, nt, 0), nt, 0, s>>>(a);
+    else k_render_bwd<32><<<num_sms() * resident_blocks(k_render_bwd<32>, nt, 0), nt, 0, s>>>(a);
     kt__.stop();
   }
   FGS_LAUNCH_CHECK();

@@ -82,6 +82,7 @@ __global__ void __launch_bounds__(1024) k_bucket_setup(int T, const uint32_t* __
   if (tid == 0) {
     bucket_sum[0] = (uint32_t)min((long long)total, max_buckets);
     bucket_sum[1] = total;
+    bucket_sum[2] = 0;  // forward work cursor
     if ((long long)total > max_buckets) raise_error(kErrCapacity);
   }
 }
@@ -92,20 +93,21 @@ struct FwdArgs {
   const uint32_t* ranges;
   const uint32_t* bucket_tile;
   const uint32_t* bucket_off;
-  const uint32_t* bucket_sum;
+  uint32_t* bucket_sum;
   float4* samples;
   int W, H, bx, by, gx, bs;
 };
 
 template <int BX>
-__global__ void __launch_bounds__(kFwdWarps * kWarp) k_render_fwd(const FwdArgs a) {
+__global__ void __launch_bounds__(kFwdWarps * kWarp, 8) k_render_fwd(const FwdArgs a) {
   using M = TileMap<BX>;
   constexpr int BY = kTilePixels / BX;
   __shared__ BucketStage s_stage[kFwdWarps];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   BucketStage& st = s_stage[warp];
   const int B = (int)a.bucket_sum[0];
-  for (int b = blockIdx.x * kFwdWarps + warp; b < B; b += gridDim.x * kFwdWarps) {
+  for (int b = next_bucket(a.bucket_sum + 2, lane); b < B;) {
+    const int b_next = next_bucket(a.bucket_sum + 2, lane);
     const BucketInfo bi = bucket_info(b, a.bucket_tile, a.bucket_off, a.ranges, a.bs);
     const int tx0 = (bi.tile % a.gx) * BX, ty0 = (bi.tile / a.gx) * BY;
     stage_bucket<BX>(st, a.splat, a.vals + bi.start, bi.n, lane, tx0, ty0);
@@ -158,6 +160,7 @@ __global__ void __launch_bounds__(kFwdWarps * kWarp) k_render_fwd(const FwdArgs 
         const int k = r * M::kCols + cc;
         out[M::pix(r, cc, lane)] = make_float4(Cr[k], Cg[k], Cb[k], T[k]);
       }
+    b = b_next;
   }
 }
 
@@ -299,10 +302,10 @@ extern "C" fgs_status fgs_render_fwd(int P, int64_t num_rendered, int width, int
              width, height, block_x, block_y, gx, bucket_size};
   {
     KernelTimer kt__(FGS_K_RENDER_FWD, s);
-    const int grid = num_sms() * 8;
-    if (block_x == 8) k_render_fwd<8><<<grid, kFwdWarps * kWarp, 0, s>>>(fa);
-    else if (block_x == 16) k_render_fwd<16><<<grid, kFwdWarps * kWarp, 0, s>>>(fa);
-    else k_render_fwd<32><<<grid, kFwdWarps * kWarp, 0, s>>>(fa);
+    const int nt = kFwdWarps * kWarp;
+    if (block_x == 8) k_render_fwd<8><<<num_sms() * resident_blocks(k_render_fwd<8>, nt, 0), nt, 0, s>>>(fa);
+    else if (block_x == 16) k_render_fwd<16><<<num_sms() * resident_blocks(k_render_fwd<16>, nt, 0), nt, 0, s>>>(fa);
+    else k_render_fwd<32><<<num_sms() * resident_blocks(k_render_fwd<32>, nt, 0), nt, 0, s>>>(fa);
     kt__.stop();
   }
   FGS_LAUNCH_CHECK();

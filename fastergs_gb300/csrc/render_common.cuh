@@ -16,7 +16,7 @@ struct ImageState {
   float* pix_color;         // 3 * HW
   uint32_t* max_contrib;    // T
   uint32_t* bucket_off;     // T (inclusive scan of bucket counts)
-  uint32_t* bucket_sum;     // 1
+  uint32_t* bucket_sum;     // [0] buckets (capped), [1] buckets (uncapped), [2], [3] work cursors
   size_t bytes;
 };
 
@@ -122,6 +122,24 @@ __device__ __forceinline__ void stage_bucket(BucketStage& st, const float* __res
 // subtract exactly, the fraction adds once.
 __device__ __forceinline__ float centre_offset(float whole, float frac, float pixel) {
   return (whole - pixel) + frac;
+}
+
+// Dynamic bucket scheduling for the persistent compositing kernels: every
+// warp takes the next unprocessed bucket from a device cursor, so buckets of
+// very different cost balance across SMs.  Lane 0 fetches; the next index is
+// requested before the current bucket is processed to hide the atomic.
+__device__ __forceinline__ int next_bucket(uint32_t* cursor, int lane) {
+  uint32_t b = 0;
+  if (lane == 0) b = atomicAdd(cursor, 1u);
+  return (int)__shfl_sync(0xffffffffu, b, 0);
+}
+
+// Blocks per SM that a kernel can keep resident, for sizing persistent grids.
+template <typename K>
+inline int resident_blocks(K kernel, int threads, size_t smem) {
+  int n = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kernel, threads, smem) != cudaSuccess || n < 1) n = 1;
+  return n;
 }
 
 // Bucket b -> (tile, first pair, pair count, index of the bucket in its tile).
