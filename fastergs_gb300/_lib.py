@@ -18,6 +18,20 @@ _LOCK = threading.Lock()
 vp, i32, i64, f32, sz = C.c_void_p, C.c_int, C.c_int64, C.c_float, C.c_size_t
 u32p = C.POINTER(C.c_uint32)
 
+
+class Camera(C.Structure):
+    """fgs_camera: one view of a batched frame (device pointers, host struct)."""
+    _fields_ = [("viewmatrix", vp), ("projmatrix", vp), ("campos", vp), ("bg", vp), ("width", i32),
+                ("height", i32), ("tan_fovx", f32), ("tan_fovy", f32), ("scale_modifier", f32), ("mult", f32)]
+
+
+class TuneConfig(C.Structure):
+    """fgs_tune_config: bucket size, tile shape and packet width of a launch."""
+    _fields_ = [("bucket_size", i32), ("block_x", i32), ("block_y", i32), ("packet", i32)]
+
+
+camp, tunep = C.POINTER(Camera), C.POINTER(TuneConfig)
+
 # name: (restype, argtypes) -- mirrors include/fgs.h
 SIGNATURES = {
     "fgs_status_string": (C.c_char_p, [i32]),
@@ -38,6 +52,13 @@ SIGNATURES = {
                                  vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp]),
     "fgs_densify_stats": (i32, [i32, vp, vp, vp, vp, vp, vp, vp]),
     "fgs_adam_update": (i32, [vp, vp, vp, vp, vp, f32, f32, f32, f32, C.c_uint32, C.c_uint32, vp]),
+    "fgs_batch_workspace_bytes": (i32, [i32, i32, camp, tunep, i64, C.POINTER(C.c_size_t)]),
+    "fgs_render_batched_fwd": (i32, [i32, i32, i32, vp, vp, vp, vp, vp, vp, vp, vp, i32, camp, tunep, i64, vp, sz,
+                                     vp, vp, vp]),
+    "fgs_render_batched_bwd": (i32, [i32, i32, i32, vp, vp, vp, vp, vp, i32, camp, tunep, i64, vp, sz, vp, vp,
+                                     vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp]),
+    "fgs_batch_status": (i32, [i32, i32, camp, tunep, i64, vp, C.POINTER(C.c_int64), C.POINTER(C.c_int64), vp]),
+    "fgs_batch_offsets": (i32, [i32, i32, camp, tunep, i64, C.POINTER(C.c_int64), i32]),
     "fgs_kernel_timer": (i32, [i32, i32]),
     "fgs_kernel_timer_read": (i32, [i32, C.POINTER(C.c_double), C.POINTER(C.c_int)]),
 }

@@ -22,6 +22,7 @@ namespace {
 constexpr int kBwdWarps = 4;
 
 struct BwdArgs {
+  Views views;
   const float* splat;
   const uint32_t* vals;
   const uint32_t* ranges;
@@ -30,13 +31,12 @@ struct BwdArgs {
   uint32_t* bucket_sum;
   const uint32_t* max_contrib;
   const float4* samples;
-  const float* pix_color;
-  const float* Ts_final;
+  const float* pix_color;    // per view (3, H, W) at 3 * pix_off
+  const float* Ts_final;     // per view (H, W) at pix_off
   const int* last_contrib;
-  const float* dL;
-  const float* bg;
-  float* grad;
-  int W, H, bx, by, gx, bs;
+  const float* dL;           // per view (3, H, W) at 3 * pix_off
+  float* grad;               // gradient record per (view, Gaussian) record
+  int bs;
 };
 
 // Sum 16 per-lane values over the warp.  On return lane l holds the total of
@@ -80,17 +80,7 @@ __global__ void __launch_bounds__(kBwdWarps * kWarp, 5) k_render_bwd(const BwdAr
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   BucketStage& st = s_stage[warp];
   const int B = (int)a.bucket_sum[0];
-  const int HW = a.W * a.H;
-  const float hx = 0.5f * (float)a.W, hy = 0.5f * (float)a.H;
-  const float bgr = a.bg[0], bgg = a.bg[1], bgb = a.bg[2];
-  // Scale applied after the reduction to the value a lane ends up holding:
-  // mean2D x/|x| need ln2 * W/2, y/|y| ln2 * H/2, conic -0.5 (ln2 * -0.5 log2e),
-  // colour 1, opacity ln2 * log2e / o = 1 / o (applied per Gaussian).
-  const int vid = (lane >> 1) & 15;
-  const float vscale = (vid == 0 || vid == 2)   ? kLn2 * hx
-                       : (vid == 1 || vid == 3) ? kLn2 * hy
-                       : (vid >= 4 && vid <= 7) ? -0.5f
-                                                : 1.0f;
+  const int vid = (lane >> 1) & 15;  // value a lane holds after the transpose reduction
 
   for (int b = next_bucket(a.bucket_sum + 3, lane); b < B;) {
     const int b_next = next_bucket(a.bucket_sum + 3, lane);
@@ -100,7 +90,22 @@ __global__ void __launch_bounds__(kBwdWarps * kWarp, 5) k_render_bwd(const BwdAr
       b = b_next;
       continue;
     }
-    const int tx0 = (bi.tile % a.gx) * BX, ty0 = (bi.tile / a.gx) * BY;
+    const ViewDesc& cam = a.views.v[a.views.of_tile((uint32_t)bi.tile)];
+    const int lt = bi.tile - (int)cam.tile_off;  // tile index inside its view
+    const int tx0 = (lt % cam.gx) * BX, ty0 = (lt / cam.gx) * BY;
+    const int HW = cam.W * cam.H;
+    const float* dL = a.dL + 3 * (size_t)cam.pix_off;
+    const float* pcol = a.pix_color + 3 * (size_t)cam.pix_off;
+    const float* Tfin = a.Ts_final + cam.pix_off;
+    const int* lcon = a.last_contrib + cam.pix_off;
+    const float bgr = cam.bg[0], bgg = cam.bg[1], bgb = cam.bg[2];
+    // Scale applied after the reduction to the value a lane ends up holding:
+    // mean2D x/|x| need ln2 * W/2, y/|y| ln2 * H/2 (NDC), conic -0.5
+    // (ln2 * -0.5 log2e), colour 1, opacity ln2 * log2e / o = 1 / o (per Gaussian).
+    const float vscale = (vid == 0 || vid == 2)   ? kLn2 * 0.5f * (float)cam.W
+                         : (vid == 1 || vid == 3) ? kLn2 * 0.5f * (float)cam.H
+                         : (vid >= 4 && vid <= 7) ? -0.5f
+                                                  : 1.0f;
     stage_bucket<BX>(st, a.splat, a.vals + bi.start, bi.n, lane, tx0, ty0);
     float pxc[M::kCols], pyr[M::kRows];
 #pragma unroll
@@ -118,21 +123,21 @@ __global__ void __launch_bounds__(kBwdWarps * kWarp, 5) k_render_bwd(const BwdAr
         const int k = r * M::kCols + cc;
         const int gxp = (int)pxc[cc], gyp = (int)pyr[r];
         T[k] = 0.f; Pd[k] = 0.f; Lr[k] = 0.f; Lg[k] = 0.f; Lb[k] = 0.f; K[k] = 0.f;
-        if (gxp < a.W && gyp < a.H) {
-          const int pix = gyp * a.W + gxp;
-          if ((uint32_t)a.last_contrib[pix] > thres) {
+        if (gxp < cam.W && gyp < cam.H) {
+          const int pix = gyp * cam.W + gxp;
+          if ((uint32_t)lcon[pix] > thres) {
             alive |= 1u << k;
             const float4 prev = bi.local > 0 ? a.samples[(size_t)(b - 1) * kTilePixels + M::pix(r, cc, lane)]
                                              : make_float4(0.f, 0.f, 0.f, 1.f);
-            Lr[k] = a.dL[pix];
-            Lg[k] = a.dL[HW + pix];
-            Lb[k] = a.dL[2 * HW + pix];
+            Lr[k] = dL[pix];
+            Lg[k] = dL[HW + pix];
+            Lb[k] = dL[2 * HW + pix];
             T[k] = prev.w;
             Pd[k] = prev.x * Lr[k] + prev.y * Lg[k] + prev.z * Lb[k];
             // K = C_final . dL + T_final * (bg . dL): everything behind a
             // Gaussian is K - (prefix up to and including it) . dL.
-            K[k] = a.pix_color[pix] * Lr[k] + a.pix_color[HW + pix] * Lg[k] +
-                   a.pix_color[2 * HW + pix] * Lb[k] + a.Ts_final[pix] * (bgr * Lr[k] + bgg * Lg[k] + bgb * Lb[k]);
+            K[k] = pcol[pix] * Lr[k] + pcol[HW + pix] * Lg[k] + pcol[2 * HW + pix] * Lb[k] +
+                   Tfin[pix] * (bgr * Lr[k] + bgg * Lg[k] + bgb * Lb[k]);
           }
         }
       }
@@ -211,233 +216,215 @@ __global__ void __launch_bounds__(kBwdWarps * kWarp, 5) k_render_bwd(const BwdAr
   }
 }
 
-struct PbwdArgs {
-  int P, D, M;
-  const float* means;
-  const int* radii;
-  const float* dc;
-  const float* shs;
-  const float* splat;
-  const float* scales;
-  const float* rots;
-  float smod;
-  const float* view;
-  const float* proj;
-  float fx, fy, tanx, tany;
-  const float* campos;
-  const float* grad;
-  float* dmean2D;
-  float* dconic;
-  float* dopac;
-  float* dcolor;
-  float* dmean3D;
-  float* dcov3D;
-  float* ddc;
-  float* dsh;
-  float* dscale;
-  float* drot;
-  float* accum;
-  float* accum_abs;
-  float* max_radii;
-  float* denom;
-};
-
+// One SH basis term: d colour / d coefficient = B, d B / d direction = (bx, by, bz).
+// out receives B * drgb (assigned for the first contributing view, added after).
 __device__ __forceinline__ void sh_term(float B, float bx, float by, float bz, const float* co, float* out,
-                                        float3 drgb, float3& ddir) {
-  out[0] = B * drgb.x;
-  out[1] = B * drgb.y;
-  out[2] = B * drgb.z;
+                                        float3 drgb, float3& ddir, bool add) {
+  out[0] = (add ? out[0] : 0.f) + B * drgb.x;
+  out[1] = (add ? out[1] : 0.f) + B * drgb.y;
+  out[2] = (add ? out[2] : 0.f) + B * drgb.z;
   const float dot = co[0] * drgb.x + co[1] * drgb.y + co[2] * drgb.z;
   ddir.x = fmaf(bx, dot, ddir.x);
   ddir.y = fmaf(by, dot, ddir.y);
   ddir.z = fmaf(bz, dot, ddir.z);
 }
 
+// One thread per Gaussian; loops over the views and sums their gradients
+// (FB backward.cu:250-539, 892-918 for one view).
 __global__ void __launch_bounds__(256) k_preprocess_bwd(const PbwdArgs a) {
   const int i = blockIdx.x * 256 + threadIdx.x;
   if (i >= a.P) return;
-  const float4* gr = reinterpret_cast<const float4*>(a.grad + (size_t)i * FGS_GRAD_STRIDE);
-  const float4 gm2 = gr[0], gcn = gr[1], gco = gr[2];
-  reinterpret_cast<float4*>(a.dmean2D)[i] = gm2;
-  reinterpret_cast<float4*>(a.dconic)[i] = make_float4(gcn.x, gcn.y, 0.f, gcn.w);
-  a.dcolor[3 * (size_t)i] = gco.x;
-  a.dcolor[3 * (size_t)i + 1] = gco.y;
-  a.dcolor[3 * (size_t)i + 2] = gco.z;
-  a.dopac[i] = gco.w;
-  float* gm = a.dmean3D + 3 * (size_t)i;
-  float* gc = a.dcov3D + 6 * (size_t)i;
-  float* gdc = a.ddc + 3 * (size_t)i;
   float* gsh = a.dsh ? a.dsh + (size_t)i * a.M * 3 : nullptr;
-  float* gs = a.dscale + 3 * (size_t)i;
-  const int radius = a.radii[i];
-  if (!(radius > 0)) {
-    gm[0] = gm[1] = gm[2] = 0.f;
-    for (int k = 0; k < 6; ++k) gc[k] = 0.f;
-    gdc[0] = gdc[1] = gdc[2] = 0.f;
-    if (gsh) for (int k = 0; k < 3 * a.M; ++k) gsh[k] = 0.f;
-    gs[0] = gs[1] = gs[2] = 0.f;
-    reinterpret_cast<float4*>(a.drot)[i] = make_float4(0.f, 0.f, 0.f, 0.f);
-    return;
-  }
+  const int used = (a.D + 1) * (a.D + 1) - 1;
+  float m3[3] = {0.f, 0.f, 0.f}, gc[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f}, gs[3] = {0.f, 0.f, 0.f};
+  float gq[4] = {0.f, 0.f, 0.f, 0.f}, gdc[3] = {0.f, 0.f, 0.f};
+  float4 gco_sum = make_float4(0.f, 0.f, 0.f, 0.f);
+  bool sh_written = false;
   const float3 p = make_float3(a.means[3 * (size_t)i], a.means[3 * (size_t)i + 1], a.means[3 * (size_t)i + 2]);
-  // --- rotation / covariance (raw quaternion, FB backward.cu:407-430)
+  // --- rotation of the raw quaternion (FB backward.cu:407-430)
   const float4 q = reinterpret_cast<const float4*>(a.rots)[i];
   const float qr = q.x, qx = q.y, qy = q.z, qz = q.w;
   float R[3][3];
   R[0][0] = 1.f - 2.f * (qy * qy + qz * qz); R[0][1] = 2.f * (qx * qy - qr * qz); R[0][2] = 2.f * (qx * qz + qr * qy);
   R[1][0] = 2.f * (qx * qy + qr * qz); R[1][1] = 1.f - 2.f * (qx * qx + qz * qz); R[1][2] = 2.f * (qy * qz - qr * qx);
   R[2][0] = 2.f * (qx * qz - qr * qy); R[2][1] = 2.f * (qy * qz + qr * qx); R[2][2] = 1.f - 2.f * (qx * qx + qy * qy);
-  const float sv[3] = {a.smod * a.scales[3 * (size_t)i], a.smod * a.scales[3 * (size_t)i + 1],
-                       a.smod * a.scales[3 * (size_t)i + 2]};
-  const float s2[3] = {sv[0] * sv[0], sv[1] * sv[1], sv[2] * sv[2]};
-  // --- conic -> cov2D -> cov3D / mean (FB backward.cu:250-403)
-  const float3 t = xform_point3(a.view, p);
-  const float limx = 1.3f * a.tanx, limy = 1.3f * a.tany;
-  const float txtz = t.x / t.z, tytz = t.y / t.z;
-  const float tx = fminf(limx, fmaxf(-limx, txtz)) * t.z;
-  const float ty = fminf(limy, fmaxf(-limy, tytz)) * t.z;
-  const float xm = (txtz < -limx || txtz > limx) ? 0.f : 1.f;
-  const float ym = (tytz < -limy || tytz > limy) ? 0.f : 1.f;
-  const float iz = 1.f / t.z, iz2 = iz * iz, iz3 = iz2 * iz;
-  const float j00 = a.fx * iz, j02 = -a.fx * tx * iz2, j11 = a.fy * iz, j12 = -a.fy * ty * iz2;
-  const float* V = a.view;
-  float M0[3], M1[3];
+  float dR[3][3];  // dL/dR of the raw quaternion's rotation, summed over views
 #pragma unroll
-  for (int b = 0; b < 3; ++b) {
-    M0[b] = j00 * V[b * 4 + 0] + j02 * V[b * 4 + 2];
-    M1[b] = j11 * V[b * 4 + 1] + j12 * V[b * 4 + 2];
-  }
-  const ScreenCov sc2 = screen_cov(M0, M1, R, s2);
-  const float idet = 1.f / sc2.det;
-  const float ia = sc2.c * idet, ib = -sc2.b * idet, ic = sc2.a * idet;  // C = Sigma2^-1 (the conic)
-  const float gx = gcn.x, gy = gcn.y, gz = gcn.w;  // dL/dconic, off-diagonal halved as FB stores it
-  // FB divides by den^2 + 1e-7 instead of den^2 (backward.cu:304); keep that factor.
-  const float rr = sc2.det * sc2.det / (sc2.det * sc2.det + 0.0000001f);
-  // dL/dSigma2 = rr * E with E = -C Gm C.  FB forms E and then projects it on
-  // each principal axis N_k (backward.cu:310-347, 445-454), which cancels with
-  // the square of the footprint's condition number; here every axis term is
-  // formed from v_k = C N_k instead: N_k^T E N_k = -v_k^T Gm v_k.
-  float dM0[3] = {0.f, 0.f, 0.f}, dM1[3] = {0.f, 0.f, 0.f};
-  float dR[3][3];  // dL/dR, R the rotation of the raw quaternion
+  for (int r = 0; r < 3; ++r)
 #pragma unroll
-  for (int k = 0; k < 3; ++k) {
-    const float v0 = ia * sc2.N0[k] + ib * sc2.N1[k];
-    const float v1 = ib * sc2.N0[k] + ic * sc2.N1[k];
-    const float g0 = gx * v0 + gy * v1, g1 = gy * v0 + gz * v1;
-    gs[k] = -2.f * sv[k] * rr * (v0 * g0 + v1 * g1);  // w.r.t. the modified scale, as FB returns it
-    const float y0 = ia * g0 + ib * g1, y1 = ib * g0 + ic * g1;
-    const float f = -2.f * s2[k] * rr;
+    for (int c = 0; c < 3; ++c) dR[r][c] = 0.f;
+
+  for (int vi = 0; vi < a.views.V; ++vi) {
+    const ViewDesc& cam = a.views.v[vi];
+    const size_t rid = (size_t)vi * a.P + i;
+    const float4* gr = reinterpret_cast<const float4*>(a.grad + rid * FGS_GRAD_STRIDE);
+    const float4 gm2 = gr[0], gcn = gr[1], gco = gr[2];
+    if (a.dmean2D) reinterpret_cast<float4*>(a.dmean2D)[rid] = gm2;
+    if (a.dconic) reinterpret_cast<float4*>(a.dconic)[rid] = make_float4(gcn.x, gcn.y, 0.f, gcn.w);
+    gco_sum.x += gco.x; gco_sum.y += gco.y; gco_sum.z += gco.z; gco_sum.w += gco.w;
+    const int radius = a.radii[rid];
+    if (!(radius > 0)) continue;
+    const float sv[3] = {cam.smod * a.scales[3 * (size_t)i], cam.smod * a.scales[3 * (size_t)i + 1],
+                         cam.smod * a.scales[3 * (size_t)i + 2]};
+    const float s2[3] = {sv[0] * sv[0], sv[1] * sv[1], sv[2] * sv[2]};
+    // --- conic -> cov2D -> cov3D / mean (FB backward.cu:250-403)
+    const float3 t = xform_point3(cam.view, p);
+    const float limx = 1.3f * cam.tanx, limy = 1.3f * cam.tany;
+    const float txtz = t.x / t.z, tytz = t.y / t.z;
+    const float tx = fminf(limx, fmaxf(-limx, txtz)) * t.z;
+    const float ty = fminf(limy, fmaxf(-limy, tytz)) * t.z;
+    const float xm = (txtz < -limx || txtz > limx) ? 0.f : 1.f;
+    const float ym = (tytz < -limy || tytz > limy) ? 0.f : 1.f;
+    const float iz = 1.f / t.z, iz2 = iz * iz, iz3 = iz2 * iz;
+    const float j00 = cam.fx * iz, j02 = -cam.fx * tx * iz2, j11 = cam.fy * iz, j12 = -cam.fy * ty * iz2;
+    const float* V = cam.view;
+    float M0[3], M1[3];
 #pragma unroll
     for (int b = 0; b < 3; ++b) {
-      dR[b][k] = f * (M0[b] * y0 + M1[b] * y1);
-      dM0[b] = fmaf(f * y0, R[b][k], dM0[b]);
-      dM1[b] = fmaf(f * y1, R[b][k], dM1[b]);
+      M0[b] = j00 * V[b * 4 + 0] + j02 * V[b * 4 + 2];
+      M1[b] = j11 * V[b * 4 + 1] + j12 * V[b * 4 + 2];
     }
-  }
-  {  // dL/dcov3D in FB's storage (diagonal once, off-diagonal doubled)
-    const float c00 = ia * gx + ib * gy, c01 = ia * gy + ib * gz, c10 = ib * gx + ic * gy, c11 = ib * gy + ic * gz;
-    const float E00 = -rr * (c00 * ia + c01 * ib), E01 = -rr * (c00 * ib + c01 * ic), E11 = -rr * (c10 * ib + c11 * ic);
-    float G[3][3];
+    const ScreenCov sc2 = screen_cov(M0, M1, R, s2);
+    const float idet = 1.f / sc2.det;
+    const float ia = sc2.c * idet, ib = -sc2.b * idet, ic = sc2.a * idet;  // C = Sigma2^-1 (the conic)
+    const float gx = gcn.x, gy = gcn.y, gz = gcn.w;  // dL/dconic, off-diagonal halved as FB stores it
+    // FB divides by den^2 + 1e-7 instead of den^2 (backward.cu:304); keep that factor.
+    const float rr = sc2.det * sc2.det / (sc2.det * sc2.det + 0.0000001f);
+    // dL/dSigma2 = rr * E with E = -C Gm C.  FB forms E and then projects it on
+    // each principal axis N_k (backward.cu:310-347, 445-454), which cancels with
+    // the square of the footprint's condition number; here every axis term is
+    // formed from v_k = C N_k instead: N_k^T E N_k = -v_k^T Gm v_k.
+    float dM0[3] = {0.f, 0.f, 0.f}, dM1[3] = {0.f, 0.f, 0.f};
 #pragma unroll
-    for (int r = 0; r < 3; ++r)
+    for (int k = 0; k < 3; ++k) {
+      const float v0 = ia * sc2.N0[k] + ib * sc2.N1[k];
+      const float v1 = ib * sc2.N0[k] + ic * sc2.N1[k];
+      const float g0 = gx * v0 + gy * v1, g1 = gy * v0 + gz * v1;
+      gs[k] += -2.f * sv[k] * rr * (v0 * g0 + v1 * g1);  // w.r.t. the modified scale, as FB returns it
+      const float y0 = ia * g0 + ib * g1, y1 = ib * g0 + ic * g1;
+      const float f = -2.f * s2[k] * rr;
 #pragma unroll
-      for (int c = 0; c < 3; ++c) G[r][c] = M0[r] * M0[c] * E00 + (M0[r] * M1[c] + M1[r] * M0[c]) * E01 + M1[r] * M1[c] * E11;
-    gc[0] = G[0][0]; gc[1] = 2.f * G[0][1]; gc[2] = 2.f * G[0][2];
-    gc[3] = G[1][1]; gc[4] = 2.f * G[1][2]; gc[5] = G[2][2];
-  }
-  // dL/dJ[a][k] = sum_b dM[a][b] * Rw[k][b], Rw[k][b] = V[b*4 + k]
-  const float dJ00 = dM0[0] * V[0] + dM0[1] * V[4] + dM0[2] * V[8];
-  const float dJ02 = dM0[0] * V[2] + dM0[1] * V[6] + dM0[2] * V[10];
-  const float dJ11 = dM1[0] * V[1] + dM1[1] * V[5] + dM1[2] * V[9];
-  const float dJ12 = dM1[0] * V[2] + dM1[1] * V[6] + dM1[2] * V[10];
-  const float dtx = xm * -a.fx * iz2 * dJ02;
-  const float dty = ym * -a.fy * iz2 * dJ12;
-  const float dtz = -a.fx * iz2 * dJ00 - a.fy * iz2 * dJ11 + 2.f * a.fx * tx * iz3 * dJ02 + 2.f * a.fy * ty * iz3 * dJ12;
-  float m3[3];
-#pragma unroll
-  for (int k = 0; k < 3; ++k) m3[k] = V[k * 4 + 0] * dtx + V[k * 4 + 1] * dty + V[k * 4 + 2] * dtz;
-  // --- screen-space mean (FB backward.cu:504-526)
-  const float4 hp = xform_point4(a.proj, p);
-  const float mw = 1.f / (hp.w + 0.0000001f);
-  const float* Pm = a.proj;
-#pragma unroll
-  for (int k = 0; k < 3; ++k) {
-    const float jx = Pm[4 * k] * mw - Pm[4 * k + 3] * hp.x * mw * mw;
-    const float jy = Pm[4 * k + 1] * mw - Pm[4 * k + 3] * hp.y * mw * mw;
-    m3[k] += jx * gm2.x + jy * gm2.y;
-  }
-  // --- SH (FB backward.cu:121-245), only when SH coefficients were given
-  if (a.shs) {
-    const float* rec = a.splat + (size_t)i * 32;
-    const float3 drgb = make_float3(gco.x * (1.f - rec[F_CLAMP]), gco.y * (1.f - rec[F_CLAMP + 1]),
-                                    gco.z * (1.f - rec[F_CLAMP + 2]));
-    const float vx = p.x - a.campos[0], vy = p.y - a.campos[1], vz = p.z - a.campos[2];
-    const float n2 = vx * vx + vy * vy + vz * vz, inv_n = rsqrtf(n2);
-    const float x = vx * inv_n, y = vy * inv_n, z = vz * inv_n;
-    const float c0 = 0.28209479177387814f;
-    gdc[0] = c0 * drgb.x; gdc[1] = c0 * drgb.y; gdc[2] = c0 * drgb.z;
-    const float* co = a.shs + (size_t)i * a.M * 3;
-    float3 dd = make_float3(0.f, 0.f, 0.f);
-    const int used = (a.D + 1) * (a.D + 1) - 1;
-    if (a.D > 0) {
-      const float c1 = 0.4886025119029199f;
-      sh_term(-c1 * y, 0.f, -c1, 0.f, co + 0, gsh + 0, drgb, dd);
-      sh_term(c1 * z, 0.f, 0.f, c1, co + 3, gsh + 3, drgb, dd);
-      sh_term(-c1 * x, -c1, 0.f, 0.f, co + 6, gsh + 6, drgb, dd);
-      if (a.D > 1) {
-        const float k2a = 1.0925484305920792f, k2b = 0.31539156525252005f, k2c = 0.5462742152960396f;
-        const float xx = x * x, yy = y * y, zz = z * z;
-        sh_term(k2a * x * y, k2a * y, k2a * x, 0.f, co + 9, gsh + 9, drgb, dd);
-        sh_term(-k2a * y * z, 0.f, -k2a * z, -k2a * y, co + 12, gsh + 12, drgb, dd);
-        sh_term(k2b * (2.f * zz - xx - yy), -2.f * k2b * x, -2.f * k2b * y, 4.f * k2b * z, co + 15, gsh + 15, drgb, dd);
-        sh_term(-k2a * x * z, -k2a * z, 0.f, -k2a * x, co + 18, gsh + 18, drgb, dd);
-        sh_term(k2c * (xx - yy), 2.f * k2c * x, -2.f * k2c * y, 0.f, co + 21, gsh + 21, drgb, dd);
-        if (a.D > 2) {
-          const float ka = 0.5900435899266435f, kb = 2.890611442640554f, kc = 0.4570457994644658f,
-                      kd = 0.3731763325901154f, ke = 1.445305721320277f;
-          sh_term(-ka * y * (3.f * xx - yy), -ka * 6.f * x * y, -ka * (3.f * xx - 3.f * yy), 0.f, co + 24, gsh + 24,
-                  drgb, dd);
-          sh_term(kb * x * y * z, kb * y * z, kb * x * z, kb * x * y, co + 27, gsh + 27, drgb, dd);
-          sh_term(-kc * y * (4.f * zz - xx - yy), kc * 2.f * x * y, -kc * (4.f * zz - xx - 3.f * yy),
-                  -kc * 8.f * y * z, co + 30, gsh + 30, drgb, dd);
-          sh_term(kd * z * (2.f * zz - 3.f * xx - 3.f * yy), -kd * 6.f * x * z, -kd * 6.f * y * z,
-                  kd * (6.f * zz - 3.f * xx - 3.f * yy), co + 33, gsh + 33, drgb, dd);
-          sh_term(-kc * x * (4.f * zz - xx - yy), -kc * (4.f * zz - 3.f * xx - yy), kc * 2.f * x * y,
-                  -kc * 8.f * x * z, co + 36, gsh + 36, drgb, dd);
-          sh_term(ke * z * (xx - yy), ke * 2.f * x * z, -ke * 2.f * y * z, ke * (xx - yy), co + 39, gsh + 39, drgb,
-                  dd);
-          sh_term(-ka * x * (xx - 3.f * yy), -ka * (3.f * xx - 3.f * yy), ka * 6.f * x * y, 0.f, co + 42, gsh + 42,
-                  drgb, dd);
-        }
+      for (int b = 0; b < 3; ++b) {
+        dR[b][k] = fmaf(f, M0[b] * y0 + M1[b] * y1, dR[b][k]);
+        dM0[b] = fmaf(f * y0, R[b][k], dM0[b]);
+        dM1[b] = fmaf(f * y1, R[b][k], dM1[b]);
       }
     }
-    for (int k = 3 * used; k < 3 * a.M; ++k) gsh[k] = 0.f;
-    // d(v / |v|)/dv applied to the direction gradient
-    const float vd = vx * dd.x + vy * dd.y + vz * dd.z;
-    const float inv3 = inv_n * inv_n * inv_n;
-    m3[0] += (dd.x * n2 - vx * vd) * inv3;
-    m3[1] += (dd.y * n2 - vy * vd) * inv3;
-    m3[2] += (dd.z * n2 - vz * vd) * inv3;
-  } else {
-    gdc[0] = gdc[1] = gdc[2] = 0.f;
-    if (gsh) for (int k = 0; k < 3 * a.M; ++k) gsh[k] = 0.f;
+    {  // dL/dcov3D in FB's storage (diagonal once, off-diagonal doubled)
+      const float c00 = ia * gx + ib * gy, c01 = ia * gy + ib * gz, c10 = ib * gx + ic * gy, c11 = ib * gy + ic * gz;
+      const float E00 = -rr * (c00 * ia + c01 * ib), E01 = -rr * (c00 * ib + c01 * ic),
+                  E11 = -rr * (c10 * ib + c11 * ic);
+      auto G = [&](int r, int c) {
+        return M0[r] * M0[c] * E00 + (M0[r] * M1[c] + M1[r] * M0[c]) * E01 + M1[r] * M1[c] * E11;
+      };
+      gc[0] += G(0, 0); gc[1] += 2.f * G(0, 1); gc[2] += 2.f * G(0, 2);
+      gc[3] += G(1, 1); gc[4] += 2.f * G(1, 2); gc[5] += G(2, 2);
+    }
+    // dL/dJ[a][k] = sum_b dM[a][b] * Rw[k][b], Rw[k][b] = V[b*4 + k]
+    const float dJ00 = dM0[0] * V[0] + dM0[1] * V[4] + dM0[2] * V[8];
+    const float dJ02 = dM0[0] * V[2] + dM0[1] * V[6] + dM0[2] * V[10];
+    const float dJ11 = dM1[0] * V[1] + dM1[1] * V[5] + dM1[2] * V[9];
+    const float dJ12 = dM1[0] * V[2] + dM1[1] * V[6] + dM1[2] * V[10];
+    const float dtx = xm * -cam.fx * iz2 * dJ02;
+    const float dty = ym * -cam.fy * iz2 * dJ12;
+    const float dtz = -cam.fx * iz2 * dJ00 - cam.fy * iz2 * dJ11 + 2.f * cam.fx * tx * iz3 * dJ02 +
+                      2.f * cam.fy * ty * iz3 * dJ12;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) m3[k] += V[k * 4 + 0] * dtx + V[k * 4 + 1] * dty + V[k * 4 + 2] * dtz;
+    // --- screen-space mean (FB backward.cu:504-526)
+    const float4 hp = xform_point4(cam.proj, p);
+    const float mw = 1.f / (hp.w + 0.0000001f);
+    const float* Pm = cam.proj;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      const float jx = Pm[4 * k] * mw - Pm[4 * k + 3] * hp.x * mw * mw;
+      const float jy = Pm[4 * k + 1] * mw - Pm[4 * k + 3] * hp.y * mw * mw;
+      m3[k] += jx * gm2.x + jy * gm2.y;
+    }
+    // --- SH (FB backward.cu:121-245), only when SH coefficients were given
+    if (a.shs) {
+      const float* rec = a.splat + rid * 32;
+      const float3 drgb = make_float3(gco.x * (1.f - rec[F_CLAMP]), gco.y * (1.f - rec[F_CLAMP + 1]),
+                                      gco.z * (1.f - rec[F_CLAMP + 2]));
+      const float vx = p.x - cam.campos[0], vy = p.y - cam.campos[1], vz = p.z - cam.campos[2];
+      const float n2 = vx * vx + vy * vy + vz * vz, inv_n = rsqrtf(n2);
+      const float x = vx * inv_n, y = vy * inv_n, z = vz * inv_n;
+      const float c0 = 0.28209479177387814f;
+      gdc[0] += c0 * drgb.x; gdc[1] += c0 * drgb.y; gdc[2] += c0 * drgb.z;
+      const float* co = a.shs + (size_t)i * a.M * 3;
+      const bool add = sh_written;
+      float3 dd = make_float3(0.f, 0.f, 0.f);
+      if (a.D > 0) {
+        const float c1 = 0.4886025119029199f;
+        sh_term(-c1 * y, 0.f, -c1, 0.f, co + 0, gsh + 0, drgb, dd, add);
+        sh_term(c1 * z, 0.f, 0.f, c1, co + 3, gsh + 3, drgb, dd, add);
+        sh_term(-c1 * x, -c1, 0.f, 0.f, co + 6, gsh + 6, drgb, dd, add);
+        if (a.D > 1) {
+          const float k2a = 1.0925484305920792f, k2b = 0.31539156525252005f, k2c = 0.5462742152960396f;
+          const float xx = x * x, yy = y * y, zz = z * z;
+          sh_term(k2a * x * y, k2a * y, k2a * x, 0.f, co + 9, gsh + 9, drgb, dd, add);
+          sh_term(-k2a * y * z, 0.f, -k2a * z, -k2a * y, co + 12, gsh + 12, drgb, dd, add);
+          sh_term(k2b * (2.f * zz - xx - yy), -2.f * k2b * x, -2.f * k2b * y, 4.f * k2b * z, co + 15, gsh + 15,
+                  drgb, dd, add);
+          sh_term(-k2a * x * z, -k2a * z, 0.f, -k2a * x, co + 18, gsh + 18, drgb, dd, add);
+          sh_term(k2c * (xx - yy), 2.f * k2c * x, -2.f * k2c * y, 0.f, co + 21, gsh + 21, drgb, dd, add);
+          if (a.D > 2) {
+            const float ka = 0.5900435899266435f, kb = 2.890611442640554f, kc = 0.4570457994644658f,
+                        kd = 0.3731763325901154f, ke = 1.445305721320277f;
+            sh_term(-ka * y * (3.f * xx - yy), -ka * 6.f * x * y, -ka * (3.f * xx - 3.f * yy), 0.f, co + 24,
+                    gsh + 24, drgb, dd, add);
+            sh_term(kb * x * y * z, kb * y * z, kb * x * z, kb * x * y, co + 27, gsh + 27, drgb, dd, add);
+            sh_term(-kc * y * (4.f * zz - xx - yy), kc * 2.f * x * y, -kc * (4.f * zz - xx - 3.f * yy),
+                    -kc * 8.f * y * z, co + 30, gsh + 30, drgb, dd, add);
+            sh_term(kd * z * (2.f * zz - 3.f * xx - 3.f * yy), -kd * 6.f * x * z, -kd * 6.f * y * z,
+                    kd * (6.f * zz - 3.f * xx - 3.f * yy), co + 33, gsh + 33, drgb, dd, add);
+            sh_term(-kc * x * (4.f * zz - xx - yy), -kc * (4.f * zz - 3.f * xx - yy), kc * 2.f * x * y,
+                    -kc * 8.f * x * z, co + 36, gsh + 36, drgb, dd, add);
+            sh_term(ke * z * (xx - yy), ke * 2.f * x * z, -ke * 2.f * y * z, ke * (xx - yy), co + 39, gsh + 39,
+                    drgb, dd, add);
+            sh_term(-ka * x * (xx - 3.f * yy), -ka * (3.f * xx - 3.f * yy), ka * 6.f * x * y, 0.f, co + 42,
+                    gsh + 42, drgb, dd, add);
+          }
+        }
+      }
+      sh_written = true;
+      // d(v / |v|)/dv applied to the direction gradient
+      const float vd = vx * dd.x + vy * dd.y + vz * dd.z;
+      const float inv3 = inv_n * inv_n * inv_n;
+      m3[0] += (dd.x * n2 - vx * vd) * inv3;
+      m3[1] += (dd.y * n2 - vy * vd) * inv3;
+      m3[2] += (dd.z * n2 - vz * vd) * inv3;
+    }
+    // --- densification statistics (FB backward.cu:892-918), once per view
+    if (a.accum) {
+      if (a.denom) a.denom[i] += 1.f;
+      if (a.max_radii) a.max_radii[i] = fmaxf(a.max_radii[i], (float)radius);
+      a.accum[i] += sqrt_approx(gm2.x * gm2.x + gm2.y * gm2.y);
+      if (a.accum_abs) a.accum_abs[i] += sqrt_approx(gm2.z * gm2.z + gm2.w * gm2.w);
+    }
   }
-  gm[0] = m3[0]; gm[1] = m3[1]; gm[2] = m3[2];
   // --- rotation (FB backward.cu:460-482): dL/dq from dL/dR of the raw quaternion
-  const float dqr = 2.f * qz * (dR[1][0] - dR[0][1]) + 2.f * qy * (dR[0][2] - dR[2][0]) + 2.f * qx * (dR[2][1] - dR[1][2]);
-  const float dqx = 2.f * qy * (dR[0][1] + dR[1][0]) + 2.f * qz * (dR[0][2] + dR[2][0]) +
-                    2.f * qr * (dR[2][1] - dR[1][2]) - 4.f * qx * (dR[1][1] + dR[2][2]);
-  const float dqy = 2.f * qx * (dR[0][1] + dR[1][0]) + 2.f * qr * (dR[0][2] - dR[2][0]) +
-                    2.f * qz * (dR[1][2] + dR[2][1]) - 4.f * qy * (dR[0][0] + dR[2][2]);
-  const float dqz = 2.f * qr * (dR[1][0] - dR[0][1]) + 2.f * qx * (dR[0][2] + dR[2][0]) +
-                    2.f * qy * (dR[1][2] + dR[2][1]) - 4.f * qz * (dR[0][0] + dR[1][1]);
-  reinterpret_cast<float4*>(a.drot)[i] = make_float4(dqr, dqx, dqy, dqz);
-  // --- densification statistics (FB backward.cu:892-918)
-  if (a.accum) {
-    if (a.denom) a.denom[i] += 1.f;
-    if (a.max_radii) a.max_radii[i] = fmaxf(a.max_radii[i], (float)radius);
-    a.accum[i] += sqrt_approx(gm2.x * gm2.x + gm2.y * gm2.y);
-    if (a.accum_abs) a.accum_abs[i] += sqrt_approx(gm2.z * gm2.z + gm2.w * gm2.w);
+  gq[0] = 2.f * qz * (dR[1][0] - dR[0][1]) + 2.f * qy * (dR[0][2] - dR[2][0]) + 2.f * qx * (dR[2][1] - dR[1][2]);
+  gq[1] = 2.f * qy * (dR[0][1] + dR[1][0]) + 2.f * qz * (dR[0][2] + dR[2][0]) + 2.f * qr * (dR[2][1] - dR[1][2]) -
+          4.f * qx * (dR[1][1] + dR[2][2]);
+  gq[2] = 2.f * qx * (dR[0][1] + dR[1][0]) + 2.f * qr * (dR[0][2] - dR[2][0]) + 2.f * qz * (dR[1][2] + dR[2][1]) -
+          4.f * qy * (dR[0][0] + dR[2][2]);
+  gq[3] = 2.f * qr * (dR[1][0] - dR[0][1]) + 2.f * qx * (dR[0][2] + dR[2][0]) + 2.f * qy * (dR[1][2] + dR[2][1]) -
+          4.f * qz * (dR[0][0] + dR[1][1]);
+  // --- outputs (zeros where no view saw the Gaussian, as FB leaves them)
+  a.dcolor[3 * (size_t)i] = gco_sum.x;
+  a.dcolor[3 * (size_t)i + 1] = gco_sum.y;
+  a.dcolor[3 * (size_t)i + 2] = gco_sum.z;
+  a.dopac[i] = gco_sum.w;
+  float* gm = a.dmean3D + 3 * (size_t)i;
+  gm[0] = m3[0]; gm[1] = m3[1]; gm[2] = m3[2];
+#pragma unroll
+  for (int k = 0; k < 6; ++k) a.dcov3D[6 * (size_t)i + k] = gc[k];
+  a.ddc[3 * (size_t)i] = gdc[0]; a.ddc[3 * (size_t)i + 1] = gdc[1]; a.ddc[3 * (size_t)i + 2] = gdc[2];
+  a.dscale[3 * (size_t)i] = gs[0]; a.dscale[3 * (size_t)i + 1] = gs[1]; a.dscale[3 * (size_t)i + 2] = gs[2];
+  reinterpret_cast<float4*>(a.drot)[i] = make_float4(gq[0], gq[1], gq[2], gq[3]);
+  if (gsh) {
+    for (int k = sh_written ? 3 * used : 0; k < 3 * a.M; ++k) gsh[k] = 0.f;
   }
 }
 
@@ -452,12 +439,41 @@ __global__ void __launch_bounds__(256) k_densify(int P, const int* radii, const 
   if (accum_abs) accum_abs[i] += sqrt_approx(g.z * g.z + g.w * g.w);
 }
 
-bool tile_shape_ok(int bx, int by) { return bx * by == kTilePixels && (bx == 8 || bx == 16 || bx == 32); }
-
 }  // namespace
 }  // namespace fgs
 
 FGS_DEFINE_ERROR_ACCESSOR(backward)
+
+namespace fgs {
+fgs_status run_render_bwd(const Views& views, int64_t records, int bucket_size, const uint32_t* values_sorted,
+                          const uint32_t* ranges, const float* splat, const float* Ts_final,
+                          const int32_t* last_contributor, const ImageState& im, const SampleState& sm,
+                          const float* dL_dpixels, float* grad_record, cudaStream_t s) {
+  FGS_TRY(cudaMemsetAsync(grad_record, 0, sizeof(float) * FGS_GRAD_STRIDE * (size_t)records, s));
+  // backward work cursor (word 3 of the image-state header); reset on every call
+  FGS_TRY(cudaMemsetAsync(im.bucket_sum + 3, 0, sizeof(uint32_t), s));
+  BwdArgs a{views, splat, values_sorted, ranges, sm.bucket_tile, im.bucket_off, im.bucket_sum, im.max_contrib,
+            sm.samples, im.pix_color, Ts_final, last_contributor, dL_dpixels, grad_record, bucket_size};
+  {
+    KernelTimer kt__(FGS_K_RENDER_BWD, s);
+    const int nt = kBwdWarps * kWarp;
+    if (views.bx == 8) k_render_bwd<8><<<num_sms() * resident_blocks(k_render_bwd<8>, nt, 0), nt, 0, s>>>(a);
+    else if (views.bx == 16) k_render_bwd<16><<<num_sms() * resident_blocks(k_render_bwd<16>, nt, 0), nt, 0, s>>>(a);
+    else k_render_bwd<32><<<num_sms() * resident_blocks(k_render_bwd<32>, nt, 0), nt, 0, s>>>(a);
+    kt__.stop();
+  }
+  FGS_LAUNCH_CHECK();
+  return FGS_OK;
+}
+
+fgs_status run_preprocess_bwd(PbwdArgs& a, cudaStream_t s) {
+  KernelTimer kt__(FGS_K_PREPROCESS_BWD, s);
+  k_preprocess_bwd<<<(a.P + 255) / 256, 256, 0, s>>>(a);
+  kt__.stop();
+  FGS_LAUNCH_CHECK();
+  return FGS_OK;
+}
+}  // namespace fgs
 
 using namespace fgs;
 
@@ -475,26 +491,11 @@ extern "C" fgs_status fgs_render_bwd(int P, int width, int height, int block_x, 
       !dL_dpixels || !grad_record || !values_sorted)
     return FGS_ERR_BAD_ARG;
   if (((uintptr_t)grad_record & 15) || ((uintptr_t)splat_buffer & 15)) return FGS_ERR_BAD_ARG;
-  const int gx = (width + block_x - 1) / block_x, gy = (height + block_y - 1) / block_y, T = gx * gy;
-  const ImageState im = carve_image(const_cast<void*>(image_state), width, height, T);
+  const Views views = single_view(width, height, block_x, block_y, nullptr, nullptr, nullptr, bg, 1.f, 1.f, 1.f, 1.f);
+  const ImageState im = carve_image(const_cast<void*>(image_state), (size_t)width * height, views.tiles);
   const SampleState sm = carve_sample(const_cast<void*>(sample_state), max_buckets > 0 ? max_buckets : 1);
-  cudaStream_t s = (cudaStream_t)stream;
-  FGS_TRY(cudaMemsetAsync(grad_record, 0, sizeof(float) * FGS_GRAD_STRIDE * (size_t)P, s));
-  // backward work cursor (word 3 of the image-state header); reset on every call
-  FGS_TRY(cudaMemsetAsync(im.bucket_sum + 3, 0, sizeof(uint32_t), s));
-  BwdArgs a{splat_buffer, values_sorted, ranges, sm.bucket_tile, im.bucket_off, im.bucket_sum, im.max_contrib,
-            sm.samples, im.pix_color, Ts_final, last_contributor, dL_dpixels, bg, grad_record,
-            width, height, block_x, block_y, gx, bucket_size};
-  {
-    KernelTimer kt__(FGS_K_RENDER_BWD, s);
-    const int nt = kBwdWarps * kWarp;
-    if (block_x == 8) k_render_bwd<8><<<num_sms() * resident_blocks(k_render_bwd<8>, nt, 0), nt, 0, s>>>(a);
-    else if (block_x == 16) k_render_bwd<16><<<num_sms() * resident_blocks(k_render_bwd<16>, nt, 0), nt, 0, s>>>(a);
-    else k_render_bwd<32><<<num_sms() * resident_blocks(k_render_bwd<32>, nt, 0), nt, 0, s>>>(a);
-    kt__.stop();
-  }
-  FGS_LAUNCH_CHECK();
-  return FGS_OK;
+  return run_render_bwd(views, P, bucket_size, values_sorted, ranges, splat_buffer, Ts_final, last_contributor, im,
+                        sm, dL_dpixels, grad_record, (cudaStream_t)stream);
 }
 
 extern "C" fgs_status fgs_preprocess_bwd(
@@ -516,23 +517,16 @@ extern "C" fgs_status fgs_preprocess_bwd(
       ((uintptr_t)rotations & 15) || ((uintptr_t)dL_drot & 15))
     return FGS_ERR_BAD_ARG;
   PbwdArgs a;
+  a.views = single_view(width, height, 16, 16, viewmatrix, projmatrix, campos, nullptr, tan_fovx, tan_fovy, 1.f,
+                        scale_modifier);
   a.P = P; a.D = D; a.M = M;
   a.means = means3D; a.radii = radii; a.dc = dc; a.shs = shs; a.splat = splat_buffer;
-  a.scales = scales; a.rots = rotations; a.smod = scale_modifier;
-  a.view = viewmatrix; a.proj = projmatrix;
-  a.fx = width / (2.0f * tan_fovx); a.fy = height / (2.0f * tan_fovy); a.tanx = tan_fovx; a.tany = tan_fovy;
-  a.campos = campos; a.grad = grad_record;
+  a.scales = scales; a.rots = rotations; a.grad = grad_record;
   a.dmean2D = dL_dmean2D; a.dconic = dL_dconic; a.dopac = dL_dopacity; a.dcolor = dL_dcolor;
-  a.dmean3D = dL_dmean3D; a.dcov3D = dL_dcov3D; a.ddc = dL_ddc; a.dsh = shs ? dL_dsh : (M > 0 ? dL_dsh : nullptr);
+  a.dmean3D = dL_dmean3D; a.dcov3D = dL_dcov3D; a.ddc = dL_ddc; a.dsh = (M > 0) ? dL_dsh : nullptr;
   a.dscale = dL_dscale; a.drot = dL_drot;
   a.accum = xyz_gradient_accum; a.accum_abs = xyz_gradient_accum_abs; a.max_radii = max_radii; a.denom = denom;
-  {
-    KernelTimer kt__(FGS_K_PREPROCESS_BWD, (cudaStream_t)stream);
-    k_preprocess_bwd<<<(P + 255) / 256, 256, 0, (cudaStream_t)stream>>>(a);
-    kt__.stop();
-  }
-  FGS_LAUNCH_CHECK();
-  return FGS_OK;
+  return run_preprocess_bwd(a, (cudaStream_t)stream);
 }
 
 extern "C" fgs_status fgs_densify_stats(int P, const int32_t* radii, const float* dL_dmean2D,

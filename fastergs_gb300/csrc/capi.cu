@@ -36,6 +36,9 @@ void timer_begin(int id, cudaStream_t s) {
   if (id < 0 || id >= FGS_K_COUNT) return;
   TimerSlot& t = g_timers[id];
   if (!t.enabled) return;
+  // no event pairs inside a CUDA graph capture: the launch is not executed now
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(s, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) return;
   std::lock_guard<std::mutex> lk(t.mu);
   cudaEvent_t e = nullptr;
   cudaEventCreate(&e);

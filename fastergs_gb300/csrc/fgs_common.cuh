@@ -95,6 +95,52 @@ __device__ __forceinline__ float4 xform_point4(const float* m, float3 p) {
                      m[2] * p.x + m[6] * p.y + m[10] * p.z + m[14], m[3] * p.x + m[7] * p.y + m[11] * p.z + m[15]);
 }
 
+// Cameras of one frame batch.  The plain (single-view) entry points use one
+// view; the batched entry points render up to kMaxViews cameras of different
+// resolutions in one launch per stage.  Tiles of all views share one global
+// tile index space (view k owns tiles [tile_off, tile_off + gx*gy)) so that a
+// single sort orders every view's pairs, and per-pixel arrays of all views are
+// concatenated (view k starts at pixel pix_off).  Passed to kernels by value.
+constexpr int kMaxViews = 32;
+struct ViewDesc {
+  const float* view;    // 4x4 column-major world -> view (device)
+  const float* proj;    // 4x4 column-major full projection (device)
+  const float* campos;  // 3 (device)
+  const float* bg;      // 3 (device), compositing only
+  float tanx, tany, fx, fy, mult, smod;
+  int W, H, gx, gy;
+  uint32_t tile_off, pix_off;
+};
+struct Views {
+  int V, bx, by;
+  uint32_t tiles;  // total tiles of all views
+  ViewDesc v[kMaxViews];
+  // view owning global tile t
+  __device__ __forceinline__ int of_tile(uint32_t t) const {
+    int k = 0;
+    for (int j = 1; j < V; ++j)
+      if (v[j].tile_off <= t) k = j;
+    return k;
+  }
+};
+inline void set_view(ViewDesc& d, int W, int H, int bx, int by, const float* view, const float* proj,
+                     const float* campos, const float* bg, float tanx, float tany, float mult, float smod) {
+  d.view = view; d.proj = proj; d.campos = campos; d.bg = bg;
+  d.tanx = tanx; d.tany = tany; d.fx = W / (2.0f * tanx); d.fy = H / (2.0f * tany);
+  d.mult = mult; d.smod = smod;
+  d.W = W; d.H = H; d.gx = (W + bx - 1) / bx; d.gy = (H + by - 1) / by;
+  d.tile_off = 0; d.pix_off = 0;
+}
+// One-view table for the plain entry points.
+inline Views single_view(int W, int H, int bx, int by, const float* view, const float* proj, const float* campos,
+                         const float* bg, float tanx, float tany, float mult, float smod) {
+  Views vs;
+  vs.V = 1; vs.bx = bx; vs.by = by;
+  set_view(vs.v[0], W, H, bx, by, view, proj, campos, bg, tanx, tany, mult, smod);
+  vs.tiles = (uint32_t)(vs.v[0].gx * vs.v[0].gy);
+  return vs;
+}
+
 // Kahan's 2x2 determinant a*d - b*c with one rounding of the cancelling part.
 __device__ __forceinline__ float det2_kahan(float a, float b, float c, float d) {
   const float w = b * c;

@@ -1,0 +1,75 @@
+// Internal launch interfaces shared by the plain and the batched entry
+// points (not part of the C ABI).
+#pragma once
+#include "fgs_common.cuh"
+
+namespace fgs {
+
+struct PreArgs {
+  Views views;
+  int P, D, M;
+  const float* means;
+  const float* colors;
+  const float* dc;
+  const float* shs;
+  const float* opac;
+  const float* scales;
+  const float* rots;
+  const uint8_t* culling;
+  float* splat;          // records, (V * P) x 32 floats, record index = view * P + Gaussian
+  unsigned long long* keys;
+  uint32_t* vals;        // record index of each pair
+  long long cap;
+  uint32_t* tasks;
+  long long task_cap;    // in tasks (2 words each)
+  unsigned int* curr;
+  int* counters;
+  int* radii;            // V * P
+  int large_tiles;       // footprints of >= large_tiles tiles are split into sub-tasks of that many tiles
+                         // (a multiple of 32; FB: 128)
+};
+
+// Preprocess + large-Gaussian emission for every view (grid.y = view).
+fgs_status run_preprocess(PreArgs& a, cudaStream_t s);
+
+// Stable radix sort of n pairs on 32 + ceil(log2 tiles) key bits.  n = n_cap,
+// or min(n_cap, *n_dev) when n_dev is given (grids are sized for n_cap).
+fgs_status run_sort(int64_t n_cap, const int32_t* n_dev, uint32_t tiles, void* temp, size_t temp_bytes,
+                    const uint64_t* keys_in, const uint32_t* values_in, uint64_t* keys_out, uint32_t* values_out,
+                    cudaStream_t s);
+size_t sort_temp_bytes(int64_t n);
+
+bool tile_shape_ok(int bx, int by);
+
+struct PbwdArgs {
+  Views views;
+  int P, D, M;
+  const float* means;
+  const int* radii;     // V * P
+  const float* dc;
+  const float* shs;
+  const float* splat;   // V * P records
+  const float* scales;
+  const float* rots;
+  const float* grad;    // V * P gradient records
+  float* dmean2D;       // V * P (optional)
+  float* dconic;        // V * P (optional)
+  float* dopac;         // summed over views from here on
+  float* dcolor;
+  float* dmean3D;
+  float* dcov3D;
+  float* ddc;
+  float* dsh;
+  float* dscale;
+  float* drot;
+  float* accum;         // densification statistics, accumulated per view
+  float* accum_abs;
+  float* max_radii;
+  float* denom;
+};
+
+fgs_status run_preprocess_bwd(PbwdArgs& a, cudaStream_t s);
+fgs_status run_tile_ranges(int64_t n_cap, const int32_t* n_dev, uint32_t tiles, const uint64_t* keys_sorted,
+                           uint32_t* ranges, cudaStream_t s);
+
+}  // namespace fgs

@@ -11,7 +11,7 @@
 //     per ~100 pairs instead of one per 32 candidates;
 //   * large Gaussians queue (id, first tile) sub-tasks that a persistent
 //     second kernel drains; the task count never travels to the host.
-#include "fgs_common.cuh"
+#include "internal.cuh"
 
 namespace fgs {
 namespace {
@@ -19,33 +19,6 @@ namespace {
 constexpr int kPreThreads = 256;
 constexpr int kPreWarps = kPreThreads / kWarp;
 constexpr int kStage = 128;  // staged pairs per warp before a flush
-
-struct PreArgs {
-  int P, D, M;
-  const float* means;
-  const float* colors;
-  const float* dc;
-  const float* shs;
-  const float* opac;
-  const float* scales;
-  const float* rots;
-  float smod;
-  int W, H, bx, by, gx, gy;
-  const float* campos;
-  const float* view;
-  const float* proj;
-  float tanx, tany, fx, fy, mult;
-  const uint8_t* culling;
-  float* splat;
-  unsigned long long* keys;
-  uint32_t* vals;
-  long long cap;
-  uint32_t* tasks;
-  long long task_cap;  // in tasks (2 words each)
-  unsigned int* curr;
-  int* counters;
-  int* radii;
-};
 
 // Ellipse chord test along one tile edge (FB preprocess.cu:168-177): does the
 // quadratic A u^2 + B u + C = 0 have a root interval meeting [l - d, r - d]?
@@ -156,6 +129,10 @@ __global__ void __launch_bounds__(kPreThreads) k_preprocess(const PreArgs a) {
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int i = blockIdx.x * kPreThreads + threadIdx.x;
+  const int vi = blockIdx.y;
+  const ViewDesc& cam = a.views.v[vi];
+  const int bx = a.views.bx, by = a.views.by;
+  const size_t rbase = (size_t)vi * a.P;  // first record of this view
 
   bool valid = false;
   int area = 0, tw = 0;
@@ -172,7 +149,7 @@ __global__ void __launch_bounds__(kPreThreads) k_preprocess(const PreArgs a) {
     do {
       if (a.culling && a.culling[i]) break;
       const float3 p = ld3(a.means + 3 * (size_t)i);
-      const float3 t = xform_point3(a.view, p);
+      const float3 t = xform_point3(cam.view, p);
       if (t.z <= 0.2f) break;                        // near cull (FB preprocess.cu:456)
       const float o = a.opac[i];
       if (255.0f * o < 1.0f) break;                  // opacity cull (FB preprocess.cu:459)
@@ -180,7 +157,7 @@ __global__ void __launch_bounds__(kPreThreads) k_preprocess(const PreArgs a) {
       // pixels in double (preprocess.cu:463-465, 494); an FP32 pixel position
       // near 1000 px is only good to 6e-5 px, which would dominate the image
       // error, so the position is formed here in FP64 and its fraction kept.
-      const float* Pm = a.proj;
+      const float* Pm = cam.proj;
       const double px = p.x, py = p.y, pz = p.z;
       auto row = [&](int r) {
         return __fma_rn((double)Pm[r], px, __fma_rn((double)Pm[4 + r], py, __fma_rn((double)Pm[8 + r], pz, (double)Pm[12 + r])));
@@ -190,8 +167,8 @@ __global__ void __launch_bounds__(kPreThreads) k_preprocess(const PreArgs a) {
       // 1/wden: FP32 seed refined by one Newton step (relative error ~1e-14).
       double rw = (double)(1.0f / (float)wden);
       rw = rw * __fma_rn(-wden, rw, 2.0);
-      const double X = __fma_rn(hx * rw + 1.0, (double)a.W, -1.0) * 0.5;
-      const double Y = __fma_rn(hy * rw + 1.0, (double)a.H, -1.0) * 0.5;
+      const double X = __fma_rn(hx * rw + 1.0, (double)cam.W, -1.0) * 0.5;
+      const double Y = __fma_rn(hy * rw + 1.0, (double)cam.H, -1.0) * 0.5;
 
       // 3D covariance R diag(s^2) R^T from the raw quaternion (FB preprocess.cu:364-400).
       const float4 q = *reinterpret_cast<const float4*>(a.rots + 4 * (size_t)i);
@@ -200,8 +177,8 @@ __global__ void __launch_bounds__(kPreThreads) k_preprocess(const PreArgs a) {
       R[0][0] = 1.f - 2.f * (qy * qy + qz * qz); R[0][1] = 2.f * (qx * qy - qr * qz); R[0][2] = 2.f * (qx * qz + qr * qy);
       R[1][0] = 2.f * (qx * qy + qr * qz); R[1][1] = 1.f - 2.f * (qx * qx + qz * qz); R[1][2] = 2.f * (qy * qz - qr * qx);
       R[2][0] = 2.f * (qx * qz - qr * qy); R[2][1] = 2.f * (qy * qz + qr * qx); R[2][2] = 1.f - 2.f * (qx * qx + qy * qy);
-      const float sx = a.smod * a.scales[3 * (size_t)i], sy = a.smod * a.scales[3 * (size_t)i + 1],
-                  sz = a.smod * a.scales[3 * (size_t)i + 2];
+      const float sx = cam.smod * a.scales[3 * (size_t)i], sy = cam.smod * a.scales[3 * (size_t)i + 1],
+                  sz = cam.smod * a.scales[3 * (size_t)i + 2];
       const float s2[3] = {sx * sx, sy * sy, sz * sz};
       float S[6];
       {
@@ -212,12 +189,12 @@ __global__ void __launch_bounds__(kPreThreads) k_preprocess(const PreArgs a) {
           for (int c = r; c < 3; ++c) S[k++] = R[r][0] * s2[0] * R[c][0] + R[r][1] * s2[1] * R[c][1] + R[r][2] * s2[2] * R[c][2];
       }
       // EWA screen covariance (FB preprocess.cu:79-117).
-      const float limx = 1.3f * a.tanx, limy = 1.3f * a.tany;
+      const float limx = 1.3f * cam.tanx, limy = 1.3f * cam.tany;
       const float tx = fminf(limx, fmaxf(-limx, t.x / t.z)) * t.z;
       const float ty = fminf(limy, fmaxf(-limy, t.y / t.z)) * t.z;
-      const float j00 = a.fx / t.z, j02 = -(a.fx * tx) / (t.z * t.z);
-      const float j11 = a.fy / t.z, j12 = -(a.fy * ty) / (t.z * t.z);
-      const float* V = a.view;
+      const float j00 = cam.fx / t.z, j02 = -(cam.fx * tx) / (t.z * t.z);
+      const float j11 = cam.fy / t.z, j12 = -(cam.fy * ty) / (t.z * t.z);
+      const float* V = cam.view;
       // M = J * Rw, Rw[k][b] = V[b*4 + k]
       float M0[3], M1[3];
 #pragma unroll
@@ -238,14 +215,14 @@ __global__ void __launch_bounds__(kPreThreads) k_preprocess(const PreArgs a) {
       radius = (float)ceil(extent * (double)sqrtf(lambda));
       // Tile rectangle of the 1/256 level set (FB preprocess.cu:488-497).
       const float log2o = lg2_approx(o);
-      const float power = (kLn2 * 8.0f + kLn2 * log2o) * a.mult;
+      const float power = (kLn2 * 8.0f + kLn2 * log2o) * cam.mult;
       const int wpx = (int)(1.414214f * sqrt_approx(ca * power) + 1.0f);
       const int hpx = (int)(1.414214f * sqrt_approx(cc * power) + 1.0f);
       xy = make_float2((float)X, (float)Y);
-      rmin.x = min(a.gx, max(0, (int)((xy.x - wpx) / (float)a.bx)));
-      rmin.y = min(a.gy, max(0, (int)((xy.y - hpx) / (float)a.by)));
-      rmax.x = min(a.gx, max(0, (int)((xy.x + wpx) / (float)a.bx) + 1));
-      rmax.y = min(a.gy, max(0, (int)((xy.y + hpx) / (float)a.by) + 1));
+      rmin.x = min(cam.gx, max(0, (int)((xy.x - wpx) / (float)bx)));
+      rmin.y = min(cam.gy, max(0, (int)((xy.y - hpx) / (float)by)));
+      rmax.x = min(cam.gx, max(0, (int)((xy.x + wpx) / (float)bx) + 1));
+      rmax.y = min(cam.gy, max(0, (int)((xy.y + hpx) / (float)by) + 1));
       tw = rmax.x - rmin.x;
       area = tw * (rmax.y - rmin.y);
       if (area <= 0) break;
@@ -257,7 +234,7 @@ __global__ void __launch_bounds__(kPreThreads) k_preprocess(const PreArgs a) {
       if (a.colors) {
         rgb = ld3(a.colors + 3 * (size_t)i);
       } else {
-        const float3 cpos = ld3(a.campos);
+        const float3 cpos = ld3(cam.campos);
         float dxv = p.x - cpos.x, dyv = p.y - cpos.y, dzv = p.z - cpos.z;
         const float inv = 1.0f / sqrtf(dxv * dxv + dyv * dyv + dzv * dzv);
         rgb = sh_colour(a.D, dxv * inv, dyv * inv, dzv * inv, a.dc + 3 * (size_t)i,
@@ -282,24 +259,26 @@ __global__ void __launch_bounds__(kPreThreads) k_preprocess(const PreArgs a) {
 #pragma unroll
       for (int k = 0; k < 6; ++k) rec[F_COV3D + k] = S[k];
     } while (false);
-    a.radii[i] = valid ? (int)radius : 0;
+    a.radii[rbase + i] = valid ? (int)radius : 0;
     if (valid) {
-      float4* dst = reinterpret_cast<float4*>(a.splat + (size_t)i * 32);
+      float4* dst = reinterpret_cast<float4*>(a.splat + (rbase + i) * 32);
 #pragma unroll
       for (int k = 0; k < 8; ++k) dst[k] = make_float4(rec[4 * k], rec[4 * k + 1], rec[4 * k + 2], rec[4 * k + 3]);
     }
   }
 
-  // Large footprints: queue 128-tile sub-tasks (FB preprocess.cu:723-745).
-  const bool small = valid && area < kLargeTiles;
+  // Large footprints: queue large_tiles-tile sub-tasks (FB preprocess.cu:723-745
+  // uses 128).
+  const int LT = a.large_tiles;
+  const bool small = valid && area < LT;
   if (valid && !small) {
-    const int n = (area + kLargeTiles - 1) / kLargeTiles;
+    const int n = (area + LT - 1) / LT;
     const int base = atomicAdd(&a.counters[0], n);
     for (int j = 0; j < n; ++j) {
       const long long t = (long long)base + j;
       if (t < a.task_cap) {
-        a.tasks[2 * t] = (uint32_t)i;
-        a.tasks[2 * t + 1] = (uint32_t)(j * kLargeTiles);
+        a.tasks[2 * t] = (uint32_t)(rbase + i);
+        a.tasks[2 * t + 1] = (uint32_t)(j * LT);
       } else {
         raise_error(kErrCapacity);
       }
@@ -340,9 +319,9 @@ __global__ void __launch_bounds__(kPreThreads) k_preprocess(const PreArgs a) {
       const int local = c - g.w;
       const int ty = local / g.z, tx = local - ty * g.z;
       const int x = g.x + tx, y = g.y + ty;
-      hit = tile_hit(x * a.bx, y * a.by, a.bx, a.by, s_xy[warp][lo], s_cp[warp][lo]);
-      key = ((unsigned long long)(uint32_t)(y * a.gx + x) << 32) | s_depth[warp][lo];
-      gid = (uint32_t)(warp_first + lo);
+      hit = tile_hit(x * bx, y * by, bx, by, s_xy[warp][lo], s_cp[warp][lo]);
+      key = ((unsigned long long)(cam.tile_off + (uint32_t)(y * cam.gx + x)) << 32) | s_depth[warp][lo];
+      gid = (uint32_t)(rbase + warp_first + lo);
     }
     stage_push(st, a, lane, hit, key, gid);
   }
@@ -360,7 +339,9 @@ __global__ void __launch_bounds__(kPreThreads) k_preprocess_large(const PreArgs 
   const int gw = blockIdx.x * kPreWarps + warp, nw = gridDim.x * kPreWarps;
   WarpStage st{s_key[warp], s_val[warp], 0};
   for (long long t = gw; t < ntask; t += nw) {
-    const uint32_t id = a.tasks[2 * t], off = a.tasks[2 * t + 1];
+    const uint32_t id = a.tasks[2 * t], off = a.tasks[2 * t + 1];  // record index, first tile
+    const ViewDesc& cam = a.views.v[id / (uint32_t)a.P];
+    const int bx = a.views.bx, by = a.views.by;
     const float* r = a.splat + (size_t)id * 32;
     const float2 xy = make_float2(r[F_XY], r[F_XY + 1]);
     const uint32_t depth = __float_as_uint(r[F_DEPTH]);
@@ -368,17 +349,17 @@ __global__ void __launch_bounds__(kPreThreads) k_preprocess_large(const PreArgs 
     const int rx1 = __float_as_int(r[F_RMAX]), ry1 = __float_as_int(r[F_RMAX + 1]);
     const float4 cp = make_float4(r[F_CONIC], r[F_CONIC + 1], r[F_CONIC + 2], r[F_POWER]);
     const int w = rx1 - rx0, area = w * (ry1 - ry0);
-    const int end = min((int)off + kLargeTiles, area);
+    const int end = min((int)off + a.large_tiles, area);
 #pragma unroll 1
-    for (int k = 0; k < kLargeTiles / kWarp; ++k) {
+    for (int k = 0; k < a.large_tiles / kWarp; ++k) {
       const int c = (int)off + k * kWarp + lane;
       bool hit = false;
       unsigned long long key = 0;
       if (c < end) {
         const int ty = c / w, tx = c - ty * w;
         const int x = rx0 + tx, y = ry0 + ty;
-        hit = tile_hit(x * a.bx, y * a.by, a.bx, a.by, xy, cp);
-        key = ((unsigned long long)(uint32_t)(y * a.gx + x) << 32) | depth;
+        hit = tile_hit(x * bx, y * by, bx, by, xy, cp);
+        key = ((unsigned long long)(cam.tile_off + (uint32_t)(y * cam.gx + x)) << 32) | depth;
       }
       stage_push(st, a, lane, hit, key, id);
     }
@@ -390,6 +371,27 @@ __global__ void __launch_bounds__(kPreThreads) k_preprocess_large(const PreArgs 
 }  // namespace fgs
 
 FGS_DEFINE_ERROR_ACCESSOR(preprocess)
+
+namespace fgs {
+// Launches preprocess + large-Gaussian emission for every view of a.views
+// (grid.y = view).  Shared by the plain and the batched entry points.
+fgs_status run_preprocess(PreArgs& a, cudaStream_t s) {
+  FGS_TRY(cudaMemsetAsync(a.counters, 0, FGS_COUNTER_WORDS * sizeof(int32_t), s));
+  {
+    KernelTimer kt__(FGS_K_PREPROCESS, s);
+    k_preprocess<<<dim3((a.P + kPreThreads - 1) / kPreThreads, a.views.V), kPreThreads, 0, s>>>(a);
+    kt__.stop();
+  }
+  FGS_LAUNCH_CHECK();
+  {
+    KernelTimer kt__(FGS_K_PREPROCESS_LARGE, s);
+    k_preprocess_large<<<num_sms() * 4, kPreThreads, 0, s>>>(a);
+    kt__.stop();
+  }
+  FGS_LAUNCH_CHECK();
+  return FGS_OK;
+}
+}  // namespace fgs
 
 extern "C" fgs_status fgs_preprocess(
     int P, int D, int M, const float* means3D, const float* colors_precomp, const float* dc, const float* shs,
@@ -414,32 +416,15 @@ extern "C" fgs_status fgs_preprocess(
   if (((uintptr_t)rotations & 15) || ((uintptr_t)splat_buffer & 15) || ((uintptr_t)keys_unsorted & 7))
     return FGS_ERR_BAD_ARG;
   if ((int64_t)P > splat_rows) return FGS_ERR_CAPACITY;
-  cudaStream_t s = (cudaStream_t)stream;
   PreArgs a;
+  a.views = single_view(width, height, block_x, block_y, viewmatrix, projmatrix, campos, nullptr, tan_fovx, tan_fovy,
+                        mult, scale_modifier);
   a.P = P; a.D = D; a.M = M;
   a.means = means3D; a.colors = colors_precomp; a.dc = dc; a.shs = shs; a.opac = opacities;
-  a.scales = scales; a.rots = rotations; a.smod = scale_modifier;
-  a.W = width; a.H = height; a.bx = block_x; a.by = block_y;
-  a.gx = (width + block_x - 1) / block_x; a.gy = (height + block_y - 1) / block_y;
-  a.campos = campos; a.view = viewmatrix; a.proj = projmatrix;
-  a.tanx = tan_fovx; a.tany = tan_fovy;
-  a.fx = width / (2.0f * tan_fovx); a.fy = height / (2.0f * tan_fovy);
-  a.mult = mult; a.culling = culling; a.splat = splat_buffer;
+  a.scales = scales; a.rots = rotations; a.culling = culling; a.splat = splat_buffer;
   a.keys = reinterpret_cast<unsigned long long*>(keys_unsorted); a.vals = values_unsorted;
   a.cap = pair_capacity; a.tasks = task_scratch; a.task_cap = task_scratch_words / 2;
   a.curr = reinterpret_cast<unsigned int*>(curr_offset); a.counters = counters; a.radii = radii;
-  FGS_TRY(cudaMemsetAsync(counters, 0, FGS_COUNTER_WORDS * sizeof(int32_t), s));
-  {
-    KernelTimer kt__(FGS_K_PREPROCESS, s);
-    k_preprocess<<<(P + kPreThreads - 1) / kPreThreads, kPreThreads, 0, s>>>(a);
-    kt__.stop();
-  }
-  FGS_LAUNCH_CHECK();
-  {
-    KernelTimer kt__(FGS_K_PREPROCESS_LARGE, s);
-    k_preprocess_large<<<num_sms() * 4, kPreThreads, 0, s>>>(a);
-    kt__.stop();
-  }
-  FGS_LAUNCH_CHECK();
-  return FGS_OK;
+  a.large_tiles = kLargeTiles;
+  return run_preprocess(a, (cudaStream_t)stream);
 }

@@ -24,8 +24,10 @@ namespace {
 
 constexpr int kFwdWarps = 4;
 
-__global__ void __launch_bounds__(256) k_tile_ranges(const unsigned long long* __restrict__ keys, long long n,
-                                                     uint32_t num_tiles, uint32_t* __restrict__ ranges) {
+__global__ void __launch_bounds__(256) k_tile_ranges(const unsigned long long* __restrict__ keys, long long n_cap,
+                                                     const int* n_dev, uint32_t num_tiles,
+                                                     uint32_t* __restrict__ ranges) {
+  const long long n = n_dev ? min(n_cap, (long long)(unsigned int)*n_dev) : n_cap;
   const long long i = blockIdx.x * 256ll + threadIdx.x;
   if (i >= n) return;
   const uint32_t t = (uint32_t)(keys[i] >> 32);
@@ -88,6 +90,7 @@ __global__ void __launch_bounds__(1024) k_bucket_setup(int T, const uint32_t* __
 }
 
 struct FwdArgs {
+  Views views;
   const float* splat;
   const uint32_t* vals;
   const uint32_t* ranges;
@@ -95,7 +98,7 @@ struct FwdArgs {
   const uint32_t* bucket_off;
   uint32_t* bucket_sum;
   float4* samples;
-  int W, H, bx, by, gx, bs;
+  int bs;
 };
 
 template <int BX>
@@ -109,7 +112,9 @@ __global__ void __launch_bounds__(kFwdWarps * kWarp, 8) k_render_fwd(const FwdAr
   for (int b = next_bucket(a.bucket_sum + 2, lane); b < B;) {
     const int b_next = next_bucket(a.bucket_sum + 2, lane);
     const BucketInfo bi = bucket_info(b, a.bucket_tile, a.bucket_off, a.ranges, a.bs);
-    const int tx0 = (bi.tile % a.gx) * BX, ty0 = (bi.tile / a.gx) * BY;
+    const ViewDesc& cam = a.views.v[a.views.of_tile((uint32_t)bi.tile)];
+    const int lt = bi.tile - (int)cam.tile_off;  // tile index inside its view
+    const int tx0 = (lt % cam.gx) * BX, ty0 = (lt / cam.gx) * BY;
     stage_bucket<BX>(st, a.splat, a.vals + bi.start, bi.n, lane, tx0, ty0);
     float pxc[M::kCols], pyr[M::kRows];
 #pragma unroll
@@ -165,17 +170,17 @@ __global__ void __launch_bounds__(kFwdWarps * kWarp, 8) k_render_fwd(const FwdAr
 }
 
 struct MergeArgs {
+  Views views;
   const uint32_t* ranges;
   const uint32_t* bucket_off;
   const uint32_t* bucket_sum;
   float4* samples;
-  const float* bg;
-  float* out_color;
-  float* pix_color;
-  int* last_contrib;
+  float* out_color;     // per view (3, H, W), view k at 3 * pix_off
+  float* pix_color;     // same layout, without background
+  int* last_contrib;    // per view (H, W), view k at pix_off
   float* Ts_final;
   uint32_t* max_contrib;
-  int W, H, bx, by, gx, bs;
+  int bs;
 };
 
 // Per pixel: fold the tile's buckets front to back, storing the running
@@ -183,8 +188,10 @@ struct MergeArgs {
 __global__ void __launch_bounds__(kTilePixels) k_merge(const MergeArgs a) {
   __shared__ uint32_t s_max[kTilePixels / kWarp];
   const int tile = blockIdx.x, p = threadIdx.x;
-  const int px = (tile % a.gx) * a.bx + p % a.bx, py = (tile / a.gx) * a.by + p / a.bx;
-  const bool in = px < a.W && py < a.H;
+  const ViewDesc& cam = a.views.v[a.views.of_tile((uint32_t)tile)];
+  const int lt = tile - (int)cam.tile_off, bx = a.views.bx, by = a.views.by;
+  const int px = (lt % cam.gx) * bx + p % bx, py = (lt / cam.gx) * by + p / bx;
+  const bool in = px < cam.W && py < cam.H;
   // bucket_sum[0] is the bucket count clamped to the sample capacity.
   const int cap = (int)a.bucket_sum[0];
   const int first = min(cap, tile ? (int)a.bucket_off[tile - 1] : 0);
@@ -207,15 +214,18 @@ __global__ void __launch_bounds__(kTilePixels) k_merge(const MergeArgs a) {
       cur = nxt;
       s += kTilePixels;
     }
-    const int pix = py * a.W + px, HW = a.W * a.H;
-    a.last_contrib[pix] = (int)contrib;
-    a.Ts_final[pix] = T;
-    a.out_color[pix] = Cr + T * a.bg[0];
-    a.out_color[HW + pix] = Cg + T * a.bg[1];
-    a.out_color[2 * HW + pix] = Cb + T * a.bg[2];
-    a.pix_color[pix] = Cr;
-    a.pix_color[HW + pix] = Cg;
-    a.pix_color[2 * HW + pix] = Cb;
+    const size_t HW = (size_t)cam.W * cam.H;
+    const size_t pix = (size_t)py * cam.W + px;
+    a.last_contrib[cam.pix_off + pix] = (int)contrib;
+    a.Ts_final[cam.pix_off + pix] = T;
+    float* oc = a.out_color + 3 * (size_t)cam.pix_off;
+    float* pc = a.pix_color + 3 * (size_t)cam.pix_off;
+    oc[pix] = Cr + T * cam.bg[0];
+    oc[HW + pix] = Cg + T * cam.bg[1];
+    oc[2 * HW + pix] = Cb + T * cam.bg[2];
+    pc[pix] = Cr;
+    pc[HW + pix] = Cg;
+    pc[2 * HW + pix] = Cb;
   }
   const uint32_t m = __reduce_max_sync(0xffffffffu, contrib);
   if ((p & 31) == 0) s_max[p >> 5] = m;
@@ -227,28 +237,70 @@ __global__ void __launch_bounds__(kTilePixels) k_merge(const MergeArgs a) {
   }
 }
 
-bool tile_shape_ok(int bx, int by) { return bx * by == kTilePixels && (bx == 8 || bx == 16 || bx == 32); }
 
 }  // namespace
 }  // namespace fgs
 
 FGS_DEFINE_ERROR_ACCESSOR(render)
 
+namespace fgs {
+fgs_status run_tile_ranges(int64_t n_cap, const int32_t* n_dev, uint32_t tiles, const uint64_t* keys_sorted,
+                           uint32_t* ranges, cudaStream_t s) {
+  FGS_TRY(cudaMemsetAsync(ranges, 0, sizeof(uint32_t) * 2 * (size_t)tiles, s));
+  if (n_cap > 0) {
+    KernelTimer kt__(FGS_K_TILE_RANGES, s);
+    k_tile_ranges<<<(unsigned)((n_cap + 255) / 256), 256, 0, s>>>(
+        reinterpret_cast<const unsigned long long*>(keys_sorted), n_cap, n_dev, tiles, ranges);
+    kt__.stop();
+    FGS_LAUNCH_CHECK();
+  }
+  return FGS_OK;
+}
+
+fgs_status run_render_fwd(const Views& views, int64_t n_cap, const int32_t* n_dev, int bucket_size,
+                          const float* splat, const uint64_t* keys_sorted, const uint32_t* values_sorted,
+                          uint32_t* ranges, float* out_color, int32_t* last_contributor, float* Ts_final,
+                          const ImageState& im, const SampleState& sm, int64_t max_buckets, cudaStream_t s) {
+  fgs_status st = run_tile_ranges(n_cap, n_dev, views.tiles, keys_sorted, ranges, s);
+  if (st != FGS_OK) return st;
+  {
+    KernelTimer kt__(FGS_K_BUCKET_SETUP, s);
+    k_bucket_setup<<<1, 1024, 0, s>>>((int)views.tiles, ranges, bucket_size, max_buckets, im.bucket_off,
+                                      sm.bucket_tile, im.bucket_sum);
+    kt__.stop();
+  }
+  FGS_LAUNCH_CHECK();
+  FwdArgs fa{views, splat, values_sorted, ranges, sm.bucket_tile, im.bucket_off, im.bucket_sum, sm.samples,
+             bucket_size};
+  {
+    KernelTimer kt__(FGS_K_RENDER_FWD, s);
+    const int nt = kFwdWarps * kWarp;
+    if (views.bx == 8) k_render_fwd<8><<<num_sms() * resident_blocks(k_render_fwd<8>, nt, 0), nt, 0, s>>>(fa);
+    else if (views.bx == 16) k_render_fwd<16><<<num_sms() * resident_blocks(k_render_fwd<16>, nt, 0), nt, 0, s>>>(fa);
+    else k_render_fwd<32><<<num_sms() * resident_blocks(k_render_fwd<32>, nt, 0), nt, 0, s>>>(fa);
+    kt__.stop();
+  }
+  FGS_LAUNCH_CHECK();
+  MergeArgs ma{views, ranges, im.bucket_off, im.bucket_sum, sm.samples, out_color, im.pix_color, last_contributor,
+               Ts_final, im.max_contrib, bucket_size};
+  {
+    KernelTimer kt__(FGS_K_MERGE, s);
+    k_merge<<<views.tiles, kTilePixels, 0, s>>>(ma);
+    kt__.stop();
+  }
+  FGS_LAUNCH_CHECK();
+  return FGS_OK;
+}
+
+bool tile_shape_ok(int bx, int by) { return bx * by == kTilePixels && (bx == 8 || bx == 16 || bx == 32); }
+}  // namespace fgs
+
 using namespace fgs;
 
 extern "C" fgs_status fgs_tile_ranges(int64_t num_rendered, int num_tiles, const uint64_t* keys_sorted,
                                       uint32_t* ranges, void* stream) {
   if (num_rendered < 0 || num_tiles <= 0 || !ranges || (num_rendered > 0 && !keys_sorted)) return FGS_ERR_BAD_ARG;
-  cudaStream_t s = (cudaStream_t)stream;
-  FGS_TRY(cudaMemsetAsync(ranges, 0, sizeof(uint32_t) * 2 * (size_t)num_tiles, s));
-  if (num_rendered > 0) {
-    KernelTimer kt__(FGS_K_TILE_RANGES, s);
-    k_tile_ranges<<<(unsigned)((num_rendered + 255) / 256), 256, 0, s>>>(
-        reinterpret_cast<const unsigned long long*>(keys_sorted), num_rendered, (uint32_t)num_tiles, ranges);
-    kt__.stop();
-    FGS_LAUNCH_CHECK();
-  }
-  return FGS_OK;
+  return run_tile_ranges(num_rendered, nullptr, (uint32_t)num_tiles, keys_sorted, ranges, (cudaStream_t)stream);
 }
 
 extern "C" int64_t fgs_max_buckets(int64_t num_rendered, int width, int height, int block_x, int block_y,
@@ -262,8 +314,8 @@ extern "C" int64_t fgs_max_buckets(int64_t num_rendered, int width, int height, 
 extern "C" fgs_status fgs_state_bytes(int width, int height, int block_x, int block_y, int64_t max_buckets,
                                       size_t* image_bytes, size_t* sample_bytes) {
   if (width <= 0 || height <= 0 || block_x <= 0 || block_y <= 0 || max_buckets < 0) return FGS_ERR_BAD_ARG;
-  const int T = ((width + block_x - 1) / block_x) * ((height + block_y - 1) / block_y);
-  if (image_bytes) *image_bytes = carve_image(nullptr, width, height, T).bytes;
+  const size_t T = (size_t)((width + block_x - 1) / block_x) * ((height + block_y - 1) / block_y);
+  if (image_bytes) *image_bytes = carve_image(nullptr, (size_t)width * height, T).bytes;
   if (sample_bytes) *sample_bytes = carve_sample(nullptr, std::max<int64_t>(max_buckets, 1)).bytes;
   return FGS_OK;
 }
@@ -284,39 +336,15 @@ extern "C" fgs_status fgs_render_fwd(int P, int64_t num_rendered, int width, int
     return FGS_ERR_BAD_ARG;
   if (((uintptr_t)splat_buffer & 15) || ((uintptr_t)image_state & 255) || ((uintptr_t)sample_state & 255))
     return FGS_ERR_BAD_ARG;
-  const int gx = (width + block_x - 1) / block_x, gy = (height + block_y - 1) / block_y, T = gx * gy;
-  const ImageState im = carve_image(image_state, width, height, T);
+  const Views views = single_view(width, height, block_x, block_y, nullptr, nullptr, nullptr, bg, 1.f, 1.f, 1.f, 1.f);
+  const ImageState im = carve_image(image_state, (size_t)width * height, views.tiles);
   const SampleState sm = carve_sample(sample_state, std::max<int64_t>(max_buckets, 1));
   if (image_bytes < im.bytes || sample_bytes < sm.bytes) return FGS_ERR_CAPACITY;
   cudaStream_t s = (cudaStream_t)stream;
-  fgs_status st = fgs_tile_ranges(num_rendered, T, keys_sorted, ranges, stream);
+  const fgs_status st = run_render_fwd(views, num_rendered, nullptr, bucket_size, splat_buffer, keys_sorted,
+                                       values_sorted, ranges, out_color, last_contributor, Ts_final, im, sm,
+                                       max_buckets, s);
   if (st != FGS_OK) return st;
-  {
-    KernelTimer kt__(FGS_K_BUCKET_SETUP, s);
-    k_bucket_setup<<<1, 1024, 0, s>>>(T, ranges, bucket_size, max_buckets, im.bucket_off, sm.bucket_tile,
-                                    im.bucket_sum);
-    kt__.stop();
-  }
-  FGS_LAUNCH_CHECK();
-  FwdArgs fa{splat_buffer, values_sorted, ranges, sm.bucket_tile, im.bucket_off, im.bucket_sum, sm.samples,
-             width, height, block_x, block_y, gx, bucket_size};
-  {
-    KernelTimer kt__(FGS_K_RENDER_FWD, s);
-    const int nt = kFwdWarps * kWarp;
-    if (block_x == 8) k_render_fwd<8><<<num_sms() * resident_blocks(k_render_fwd<8>, nt, 0), nt, 0, s>>>(fa);
-    else if (block_x == 16) k_render_fwd<16><<<num_sms() * resident_blocks(k_render_fwd<16>, nt, 0), nt, 0, s>>>(fa);
-    else k_render_fwd<32><<<num_sms() * resident_blocks(k_render_fwd<32>, nt, 0), nt, 0, s>>>(fa);
-    kt__.stop();
-  }
-  FGS_LAUNCH_CHECK();
-  MergeArgs ma{ranges, im.bucket_off, im.bucket_sum, sm.samples, bg, out_color, im.pix_color, last_contributor, Ts_final,
-               im.max_contrib, width, height, block_x, block_y, gx, bucket_size};
-  {
-    KernelTimer kt__(FGS_K_MERGE, s);
-    k_merge<<<T, kTilePixels, 0, s>>>(ma);
-    kt__.stop();
-  }
-  FGS_LAUNCH_CHECK();
   if (bucket_sum_host) {
     uint32_t hs[2] = {0, 0};
     FGS_TRY(cudaMemcpyAsync(hs, im.bucket_sum, sizeof(hs), cudaMemcpyDeviceToHost, s));

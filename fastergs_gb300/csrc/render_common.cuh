@@ -1,6 +1,10 @@
 // State layout shared by the forward and backward composite kernels.
 #pragma once
-#include "fgs_common.cuh"
+#include <map>
+#include <mutex>
+#include <tuple>
+
+#include "internal.cuh"
 
 namespace fgs {
 
@@ -33,12 +37,13 @@ struct SampleState {
 
 inline size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
 
-inline ImageState carve_image(void* base, int W, int H, int T) {
+// pixels: all pixels of all views (colour planes of view k at 3 * pix_off).
+inline ImageState carve_image(void* base, size_t pixels, size_t T) {
   char* p = static_cast<char*>(base);
   ImageState s;
   size_t off = 0;
   s.bucket_sum = reinterpret_cast<uint32_t*>(p + off);  off = align_up(off + 16, 256);
-  s.pix_color = reinterpret_cast<float*>(p + off);      off = align_up(off + sizeof(float) * 3 * (size_t)W * H, 256);
+  s.pix_color = reinterpret_cast<float*>(p + off);      off = align_up(off + sizeof(float) * 3 * pixels, 256);
   s.max_contrib = reinterpret_cast<uint32_t*>(p + off); off = align_up(off + sizeof(uint32_t) * (size_t)T, 256);
   s.bucket_off = reinterpret_cast<uint32_t*>(p + off);  off = align_up(off + sizeof(uint32_t) * (size_t)T, 256);
   s.bytes = off;
@@ -135,10 +140,21 @@ __device__ __forceinline__ int next_bucket(uint32_t* cursor, int lane) {
 }
 
 // Blocks per SM that a kernel can keep resident, for sizing persistent grids.
+// Cached per (kernel, block size, device) so that launches issue no runtime
+// queries (and stay cheap while a CUDA graph is being captured).
 template <typename K>
 inline int resident_blocks(K kernel, int threads, size_t smem) {
+  static std::mutex mu;
+  static std::map<std::tuple<const void*, int, size_t, int>, int> cache;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  const auto key = std::make_tuple(reinterpret_cast<const void*>(kernel), threads, smem, dev);
+  std::lock_guard<std::mutex> lk(mu);
+  const auto it = cache.find(key);
+  if (it != cache.end()) return it->second;
   int n = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kernel, threads, smem) != cudaSuccess || n < 1) n = 1;
+  cache.emplace(key, n);
   return n;
 }
 
@@ -158,5 +174,18 @@ __device__ __forceinline__ BucketInfo bucket_info(int b, const uint32_t* __restr
   bi.n = min(bs, re - bi.start);
   return bi;
 }
+
+// Launch sequences shared by the plain and the batched entry points.
+// Forward: tile ranges, bucket setup, persistent composite, merge.  n_dev,
+// when given, is the device-side pair count (clamped to n_cap).
+fgs_status run_render_fwd(const Views& views, int64_t n_cap, const int32_t* n_dev, int bucket_size,
+                          const float* splat, const uint64_t* keys_sorted, const uint32_t* values_sorted,
+                          uint32_t* ranges, float* out_color, int32_t* last_contributor, float* Ts_final,
+                          const ImageState& im, const SampleState& sm, int64_t max_buckets, cudaStream_t s);
+// Backward composite into grad_record (records x FGS_GRAD_STRIDE, zeroed here).
+fgs_status run_render_bwd(const Views& views, int64_t records, int bucket_size, const uint32_t* values_sorted,
+                          const uint32_t* ranges, const float* splat, const float* Ts_final,
+                          const int32_t* last_contributor, const ImageState& im, const SampleState& sm,
+                          const float* dL_dpixels, float* grad_record, cudaStream_t s);
 
 }  // namespace fgs

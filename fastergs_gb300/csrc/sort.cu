@@ -14,10 +14,11 @@
 //     ceil(log2(tiles)) tile bits, i.e. 5-6 passes for 256..32768 tiles.
 // Every look-back wait is bounded (kSpinLimit polls); on expiry the kernel
 // records kErrTimeout in the error word and continues, so it never hangs.
+#include <atomic>
 #include <algorithm>
 #include <mutex>
 
-#include "fgs_common.cuh"
+#include "internal.cuh"
 
 namespace fgs {
 namespace {
@@ -55,9 +56,16 @@ constexpr SortLayout layout_for(int64_t n) {
 }
 
 // All pass histograms in one read of the keys.
-__global__ void __launch_bounds__(kSortThreads) k_histogram(const unsigned long long* keys, long long n,
-                                                            int passes, uint32_t* hist) {
+// Pair count: the host bound, or min(bound, *n_dev) when the count lives on
+// the device (batched / graph-captured frames).
+__device__ __forceinline__ long long pair_count(long long n_cap, const int* n_dev) {
+  return n_dev ? min(n_cap, (long long)(unsigned int)*n_dev) : n_cap;
+}
+
+__global__ void __launch_bounds__(kSortThreads) k_histogram(const unsigned long long* keys, long long n_cap,
+                                                            const int* n_dev, int passes, uint32_t* hist) {
   __shared__ uint32_t s_h[kMaxPasses][kRadix];
+  const long long n = pair_count(n_cap, n_dev);
   for (int j = threadIdx.x; j < kMaxPasses * kRadix; j += kSortThreads) (&s_h[0][0])[j] = 0;
   __syncthreads();
   for (long long k = blockIdx.x * (long long)kSortThreads + threadIdx.x; k < n;
@@ -98,8 +106,8 @@ __device__ __forceinline__ uint32_t block_excl_scan_256(uint32_t v, uint32_t* s_
 
 __global__ void __launch_bounds__(kSortThreads) k_onesweep(
     const unsigned long long* __restrict__ keys_in, const uint32_t* __restrict__ vals_in,
-    unsigned long long* __restrict__ keys_out, uint32_t* __restrict__ vals_out, long long n, int shift,
-    const uint32_t* __restrict__ hist, uint32_t* lookback, uint32_t* tile_counter) {
+    unsigned long long* __restrict__ keys_out, uint32_t* __restrict__ vals_out, long long n_cap, const int* n_dev,
+    int shift, const uint32_t* __restrict__ hist, uint32_t* lookback, uint32_t* tile_counter) {
   extern __shared__ __align__(16) unsigned char s_dyn[];  // kSortDynSmem bytes
   unsigned long long* s_keys = reinterpret_cast<unsigned long long*>(s_dyn);
   uint32_t* s_vals = reinterpret_cast<uint32_t*>(s_dyn + sizeof(unsigned long long) * kSortTile);
@@ -115,6 +123,8 @@ __global__ void __launch_bounds__(kSortThreads) k_onesweep(
   __syncthreads();
   const uint32_t tile = s_tile;
   const long long tile_base = (long long)tile * kSortTile;
+  const long long n = pair_count(n_cap, n_dev);
+  if (tile_base >= n) return;  // grid sized for the capacity; this tile is empty
 
   // Load: warp w owns keys [tile_base + w*512, +512), 32 consecutive per step,
   // so (warp, step, lane) is the input order and the ranks below are stable.
@@ -227,26 +237,20 @@ __global__ void __launch_bounds__(kSortThreads) k_onesweep(
 
 FGS_DEFINE_ERROR_ACCESSOR(sort)
 
-extern "C" size_t fgs_sort_temp_bytes(int64_t num_rendered) {
-  if (num_rendered < 1) num_rendered = 1;
-  return fgs::layout_for(num_rendered).total;
-}
+extern "C" size_t fgs_sort_temp_bytes(int64_t num_rendered) { return fgs::sort_temp_bytes(num_rendered); }
 
-extern "C" fgs_status fgs_sort(int64_t num_rendered, int width, int height, int block_x, int block_y, void* temp,
-                               size_t temp_bytes, const uint64_t* keys_in, const uint32_t* values_in,
-                               uint64_t* keys_out, uint32_t* values_out, void* stream) {
-  using namespace fgs;
-  if (num_rendered < 0 || width <= 0 || height <= 0 || block_x <= 0 || block_y <= 0) return FGS_ERR_BAD_ARG;
-  if (num_rendered == 0) return FGS_OK;
-  if (num_rendered >= (int64_t)kValueMask) return FGS_ERR_CAPACITY;
+namespace fgs {
+fgs_status run_sort(int64_t n_cap, const int32_t* n_dev, uint32_t tiles, void* temp, size_t temp_bytes,
+                    const uint64_t* keys_in, const uint32_t* values_in, uint64_t* keys_out, uint32_t* values_out,
+                    cudaStream_t s) {
+  if (n_cap == 0) return FGS_OK;
+  if (n_cap >= (int64_t)kValueMask) return FGS_ERR_CAPACITY;
   if (!temp || !keys_in || !values_in || !keys_out || !values_out) return FGS_ERR_BAD_ARG;
   if (((uintptr_t)temp & 255) || ((uintptr_t)keys_in & 7) || ((uintptr_t)keys_out & 7)) return FGS_ERR_BAD_ARG;
-  const SortLayout L = layout_for(num_rendered);
+  const SortLayout L = layout_for(n_cap);
   if (temp_bytes < L.total) return FGS_ERR_CAPACITY;
-  const uint32_t tiles = (uint32_t)(((width + block_x - 1) / block_x) * ((height + block_y - 1) / block_y));
   const int bits = 32 + tile_bits(tiles);
   const int passes = (bits + 7) / 8;
-  cudaStream_t s = (cudaStream_t)stream;
   char* base = static_cast<char*>(temp);
   uint32_t* hist = reinterpret_cast<uint32_t*>(base + L.hist);
   uint32_t* counters = reinterpret_cast<uint32_t*>(base + L.counters);
@@ -255,19 +259,24 @@ extern "C" fgs_status fgs_sort(int64_t num_rendered, int width, int height, int 
   auto* alt_v = reinterpret_cast<uint32_t*>(base + L.alt_vals);
   // hist, counters and the look-back words of every pass start at zero.
   FGS_TRY(cudaMemsetAsync(base, 0, L.alt_keys, s));
-  const int hist_blocks = (int)std::min<int64_t>((num_rendered + kSortThreads * 8 - 1) / (kSortThreads * 8),
+  const int hist_blocks = (int)std::min<int64_t>((n_cap + kSortThreads * 8 - 1) / (kSortThreads * 8),
                                                  (int64_t)num_sms() * 8);
   {
     KernelTimer kt__(FGS_K_SORT_HIST, s);
-    k_histogram<<<hist_blocks, kSortThreads, 0, s>>>(reinterpret_cast<const unsigned long long*>(keys_in),
-                                                   num_rendered, passes, hist);
+    k_histogram<<<hist_blocks, kSortThreads, 0, s>>>(reinterpret_cast<const unsigned long long*>(keys_in), n_cap,
+                                                     n_dev, passes, hist);
     kt__.stop();
   }
   FGS_LAUNCH_CHECK();
-  static bool smem_set = false;  // per process; the attribute is per function, not per device
-  if (!smem_set) {
+  // The dynamic shared-memory opt-in is a per-device function attribute; set
+  // once per device (before any capture, by the first call).
+  static std::atomic<bool> smem_set[64];
+  int dev = 0;
+  FGS_TRY(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) return FGS_ERR_UNSUPPORTED;
+  if (!smem_set[dev].load()) {
     FGS_TRY(cudaFuncSetAttribute(k_onesweep, cudaFuncAttributeMaxDynamicSharedMemorySize, kSortDynSmem));
-    smem_set = true;
+    smem_set[dev].store(true);
   }
   const unsigned long long* src_k = reinterpret_cast<const unsigned long long*>(keys_in);
   const uint32_t* src_v = values_in;
@@ -278,16 +287,30 @@ extern "C" fgs_status fgs_sort(int64_t num_rendered, int width, int height, int 
     uint32_t* dv = to_out ? values_out : alt_v;
     {
       KernelTimer kt__(FGS_K_SORT_PASS, s);
-      k_onesweep<<<(unsigned)L.tiles, kSortThreads, kSortDynSmem, s>>>(src_k, src_v, dk, dv, num_rendered, 8 * p,
-                                                          hist + p * kRadix,
-                                                          lookback + (size_t)p * L.tiles * kRadix, counters + p);
+      k_onesweep<<<(unsigned)L.tiles, kSortThreads, kSortDynSmem, s>>>(src_k, src_v, dk, dv, n_cap, n_dev, 8 * p,
+                                                                      hist + p * kRadix,
+                                                                      lookback + (size_t)p * L.tiles * kRadix,
+                                                                      counters + p);
       kt__.stop();
     }
-  FGS_LAUNCH_CHECK();
+    FGS_LAUNCH_CHECK();
     src_k = dk;
     src_v = dv;
   }
   return FGS_OK;
+}
+
+size_t sort_temp_bytes(int64_t n) { return layout_for(n < 1 ? 1 : n).total; }
+}  // namespace fgs
+
+extern "C" fgs_status fgs_sort(int64_t num_rendered, int width, int height, int block_x, int block_y, void* temp,
+                               size_t temp_bytes, const uint64_t* keys_in, const uint32_t* values_in,
+                               uint64_t* keys_out, uint32_t* values_out, void* stream) {
+  using namespace fgs;
+  if (num_rendered < 0 || width <= 0 || height <= 0 || block_x <= 0 || block_y <= 0) return FGS_ERR_BAD_ARG;
+  const uint32_t tiles = (uint32_t)(((width + block_x - 1) / block_x) * ((height + block_y - 1) / block_y));
+  return run_sort(num_rendered, nullptr, tiles, temp, temp_bytes, keys_in, values_in, keys_out, values_out,
+                  (cudaStream_t)stream);
 }
 
 // ---------------------------------------------------------------------------

@@ -181,6 +181,95 @@ fgs_status fgs_adam_update(float* param, const float* grad, float* exp_avg, floa
                            const uint8_t* visible, float lr, float b1, float b2, float eps,
                            uint32_t N, uint32_t M, void* stream);
 
+/*
+ * Batched multi-camera rendering.  No counterpart in FB, which renders one
+ * camera per call and reads the pair and bucket counts back to the host
+ * three times per step (FB __init__.py:106-132, rasterizer_imp.cu:141-147),
+ * so it cannot be captured in a CUDA graph.  Here one call renders up to
+ * FGS_MAX_VIEWS cameras of different resolutions with one launch per stage
+ * (preprocess with grid.y = camera, one sort over a global tile index space,
+ * one persistent composite launch over the buckets of every camera, one
+ * merge), with no host synchronisation, so fwd and bwd can be captured in a
+ * CUDA graph and replayed.  Capacities are fixed by the caller; a frame that
+ * overflows pair_capacity skips the extra writes, latches a device flag and
+ * is reported by fgs_batch_status.
+ *
+ * Per-camera outputs are concatenated: camera k's image (3, H_k, W_k) starts
+ * at float offset 3 * sum_{j<k} H_j W_j of out_color / dL_dpixels, and its
+ * radii at k * P of radii (num_views, P).
+ */
+#define FGS_MAX_VIEWS 32
+typedef struct {
+  const float* viewmatrix;  /* 4x4 column-major world -> view, device */
+  const float* projmatrix;  /* 4x4 column-major full projection, device */
+  const float* campos;      /* 3, device */
+  const float* bg;          /* 3, device */
+  int width, height;
+  float tan_fovx, tan_fovy;
+  float scale_modifier;     /* FB GaussianRasterizationSettings.scale_modifier */
+  float mult;               /* FB GaussianRasterizationSettings.mult */
+} fgs_camera;
+
+/* Launch configuration picked by the autotuner; FB's fixed choice is
+ * {128, 16, 16, 4}.  bucket_size 1..128 Gaussians per bucket; tile 16x16,
+ * 8x32 or 32x8 pixels; packet 1, 2, 4 or 8: footprints of at least
+ * 32*packet tiles are split into sub-tasks of 32*packet tiles, smaller ones
+ * are lane-packed by the preprocess warps.  The tile shape and the bucket
+ * size change images at the level of the T < 1e-4 stopping rule (which acts
+ * per bucket); packet changes only the order in which pairs are emitted. */
+typedef struct {
+  int bucket_size;
+  int block_x, block_y;
+  int packet;
+} fgs_tune_config;
+
+/* Workspace bytes (256-byte aligned base required) of a batched frame. */
+fgs_status fgs_batch_workspace_bytes(int P, int num_views, const fgs_camera* cams, const fgs_tune_config* cfg,
+                                     int64_t pair_capacity, size_t* bytes);
+
+/* Forward of every camera: out_color (concatenated images), radii
+ * (num_views, P).  Inputs use FB's layouts; colors_precomp replaces
+ * dc/shs when non-NULL; culling (P) is optional. */
+fgs_status fgs_render_batched_fwd(int P, int D, int M, const float* means3D, const float* colors_precomp,
+                                  const float* dc, const float* shs, const float* opacities, const float* scales,
+                                  const float* rotations, const uint8_t* culling, int num_views,
+                                  const fgs_camera* cams, const fgs_tune_config* cfg, int64_t pair_capacity,
+                                  void* workspace, size_t workspace_bytes, float* out_color, int32_t* radii,
+                                  void* stream);
+
+/* Backward of the last fgs_render_batched_fwd on the same workspace.
+ * Gradients are summed over cameras and fully written; the optional
+ * densification statistics are accumulated once per camera, as FB's
+ * per-camera backward does.  dL_dcolor (P,3) and dL_dcov3D (P,6) are
+ * summed over cameras too. */
+fgs_status fgs_render_batched_bwd(int P, int D, int M, const float* means3D, const float* dc, const float* shs,
+                                  const float* scales, const float* rotations, int num_views,
+                                  const fgs_camera* cams, const fgs_tune_config* cfg, int64_t pair_capacity,
+                                  void* workspace, size_t workspace_bytes, const int32_t* radii,
+                                  const float* dL_dpixels, float* dL_dmean3D, float* dL_ddc, float* dL_dsh,
+                                  float* dL_dopacity, float* dL_dscale, float* dL_drot, float* dL_dcolor,
+                                  float* dL_dcov3D, float* xyz_gradient_accum, float* xyz_gradient_accum_abs,
+                                  float* max_radii, float* denom, void* stream);
+
+/* Reads the pair and bucket counts of the last batched forward on this
+ * workspace (synchronises the stream).  Returns FGS_ERR_CAPACITY when the
+ * frame overflowed pair_capacity (or its bucket bound); the counts are then
+ * the sizes the frame needed. */
+fgs_status fgs_batch_status(int P, int num_views, const fgs_camera* cams, const fgs_tune_config* cfg,
+                            int64_t pair_capacity, const void* workspace, int64_t* pairs, int64_t* buckets,
+                            void* stream);
+
+/* Byte offsets inside a batched workspace, for inspection and tests:
+ * [0] pair count (int32), [1] splat records (num_views*P, FGS_SPLAT_STRIDE
+ * floats, record = camera * P + Gaussian), [2] unsorted keys, [3] unsorted
+ * values, [4] sorted keys (u64, global tile << 32 | depth), [5] sorted
+ * values (record indices), [6] tile ranges (u32 pairs over the global tile
+ * index space, camera after camera), [7] last contributor (int32 per pixel,
+ * cameras concatenated), [8] final transmittance, [9] gradient records
+ * (num_views*P, FGS_GRAD_STRIDE).  n >= 10. */
+fgs_status fgs_batch_offsets(int P, int num_views, const fgs_camera* cams, const fgs_tune_config* cfg,
+                             int64_t pair_capacity, int64_t* offsets, int n);
+
 /* Kernel-level timing for benchmarks.  While enabled for a kernel id, the
  * library records a CUDA event pair around every launch of that kernel on its
  * launch stream; fgs_kernel_timer_read synchronises those events and returns
