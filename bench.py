@@ -49,6 +49,10 @@ def parse():
     ap.add_argument("--gaussians", type=int, default=1_000_000)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--cameras", type=int, default=16)
+    ap.add_argument("--tune", choices=["sweep", "default"], default="sweep",
+                    help="batched launch config: autotuner sweep (18 configs) or FB's fixed choice")
     return ap.parse_args()
 
 
@@ -279,8 +283,129 @@ def gpu_bench(args, rank, local, world):
         e2e_ms = max_over_ranks(ev0.elapsed_time(ev1) / args.steps, world, dev)
         e2e = {"value": e2e_ms / world, "unit": "ms/step", "h2d_bytes_per_step": int(in_bytes),
                "d2h_bytes_per_step": int(out_bytes), "wall_ms_per_step": (time.perf_counter() - t0) * 1e3 / args.steps}
+    batched = None
+    if not args.no_batched and world == 1:
+        batched = []
+        c4 = scenes.cameras_c4(seed=0, n=args.cameras)
+        batched.append(batched_bench(args, dev, s, dev_in, c4, f"c4: {args.cameras} cameras on a radius-8 circle, "
+                                     "resolutions seeded from {640x360 .. 1920x1080}, FoV U[40,70] deg"))
+        same = [scenes.make_camera(1297, 840, c.fovx * 180.0 / math.pi, eye=tuple(float(x) for x in c.campos),
+                                   target=(0.0, 0.0, 7.0)) for c in c4]
+        batched.append(batched_bench(args, dev, s, dev_in, same, f"{args.cameras} cameras at 1297x840 on the same "
+                                     "circle"))
     return dict(ms_step=ms_step_job, fwd_ms=fwd_ms, clocks=clocks, ktimes=ktimes, K=K,
-                launches_per_step=launches_per_step, e2e=e2e, P=s.P, W=cam.width, H=cam.height)
+                launches_per_step=launches_per_step, e2e=e2e, P=s.P, W=cam.width, H=cam.height, batched=batched)
+
+
+def batched_bench(args, dev, s, dev_in, cams, label):
+    """16 cameras of one 1M-Gaussian scene: 16 sequential plain-path calls
+    (public API, autograd, FB's host reads of the pair and bucket counts)
+    against one batched step captured in a CUDA graph.  Times are per
+    16-camera step, CUDA events on the launch stream."""
+    import torch
+    import fastergs_gb300 as fgs
+    from fastergs_gb300 import _lib, scenes
+    from fastergs_gb300.batched import BatchedRasterizer, CapturedStep, TuneConfig
+    from fastergs_gb300 import tune as tuner
+    t = lambda a: torch.tensor(np.asarray(a, np.float32), device=dev)
+    sets = [fgs.GaussianRasterizationSettings(
+        image_height=c.height, image_width=c.width, tanfovx=c.tanfovx, tanfovy=c.tanfovy,
+        bg=torch.zeros(3, device=dev), scale_modifier=1.0, viewmatrix=t(c.viewmatrix), projmatrix=t(c.projmatrix),
+        sh_degree=s.sh_degree, campos=t(c.campos), mult=1.0, prefiltered=False, debug=False) for c in cams]
+    dLs = [torch.from_numpy(scenes.upstream_grad(k, c.height, c.width)).to(dev) for k, c in enumerate(cams)]
+    stream = torch.cuda.current_stream(dev)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    reps = max(3, min(args.steps, 10))
+
+    # plain: one drop-in call per camera; size FB's shared Buffer for the largest view
+    slot = fgs._RasterizeGaussians.__dict__["buffer"]
+    cap = slot._buf.MAX_NUM_RENDERED if slot._buf is not None else 1 << 22
+    while True:
+        try:
+            with torch.no_grad():
+                for st in sets:
+                    fgs.GaussianRasterizer(st)(means3D=dev_in["means"], opacities=dev_in["opacities"],
+                                               dc=dev_in["dc"], shs=dev_in["shs"], scales=dev_in["scales"],
+                                               rotations=dev_in["rotations"])
+            break
+        except RuntimeError as e:
+            if "Too many k-v pairs" not in str(e):
+                raise
+            cap *= 2
+            slot._buf = None
+            torch.cuda.empty_cache()
+            slot._buf = fgs.Buffer(device=dev, MAX_NUM_RENDERED=cap)
+
+    def plain_step(backward=True):
+        for st, dL in zip(sets, dLs):
+            leaves = {k: v.detach().requires_grad_(backward) for k, v in dev_in.items()}
+            img, _ = fgs.GaussianRasterizer(st)(means3D=leaves["means"], opacities=leaves["opacities"],
+                                                dc=leaves["dc"], shs=leaves["shs"], scales=leaves["scales"],
+                                                rotations=leaves["rotations"])
+            if backward:
+                torch.autograd.backward(img, grad_tensors=dL)
+
+    def timed(fn, n):
+        for _ in range(2):
+            fn()
+        torch.cuda.synchronize()
+        ev0.record(stream)
+        for _ in range(n):
+            fn()
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        return ev0.elapsed_time(ev1) / n
+
+    plain_ms = timed(plain_step, reps)
+    with torch.no_grad():
+        plain_fwd_ms = timed(lambda: plain_step(False), reps)
+
+    params = {"means3D": dev_in["means"], "opacities": dev_in["opacities"], "dc": dev_in["dc"],
+              "shs": dev_in["shs"], "scales": dev_in["scales"], "rotations": dev_in["rotations"]}
+    table = []
+    if args.tune == "sweep":
+        cfg, table = tuner.autotune(sets, params, s.sh_degree, backward=True, reps=3, warmup=1, force=True)
+    else:
+        cfg = TuneConfig()
+    rast = BatchedRasterizer(sets, s.P, tune=cfg)
+    pairs = rast.fit(params["means3D"], params["opacities"], params["dc"], params["shs"], None, params["scales"],
+                     params["rotations"], None, s.sh_degree, headroom=1.15)
+    flat_dL = torch.cat([d.reshape(-1) for d in dLs])
+    step = CapturedStep(rast, params, flat_dL, sh_degree=s.sh_degree)
+    batched_ms = timed(step.replay, reps)
+    fwd = CapturedStep(rast, params, flat_dL, sh_degree=s.sh_degree, with_backward=False)
+    batched_fwd_ms = timed(fwd.replay, reps)
+    rast.status()  # raises if any replay overflowed
+    # per-kernel device time of the batched path (eager launches; timers skip graph capture)
+    _lib.kernel_timers(True)
+    _lib.read_kernel_timers()
+    for _ in range(reps):
+        rast.forward(params["means3D"], params["opacities"], params["dc"], params["shs"], None, params["scales"],
+                     params["rotations"], None, s.sh_degree)
+        rast.backward(flat_dL, params["means3D"], params["dc"], params["shs"], params["scales"],
+                      params["rotations"], s.sh_degree, out=step.grads)
+    torch.cuda.synchronize()
+    kt = _lib.read_kernel_timers()
+    _lib.kernel_timers(False)
+    kernels = {k: {"ms_per_step": round(v[0] / reps, 4), "launches_per_step": v[1] / reps}
+               for k, v in kt.items() if v[1]}
+    V = len(cams)
+    out = {
+        "workload": label, "cameras": V, "resolutions": sorted({f"{c.width}x{c.height}" for c in cams}),
+        "pixels": int(sum(c.width * c.height for c in cams)), "pairs": int(pairs),
+        "tune": cfg.__dict__.copy(), "tune_sweep_ms": {f"b{r['config']['bucket_size']}_{r['config']['block_x']}x"
+                                                       f"{r['config']['block_y']}_p{r['config']['packet']}":
+                                                       round(r["ms"], 3) for r in table},
+        "plain_ms_per_step": round(plain_ms, 3), "batched_ms_per_step": round(batched_ms, 3),
+        "speedup_fwd_bwd": round(plain_ms / batched_ms, 3),
+        "plain_render_fps": round(1000.0 * V / plain_fwd_ms, 1),
+        "batched_render_fps": round(1000.0 * V / batched_fwd_ms, 1),
+        "speedup_render": round(plain_fwd_ms / batched_fwd_ms, 3),
+        "batched_kernels": kernels,
+    }
+    del step, fwd, rast
+    torch.cuda.empty_cache()
+    return out
 
 
 def roofline(res, peaks):
@@ -362,6 +487,7 @@ def main():
         "render_ms": round(res["fwd_ms"], 4),
         "e2e": res["e2e"], "gpu_launches": int(round(res["launches_per_step"] * args.steps)),
         "clocks": res["clocks"], "roofline": roof, "kernels": table, "cpu_baseline": cb,
+        "batched": res["batched"],
     }
     print(json.dumps(line), flush=True)
     barrier(world)
