@@ -66,6 +66,52 @@ __device__ __forceinline__ float sqrt_approx(float x) {
   asm("sqrt.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
   return y;
 }
+// Float-float arithmetic: a value is hi + lo with |lo| <= ulp(hi) / 2, good to
+// about 44 bits.  Built from the error-free transforms TwoSum (Knuth, TAOCP
+// vol. 2, 4.2.2) and the FMA product (Dekker 1971 with a fused multiply-add).
+// Explicit _rn intrinsics keep the compiler from contracting the transforms.
+// On sm_103 FP64 issues at a small fraction of the FP32 rate, so this is the
+// cheap way to get pixel positions far below FP32 resolution.
+struct ff {
+  float hi, lo;
+};
+__device__ __forceinline__ ff ff_two_sum(float a, float b) {
+  const float s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  return {s, __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb))};
+}
+__device__ __forceinline__ ff ff_fast_sum(float a, float b) {  // needs |a| >= |b| or a == 0
+  const float s = __fadd_rn(a, b);
+  return {s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+__device__ __forceinline__ ff ff_prod(float a, float b) {
+  const float p = __fmul_rn(a, b);
+  return {p, __fmaf_rn(a, b, -p)};
+}
+__device__ __forceinline__ ff ff_add(ff a, ff b) {
+  const ff s = ff_two_sum(a.hi, b.hi);
+  return ff_fast_sum(s.hi, __fadd_rn(s.lo, __fadd_rn(a.lo, b.lo)));
+}
+__device__ __forceinline__ ff ff_add_f(ff a, float b) {
+  const ff s = ff_two_sum(a.hi, b);
+  return ff_fast_sum(s.hi, __fadd_rn(s.lo, a.lo));
+}
+__device__ __forceinline__ ff ff_mul_f(ff a, float b) {
+  const ff p = ff_prod(a.hi, b);
+  return ff_fast_sum(p.hi, __fmaf_rn(a.lo, b, p.lo));
+}
+// a / b: quotient of the leading parts, then one correction from the exact
+// remainder a - q1 b.
+__device__ __forceinline__ ff ff_div(ff a, ff b) {
+  const float q1 = __fdiv_rn(a.hi, b.hi);
+  const ff p = ff_prod(q1, b.hi);
+  float r = __fsub_rn(a.hi, p.hi);
+  r = __fsub_rn(r, p.lo);
+  r = __fadd_rn(r, a.lo);
+  r = __fmaf_rn(-q1, b.lo, r);
+  return ff_fast_sum(q1, __fdiv_rn(r, b.hi));
+}
+
 __device__ __forceinline__ uint32_t lanemask_lt() {
   uint32_t m;
   asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));

@@ -119,7 +119,7 @@ __device__ __forceinline__ float3 sh_colour(int D, float x, float y, float z, co
   return f3(fmaxf(r.x, 0.0f), fmaxf(r.y, 0.0f), fmaxf(r.z, 0.0f));
 }
 
-__global__ void __launch_bounds__(kPreThreads) k_preprocess(const PreArgs a) {
+__global__ void __launch_bounds__(kPreThreads, 3) k_preprocess(const PreArgs a) {
   __shared__ float2 s_xy[kPreWarps][kWarp];
   __shared__ float4 s_cp[kPreWarps][kWarp];    // conic a, b, c, power
   __shared__ int4 s_geo[kPreWarps][kWarp];     // rect min x, min y, width, candidate start
@@ -128,8 +128,12 @@ __global__ void __launch_bounds__(kPreThreads) k_preprocess(const PreArgs a) {
   __shared__ uint32_t s_val[kPreWarps][kStage];
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int i = blockIdx.x * kPreThreads + threadIdx.x;
-  const int vi = blockIdx.y;
+  // Block b covers Gaussians [(b / V) * 256, +256) of view b % V: the views of
+  // one Gaussian chunk run back to back, so its parameters come from L2 after
+  // the first view instead of being re-read from HBM per view.
+  const int vi = (int)(blockIdx.x % (unsigned)a.views.V);
+  const int chunk = (int)(blockIdx.x / (unsigned)a.views.V);
+  const int i = chunk * kPreThreads + threadIdx.x;
   const ViewDesc& cam = a.views.v[vi];
   const int bx = a.views.bx, by = a.views.by;
   const size_t rbase = (size_t)vi * a.P;  // first record of this view
@@ -153,22 +157,29 @@ __global__ void __launch_bounds__(kPreThreads) k_preprocess(const PreArgs a) {
       if (t.z <= 0.2f) break;                        // near cull (FB preprocess.cu:456)
       const float o = a.opac[i];
       if (255.0f * o < 1.0f) break;                  // opacity cull (FB preprocess.cu:459)
-      // Projection to pixels in FP64.  FB projects in FP32 and converts NDC to
-      // pixels in double (preprocess.cu:463-465, 494); an FP32 pixel position
-      // near 1000 px is only good to 6e-5 px, which would dominate the image
-      // error, so the position is formed here in FP64 and its fraction kept.
+      // Projection to pixels in float-float.  FB projects in FP32 and converts
+      // NDC to pixels in double (preprocess.cu:463-465, 494); an FP32 pixel
+      // position near 1000 px is only good to 6e-5 px, which would dominate
+      // the image error, so the homogeneous coordinates are summed from exact
+      // products, divided and scaled in float-float (the value FP64 gives, to
+      // ~1e-12 relative) and the position's fraction is kept.
       const float* Pm = cam.proj;
-      const double px = p.x, py = p.y, pz = p.z;
       auto row = [&](int r) {
-        return __fma_rn((double)Pm[r], px, __fma_rn((double)Pm[4 + r], py, __fma_rn((double)Pm[8 + r], pz, (double)Pm[12 + r])));
+        ff acc = ff_prod(Pm[r], p.x);
+        acc = ff_add(acc, ff_prod(Pm[4 + r], p.y));
+        acc = ff_add(acc, ff_prod(Pm[8 + r], p.z));
+        return ff_add_f(acc, Pm[12 + r]);
       };
-      const double hx = row(0), hy = row(1), hw = row(3);
-      const double wden = hw + 1e-7;
-      // 1/wden: FP32 seed refined by one Newton step (relative error ~1e-14).
-      double rw = (double)(1.0f / (float)wden);
-      rw = rw * __fma_rn(-wden, rw, 2.0);
-      const double X = __fma_rn(hx * rw + 1.0, (double)cam.W, -1.0) * 0.5;
-      const double Y = __fma_rn(hy * rw + 1.0, (double)cam.H, -1.0) * 0.5;
+      const ff hx = row(0), hy = row(1), hw = row(3);
+      constexpr float kEpsHi = 1e-7f;
+      constexpr float kEpsLo = (float)(1e-7 - (double)kEpsHi);
+      const ff wden = ff_add(hw, ff{kEpsHi, kEpsLo});  // p_w + 1e-7 (FB preprocess.cu:464)
+      auto to_px = [&](ff h, int n) {  // ((h / w + 1) * n - 1) / 2
+        ff t = ff_add_f(ff_div(h, wden), 1.0f);
+        t = ff_add_f(ff_mul_f(t, (float)n), -1.0f);
+        return ff{0.5f * t.hi, 0.5f * t.lo};
+      };
+      const ff X = to_px(hx, cam.W), Y = to_px(hy, cam.H);
 
       // 3D covariance R diag(s^2) R^T from the raw quaternion (FB preprocess.cu:364-400).
       const float4 q = *reinterpret_cast<const float4*>(a.rots + 4 * (size_t)i);
@@ -218,7 +229,7 @@ __global__ void __launch_bounds__(kPreThreads) k_preprocess(const PreArgs a) {
       const float power = (kLn2 * 8.0f + kLn2 * log2o) * cam.mult;
       const int wpx = (int)(1.414214f * sqrt_approx(ca * power) + 1.0f);
       const int hpx = (int)(1.414214f * sqrt_approx(cc * power) + 1.0f);
-      xy = make_float2((float)X, (float)Y);
+      xy = make_float2(X.hi, Y.hi);
       rmin.x = min(cam.gx, max(0, (int)((xy.x - wpx) / (float)bx)));
       rmin.y = min(cam.gy, max(0, (int)((xy.y - hpx) / (float)by)));
       rmax.x = min(cam.gx, max(0, (int)((xy.x + wpx) / (float)bx) + 1));
@@ -249,8 +260,9 @@ __global__ void __launch_bounds__(kPreThreads) k_preprocess(const PreArgs a) {
       rec[F_CHOL + 1] = -cb / cc;
       rec[F_CHOL + 2] = (-0.5f * kLog2e) / cc;
       rec[F_LOG2O] = log2o;
-      rec[F_FRAC] = (float)(X - (double)floorf(xy.x));
-      rec[F_FRAC + 1] = (float)(Y - (double)floorf(xy.y));
+      // X - floor(X.hi): the first difference is exact (a fraction of X.hi)
+      rec[F_FRAC] = __fadd_rn(__fsub_rn(X.hi, floorf(X.hi)), X.lo);
+      rec[F_FRAC + 1] = __fadd_rn(__fsub_rn(Y.hi, floorf(Y.hi)), Y.lo);
       rec[F_RMIN] = __int_as_float(rmin.x); rec[F_RMIN + 1] = __int_as_float(rmin.y);
       rec[F_RMAX] = __int_as_float(rmax.x); rec[F_RMAX + 1] = __int_as_float(rmax.y);
       rec[F_CONIC] = conic.x; rec[F_CONIC + 1] = conic.y; rec[F_CONIC + 2] = conic.z;
@@ -302,7 +314,7 @@ __global__ void __launch_bounds__(kPreThreads) k_preprocess(const PreArgs a) {
   __syncwarp();
 
   WarpStage st{s_key[warp], s_val[warp], 0};
-  const int warp_first = blockIdx.x * kPreThreads + warp * kWarp;
+  const int warp_first = chunk * kPreThreads + warp * kWarp;
   for (int base = 0; base < total; base += kWarp) {
     const int c = base + lane;
     bool hit = false;
@@ -379,7 +391,8 @@ fgs_status run_preprocess(PreArgs& a, cudaStream_t s) {
   FGS_TRY(cudaMemsetAsync(a.counters, 0, FGS_COUNTER_WORDS * sizeof(int32_t), s));
   {
     KernelTimer kt__(FGS_K_PREPROCESS, s);
-    k_preprocess<<<dim3((a.P + kPreThreads - 1) / kPreThreads, a.views.V), kPreThreads, 0, s>>>(a);
+    const unsigned blocks = (unsigned)((a.P + kPreThreads - 1) / kPreThreads) * (unsigned)a.views.V;
+    k_preprocess<<<blocks, kPreThreads, 0, s>>>(a);
     kt__.stop();
   }
   FGS_LAUNCH_CHECK();

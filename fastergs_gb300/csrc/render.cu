@@ -50,16 +50,23 @@ __global__ void __launch_bounds__(256) k_tile_ranges(const unsigned long long* _
 // One CTA: bucket counts per tile, inclusive scan, bucket -> tile map.
 // FB does this with perTileBucketCount + cub::DeviceScan + a host copy of the
 // total + perBucketRange (render.cu:13-49, 418-434).
-__global__ void __launch_bounds__(1024) k_bucket_setup(int T, const uint32_t* __restrict__ ranges, int bs,
-                                                       long long max_buckets, uint32_t* __restrict__ bucket_off,
-                                                       uint32_t* __restrict__ bucket_tile, uint32_t* bucket_sum) {
-  __shared__ uint32_t s_warp[32];
+// Bucket bookkeeping (FB render.cu:418-433 counts buckets per tile, scans them
+// with CUB and copies the total to the host): per tile ceil(n / bs) buckets, their
+// inclusive offsets, and the owning tile of every bucket.  Two launches, no
+// host read: k_bucket_count scans 1024 tiles per block, k_bucket_fill adds
+// the preceding blocks' totals and writes the bucket -> tile table.
+__device__ __forceinline__ uint32_t tile_buckets(const uint32_t* __restrict__ ranges, int t, int bs) {
+  return (ranges[2 * t + 1] - ranges[2 * t] + (uint32_t)bs - 1) / (uint32_t)bs;
+}
+
+__global__ void __launch_bounds__(kScanTiles) k_bucket_count(int T, const uint32_t* __restrict__ ranges, int bs,
+                                                             uint32_t* __restrict__ bucket_off,
+                                                             uint32_t* __restrict__ block_sums) {
+  __shared__ uint32_t s_warp[kScanTiles / 32];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int chunk = (T + 1023) / 1024;
-  const int t0 = min(T, tid * chunk), t1 = min(T, t0 + chunk);
-  uint32_t local = 0;
-  for (int t = t0; t < t1; ++t) local += (ranges[2 * t + 1] - ranges[2 * t] + bs - 1) / bs;
-  uint32_t incl = local;
+  const int t = blockIdx.x * kScanTiles + tid;
+  const uint32_t nb = t < T ? tile_buckets(ranges, t, bs) : 0u;
+  uint32_t incl = nb;
 #pragma unroll
   for (int o = 1; o < 32; o <<= 1) {
     const uint32_t u = __shfl_up_sync(0xffffffffu, incl, o);
@@ -67,26 +74,52 @@ __global__ void __launch_bounds__(1024) k_bucket_setup(int T, const uint32_t* __
   }
   if (lane == 31) s_warp[warp] = incl;
   __syncthreads();
-  uint32_t wbase = 0, total = 0;
-  for (int w = 0; w < 32; ++w) {
-    const uint32_t x = s_warp[w];
-    if (w < warp) wbase += x;
-    total += x;
+  if (warp == 0) {
+    uint32_t w = s_warp[lane];
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t u = __shfl_up_sync(0xffffffffu, w, o);
+      if (lane >= o) w += u;
+    }
+    s_warp[lane] = w;  // inclusive over warps
   }
-  uint32_t run = wbase + incl - local;
-  for (int t = t0; t < t1; ++t) {
-    const uint32_t nb = (ranges[2 * t + 1] - ranges[2 * t] + bs - 1) / bs;
-    for (uint32_t j = 0; j < nb; ++j)
-      if ((long long)(run + j) < max_buckets) bucket_tile[run + j] = (uint32_t)t;
-    run += nb;
-    bucket_off[t] = run;
+  __syncthreads();
+  incl += warp ? s_warp[warp - 1] : 0u;
+  if (t < T) bucket_off[t] = incl;
+  if (tid == kScanTiles - 1) block_sums[blockIdx.x] = incl;
+}
+
+__global__ void __launch_bounds__(kScanTiles) k_bucket_fill(int T, const uint32_t* __restrict__ ranges, int bs,
+                                                            long long max_buckets, uint32_t* __restrict__ bucket_off,
+                                                            const uint32_t* __restrict__ block_sums,
+                                                            uint32_t* __restrict__ bucket_tile,
+                                                            uint32_t* bucket_sum) {
+  __shared__ uint32_t s_base;
+  const int tid = threadIdx.x;
+  if (tid < 32) {
+    uint32_t acc = 0;
+    for (int j = tid; j < (int)blockIdx.x; j += 32) acc += block_sums[j];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (tid == 0) {
+      s_base = acc;
+      if (blockIdx.x == gridDim.x - 1) {
+        const uint32_t total = acc + block_sums[blockIdx.x];
+        bucket_sum[0] = (uint32_t)min((long long)total, max_buckets);
+        bucket_sum[1] = total;
+        bucket_sum[2] = 0;  // forward work cursor
+        if ((long long)total > max_buckets) raise_error(kErrCapacity);
+      }
+    }
   }
-  if (tid == 0) {
-    bucket_sum[0] = (uint32_t)min((long long)total, max_buckets);
-    bucket_sum[1] = total;
-    bucket_sum[2] = 0;  // forward work cursor
-    if ((long long)total > max_buckets) raise_error(kErrCapacity);
-  }
+  __syncthreads();
+  const int t = blockIdx.x * kScanTiles + tid;
+  if (t >= T) return;
+  const uint32_t nb = tile_buckets(ranges, t, bs);
+  const uint32_t end = bucket_off[t] + s_base;
+  bucket_off[t] = end;
+  for (uint32_t j = end - nb; j < end; ++j)
+    if ((long long)j < max_buckets) bucket_tile[j] = (uint32_t)t;
 }
 
 struct FwdArgs {
@@ -265,8 +298,11 @@ fgs_status run_render_fwd(const Views& views, int64_t n_cap, const int32_t* n_de
   if (st != FGS_OK) return st;
   {
     KernelTimer kt__(FGS_K_BUCKET_SETUP, s);
-    k_bucket_setup<<<1, 1024, 0, s>>>((int)views.tiles, ranges, bucket_size, max_buckets, im.bucket_off,
-                                      sm.bucket_tile, im.bucket_sum);
+    const unsigned nblk = (views.tiles + kScanTiles - 1) / kScanTiles;
+    k_bucket_count<<<nblk, kScanTiles, 0, s>>>((int)views.tiles, ranges, bucket_size, im.bucket_off,
+                                               im.block_sums);
+    k_bucket_fill<<<nblk, kScanTiles, 0, s>>>((int)views.tiles, ranges, bucket_size, max_buckets, im.bucket_off,
+                                              im.block_sums, sm.bucket_tile, im.bucket_sum);
     kt__.stop();
   }
   FGS_LAUNCH_CHECK();

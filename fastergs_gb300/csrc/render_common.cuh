@@ -21,8 +21,10 @@ struct ImageState {
   uint32_t* max_contrib;    // T
   uint32_t* bucket_off;     // T (inclusive scan of bucket counts)
   uint32_t* bucket_sum;     // [0] buckets (capped), [1] buckets (uncapped), [2], [3] work cursors
+  uint32_t* block_sums;     // ceil(T / kScanTiles) bucket totals of the bucket-setup scan blocks
   size_t bytes;
 };
+constexpr int kScanTiles = 1024;  // tiles per bucket-setup scan block
 
 // Per-bucket state (FB SampleState, rasterizer_imp.h:91-102): the owning tile
 // of each bucket and, per (bucket, pixel), a float4 (C.rgb, T).  The forward
@@ -46,6 +48,8 @@ inline ImageState carve_image(void* base, size_t pixels, size_t T) {
   s.pix_color = reinterpret_cast<float*>(p + off);      off = align_up(off + sizeof(float) * 3 * pixels, 256);
   s.max_contrib = reinterpret_cast<uint32_t*>(p + off); off = align_up(off + sizeof(uint32_t) * (size_t)T, 256);
   s.bucket_off = reinterpret_cast<uint32_t*>(p + off);  off = align_up(off + sizeof(uint32_t) * (size_t)T, 256);
+  s.block_sums = reinterpret_cast<uint32_t*>(p + off);
+  off = align_up(off + sizeof(uint32_t) * ((size_t)T + kScanTiles - 1) / kScanTiles, 256);
   s.bytes = off;
   return s;
 }
