@@ -419,10 +419,10 @@ def roofline(res, peaks):
         "preprocess": P * (56 + 4 * sh_floats) + P * 44 + 12 * K,
         "sort_pass": 24 * K,
         "sort_hist": 8 * K,
+        # composite: records of every pair, plus the folded prefix written once per bucket
         "render_fwd": 40 * K + 16 * 256 * math.ceil(K / 128),
         "render_bwd": 40 * K + 16 * 256 * math.ceil(K / 128) + 48 * K,
         "preprocess_bwd": P * (56 + 4 * sh_floats + 48) + P * (56 + 4 * sh_floats),
-        "merge": 32 * 256 * math.ceil(K / 128),
         "tile_ranges": 8 * K,
     }
     dom = max(steps_ms, key=lambda k: steps_ms[k])

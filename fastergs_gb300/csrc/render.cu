@@ -9,12 +9,21 @@
 //   * bucket bookkeeping never leaves the device (FB copies the bucket total
 //     to the host mid-frame); the composite kernel is persistent and reads the
 //     total from device memory;
+//   * the merge is fused into the composite as a per-tile chain: a warp that
+//     finishes bucket k of a tile folds it into the tile's running prefix as
+//     soon as bucket k-1 has been folded (the same operations, in the same
+//     order, as FB's merge), and publishes which pixels are still above the
+//     1e-4 cut-off.  Buckets are handed out round by round (every tile's
+//     bucket 0, then every tile's bucket 1, ...), so when a warp starts a
+//     bucket the tile's earlier buckets are usually folded already, and the
+//     8x4 sub-blocks whose pixels have all stopped are skipped: FB composites
+//     them and the merge discards them;
 //   * a bucket's records are staged once into shared memory (coalesced
 //     per-lane loads, structure-of-arrays) and broadcast from there;
 //   * each lane owns a column strip of 8 pixels, so a Gaussian's row terms are
 //     shared and every sample store is a contiguous 512-byte warp store;
-//   * the sample state is 16 bytes per pixel and bucket, updated in place by
-//     the merge (FB keeps 40).
+//   * the sample state is 16 bytes per pixel and bucket and holds the prefix
+//     after the bucket (FB keeps 40).
 #include <algorithm>
 
 #include "render_common.cuh"
@@ -47,79 +56,153 @@ __global__ void __launch_bounds__(256) k_tile_ranges(const unsigned long long* _
   if (i == n - 1) ranges[2 * t + 1] = (uint32_t)n;
 }
 
-// One CTA: bucket counts per tile, inclusive scan, bucket -> tile map.
-// FB does this with perTileBucketCount + cub::DeviceScan + a host copy of the
-// total + perBucketRange (render.cu:13-49, 418-434).
 // Bucket bookkeeping (FB render.cu:418-433 counts buckets per tile, scans them
-// with CUB and copies the total to the host): per tile ceil(n / bs) buckets, their
-// inclusive offsets, and the owning tile of every bucket.  Two launches, no
-// host read: k_bucket_count scans 1024 tiles per block, k_bucket_fill adds
-// the preceding blocks' totals and writes the bucket -> tile table.
+// with CUB and copies the total to the host), plus the forward work queue.
+// Per tile: nb = ceil(n / bs) buckets, their inclusive offsets and the
+// bucket -> tile map.  Queue order: round k < kRounds holds bucket k of every
+// tile that has one, in tile order; buckets k >= kRounds follow, tile after
+// tile.  A tile's bucket k therefore always comes after its bucket k-1,
+// which is what the composite's per-tile chain waits on.  Both kernels scan
+// kScanValues per tile: [nb > 0], ..., [nb > kRounds-1], max(nb - kRounds, 0), nb.
 __device__ __forceinline__ uint32_t tile_buckets(const uint32_t* __restrict__ ranges, int t, int bs) {
   return (ranges[2 * t + 1] - ranges[2 * t] + (uint32_t)bs - 1) / (uint32_t)bs;
 }
 
-__global__ void __launch_bounds__(kScanTiles) k_bucket_count(int T, const uint32_t* __restrict__ ranges, int bs,
-                                                             uint32_t* __restrict__ bucket_off,
-                                                             uint32_t* __restrict__ block_sums) {
-  __shared__ uint32_t s_warp[kScanTiles / 32];
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int t = blockIdx.x * kScanTiles + tid;
-  const uint32_t nb = t < T ? tile_buckets(ranges, t, bs) : 0u;
-  uint32_t incl = nb;
+__device__ __forceinline__ void scan_values(uint32_t nb, uint32_t (&v)[kScanValues]) {
 #pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    const uint32_t u = __shfl_up_sync(0xffffffffu, incl, o);
-    if (lane >= o) incl += u;
-  }
-  if (lane == 31) s_warp[warp] = incl;
-  __syncthreads();
-  if (warp == 0) {
-    uint32_t w = s_warp[lane];
+  for (int j = 0; j < kRounds; ++j) v[j] = nb > (uint32_t)j ? 1u : 0u;
+  v[kRounds] = nb > (uint32_t)kRounds ? nb - kRounds : 0u;
+  v[kRounds + 1] = nb;
+}
+
+// Inclusive block scan (kScanTiles threads) of every value; tot = block totals.
+__device__ __forceinline__ void block_scan(uint32_t (&v)[kScanValues], uint32_t (&tot)[kScanValues],
+                                           uint32_t (*s_warp)[kScanValues]) {
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+#pragma unroll
+  for (int j = 0; j < kScanValues; ++j) {
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
-      const uint32_t u = __shfl_up_sync(0xffffffffu, w, o);
-      if (lane >= o) w += u;
+      const uint32_t u = __shfl_up_sync(0xffffffffu, v[j], o);
+      if (lane >= o) v[j] += u;
     }
-    s_warp[lane] = w;  // inclusive over warps
+    if (lane == 31) s_warp[warp][j] = v[j];
   }
   __syncthreads();
-  incl += warp ? s_warp[warp - 1] : 0u;
-  if (t < T) bucket_off[t] = incl;
-  if (tid == kScanTiles - 1) block_sums[blockIdx.x] = incl;
+  if (warp == 0) {
+#pragma unroll
+    for (int j = 0; j < kScanValues; ++j) {
+      uint32_t w = s_warp[lane][j];
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t u = __shfl_up_sync(0xffffffffu, w, o);
+        if (lane >= o) w += u;
+      }
+      s_warp[lane][j] = w;  // inclusive over warps
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int j = 0; j < kScanValues; ++j) {
+    v[j] += warp ? s_warp[warp - 1][j] : 0u;
+    tot[j] = s_warp[kScanTiles / 32 - 1][j];
+  }
+}
+
+__global__ void __launch_bounds__(kScanTiles) k_bucket_count(int T, const uint32_t* __restrict__ ranges, int bs,
+                                                             uint32_t* __restrict__ block_sums) {
+  __shared__ uint32_t s_warp[kScanTiles / 32][kScanValues];
+  const int t = blockIdx.x * kScanTiles + threadIdx.x;
+  uint32_t v[kScanValues], tot[kScanValues];
+  scan_values(t < T ? tile_buckets(ranges, t, bs) : 0u, v);
+  block_scan(v, tot, s_warp);
+  if (threadIdx.x < kScanValues) {
+#pragma unroll
+    for (int j = 0; j < kScanValues; ++j)
+      if ((int)threadIdx.x == j) block_sums[(size_t)blockIdx.x * kScanValues + j] = tot[j];
+  }
 }
 
 __global__ void __launch_bounds__(kScanTiles) k_bucket_fill(int T, const uint32_t* __restrict__ ranges, int bs,
-                                                            long long max_buckets, uint32_t* __restrict__ bucket_off,
-                                                            const uint32_t* __restrict__ block_sums,
+                                                            long long max_buckets, const uint32_t* __restrict__ block_sums,
+                                                            uint32_t* __restrict__ bucket_off,
                                                             uint32_t* __restrict__ bucket_tile,
-                                                            uint32_t* bucket_sum) {
-  __shared__ uint32_t s_base;
-  const int tid = threadIdx.x;
-  if (tid < 32) {
-    uint32_t acc = 0;
-    for (int j = tid; j < (int)blockIdx.x; j += 32) acc += block_sums[j];
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-    if (tid == 0) {
-      s_base = acc;
-      if (blockIdx.x == gridDim.x - 1) {
-        const uint32_t total = acc + block_sums[blockIdx.x];
-        bucket_sum[0] = (uint32_t)min((long long)total, max_buckets);
-        bucket_sum[1] = total;
-        bucket_sum[2] = 0;  // forward work cursor
-        if ((long long)total > max_buckets) raise_error(kErrCapacity);
-      }
+                                                            uint32_t* __restrict__ bucket_queue,
+                                                            uint32_t* __restrict__ tile_stage, uint32_t* bucket_sum) {
+  __shared__ uint32_t s_warp[kScanTiles / 32][kScanValues];
+  __shared__ uint32_t s_base[kScanValues], s_total[kScanValues];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  if (warp < kScanValues) {  // totals of the preceding blocks and of all blocks, one value per warp
+    uint32_t before = 0, all = 0;
+    for (int i = lane; i < (int)gridDim.x; i += 32) {
+      const uint32_t x = block_sums[(size_t)i * kScanValues + warp];
+      all += x;
+      if (i < (int)blockIdx.x) before += x;
     }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      before += __shfl_xor_sync(0xffffffffu, before, o);
+      all += __shfl_xor_sync(0xffffffffu, all, o);
+    }
+    if (lane == 0) { s_base[warp] = before; s_total[warp] = all; }
   }
-  __syncthreads();
   const int t = blockIdx.x * kScanTiles + tid;
+  const uint32_t nb = t < T ? tile_buckets(ranges, t, bs) : 0u;
+  uint32_t v[kScanValues], tot[kScanValues];
+  scan_values(nb, v);
+  block_scan(v, tot, s_warp);  // its barriers also publish s_base / s_total
+  const uint32_t total = s_total[kRounds + 1];
+  const bool overflow = (long long)total > max_buckets;
+  if (blockIdx.x == 0 && tid == 0) {
+    bucket_sum[0] = overflow ? 0u : total;  // nothing is composited when the samples do not fit
+    bucket_sum[1] = total;
+    bucket_sum[2] = 0;  // forward work cursor
+    if (overflow) raise_error(kErrCapacity);
+  }
   if (t >= T) return;
-  const uint32_t nb = tile_buckets(ranges, t, bs);
-  const uint32_t end = bucket_off[t] + s_base;
+  tile_stage[t] = 0;
+  const uint32_t end = s_base[kRounds + 1] + v[kRounds + 1];
   bucket_off[t] = end;
-  for (uint32_t j = end - nb; j < end; ++j)
-    if ((long long)j < max_buckets) bucket_tile[j] = (uint32_t)t;
+  if (overflow) return;
+  const uint32_t b0 = end - nb;
+  uint32_t round_off = 0;
+#pragma unroll
+  for (int k = 0; k < kRounds; ++k) {
+    if ((uint32_t)k < nb) {
+      bucket_queue[round_off + s_base[k] + v[k] - 1] = b0 + k;  // exclusive rank = inclusive - 1
+    }
+    round_off += s_total[k];
+  }
+  const uint32_t tail = round_off + s_base[kRounds] + v[kRounds] - (nb > kRounds ? nb - kRounds : 0u);
+  for (uint32_t k = kRounds; k < nb; ++k) bucket_queue[tail + (k - kRounds)] = b0 + k;
+  for (uint32_t j = 0; j < nb; ++j) bucket_tile[b0 + j] = (uint32_t)t;
+}
+
+// Tiles without buckets (and every tile when the buckets did not fit): the
+// merge's output for an empty list, background with T = 1.
+__global__ void __launch_bounds__(kTilePixels) k_empty_tiles(const Views views, const uint32_t* __restrict__ ranges,
+                                                             const uint32_t* bucket_sum, float* __restrict__ out_color,
+                                                             float* __restrict__ pix_color,
+                                                             int* __restrict__ last_contrib,
+                                                             float* __restrict__ Ts_final,
+                                                             uint32_t* __restrict__ max_contrib) {
+  const int tile = blockIdx.x, p = threadIdx.x;
+  if (ranges[2 * tile + 1] > ranges[2 * tile] && bucket_sum[0] != 0) return;
+  const ViewDesc& cam = views.v[views.of_tile((uint32_t)tile)];
+  const int lt = tile - (int)cam.tile_off, bx = views.bx, by = views.by;
+  const int px = (lt % cam.gx) * bx + p % bx, py = (lt / cam.gx) * by + p / bx;
+  if (p == 0) max_contrib[tile] = 0;
+  if (px >= cam.W || py >= cam.H) return;
+  const size_t HW = (size_t)cam.W * cam.H, pix = (size_t)py * cam.W + px;
+  float* oc = out_color + 3 * (size_t)cam.pix_off;
+  float* pc = pix_color + 3 * (size_t)cam.pix_off;
+#pragma unroll
+  for (int ch = 0; ch < 3; ++ch) {
+    oc[ch * HW + pix] = cam.bg[ch];
+    pc[ch * HW + pix] = 0.f;
+  }
+  last_contrib[cam.pix_off + pix] = 0;
+  Ts_final[cam.pix_off + pix] = 1.f;
 }
 
 struct FwdArgs {
@@ -128,11 +211,38 @@ struct FwdArgs {
   const uint32_t* vals;
   const uint32_t* ranges;
   const uint32_t* bucket_tile;
+  const uint32_t* bucket_queue;
   const uint32_t* bucket_off;
   uint32_t* bucket_sum;
   float4* samples;
+  uint32_t* tile_stage;
+  uint32_t* tile_alive;
+  float* out_color;     // per view (3, H, W), view k at 3 * pix_off
+  float* pix_color;     // same layout, without background
+  int* last_contrib;    // per view (H, W), view k at pix_off
+  float* Ts_final;
+  uint32_t* max_contrib;
   int bs;
 };
+
+// Waits until the tile's first `stage` buckets are folded into its prefix.
+// Lane 0 polls (bounded); the bucket it waits for was handed out earlier and
+// its warp is running, so the wait ends unless something is broken, in which
+// case the timeout bit is raised and the warp carries on.
+__device__ __forceinline__ void wait_stage(const uint32_t* tile_stage, uint32_t stage, int lane) {
+  if (lane == 0) {
+    int spins = 0;
+    while (ld_acquire_u32(tile_stage) < stage) {
+      if (++spins > kSpinLimit) {
+        raise_error(kErrTimeout);
+        break;
+      }
+      if (spins > 64) __nanosleep(128);
+    }
+  }
+  __syncwarp();
+  (void)ld_acquire_u32(tile_stage);  // every lane acquires the folded prefix
+}
 
 template <int BX>
 __global__ void __launch_bounds__(kFwdWarps * kWarp, 8) k_render_fwd(const FwdArgs a) {
@@ -142,134 +252,133 @@ __global__ void __launch_bounds__(kFwdWarps * kWarp, 8) k_render_fwd(const FwdAr
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   BucketStage& st = s_stage[warp];
   const int B = (int)a.bucket_sum[0];
-  for (int b = next_bucket(a.bucket_sum + 2, lane); b < B;) {
-    const int b_next = next_bucket(a.bucket_sum + 2, lane);
+  for (int q = next_bucket(a.bucket_sum + 2, lane); q < B;) {
+    const int q_next = next_bucket(a.bucket_sum + 2, lane);
+    const int b = (int)a.bucket_queue[q];
     const BucketInfo bi = bucket_info(b, a.bucket_tile, a.bucket_off, a.ranges, a.bs);
     const ViewDesc& cam = a.views.v[a.views.of_tile((uint32_t)bi.tile)];
     const int lt = bi.tile - (int)cam.tile_off;  // tile index inside its view
     const int tx0 = (lt % cam.gx) * BX, ty0 = (lt / cam.gx) * BY;
-    stage_bucket<BX>(st, a.splat, a.vals + bi.start, bi.n, lane, tx0, ty0);
-    float pxc[M::kCols], pyr[M::kRows];
-#pragma unroll
-    for (int c = 0; c < M::kCols; ++c) pxc[c] = (float)(tx0 + 8 * c + (lane & 7));
-#pragma unroll
-    for (int r = 0; r < M::kRows; ++r) pyr[r] = (float)(ty0 + 4 * r + (lane >> 3));
+    uint32_t* stage_word = a.tile_stage + bi.tile;
+    uint32_t* alive_words = a.tile_alive + (size_t)bi.tile * kPxPerThread;
+
+    // Sub-blocks that may still need this bucket: from whatever prefix state
+    // the tile has published so far (a superset of the state after bucket k-1).
+    uint32_t spec = (1u << kPxPerThread) - 1u;
+    if (bi.local > 0) {
+      uint32_t w = 0u;
+      if (lane < kPxPerThread) w = ld_acquire_u32(stage_word) > 0 ? ld_volatile_u32(alive_words + lane) : ~0u;
+      spec = __ballot_sync(0xffffffffu, w != 0u);
+    }
+
     float T[kPxPerThread], Cr[kPxPerThread], Cg[kPxPerThread], Cb[kPxPerThread];
 #pragma unroll
     for (int k = 0; k < kPxPerThread; ++k) { T[k] = 1.f; Cr[k] = 0.f; Cg[k] = 0.f; Cb[k] = 0.f; }
-    for (int g = 0; g < bi.n; ++g) {
-      const uint32_t mask = st.mask[g];
-      if (mask == 0) continue;  // alpha < 1/256 on the whole tile
-      const float4 pos = st.pos[g];
-      const float4 q = st.quad[g];   // A1, P, C1, log2 o
-      const float4 c = st.rgb[g];
-      float dx[M::kCols];
+    if (spec != 0u) {
+      stage_bucket<BX>(st, a.splat, a.vals + bi.start, bi.n, lane, tx0, ty0);
+      float pxc[M::kCols], pyr[M::kRows];
 #pragma unroll
-      for (int cc = 0; cc < M::kCols; ++cc) dx[cc] = centre_offset(pos.x, pos.z, pxc[cc]);
+      for (int c = 0; c < M::kCols; ++c) pxc[c] = (float)(tx0 + 8 * c + (lane & 7));
 #pragma unroll
-      for (int r = 0; r < M::kRows; ++r) {
-        const uint32_t rm = (mask >> (r * M::kCols)) & ((1u << M::kCols) - 1u);
-        if (rm == 0) continue;
-        const float dy = centre_offset(pos.y, pos.w, pyr[r]);
-        const float f = fmaf(q.z * dy, dy, q.w);  // log2 o + C1 dy^2
+      for (int r = 0; r < M::kRows; ++r) pyr[r] = (float)(ty0 + 4 * r + (lane >> 3));
+      for (int g = 0; g < bi.n; ++g) {
+        const uint32_t mask = st.mask[g] & spec;
+        if (mask == 0) continue;  // alpha < 1/256 on every live sub-block
+        const float4 pos = st.pos[g];
+        const float4 q4 = st.quad[g];   // A1, P, C1, log2 o
+        const float4 c = st.rgb[g];
+        float dx[M::kCols];
 #pragma unroll
-        for (int cc = 0; cc < M::kCols; ++cc) {
-          if (!((rm >> cc) & 1u)) continue;
-          const int k = r * M::kCols + cc;
-          // alpha = o * exp(-q/2) = 2^(log2 o + A1 (dx + P dy)^2 + C1 dy^2)
-          const float w = fmaf(q.y, dy, dx[cc]);
-          const float e = fmaf(q.x * w, w, f);
-          float al = fminf(kAlphaMax, ex2_approx(e));
-          al = al < kAlphaCut ? 0.f : al;
-          const float wt = al * T[k];
-          Cr[k] = fmaf(c.x, wt, Cr[k]);
-          Cg[k] = fmaf(c.y, wt, Cg[k]);
-          Cb[k] = fmaf(c.z, wt, Cb[k]);
-          T[k] = fmaf(-al, T[k], T[k]);  // T (1 - alpha), rounded once
+        for (int cc = 0; cc < M::kCols; ++cc) dx[cc] = centre_offset(pos.x, pos.z, pxc[cc]);
+#pragma unroll
+        for (int r = 0; r < M::kRows; ++r) {
+          const uint32_t rm = (mask >> (r * M::kCols)) & ((1u << M::kCols) - 1u);
+          if (rm == 0) continue;
+          const float dy = centre_offset(pos.y, pos.w, pyr[r]);
+          const float f = fmaf(q4.z * dy, dy, q4.w);  // log2 o + C1 dy^2
+#pragma unroll
+          for (int cc = 0; cc < M::kCols; ++cc) {
+            if (!((rm >> cc) & 1u)) continue;
+            const int k = r * M::kCols + cc;
+            // alpha = o * exp(-q/2) = 2^(log2 o + A1 (dx + P dy)^2 + C1 dy^2)
+            const float w = fmaf(q4.y, dy, dx[cc]);
+            const float e = fmaf(q4.x * w, w, f);
+            float al = fminf(kAlphaMax, ex2_approx(e));
+            al = al < kAlphaCut ? 0.f : al;
+            const float wt = al * T[k];
+            Cr[k] = fmaf(c.x, wt, Cr[k]);
+            Cg[k] = fmaf(c.y, wt, Cg[k]);
+            Cb[k] = fmaf(c.z, wt, Cb[k]);
+            T[k] = fmaf(-al, T[k], T[k]);  // T (1 - alpha), rounded once
+          }
         }
       }
+      __syncwarp();
     }
-    __syncwarp();
+
+    // Fold into the tile's prefix (FB's merge, render.cu:285-391, per pixel
+    // and in bucket order): C += T_prefix * C_b, T_prefix *= T_b; a pixel
+    // stops after the bucket that takes T below 1e-4, or at the tile's last
+    // bucket, and then writes its outputs.
+    if (bi.local > 0) wait_stage(stage_word, (uint32_t)bi.local, lane);
+    const int nb_tile = (int)a.bucket_off[bi.tile] - (bi.tile ? (int)a.bucket_off[bi.tile - 1] : 0);
+    const bool last_bucket = bi.local == nb_tile - 1;
+    const int ntile = (int)(a.ranges[2 * bi.tile + 1] - a.ranges[2 * bi.tile]);
+    const int contrib = min(ntile, (bi.local + 1) * a.bs);
+    const uint32_t prev_w = (bi.local > 0 && lane < kPxPerThread) ? ld_volatile_u32(alive_words + lane) : 0u;
+    const size_t HW = (size_t)cam.W * cam.H;
     float4* out = a.samples + (size_t)b * kTilePixels;
+    const float4* prev = a.samples + (size_t)(b - 1) * kTilePixels;
+    bool any_before = false, any_after = false;
+    uint32_t my_word = 0;
 #pragma unroll
     for (int r = 0; r < M::kRows; ++r)
 #pragma unroll
       for (int cc = 0; cc < M::kCols; ++cc) {
         const int k = r * M::kCols + cc;
-        out[M::pix(r, cc, lane)] = make_float4(Cr[k], Cg[k], Cb[k], T[k]);
+        const int p = M::pix(r, cc, lane);
+        const int px = tx0 + 8 * cc + (lane & 7), py = ty0 + 4 * r + (lane >> 3);
+        bool alive;
+        if (bi.local == 0) {
+          alive = px < cam.W && py < cam.H;
+        } else {
+          alive = (__shfl_sync(0xffffffffu, prev_w, k) >> lane) & 1u;
+        }
+        any_before |= __any_sync(0xffffffffu, alive);
+        if (alive) {
+          const float4 pre = bi.local > 0 ? __ldcg(prev + p) : make_float4(0.f, 0.f, 0.f, 1.f);
+          const float nr = fmaf(pre.w, Cr[k], pre.x);
+          const float ng = fmaf(pre.w, Cg[k], pre.y);
+          const float nbl = fmaf(pre.w, Cb[k], pre.z);
+          const float nt = pre.w * T[k];
+          out[p] = make_float4(nr, ng, nbl, nt);
+          if (nt < kTMin || last_bucket) {
+            alive = false;
+            const size_t pix = (size_t)py * cam.W + px;
+            float* oc = a.out_color + 3 * (size_t)cam.pix_off;
+            float* pc = a.pix_color + 3 * (size_t)cam.pix_off;
+            oc[pix] = nr + nt * cam.bg[0];
+            oc[HW + pix] = ng + nt * cam.bg[1];
+            oc[2 * HW + pix] = nbl + nt * cam.bg[2];
+            pc[pix] = nr;
+            pc[HW + pix] = ng;
+            pc[2 * HW + pix] = nbl;
+            a.last_contrib[cam.pix_off + pix] = contrib;
+            a.Ts_final[cam.pix_off + pix] = nt;
+          }
+        }
+        const uint32_t word = __ballot_sync(0xffffffffu, alive);
+        any_after |= word != 0u;
+        if (lane == k) my_word = word;
       }
-    b = b_next;
+    if (lane < kPxPerThread) st_volatile_u32(alive_words + lane, my_word);
+    if (lane == 0 && any_before && !any_after) a.max_contrib[bi.tile] = (uint32_t)contrib;
+    __threadfence();
+    __syncwarp();
+    if (lane == 0) st_release_u32(stage_word, (uint32_t)bi.local + 1u);
+    q = q_next;
   }
 }
-
-struct MergeArgs {
-  Views views;
-  const uint32_t* ranges;
-  const uint32_t* bucket_off;
-  const uint32_t* bucket_sum;
-  float4* samples;
-  float* out_color;     // per view (3, H, W), view k at 3 * pix_off
-  float* pix_color;     // same layout, without background
-  int* last_contrib;    // per view (H, W), view k at pix_off
-  float* Ts_final;
-  uint32_t* max_contrib;
-  int bs;
-};
-
-// Per pixel: fold the tile's buckets front to back, storing the running
-// prefix in place (FB mergeResults, render.cu:285-391).
-__global__ void __launch_bounds__(kTilePixels) k_merge(const MergeArgs a) {
-  __shared__ uint32_t s_max[kTilePixels / kWarp];
-  const int tile = blockIdx.x, p = threadIdx.x;
-  const ViewDesc& cam = a.views.v[a.views.of_tile((uint32_t)tile)];
-  const int lt = tile - (int)cam.tile_off, bx = a.views.bx, by = a.views.by;
-  const int px = (lt % cam.gx) * bx + p % bx, py = (lt / cam.gx) * by + p / bx;
-  const bool in = px < cam.W && py < cam.H;
-  // bucket_sum[0] is the bucket count clamped to the sample capacity.
-  const int cap = (int)a.bucket_sum[0];
-  const int first = min(cap, tile ? (int)a.bucket_off[tile - 1] : 0);
-  const int last = min(cap, (int)a.bucket_off[tile]);
-  const int rs = (int)a.ranges[2 * tile], re = (int)a.ranges[2 * tile + 1];
-  float T = 1.f, Cr = 0.f, Cg = 0.f, Cb = 0.f;
-  uint32_t contrib = 0;
-  if (in) {
-    float4* s = a.samples + (size_t)first * kTilePixels + p;
-    float4 cur = first < last ? s[0] : make_float4(0.f, 0.f, 0.f, 1.f);
-    for (int b = first; b < last; ++b) {
-      const float4 nxt = (b + 1 < last) ? s[kTilePixels] : cur;
-      Cr = fmaf(T, cur.x, Cr);
-      Cg = fmaf(T, cur.y, Cg);
-      Cb = fmaf(T, cur.z, Cb);
-      T *= cur.w;
-      *s = make_float4(Cr, Cg, Cb, T);
-      contrib += (uint32_t)min(a.bs, re - (rs + (b - first) * a.bs));
-      if (T < kTMin) break;
-      cur = nxt;
-      s += kTilePixels;
-    }
-    const size_t HW = (size_t)cam.W * cam.H;
-    const size_t pix = (size_t)py * cam.W + px;
-    a.last_contrib[cam.pix_off + pix] = (int)contrib;
-    a.Ts_final[cam.pix_off + pix] = T;
-    float* oc = a.out_color + 3 * (size_t)cam.pix_off;
-    float* pc = a.pix_color + 3 * (size_t)cam.pix_off;
-    oc[pix] = Cr + T * cam.bg[0];
-    oc[HW + pix] = Cg + T * cam.bg[1];
-    oc[2 * HW + pix] = Cb + T * cam.bg[2];
-    pc[pix] = Cr;
-    pc[HW + pix] = Cg;
-    pc[2 * HW + pix] = Cb;
-  }
-  const uint32_t m = __reduce_max_sync(0xffffffffu, contrib);
-  if ((p & 31) == 0) s_max[p >> 5] = m;
-  __syncthreads();
-  if (p == 0) {
-    uint32_t mm = 0;
-    for (int w = 0; w < kTilePixels / kWarp; ++w) mm = max(mm, s_max[w]);
-    a.max_contrib[tile] = mm;
-  }
-}
-
 
 }  // namespace
 }  // namespace fgs
@@ -299,15 +408,16 @@ fgs_status run_render_fwd(const Views& views, int64_t n_cap, const int32_t* n_de
   {
     KernelTimer kt__(FGS_K_BUCKET_SETUP, s);
     const unsigned nblk = (views.tiles + kScanTiles - 1) / kScanTiles;
-    k_bucket_count<<<nblk, kScanTiles, 0, s>>>((int)views.tiles, ranges, bucket_size, im.bucket_off,
-                                               im.block_sums);
-    k_bucket_fill<<<nblk, kScanTiles, 0, s>>>((int)views.tiles, ranges, bucket_size, max_buckets, im.bucket_off,
-                                              im.block_sums, sm.bucket_tile, im.bucket_sum);
+    k_bucket_count<<<nblk, kScanTiles, 0, s>>>((int)views.tiles, ranges, bucket_size, im.block_sums);
+    k_bucket_fill<<<nblk, kScanTiles, 0, s>>>((int)views.tiles, ranges, bucket_size, max_buckets, im.block_sums,
+                                              im.bucket_off, sm.bucket_tile, sm.bucket_queue, im.tile_stage,
+                                              im.bucket_sum);
     kt__.stop();
   }
   FGS_LAUNCH_CHECK();
-  FwdArgs fa{views, splat, values_sorted, ranges, sm.bucket_tile, im.bucket_off, im.bucket_sum, sm.samples,
-             bucket_size};
+  FwdArgs fa{views, splat, values_sorted, ranges, sm.bucket_tile, sm.bucket_queue, im.bucket_off, im.bucket_sum,
+             sm.samples, im.tile_stage, im.tile_alive, out_color, im.pix_color, last_contributor, Ts_final,
+             im.max_contrib, bucket_size};
   {
     KernelTimer kt__(FGS_K_RENDER_FWD, s);
     const int nt = kFwdWarps * kWarp;
@@ -317,11 +427,10 @@ fgs_status run_render_fwd(const Views& views, int64_t n_cap, const int32_t* n_de
     kt__.stop();
   }
   FGS_LAUNCH_CHECK();
-  MergeArgs ma{views, ranges, im.bucket_off, im.bucket_sum, sm.samples, out_color, im.pix_color, last_contributor,
-               Ts_final, im.max_contrib, bucket_size};
   {
-    KernelTimer kt__(FGS_K_MERGE, s);
-    k_merge<<<views.tiles, kTilePixels, 0, s>>>(ma);
+    KernelTimer kt__(FGS_K_EMPTY_TILES, s);
+    k_empty_tiles<<<views.tiles, kTilePixels, 0, s>>>(views, ranges, im.bucket_sum, out_color, im.pix_color,
+                                                      last_contributor, Ts_final, im.max_contrib);
     kt__.stop();
   }
   FGS_LAUNCH_CHECK();

@@ -14,25 +14,32 @@ constexpr int kMaxBucket = 128;    // largest supported bucket size
 
 // Per-image state (FB ImageState, rasterizer_imp.h:76-88), carved from one
 // caller buffer:  pixel colour planes (3, H*W) without background,
-// per-tile max contributor count, per-tile inclusive bucket offsets, and a
-// 16-byte header holding the bucket total.
+// per-tile max contributor count, per-tile inclusive bucket offsets, a
+// 16-byte header holding the bucket total and work cursors, the bucket-setup
+// scan's block totals, and the per-tile chain state of the forward composite
+// (number of buckets folded into the tile's running prefix, and which pixels
+// are still above the transmittance cut-off).
+constexpr int kScanTiles = 1024;  // tiles per bucket-setup scan block
+constexpr int kRounds = 8;        // leading bucket rounds of the forward work queue
+constexpr int kScanValues = kRounds + 2;
 struct ImageState {
   float* pix_color;         // 3 * HW
   uint32_t* max_contrib;    // T
   uint32_t* bucket_off;     // T (inclusive scan of bucket counts)
-  uint32_t* bucket_sum;     // [0] buckets (capped), [1] buckets (uncapped), [2], [3] work cursors
-  uint32_t* block_sums;     // ceil(T / kScanTiles) bucket totals of the bucket-setup scan blocks
+  uint32_t* bucket_sum;     // [0] buckets to render, [1] buckets needed, [2], [3] work cursors
+  uint32_t* block_sums;     // ceil(T / kScanTiles) x kScanValues
+  uint32_t* tile_stage;     // T: buckets of the tile folded into its prefix
+  uint32_t* tile_alive;     // T x 8: per 8x4 sub-block, lanes whose pixel is still compositing
   size_t bytes;
 };
-constexpr int kScanTiles = 1024;  // tiles per bucket-setup scan block
 
 // Per-bucket state (FB SampleState, rasterizer_imp.h:91-102): the owning tile
-// of each bucket and, per (bucket, pixel), a float4 (C.rgb, T).  The forward
-// composite writes the bucket-local values; the merge overwrites them in place
-// with the running prefix after the bucket, which is all the backward needs
-// (16 bytes per pixel and bucket instead of FB's 40).
+// of each bucket, the forward work queue, and per (bucket, pixel) a float4
+// (C.rgb, T) holding the running prefix after the bucket, which is all the
+// backward needs (16 bytes per pixel and bucket instead of FB's 40).
 struct SampleState {
   uint32_t* bucket_tile;    // max_buckets
+  uint32_t* bucket_queue;   // max_buckets: forward processing order
   float4* samples;          // max_buckets * 256
   size_t bytes;
 };
@@ -44,12 +51,14 @@ inline ImageState carve_image(void* base, size_t pixels, size_t T) {
   char* p = static_cast<char*>(base);
   ImageState s;
   size_t off = 0;
+  const size_t nblk = (T + kScanTiles - 1) / kScanTiles;
   s.bucket_sum = reinterpret_cast<uint32_t*>(p + off);  off = align_up(off + 16, 256);
   s.pix_color = reinterpret_cast<float*>(p + off);      off = align_up(off + sizeof(float) * 3 * pixels, 256);
-  s.max_contrib = reinterpret_cast<uint32_t*>(p + off); off = align_up(off + sizeof(uint32_t) * (size_t)T, 256);
-  s.bucket_off = reinterpret_cast<uint32_t*>(p + off);  off = align_up(off + sizeof(uint32_t) * (size_t)T, 256);
-  s.block_sums = reinterpret_cast<uint32_t*>(p + off);
-  off = align_up(off + sizeof(uint32_t) * ((size_t)T + kScanTiles - 1) / kScanTiles, 256);
+  s.max_contrib = reinterpret_cast<uint32_t*>(p + off); off = align_up(off + sizeof(uint32_t) * T, 256);
+  s.bucket_off = reinterpret_cast<uint32_t*>(p + off);  off = align_up(off + sizeof(uint32_t) * T, 256);
+  s.block_sums = reinterpret_cast<uint32_t*>(p + off);  off = align_up(off + sizeof(uint32_t) * nblk * kScanValues, 256);
+  s.tile_stage = reinterpret_cast<uint32_t*>(p + off);  off = align_up(off + sizeof(uint32_t) * T, 256);
+  s.tile_alive = reinterpret_cast<uint32_t*>(p + off);  off = align_up(off + sizeof(uint32_t) * 8 * T, 256);
   s.bytes = off;
   return s;
 }
@@ -59,6 +68,7 @@ inline SampleState carve_sample(void* base, int64_t max_buckets) {
   SampleState s;
   size_t off = 0;
   s.bucket_tile = reinterpret_cast<uint32_t*>(p + off); off = align_up(off + sizeof(uint32_t) * (size_t)max_buckets, 256);
+  s.bucket_queue = reinterpret_cast<uint32_t*>(p + off); off = align_up(off + sizeof(uint32_t) * (size_t)max_buckets, 256);
   s.samples = reinterpret_cast<float4*>(p + off);       off = align_up(off + sizeof(float4) * kTilePixels * (size_t)max_buckets, 256);
   s.bytes = off;
   return s;

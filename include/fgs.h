@@ -277,7 +277,7 @@ fgs_status fgs_batch_offsets(int P, int num_views, const fgs_camera* cams, const
  * counterpart in FB (its DEBUG_TIME macros are unused, ops.h:10-14). */
 enum {
   FGS_K_PREPROCESS = 0, FGS_K_PREPROCESS_LARGE = 1, FGS_K_SORT_HIST = 2, FGS_K_SORT_PASS = 3,
-  FGS_K_TILE_RANGES = 4, FGS_K_BUCKET_SETUP = 5, FGS_K_RENDER_FWD = 6, FGS_K_MERGE = 7,
+  FGS_K_TILE_RANGES = 4, FGS_K_BUCKET_SETUP = 5, FGS_K_RENDER_FWD = 6, FGS_K_EMPTY_TILES = 7,
   FGS_K_RENDER_BWD = 8, FGS_K_PREPROCESS_BWD = 9, FGS_K_COUNT = 10
 };
 fgs_status fgs_kernel_timer(int kernel_id, int enable);
