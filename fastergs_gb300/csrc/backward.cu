@@ -77,6 +77,9 @@ __global__ void __launch_bounds__(kBwdWarps * kWarp, 5) k_render_bwd(const BwdAr
   using M = TileMap<BX>;
   constexpr int BY = kTilePixels / BX;
   __shared__ BucketStage s_stage[kBwdWarps];
+  // Per pixel (slot k * 32 + lane): dL/dpixel rgb and K, read once per
+  // evaluation with one 16-byte load instead of holding 32 registers.
+  __shared__ float4 s_lk[kBwdWarps][kTilePixels];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   BucketStage& st = s_stage[warp];
   const int B = (int)a.bucket_sum[0];
@@ -113,8 +116,8 @@ __global__ void __launch_bounds__(kBwdWarps * kWarp, 5) k_render_bwd(const BwdAr
 #pragma unroll
     for (int r = 0; r < M::kRows; ++r) pyr[r] = (float)(ty0 + 4 * r + (lane >> 3));
 
-    float T[kPxPerThread], Pd[kPxPerThread], Lr[kPxPerThread], Lg[kPxPerThread], Lb[kPxPerThread],
-        K[kPxPerThread];
+    float T[kPxPerThread], Pd[kPxPerThread];
+    float4* lk = s_lk[warp];
     uint32_t alive = 0;
 #pragma unroll
     for (int r = 0; r < M::kRows; ++r)
@@ -122,34 +125,41 @@ __global__ void __launch_bounds__(kBwdWarps * kWarp, 5) k_render_bwd(const BwdAr
       for (int cc = 0; cc < M::kCols; ++cc) {
         const int k = r * M::kCols + cc;
         const int gxp = (int)pxc[cc], gyp = (int)pyr[r];
-        T[k] = 0.f; Pd[k] = 0.f; Lr[k] = 0.f; Lg[k] = 0.f; Lb[k] = 0.f; K[k] = 0.f;
+        T[k] = 0.f; Pd[k] = 0.f;
+        float4 l4 = make_float4(0.f, 0.f, 0.f, 0.f);
         if (gxp < cam.W && gyp < cam.H) {
           const int pix = gyp * cam.W + gxp;
           if ((uint32_t)lcon[pix] > thres) {
             alive |= 1u << k;
             const float4 prev = bi.local > 0 ? a.samples[(size_t)(b - 1) * kTilePixels + M::pix(r, cc, lane)]
                                              : make_float4(0.f, 0.f, 0.f, 1.f);
-            Lr[k] = dL[pix];
-            Lg[k] = dL[HW + pix];
-            Lb[k] = dL[2 * HW + pix];
+            l4.x = dL[pix];
+            l4.y = dL[HW + pix];
+            l4.z = dL[2 * HW + pix];
             T[k] = prev.w;
-            Pd[k] = prev.x * Lr[k] + prev.y * Lg[k] + prev.z * Lb[k];
+            Pd[k] = prev.x * l4.x + prev.y * l4.y + prev.z * l4.z;
             // K = C_final . dL + T_final * (bg . dL): everything behind a
             // Gaussian is K - (prefix up to and including it) . dL.
-            K[k] = pcol[pix] * Lr[k] + pcol[HW + pix] * Lg[k] + pcol[2 * HW + pix] * Lb[k] +
-                   Tfin[pix] * (bgr * Lr[k] + bgg * Lg[k] + bgb * Lb[k]);
+            l4.w = pcol[pix] * l4.x + pcol[HW + pix] * l4.y + pcol[2 * HW + pix] * l4.z +
+                   Tfin[pix] * (bgr * l4.x + bgg * l4.y + bgb * l4.z);
           }
         }
+        lk[k * kWarp + lane] = l4;
       }
-    if (__any_sync(0xffffffffu, alive) == 0) {
+    // sub-blocks with at least one pixel that this bucket reaches
+    uint32_t live_sb = 0;
+#pragma unroll
+    for (int k = 0; k < kPxPerThread; ++k)
+      if (__any_sync(0xffffffffu, (alive >> k) & 1u)) live_sb |= 1u << k;
+    if (live_sb == 0) {
       __syncwarp();
       b = b_next;
       continue;
     }
 
     for (int g = 0; g < bi.n; ++g) {
-      const uint32_t mask = st.mask[g];
-      if (mask == 0) continue;  // alpha < 1/256 on the whole tile: no contribution
+      const uint32_t mask = st.mask[g] & live_sb;
+      if (mask == 0) continue;  // alpha < 1/256 on every reached sub-block: no contribution
       const float4 pos = st.pos[g];
       const float4 q = st.quad[g];   // A1, P, C1, log2 o
       const float4 c = st.rgb[g];
@@ -177,15 +187,16 @@ __global__ void __launch_bounds__(kBwdWarps * kWarp, 5) k_render_bwd(const BwdAr
           const float al = fminf(kAlphaMax, ex2_approx(e));
           if (((alive >> k) & 1u) && al >= kAlphaCut) {
             any = true;
+            const float4 l4 = lk[k * kWarp + lane];  // dL rgb, K
             const float wt = al * T[k];
-            const float cd = c.x * Lr[k] + c.y * Lg[k] + c.z * Lb[k];
+            const float cd = c.x * l4.x + c.y * l4.y + c.z * l4.z;
             Pd[k] = fmaf(wt, cd, Pd[k]);
-            const float inv = __frcp_rn(1.f - al);
-            const float dLda = T[k] * cd - inv * (K[k] - Pd[k]);
+            const float inv = rcp_approx(1.f - al);  // 1 - alpha >= 0.01
+            const float dLda = T[k] * cd - inv * (l4.w - Pd[k]);
             T[k] = fmaf(-al, T[k], T[k]);
-            v[8] = fmaf(wt, Lr[k], v[8]);
-            v[9] = fmaf(wt, Lg[k], v[9]);
-            v[10] = fmaf(wt, Lb[k], v[10]);
+            v[8] = fmaf(wt, l4.x, v[8]);
+            v[9] = fmaf(wt, l4.y, v[9]);
+            v[10] = fmaf(wt, l4.z, v[10]);
             const float dp = dLda * al;  // dL/dexponent / ln2
             // d exponent / d(centre x) = 2 A1 w, d / d(centre y) = 2 A1 P w + 2 C1 dy
             const float gw = A2 * w;
