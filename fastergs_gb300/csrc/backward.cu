@@ -202,13 +202,16 @@ __global__ void __launch_bounds__(kBwdWarps * kWarp, 5) k_render_bwd(const BwdAr
             const float gw = A2 * w;
             const float tx = dp * gw;
             const float ty = dp * fmaf(gw, q.y, c2dy);
-            const float ddx = dx[cc];
             v[0] += tx;
             v[1] += ty;
             v[2] += fabsf(tx);
             v[3] += fabsf(ty);
-            v[4] = fmaf(dp, ddx * ddx, v[4]);
-            v[5] = fmaf(dp * ddx, dy, v[5]);
+            // Conic-gradient moments in the exponent's own frame (w, dy),
+            // w = dx + P dy.  In pixel coordinates a thin footprint's
+            // cross-axis gradient is a small difference of large sums; here
+            // each frame axis is summed on its own.
+            v[4] = fmaf(dp, w * w, v[4]);
+            v[5] = fmaf(dp * w, dy, v[5]);
             v[7] = fmaf(dp * dy, dy, v[7]);
             v[11] += dp;
           }
@@ -270,10 +273,17 @@ __global__ void __launch_bounds__(256) k_preprocess_bwd(const PbwdArgs a) {
     const size_t rid = (size_t)vi * a.P + i;
     const float4* gr = reinterpret_cast<const float4*>(a.grad + rid * FGS_GRAD_STRIDE);
     const float4 gm2 = gr[0], gcn = gr[1], gco = gr[2];
-    if (a.dmean2D) reinterpret_cast<float4*>(a.dmean2D)[rid] = gm2;
-    if (a.dconic) reinterpret_cast<float4*>(a.dconic)[rid] = make_float4(gcn.x, gcn.y, 0.f, gcn.w);
-    gco_sum.x += gco.x; gco_sum.y += gco.y; gco_sum.z += gco.z; gco_sum.w += gco.w;
     const int radius = a.radii[rid];
+    // gcn: -1/2 x the conic-gradient moments sum dp w^2, dp w dy, dp dy^2 in
+    // the (w = dx + P dy, dy) frame of the record's exponent.  In pixel
+    // coordinates dL/dconic (off-diagonal halved, as FB stores it) is
+    // G = Ms S Ms^T with Ms = [[1, -P], [0, 1]].
+    const float Pc = radius > 0 ? a.splat[rid * 32 + F_CHOL + 1] : 0.f;
+    const float sww = gcn.x, swy = gcn.y, syy = gcn.w;
+    const float gz = syy, gy = fmaf(-Pc, syy, swy), gx = fmaf(-Pc, gy, fmaf(-Pc, swy, sww));
+    if (a.dmean2D) reinterpret_cast<float4*>(a.dmean2D)[rid] = gm2;
+    if (a.dconic) reinterpret_cast<float4*>(a.dconic)[rid] = make_float4(gx, gy, 0.f, gz);
+    gco_sum.x += gco.x; gco_sum.y += gco.y; gco_sum.z += gco.z; gco_sum.w += gco.w;
     if (!(radius > 0)) continue;
     const float sv[3] = {cam.smod * a.scales[3 * (size_t)i], cam.smod * a.scales[3 * (size_t)i + 1],
                          cam.smod * a.scales[3 * (size_t)i + 2]};
@@ -298,7 +308,6 @@ __global__ void __launch_bounds__(256) k_preprocess_bwd(const PbwdArgs a) {
     const ScreenCov sc2 = screen_cov(M0, M1, R, s2);
     const float idet = 1.f / sc2.det;
     const float ia = sc2.c * idet, ib = -sc2.b * idet, ic = sc2.a * idet;  // C = Sigma2^-1 (the conic)
-    const float gx = gcn.x, gy = gcn.y, gz = gcn.w;  // dL/dconic, off-diagonal halved as FB stores it
     // FB divides by den^2 + 1e-7 instead of den^2 (backward.cu:304); keep that factor.
     const float rr = sc2.det * sc2.det / (sc2.det * sc2.det + 0.0000001f);
     // dL/dSigma2 = rr * E with E = -C Gm C.  FB forms E and then projects it on
@@ -310,8 +319,12 @@ __global__ void __launch_bounds__(256) k_preprocess_bwd(const PbwdArgs a) {
     for (int k = 0; k < 3; ++k) {
       const float v0 = ia * sc2.N0[k] + ib * sc2.N1[k];
       const float v1 = ib * sc2.N0[k] + ic * sc2.N1[k];
-      const float g0 = gx * v0 + gy * v1, g1 = gy * v0 + gz * v1;
-      gs[k] += -2.f * sv[k] * rr * (v0 * g0 + v1 * g1);  // w.r.t. the modified scale, as FB returns it
+      // G v and v^T G v through the moment frame: u = v1 - P v0 is v's
+      // second coordinate there, so no large pixel-frame terms cancel.
+      const float u = fmaf(-Pc, v0, v1);
+      const float h0 = fmaf(sww, v0, swy * u), h1 = fmaf(swy, v0, syy * u);
+      const float g0 = fmaf(-Pc, h1, h0), g1 = h1;
+      gs[k] += -2.f * sv[k] * rr * fmaf(v0, h0, u * h1);  // w.r.t. the modified scale, as FB returns it
       const float y0 = ia * g0 + ib * g1, y1 = ib * g0 + ic * g1;
       const float f = -2.f * s2[k] * rr;
 #pragma unroll

@@ -5,7 +5,8 @@
 // ("onesweep") sort written for this GPU:
 //   * one upfront kernel builds the 8-bit digit histograms of every pass in a
 //     single read of the keys;
-//   * each pass is one kernel: a CTA ranks a 4096-key tile in shared memory
+//   * each pass is one kernel: a CTA of 512 threads (8 keys each, few enough
+//     registers for 2 CTAs = 32 warps per SM) ranks a 4096-key tile in shared memory
 //     (warp match + per-warp digit counters, so ranks are stable), publishes its
 //     per-digit counts, obtains the exclusive prefix of all earlier tiles by a
 //     decoupled look-back, and scatters through shared memory so that global
@@ -23,9 +24,9 @@
 namespace fgs {
 namespace {
 
-constexpr int kSortThreads = 256;
+constexpr int kSortThreads = 512;
 constexpr int kSortWarps = kSortThreads / kWarp;
-constexpr int kSortItems = 16;
+constexpr int kSortItems = 8;
 constexpr int kSortTile = kSortThreads * kSortItems;   // 4096 keys
 constexpr int kRadix = 256;
 constexpr int kMaxPasses = 8;
@@ -80,9 +81,9 @@ __global__ void __launch_bounds__(kSortThreads) k_histogram(const unsigned long 
   }
 }
 
-// Exclusive scan of 256 values held one per thread; returns the exclusive
-// prefix, *total receives the sum.  Uses s_tmp[kSortWarps].
-__device__ __forceinline__ uint32_t block_excl_scan_256(uint32_t v, uint32_t* s_tmp, uint32_t* total) {
+// Exclusive scan of one value per thread (kSortThreads); returns the
+// exclusive prefix, *total receives the sum.  Uses s_tmp[kSortWarps].
+__device__ __forceinline__ uint32_t block_excl_scan(uint32_t v, uint32_t* s_tmp, uint32_t* total) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   uint32_t incl = v;
 #pragma unroll
@@ -104,7 +105,7 @@ __device__ __forceinline__ uint32_t block_excl_scan_256(uint32_t v, uint32_t* s_
   return wbase + incl - v;
 }
 
-__global__ void __launch_bounds__(kSortThreads) k_onesweep(
+__global__ void __launch_bounds__(kSortThreads, 2) k_onesweep(
     const unsigned long long* __restrict__ keys_in, const uint32_t* __restrict__ vals_in,
     unsigned long long* __restrict__ keys_out, uint32_t* __restrict__ vals_out, long long n_cap, const int* n_dev,
     int shift, const uint32_t* __restrict__ hist, uint32_t* lookback, uint32_t* tile_counter) {
@@ -126,7 +127,7 @@ __global__ void __launch_bounds__(kSortThreads) k_onesweep(
   const long long n = pair_count(n_cap, n_dev);
   if (tile_base >= n) return;  // grid sized for the capacity; this tile is empty
 
-  // Load: warp w owns keys [tile_base + w*512, +512), 32 consecutive per step,
+  // Load: warp w owns keys [tile_base + w*256, +256), 32 consecutive per step,
   // so (warp, step, lane) is the input order and the ranks below are stable.
   unsigned long long k[kSortItems];
   uint32_t v[kSortItems];
@@ -154,17 +155,6 @@ __global__ void __launch_bounds__(kSortThreads) k_onesweep(
     __syncwarp();
     rank[r] = before + __popc(peers & lanemask_lt());
   }
-  __syncthreads();
-
-  // Per digit (one thread each): warp offsets, tile count, look-back.
-  const uint32_t d = tid;
-  uint32_t cnt = 0;
-#pragma unroll
-  for (int w = 0; w < kSortWarps; ++w) {
-    const uint32_t x = s_whist[w][d];
-    s_whist[w][d] = cnt;
-    cnt += x;
-  }
   // Padding keys only exist in the last tile and all sit in digit 255.
   int pad = n_invalid;
 #pragma unroll
@@ -175,40 +165,52 @@ __global__ void __launch_bounds__(kSortThreads) k_onesweep(
 #pragma unroll
   for (int w = 0; w < kSortWarps; ++w) pad_total += s_tmp[w];
   __syncthreads();
-  const uint32_t real = (d == 255) ? cnt - pad_total : cnt;
 
-  uint32_t* lb = lookback + (size_t)tile * kRadix;
-  uint32_t excl = 0;
-  if (tile == 0) {
-    st_volatile_u32(lb + d, kFlagInc | real);
-  } else {
-    st_volatile_u32(lb + d, kFlagAgg | real);
-    long long pred = (long long)tile - 1;
-    int polls = 0;
-    while (pred >= 0) {
-      const uint32_t w = ld_volatile_u32(lookback + (size_t)pred * kRadix + d);
-      const uint32_t flag = w & ~kValueMask;
-      if (flag == 0) {
-        if (++polls > kSpinLimit) {
-          raise_error(kErrTimeout);
-          break;
-        }
-        __nanosleep(64);
-        continue;
-      }
-      excl += w & kValueMask;
-      if (flag == kFlagInc) break;
-      --pred;
+  // Per digit (threads 0..255): warp offsets, tile count, look-back.
+  const uint32_t d = (uint32_t)tid;
+  uint32_t cnt = 0, excl = 0;
+  if (tid < kRadix) {
+#pragma unroll
+    for (int w = 0; w < kSortWarps; ++w) {
+      const uint32_t x = s_whist[w][d];
+      s_whist[w][d] = cnt;
+      cnt += x;
     }
-    st_volatile_u32(lb + d, kFlagInc | (excl + real));
+    const uint32_t real = (d == 255) ? cnt - pad_total : cnt;
+    uint32_t* lb = lookback + (size_t)tile * kRadix;
+    if (tile == 0) {
+      st_volatile_u32(lb + d, kFlagInc | real);
+    } else {
+      st_volatile_u32(lb + d, kFlagAgg | real);
+      long long pred = (long long)tile - 1;
+      int polls = 0;
+      while (pred >= 0) {
+        const uint32_t w = ld_volatile_u32(lookback + (size_t)pred * kRadix + d);
+        const uint32_t flag = w & ~kValueMask;
+        if (flag == 0) {
+          if (++polls > kSpinLimit) {
+            raise_error(kErrTimeout);
+            break;
+          }
+          __nanosleep(64);
+          continue;
+        }
+        excl += w & kValueMask;
+        if (flag == kFlagInc) break;
+        --pred;
+      }
+      st_volatile_u32(lb + d, kFlagInc | (excl + real));
+    }
   }
 
   // Global digit base of this pass, tile-local digit offsets.
   uint32_t gtot, ttot;
-  const uint32_t gbase = block_excl_scan_256(hist[d], s_tmp, &gtot);
-  const uint32_t toff = block_excl_scan_256(cnt, s_tmp, &ttot);
-  s_toff[d] = toff;
-  s_dst[d] = gbase + excl - toff;  // global position of shared slot i = s_dst[digit] + i
+  const uint32_t gbase = block_excl_scan(tid < kRadix ? hist[d] : 0u, s_tmp, &gtot);
+  const uint32_t toff = block_excl_scan(cnt, s_tmp, &ttot);
+  if (tid < kRadix) {
+    s_toff[d] = toff;
+    s_dst[d] = gbase + excl - toff;  // global position of shared slot i = s_dst[digit] + i
+  }
   __syncthreads();
 
 #pragma unroll

@@ -35,7 +35,11 @@ typedef enum {
 /* Number of int32 words of the device counter block used by fgs_preprocess. */
 #define FGS_COUNTER_WORDS 16
 /* Floats per Gaussian of the interleaved gradient record written by
- * fgs_render_bwd: [dmean2D.xyzw | dconic.xyzw | dcolor.rgb, dopacity]. */
+ * fgs_render_bwd: [dmean2D.xyzw | conic moments | dcolor.rgb, dopacity].
+ * The conic moments are -1/2 x (sum dp w^2, sum dp w dy, 0, sum dp dy^2)
+ * over the Gaussian's pixels, dp = dL/d(exponent), in the frame
+ * w = dx + P dy of the splat record's exponent (P = record float 7);
+ * fgs_preprocess_bwd turns them into FB's dL/dconic. */
 #define FGS_GRAD_STRIDE 12
 /* Floats per Gaussian of the splat record (FB rasterizer_imp.h:27-38). */
 #define FGS_SPLAT_STRIDE 32
