@@ -50,6 +50,7 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--no-checkpoint", action="store_true")
     ap.add_argument("--cameras", type=int, default=16)
     ap.add_argument("--tune", choices=["sweep", "default"], default="sweep",
                     help="batched launch config: autotuner sweep (18 configs) or FB's fixed choice")
@@ -293,8 +294,15 @@ def gpu_bench(args, rank, local, world):
                                    target=(0.0, 0.0, 7.0)) for c in c4]
         batched.append(batched_bench(args, dev, s, dev_in, same, f"{args.cameras} cameras at 1297x840 on the same "
                                      "circle"))
+    checkpoint = None
+    if not args.no_checkpoint and world == 1:
+        del dev_in
+        fgs._RasterizeGaussians.__dict__["buffer"]._buf = None  # the drop-in path's shared buffers
+        torch.cuda.empty_cache()
+        checkpoint = checkpoint_bench(args, dev)
     return dict(ms_step=ms_step_job, fwd_ms=fwd_ms, clocks=clocks, ktimes=ktimes, K=K,
-                launches_per_step=launches_per_step, e2e=e2e, P=s.P, W=cam.width, H=cam.height, batched=batched)
+                launches_per_step=launches_per_step, e2e=e2e, P=s.P, W=cam.width, H=cam.height, batched=batched,
+                checkpoint=checkpoint)
 
 
 def batched_bench(args, dev, s, dev_in, cams, label):
@@ -408,6 +416,61 @@ def batched_bench(args, dev, s, dev_in, cams, label):
     return out
 
 
+def checkpoint_bench(args, dev):
+    """C5b: 6M Gaussians in 64 Zipf-weighted clusters, 3840x2160, SH degree 3,
+    one fwd+bwd step (CUDA graph, batched path with one camera) with every
+    bucket's prefix stored versus recomputed in the backward.  Reports the
+    device memory held during the step (parameters, gradients, workspace) and
+    the step time of each mode."""
+    import torch
+    import fastergs_gb300 as fgs
+    from fastergs_gb300 import scenes
+    from fastergs_gb300.batched import BatchedRasterizer, CapturedStep, TuneConfig
+    s = scenes.scene_c5b(seed=0)
+    cam = s.camera
+    m, sc, rot, op, dc, shs = s.activated()
+    params = {k: torch.from_numpy(np.ascontiguousarray(v)).to(dev)
+              for k, v in dict(means3D=m, scales=sc, rotations=rot, opacities=op, dc=dc, shs=shs).items()}
+    t = lambda a: torch.tensor(np.asarray(a, np.float32), device=dev)
+    st = fgs.GaussianRasterizationSettings(
+        image_height=cam.height, image_width=cam.width, tanfovx=cam.tanfovx, tanfovy=cam.tanfovy,
+        bg=torch.zeros(3, device=dev), scale_modifier=1.0, viewmatrix=t(cam.viewmatrix), projmatrix=t(cam.projmatrix),
+        sh_degree=s.sh_degree, campos=t(cam.campos), mult=1.0, prefiltered=False, debug=False)
+    dL = torch.from_numpy(scenes.upstream_grad(0, cam.height, cam.width)).to(dev).reshape(-1)
+    stream = torch.cuda.current_stream(dev)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    reps = max(3, min(args.steps, 10))
+    out = {"workload": "c5b: 6M Gaussians, 64 Zipf clusters, 3840x2160, SH degree 3, fwd+bwd",
+           "gaussians": s.P, "width": cam.width, "height": cam.height}
+    for name, rec in (("store", False), ("recompute", True)):
+        torch.cuda.synchronize(dev)
+        torch.cuda.empty_cache()
+        rast = BatchedRasterizer([st], s.P, tune=TuneConfig(recompute=rec))
+        pairs = rast.fit(params["means3D"], params["opacities"], params["dc"], params["shs"], None,
+                         params["scales"], params["rotations"], None, s.sh_degree, headroom=1.05)
+        step = CapturedStep(rast, params, dL, sh_degree=s.sh_degree)
+        torch.cuda.synchronize(dev)
+        torch.cuda.reset_peak_memory_stats(dev)
+        step.replay()
+        ev0.record(stream)
+        for _ in range(reps):
+            step.replay()
+        ev1.record(stream)
+        torch.cuda.synchronize(dev)
+        _, buckets = rast.status()
+        out[name] = {"ms_per_step": round(ev0.elapsed_time(ev1) / reps, 3),
+                     "peak_hbm_gb": round(torch.cuda.max_memory_allocated(dev) / 1e9, 3),
+                     "workspace_gb": round(rast.workspace.numel() / 1e9, 3), "pairs": int(pairs),
+                     "buckets": int(buckets)}
+        del step, rast
+    # FB's sample state for the same frame: 40 bytes per pixel and bucket
+    out["fb_sample_state_gb"] = round(out["store"]["buckets"] * 256 * 40 / 1e9, 3)
+    out["peak_hbm_saved_gb"] = round(out["store"]["peak_hbm_gb"] - out["recompute"]["peak_hbm_gb"], 3)
+    del params
+    torch.cuda.empty_cache()
+    return out
+
+
 def roofline(res, peaks):
     """Roofline objects for the dominant kernel (by device time)."""
     P, K = res["P"], res["K"]
@@ -487,7 +550,7 @@ def main():
         "render_ms": round(res["fwd_ms"], 4),
         "e2e": res["e2e"], "gpu_launches": int(round(res["launches_per_step"] * args.steps)),
         "clocks": res["clocks"], "roofline": roof, "kernels": table, "cpu_baseline": cb,
-        "batched": res["batched"],
+        "batched": res["batched"], "checkpoint": res["checkpoint"],
     }
     print(json.dumps(line), flush=True)
     barrier(world)

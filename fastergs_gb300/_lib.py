@@ -27,7 +27,7 @@ class Camera(C.Structure):
 
 class TuneConfig(C.Structure):
     """fgs_tune_config: bucket size, tile shape and packet width of a launch."""
-    _fields_ = [("bucket_size", i32), ("block_x", i32), ("block_y", i32), ("packet", i32)]
+    _fields_ = [("bucket_size", i32), ("block_x", i32), ("block_y", i32), ("packet", i32), ("recompute", i32)]
 
 
 camp, tunep = C.POINTER(Camera), C.POINTER(TuneConfig)

@@ -40,9 +40,10 @@ class TuneConfig:
     block_x: int = 16
     block_y: int = 16
     packet: int = 4
+    recompute: bool = False  # rebuild bucket prefixes in the backward instead of storing them
 
     def as_c(self) -> _lib.TuneConfig:
-        return _lib.TuneConfig(self.bucket_size, self.block_x, self.block_y, self.packet)
+        return _lib.TuneConfig(self.bucket_size, self.block_x, self.block_y, self.packet, int(self.recompute))
 
 
 class BatchOverflow(RuntimeError):

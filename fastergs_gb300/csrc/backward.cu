@@ -27,10 +27,12 @@ struct BwdArgs {
   const uint32_t* vals;
   const uint32_t* ranges;
   const uint32_t* bucket_tile;
+  const uint32_t* bucket_queue;
   const uint32_t* bucket_off;
   uint32_t* bucket_sum;
   const uint32_t* max_contrib;
-  const float4* samples;
+  float4* samples;           // prefix after each bucket, or per tile in recompute mode
+  uint32_t* tile_stage;      // recompute mode: buckets folded into the tile's rebuilt prefix
   const float* pix_color;    // per view (3, H, W) at 3 * pix_off
   const float* Ts_final;     // per view (H, W) at pix_off
   const int* last_contrib;
@@ -72,7 +74,7 @@ __device__ __forceinline__ float warp_transpose_reduce16(float (&v)[16], int lan
   return v[0] + __shfl_xor_sync(0xffffffffu, v[0], 1);
 }
 
-template <int BX>
+template <int BX, bool RECOMPUTE>
 __global__ void __launch_bounds__(kBwdWarps * kWarp, 5) k_render_bwd(const BwdArgs a) {
   using M = TileMap<BX>;
   constexpr int BY = kTilePixels / BX;
@@ -85,12 +87,15 @@ __global__ void __launch_bounds__(kBwdWarps * kWarp, 5) k_render_bwd(const BwdAr
   const int B = (int)a.bucket_sum[0];
   const int vid = (lane >> 1) & 15;  // value a lane holds after the transpose reduction
 
-  for (int b = next_bucket(a.bucket_sum + 3, lane); b < B;) {
-    const int b_next = next_bucket(a.bucket_sum + 3, lane);
+  // Buckets in the forward's queue order (round by round), so that in
+  // recompute mode a tile's bucket k is always handed out after bucket k-1.
+  for (int q = next_bucket(a.bucket_sum + 3, lane); q < B;) {
+    const int q_next = next_bucket(a.bucket_sum + 3, lane);
+    const int b = (int)a.bucket_queue[q];
     const BucketInfo bi = bucket_info(b, a.bucket_tile, a.bucket_off, a.ranges, a.bs);
     const uint32_t thres = (uint32_t)(bi.local * a.bs);
     if (thres >= a.max_contrib[bi.tile]) {  // no pixel of the tile reaches this bucket
-      b = b_next;
+      q = q_next;
       continue;
     }
     const ViewDesc& cam = a.views.v[a.views.of_tile((uint32_t)bi.tile)];
@@ -116,9 +121,56 @@ __global__ void __launch_bounds__(kBwdWarps * kWarp, 5) k_render_bwd(const BwdAr
 #pragma unroll
     for (int r = 0; r < M::kRows; ++r) pyr[r] = (float)(ty0 + 4 * r + (lane >> 3));
 
+    // Prefix (C, T) before this bucket for the pixels it reaches, and which of
+    // them also reach the next bucket.
+    float4* slot = a.samples + (size_t)(RECOMPUTE ? bi.tile : b) * kTilePixels;
+    const float4* prev = RECOMPUTE ? slot : a.samples + (size_t)(b - 1) * kTilePixels;
+    if (RECOMPUTE && bi.local > 0) wait_stage(a.tile_stage + bi.tile, (uint32_t)bi.local, lane);
+    float4 pre[kPxPerThread];
+    uint32_t alive = 0, cont = 0;
+#pragma unroll
+    for (int r = 0; r < M::kRows; ++r)
+#pragma unroll
+      for (int cc = 0; cc < M::kCols; ++cc) {
+        const int k = r * M::kCols + cc;
+        const int gxp = (int)pxc[cc], gyp = (int)pyr[r];
+        pre[k] = make_float4(0.f, 0.f, 0.f, 1.f);
+        if (gxp < cam.W && gyp < cam.H) {
+          const uint32_t lc = (uint32_t)lcon[gyp * cam.W + gxp];
+          if (lc > thres) {
+            alive |= 1u << k;
+            if (RECOMPUTE && lc > thres + (uint32_t)bi.n) cont |= 1u << k;
+            if (bi.local > 0) pre[k] = __ldcg(prev + M::pix(r, cc, lane));
+          }
+        }
+      }
+    if (RECOMPUTE) {
+      // Rebuild this bucket's prefix for the pixels that go on, exactly as the
+      // forward folded it, and hand it to the tile's next bucket before the
+      // gradient work starts.
+      uint32_t cont_sb = 0;
+#pragma unroll
+      for (int k = 0; k < kPxPerThread; ++k)
+        if (__any_sync(0xffffffffu, (cont >> k) & 1u)) cont_sb |= 1u << k;
+      if (cont_sb != 0u) {
+        float Tl[kPxPerThread], Crl[kPxPerThread], Cgl[kPxPerThread], Cbl[kPxPerThread];
+        composite_bucket<BX>(st, bi.n, cont_sb, pxc, pyr, Tl, Crl, Cgl, Cbl);
+#pragma unroll
+        for (int r = 0; r < M::kRows; ++r)
+#pragma unroll
+          for (int cc = 0; cc < M::kCols; ++cc) {
+            const int k = r * M::kCols + cc;
+            if ((cont >> k) & 1u)
+              slot[M::pix(r, cc, lane)] = make_float4(fmaf(pre[k].w, Crl[k], pre[k].x),
+                                                      fmaf(pre[k].w, Cgl[k], pre[k].y),
+                                                      fmaf(pre[k].w, Cbl[k], pre[k].z), pre[k].w * Tl[k]);
+          }
+      }
+      publish_stage(a.tile_stage + bi.tile, (uint32_t)bi.local + 1u, lane);
+    }
+
     float T[kPxPerThread], Pd[kPxPerThread];
     float4* lk = s_lk[warp];
-    uint32_t alive = 0;
 #pragma unroll
     for (int r = 0; r < M::kRows; ++r)
 #pragma unroll
@@ -127,22 +179,17 @@ __global__ void __launch_bounds__(kBwdWarps * kWarp, 5) k_render_bwd(const BwdAr
         const int gxp = (int)pxc[cc], gyp = (int)pyr[r];
         T[k] = 0.f; Pd[k] = 0.f;
         float4 l4 = make_float4(0.f, 0.f, 0.f, 0.f);
-        if (gxp < cam.W && gyp < cam.H) {
+        if ((alive >> k) & 1u) {
           const int pix = gyp * cam.W + gxp;
-          if ((uint32_t)lcon[pix] > thres) {
-            alive |= 1u << k;
-            const float4 prev = bi.local > 0 ? a.samples[(size_t)(b - 1) * kTilePixels + M::pix(r, cc, lane)]
-                                             : make_float4(0.f, 0.f, 0.f, 1.f);
-            l4.x = dL[pix];
-            l4.y = dL[HW + pix];
-            l4.z = dL[2 * HW + pix];
-            T[k] = prev.w;
-            Pd[k] = prev.x * l4.x + prev.y * l4.y + prev.z * l4.z;
-            // K = C_final . dL + T_final * (bg . dL): everything behind a
-            // Gaussian is K - (prefix up to and including it) . dL.
-            l4.w = pcol[pix] * l4.x + pcol[HW + pix] * l4.y + pcol[2 * HW + pix] * l4.z +
-                   Tfin[pix] * (bgr * l4.x + bgg * l4.y + bgb * l4.z);
-          }
+          l4.x = dL[pix];
+          l4.y = dL[HW + pix];
+          l4.z = dL[2 * HW + pix];
+          T[k] = pre[k].w;
+          Pd[k] = pre[k].x * l4.x + pre[k].y * l4.y + pre[k].z * l4.z;
+          // K = C_final . dL + T_final * (bg . dL): everything behind a
+          // Gaussian is K - (prefix up to and including it) . dL.
+          l4.w = pcol[pix] * l4.x + pcol[HW + pix] * l4.y + pcol[2 * HW + pix] * l4.z +
+                 Tfin[pix] * (bgr * l4.x + bgg * l4.y + bgb * l4.z);
         }
         lk[k * kWarp + lane] = l4;
       }
@@ -153,7 +200,7 @@ __global__ void __launch_bounds__(kBwdWarps * kWarp, 5) k_render_bwd(const BwdAr
       if (__any_sync(0xffffffffu, (alive >> k) & 1u)) live_sb |= 1u << k;
     if (live_sb == 0) {
       __syncwarp();
-      b = b_next;
+      q = q_next;
       continue;
     }
 
@@ -226,7 +273,7 @@ __global__ void __launch_bounds__(kBwdWarps * kWarp, 5) k_render_bwd(const BwdAr
       }
     }
     __syncwarp();
-    b = b_next;
+    q = q_next;
   }
 }
 
@@ -472,18 +519,30 @@ namespace fgs {
 fgs_status run_render_bwd(const Views& views, int64_t records, int bucket_size, const uint32_t* values_sorted,
                           const uint32_t* ranges, const float* splat, const float* Ts_final,
                           const int32_t* last_contributor, const ImageState& im, const SampleState& sm,
-                          const float* dL_dpixels, float* grad_record, cudaStream_t s) {
+                          const float* dL_dpixels, float* grad_record, bool recompute, cudaStream_t s) {
   FGS_TRY(cudaMemsetAsync(grad_record, 0, sizeof(float) * FGS_GRAD_STRIDE * (size_t)records, s));
   // backward work cursor (word 3 of the image-state header); reset on every call
   FGS_TRY(cudaMemsetAsync(im.bucket_sum + 3, 0, sizeof(uint32_t), s));
-  BwdArgs a{views, splat, values_sorted, ranges, sm.bucket_tile, im.bucket_off, im.bucket_sum, im.max_contrib,
-            sm.samples, im.pix_color, Ts_final, last_contributor, dL_dpixels, grad_record, bucket_size};
+  // recompute mode rebuilds every tile's prefix from the start
+  if (recompute) FGS_TRY(cudaMemsetAsync(im.tile_stage, 0, sizeof(uint32_t) * views.tiles, s));
+  BwdArgs a{views, splat, values_sorted, ranges, sm.bucket_tile, sm.bucket_queue, im.bucket_off, im.bucket_sum,
+            im.max_contrib, sm.samples, im.tile_stage, im.pix_color, Ts_final, last_contributor, dL_dpixels,
+            grad_record, bucket_size};
   {
     KernelTimer kt__(FGS_K_RENDER_BWD, s);
     const int nt = kBwdWarps * kWarp;
-    if (views.bx == 8) k_render_bwd<8><<<num_sms() * resident_blocks(k_render_bwd<8>, nt, 0), nt, 0, s>>>(a);
-    else if (views.bx == 16) k_render_bwd<16><<<num_sms() * resident_blocks(k_render_bwd<16>, nt, 0), nt, 0, s>>>(a);
-    else k_render_bwd<32><<<num_sms() * resident_blocks(k_render_bwd<32>, nt, 0), nt, 0, s>>>(a);
+    auto launch = [&](auto kernel) {
+      kernel<<<num_sms() * resident_blocks(kernel, nt, 0), nt, 0, s>>>(a);
+    };
+    if (recompute) {
+      if (views.bx == 8) launch(k_render_bwd<8, true>);
+      else if (views.bx == 16) launch(k_render_bwd<16, true>);
+      else launch(k_render_bwd<32, true>);
+    } else {
+      if (views.bx == 8) launch(k_render_bwd<8, false>);
+      else if (views.bx == 16) launch(k_render_bwd<16, false>);
+      else launch(k_render_bwd<32, false>);
+    }
     kt__.stop();
   }
   FGS_LAUNCH_CHECK();
@@ -517,9 +576,10 @@ extern "C" fgs_status fgs_render_bwd(int P, int width, int height, int block_x, 
   if (((uintptr_t)grad_record & 15) || ((uintptr_t)splat_buffer & 15)) return FGS_ERR_BAD_ARG;
   const Views views = single_view(width, height, block_x, block_y, nullptr, nullptr, nullptr, bg, 1.f, 1.f, 1.f, 1.f);
   const ImageState im = carve_image(const_cast<void*>(image_state), (size_t)width * height, views.tiles);
-  const SampleState sm = carve_sample(const_cast<void*>(sample_state), max_buckets > 0 ? max_buckets : 1);
+  const int64_t mb = max_buckets > 0 ? max_buckets : 1;
+  const SampleState sm = carve_sample(const_cast<void*>(sample_state), mb, mb);
   return run_render_bwd(views, P, bucket_size, values_sorted, ranges, splat_buffer, Ts_final, last_contributor, im,
-                        sm, dL_dpixels, grad_record, (cudaStream_t)stream);
+                        sm, dL_dpixels, grad_record, false, (cudaStream_t)stream);
 }
 
 extern "C" fgs_status fgs_preprocess_bwd(

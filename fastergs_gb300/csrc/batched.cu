@@ -30,7 +30,8 @@ struct BatchLayout {
   uint32_t tiles;
 };
 
-BatchLayout plan(int P, int V, const int* W, const int* H, int bx, int by, int64_t pairs, int bucket_size) {
+BatchLayout plan(int P, int V, const int* W, const int* H, int bx, int by, int64_t pairs, int bucket_size,
+                 bool recompute) {
   BatchLayout L;
   L.pairs = pairs;
   L.tiles = 0;
@@ -44,7 +45,7 @@ BatchLayout plan(int P, int V, const int* W, const int* H, int bx, int by, int64
   L.records_n = (int64_t)V * P;
   L.sort_bytes = sort_temp_bytes(pairs);
   L.image_bytes = carve_image(nullptr, (size_t)L.pixels, L.tiles).bytes;
-  L.sample_bytes = carve_sample(nullptr, L.buckets).bytes;
+  L.sample_bytes = carve_sample(nullptr, L.buckets, recompute ? (int64_t)L.tiles : L.buckets).bytes;
   size_t off = 0;
   auto take = [&](size_t bytes) {
     const size_t at = off;
@@ -72,7 +73,8 @@ BatchLayout plan(int P, int V, const int* W, const int* H, int bx, int by, int64
 
 bool config_ok(const fgs_tune_config* c) {
   return c && c->bucket_size >= 1 && c->bucket_size <= kMaxBucket && tile_shape_ok(c->block_x, c->block_y) &&
-         (c->packet == 1 || c->packet == 2 || c->packet == 4 || c->packet == 8);
+         (c->packet == 1 || c->packet == 2 || c->packet == 4 || c->packet == 8) &&
+         (c->recompute == 0 || c->recompute == 1);
 }
 
 bool cameras_ok(int V, const fgs_camera* cams) {
@@ -104,7 +106,7 @@ Views make_views(int V, const fgs_camera* cams, int bx, int by) {
 BatchLayout plan_for(int P, int V, const fgs_camera* cams, const fgs_tune_config* c, int64_t pairs) {
   std::vector<int> W(V), H(V);
   for (int v = 0; v < V; ++v) { W[v] = cams[v].width; H[v] = cams[v].height; }
-  return plan(P, V, W.data(), H.data(), c->block_x, c->block_y, pairs, c->bucket_size);
+  return plan(P, V, W.data(), H.data(), c->block_x, c->block_y, pairs, c->bucket_size, c->recompute != 0);
 }
 
 }  // namespace
@@ -167,12 +169,12 @@ extern "C" fgs_status fgs_render_batched_fwd(int P, int D, int M, const float* m
                            reinterpret_cast<uint64_t*>(ws + L.keys_s), reinterpret_cast<uint32_t*>(ws + L.vals_s), s);
   if (st != FGS_OK) return st;
   const ImageState im = carve_image(ws + L.image, (size_t)L.pixels, L.tiles);
-  const SampleState sm = carve_sample(ws + L.sample, L.buckets);
+  const SampleState sm = carve_sample(ws + L.sample, L.buckets, cfg->recompute ? (int64_t)L.tiles : L.buckets);
   return run_render_fwd(views, pair_capacity, curr, bucket_size, reinterpret_cast<float*>(ws + L.records),
                         reinterpret_cast<uint64_t*>(ws + L.keys_s), reinterpret_cast<uint32_t*>(ws + L.vals_s),
                         reinterpret_cast<uint32_t*>(ws + L.ranges), out_color,
                         reinterpret_cast<int32_t*>(ws + L.last_contrib), reinterpret_cast<float*>(ws + L.ts_final),
-                        im, sm, L.buckets, s);
+                        im, sm, L.buckets, cfg->recompute != 0, s);
 }
 
 extern "C" fgs_status fgs_render_batched_bwd(int P, int D, int M, const float* means3D, const float* dc,
@@ -202,12 +204,13 @@ extern "C" fgs_status fgs_render_batched_bwd(int P, int D, int M, const float* m
   cudaStream_t s = (cudaStream_t)stream;
   const Views views = make_views(num_views, cams, cfg->block_x, cfg->block_y);
   const ImageState im = carve_image(ws + L.image, (size_t)L.pixels, L.tiles);
-  const SampleState sm = carve_sample(ws + L.sample, L.buckets);
+  const SampleState sm = carve_sample(ws + L.sample, L.buckets, cfg->recompute ? (int64_t)L.tiles : L.buckets);
   float* grad = reinterpret_cast<float*>(ws + L.grad);
   fgs_status st = run_render_bwd(views, L.records_n, bucket_size, reinterpret_cast<uint32_t*>(ws + L.vals_s),
                                  reinterpret_cast<uint32_t*>(ws + L.ranges), reinterpret_cast<float*>(ws + L.records),
                                  reinterpret_cast<float*>(ws + L.ts_final),
-                                 reinterpret_cast<int32_t*>(ws + L.last_contrib), im, sm, dL_dpixels, grad, s);
+                                 reinterpret_cast<int32_t*>(ws + L.last_contrib), im, sm, dL_dpixels, grad,
+                                 cfg->recompute != 0, s);
   if (st != FGS_OK) return st;
   PbwdArgs a;
   a.views = views;

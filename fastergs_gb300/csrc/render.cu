@@ -225,26 +225,7 @@ struct FwdArgs {
   int bs;
 };
 
-// Waits until the tile's first `stage` buckets are folded into its prefix.
-// Lane 0 polls (bounded); the bucket it waits for was handed out earlier and
-// its warp is running, so the wait ends unless something is broken, in which
-// case the timeout bit is raised and the warp carries on.
-__device__ __forceinline__ void wait_stage(const uint32_t* tile_stage, uint32_t stage, int lane) {
-  if (lane == 0) {
-    int spins = 0;
-    while (ld_acquire_u32(tile_stage) < stage) {
-      if (++spins > kSpinLimit) {
-        raise_error(kErrTimeout);
-        break;
-      }
-      if (spins > 64) __nanosleep(128);
-    }
-  }
-  __syncwarp();
-  (void)ld_acquire_u32(tile_stage);  // every lane acquires the folded prefix
-}
-
-template <int BX>
+template <int BX, bool RECOMPUTE>
 __global__ void __launch_bounds__(kFwdWarps * kWarp, 8) k_render_fwd(const FwdArgs a) {
   using M = TileMap<BX>;
   constexpr int BY = kTilePixels / BX;
@@ -272,49 +253,16 @@ __global__ void __launch_bounds__(kFwdWarps * kWarp, 8) k_render_fwd(const FwdAr
     }
 
     float T[kPxPerThread], Cr[kPxPerThread], Cg[kPxPerThread], Cb[kPxPerThread];
-#pragma unroll
-    for (int k = 0; k < kPxPerThread; ++k) { T[k] = 1.f; Cr[k] = 0.f; Cg[k] = 0.f; Cb[k] = 0.f; }
-    if (spec != 0u) {
-      stage_bucket<BX>(st, a.splat, a.vals + bi.start, bi.n, lane, tx0, ty0);
+    if (spec != 0u) stage_bucket<BX>(st, a.splat, a.vals + bi.start, bi.n, lane, tx0, ty0);
+    {
       float pxc[M::kCols], pyr[M::kRows];
 #pragma unroll
       for (int c = 0; c < M::kCols; ++c) pxc[c] = (float)(tx0 + 8 * c + (lane & 7));
 #pragma unroll
       for (int r = 0; r < M::kRows; ++r) pyr[r] = (float)(ty0 + 4 * r + (lane >> 3));
-      for (int g = 0; g < bi.n; ++g) {
-        const uint32_t mask = st.mask[g] & spec;
-        if (mask == 0) continue;  // alpha < 1/256 on every live sub-block
-        const float4 pos = st.pos[g];
-        const float4 q4 = st.quad[g];   // A1, P, C1, log2 o
-        const float4 c = st.rgb[g];
-        float dx[M::kCols];
-#pragma unroll
-        for (int cc = 0; cc < M::kCols; ++cc) dx[cc] = centre_offset(pos.x, pos.z, pxc[cc]);
-#pragma unroll
-        for (int r = 0; r < M::kRows; ++r) {
-          const uint32_t rm = (mask >> (r * M::kCols)) & ((1u << M::kCols) - 1u);
-          if (rm == 0) continue;
-          const float dy = centre_offset(pos.y, pos.w, pyr[r]);
-          const float f = fmaf(q4.z * dy, dy, q4.w);  // log2 o + C1 dy^2
-#pragma unroll
-          for (int cc = 0; cc < M::kCols; ++cc) {
-            if (!((rm >> cc) & 1u)) continue;
-            const int k = r * M::kCols + cc;
-            // alpha = o * exp(-q/2) = 2^(log2 o + A1 (dx + P dy)^2 + C1 dy^2)
-            const float w = fmaf(q4.y, dy, dx[cc]);
-            const float e = fmaf(q4.x * w, w, f);
-            float al = fminf(kAlphaMax, ex2_approx(e));
-            al = al < kAlphaCut ? 0.f : al;
-            const float wt = al * T[k];
-            Cr[k] = fmaf(c.x, wt, Cr[k]);
-            Cg[k] = fmaf(c.y, wt, Cg[k]);
-            Cb[k] = fmaf(c.z, wt, Cb[k]);
-            T[k] = fmaf(-al, T[k], T[k]);  // T (1 - alpha), rounded once
-          }
-        }
-      }
-      __syncwarp();
+      composite_bucket<BX>(st, bi.n, spec, pxc, pyr, T, Cr, Cg, Cb);
     }
+    __syncwarp();
 
     // Fold into the tile's prefix (FB's merge, render.cu:285-391, per pixel
     // and in bucket order): C += T_prefix * C_b, T_prefix *= T_b; a pixel
@@ -327,8 +275,8 @@ __global__ void __launch_bounds__(kFwdWarps * kWarp, 8) k_render_fwd(const FwdAr
     const int contrib = min(ntile, (bi.local + 1) * a.bs);
     const uint32_t prev_w = (bi.local > 0 && lane < kPxPerThread) ? ld_volatile_u32(alive_words + lane) : 0u;
     const size_t HW = (size_t)cam.W * cam.H;
-    float4* out = a.samples + (size_t)b * kTilePixels;
-    const float4* prev = a.samples + (size_t)(b - 1) * kTilePixels;
+    float4* out = a.samples + (size_t)(RECOMPUTE ? bi.tile : b) * kTilePixels;
+    const float4* prev = RECOMPUTE ? out : a.samples + (size_t)(b - 1) * kTilePixels;
     bool any_before = false, any_after = false;
     uint32_t my_word = 0;
 #pragma unroll
@@ -373,9 +321,7 @@ __global__ void __launch_bounds__(kFwdWarps * kWarp, 8) k_render_fwd(const FwdAr
       }
     if (lane < kPxPerThread) st_volatile_u32(alive_words + lane, my_word);
     if (lane == 0 && any_before && !any_after) a.max_contrib[bi.tile] = (uint32_t)contrib;
-    __threadfence();
-    __syncwarp();
-    if (lane == 0) st_release_u32(stage_word, (uint32_t)bi.local + 1u);
+    publish_stage(stage_word, (uint32_t)bi.local + 1u, lane);
     q = q_next;
   }
 }
@@ -402,7 +348,8 @@ fgs_status run_tile_ranges(int64_t n_cap, const int32_t* n_dev, uint32_t tiles, 
 fgs_status run_render_fwd(const Views& views, int64_t n_cap, const int32_t* n_dev, int bucket_size,
                           const float* splat, const uint64_t* keys_sorted, const uint32_t* values_sorted,
                           uint32_t* ranges, float* out_color, int32_t* last_contributor, float* Ts_final,
-                          const ImageState& im, const SampleState& sm, int64_t max_buckets, cudaStream_t s) {
+                          const ImageState& im, const SampleState& sm, int64_t max_buckets, bool recompute,
+                          cudaStream_t s) {
   fgs_status st = run_tile_ranges(n_cap, n_dev, views.tiles, keys_sorted, ranges, s);
   if (st != FGS_OK) return st;
   {
@@ -421,9 +368,18 @@ fgs_status run_render_fwd(const Views& views, int64_t n_cap, const int32_t* n_de
   {
     KernelTimer kt__(FGS_K_RENDER_FWD, s);
     const int nt = kFwdWarps * kWarp;
-    if (views.bx == 8) k_render_fwd<8><<<num_sms() * resident_blocks(k_render_fwd<8>, nt, 0), nt, 0, s>>>(fa);
-    else if (views.bx == 16) k_render_fwd<16><<<num_sms() * resident_blocks(k_render_fwd<16>, nt, 0), nt, 0, s>>>(fa);
-    else k_render_fwd<32><<<num_sms() * resident_blocks(k_render_fwd<32>, nt, 0), nt, 0, s>>>(fa);
+    auto launch = [&](auto kernel) {
+      kernel<<<num_sms() * resident_blocks(kernel, nt, 0), nt, 0, s>>>(fa);
+    };
+    if (recompute) {  // samples hold one running prefix per tile
+      if (views.bx == 8) launch(k_render_fwd<8, true>);
+      else if (views.bx == 16) launch(k_render_fwd<16, true>);
+      else launch(k_render_fwd<32, true>);
+    } else {
+      if (views.bx == 8) launch(k_render_fwd<8, false>);
+      else if (views.bx == 16) launch(k_render_fwd<16, false>);
+      else launch(k_render_fwd<32, false>);
+    }
     kt__.stop();
   }
   FGS_LAUNCH_CHECK();
@@ -461,7 +417,8 @@ extern "C" fgs_status fgs_state_bytes(int width, int height, int block_x, int bl
   if (width <= 0 || height <= 0 || block_x <= 0 || block_y <= 0 || max_buckets < 0) return FGS_ERR_BAD_ARG;
   const size_t T = (size_t)((width + block_x - 1) / block_x) * ((height + block_y - 1) / block_y);
   if (image_bytes) *image_bytes = carve_image(nullptr, (size_t)width * height, T).bytes;
-  if (sample_bytes) *sample_bytes = carve_sample(nullptr, std::max<int64_t>(max_buckets, 1)).bytes;
+  const int64_t mb = std::max<int64_t>(max_buckets, 1);
+  if (sample_bytes) *sample_bytes = carve_sample(nullptr, mb, mb).bytes;
   return FGS_OK;
 }
 
@@ -483,12 +440,13 @@ extern "C" fgs_status fgs_render_fwd(int P, int64_t num_rendered, int width, int
     return FGS_ERR_BAD_ARG;
   const Views views = single_view(width, height, block_x, block_y, nullptr, nullptr, nullptr, bg, 1.f, 1.f, 1.f, 1.f);
   const ImageState im = carve_image(image_state, (size_t)width * height, views.tiles);
-  const SampleState sm = carve_sample(sample_state, std::max<int64_t>(max_buckets, 1));
+  const int64_t mb = std::max<int64_t>(max_buckets, 1);
+  const SampleState sm = carve_sample(sample_state, mb, mb);
   if (image_bytes < im.bytes || sample_bytes < sm.bytes) return FGS_ERR_CAPACITY;
   cudaStream_t s = (cudaStream_t)stream;
   const fgs_status st = run_render_fwd(views, num_rendered, nullptr, bucket_size, splat_buffer, keys_sorted,
                                        values_sorted, ranges, out_color, last_contributor, Ts_final, im, sm,
-                                       max_buckets, s);
+                                       max_buckets, false, s);
   if (st != FGS_OK) return st;
   if (bucket_sum_host) {
     uint32_t hs[2] = {0, 0};

@@ -63,13 +63,15 @@ inline ImageState carve_image(void* base, size_t pixels, size_t T) {
   return s;
 }
 
-inline SampleState carve_sample(void* base, int64_t max_buckets) {
+// slots: prefix samples kept -- one per bucket (stored for the backward) or,
+// in recompute mode, one per tile (the running prefix, rebuilt by the backward).
+inline SampleState carve_sample(void* base, int64_t max_buckets, int64_t slots) {
   char* p = static_cast<char*>(base);
   SampleState s;
   size_t off = 0;
   s.bucket_tile = reinterpret_cast<uint32_t*>(p + off); off = align_up(off + sizeof(uint32_t) * (size_t)max_buckets, 256);
   s.bucket_queue = reinterpret_cast<uint32_t*>(p + off); off = align_up(off + sizeof(uint32_t) * (size_t)max_buckets, 256);
-  s.samples = reinterpret_cast<float4*>(p + off);       off = align_up(off + sizeof(float4) * kTilePixels * (size_t)max_buckets, 256);
+  s.samples = reinterpret_cast<float4*>(p + off);       off = align_up(off + sizeof(float4) * kTilePixels * (size_t)slots, 256);
   s.bytes = off;
   return s;
 }
@@ -143,6 +145,82 @@ __device__ __forceinline__ float centre_offset(float whole, float frac, float pi
   return (whole - pixel) + frac;
 }
 
+// Composites a staged bucket front to back from T = 1, C = 0 for this lane's
+// 8 pixels, restricted to the sub-blocks in `live` (FB renderBucket,
+// render.cu:285-391): alpha = min(0.99, o 2^e), dropped below 1/255.
+// Skipped (Gaussian, sub-block) pairs have alpha < 1/256 everywhere and would
+// leave C and T bit-for-bit unchanged.
+template <int BX>
+__device__ __forceinline__ void composite_bucket(const BucketStage& st, int n, uint32_t live,
+                                                 const float (&pxc)[TileMap<BX>::kCols],
+                                                 const float (&pyr)[TileMap<BX>::kRows], float (&T)[kPxPerThread],
+                                                 float (&Cr)[kPxPerThread], float (&Cg)[kPxPerThread],
+                                                 float (&Cb)[kPxPerThread]) {
+  using M = TileMap<BX>;
+#pragma unroll
+  for (int k = 0; k < kPxPerThread; ++k) { T[k] = 1.f; Cr[k] = 0.f; Cg[k] = 0.f; Cb[k] = 0.f; }
+  if (live == 0u) return;
+  for (int g = 0; g < n; ++g) {
+    const uint32_t mask = st.mask[g] & live;
+    if (mask == 0) continue;  // alpha < 1/256 on every live sub-block
+    const float4 pos = st.pos[g];
+    const float4 q4 = st.quad[g];   // A1, P, C1, log2 o
+    const float4 c = st.rgb[g];
+    float dx[M::kCols];
+#pragma unroll
+    for (int cc = 0; cc < M::kCols; ++cc) dx[cc] = centre_offset(pos.x, pos.z, pxc[cc]);
+#pragma unroll
+    for (int r = 0; r < M::kRows; ++r) {
+      const uint32_t rm = (mask >> (r * M::kCols)) & ((1u << M::kCols) - 1u);
+      if (rm == 0) continue;
+      const float dy = centre_offset(pos.y, pos.w, pyr[r]);
+      const float f = fmaf(q4.z * dy, dy, q4.w);  // log2 o + C1 dy^2
+#pragma unroll
+      for (int cc = 0; cc < M::kCols; ++cc) {
+        if (!((rm >> cc) & 1u)) continue;
+        const int k = r * M::kCols + cc;
+        // alpha = o * exp(-q/2) = 2^(log2 o + A1 (dx + P dy)^2 + C1 dy^2)
+        const float w = fmaf(q4.y, dy, dx[cc]);
+        const float e = fmaf(q4.x * w, w, f);
+        float al = fminf(kAlphaMax, ex2_approx(e));
+        al = al < kAlphaCut ? 0.f : al;
+        const float wt = al * T[k];
+        Cr[k] = fmaf(c.x, wt, Cr[k]);
+        Cg[k] = fmaf(c.y, wt, Cg[k]);
+        Cb[k] = fmaf(c.z, wt, Cb[k]);
+        T[k] = fmaf(-al, T[k], T[k]);  // T (1 - alpha), rounded once
+      }
+    }
+  }
+}
+
+// Waits until a tile's first `stage` buckets are folded into its prefix.
+// Lane 0 polls (bounded); the bucket it waits for was handed out earlier and
+// its warp is running, so the wait ends unless something is broken, in which
+// case the timeout bit is raised and the warp carries on.
+__device__ __forceinline__ void wait_stage(const uint32_t* tile_stage, uint32_t stage, int lane) {
+  if (lane == 0) {
+    int spins = 0;
+    while (ld_acquire_u32(tile_stage) < stage) {
+      if (++spins > kSpinLimit) {
+        raise_error(kErrTimeout);
+        break;
+      }
+      if (spins > 64) __nanosleep(128);
+    }
+  }
+  __syncwarp();
+  (void)ld_acquire_u32(tile_stage);  // every lane acquires the folded prefix
+}
+
+// Publishes that the tile's first `stage` buckets are folded (after every
+// lane's prefix stores).
+__device__ __forceinline__ void publish_stage(uint32_t* tile_stage, uint32_t stage, int lane) {
+  __threadfence();
+  __syncwarp();
+  if (lane == 0) st_release_u32(tile_stage, stage);
+}
+
 // Dynamic bucket scheduling for the persistent compositing kernels: every
 // warp takes the next unprocessed bucket from a device cursor, so buckets of
 // very different cost balance across SMs.  Lane 0 fetches; the next index is
@@ -192,14 +270,19 @@ __device__ __forceinline__ BucketInfo bucket_info(int b, const uint32_t* __restr
 // Launch sequences shared by the plain and the batched entry points.
 // Forward: tile ranges, bucket setup, persistent composite, merge.  n_dev,
 // when given, is the device-side pair count (clamped to n_cap).
+// recompute: the sample state holds one running prefix per tile instead of
+// one prefix per bucket (carve_sample with slots = tiles).
 fgs_status run_render_fwd(const Views& views, int64_t n_cap, const int32_t* n_dev, int bucket_size,
                           const float* splat, const uint64_t* keys_sorted, const uint32_t* values_sorted,
                           uint32_t* ranges, float* out_color, int32_t* last_contributor, float* Ts_final,
-                          const ImageState& im, const SampleState& sm, int64_t max_buckets, cudaStream_t s);
+                          const ImageState& im, const SampleState& sm, int64_t max_buckets, bool recompute,
+                          cudaStream_t s);
 // Backward composite into grad_record (records x FGS_GRAD_STRIDE, zeroed here).
+// In recompute mode every needed bucket's prefix is rebuilt from the tile's
+// running prefix, in bucket order per tile.
 fgs_status run_render_bwd(const Views& views, int64_t records, int bucket_size, const uint32_t* values_sorted,
                           const uint32_t* ranges, const float* splat, const float* Ts_final,
                           const int32_t* last_contributor, const ImageState& im, const SampleState& sm,
-                          const float* dL_dpixels, float* grad_record, cudaStream_t s);
+                          const float* dL_dpixels, float* grad_record, bool recompute, cudaStream_t s);
 
 }  // namespace fgs

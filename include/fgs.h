@@ -215,16 +215,22 @@ typedef struct {
 } fgs_camera;
 
 /* Launch configuration picked by the autotuner; FB's fixed choice is
- * {128, 16, 16, 4}.  bucket_size 1..128 Gaussians per bucket; tile 16x16,
+ * {128, 16, 16, 4, 0}.  bucket_size 1..128 Gaussians per bucket; tile 16x16,
  * 8x32 or 32x8 pixels; packet 1, 2, 4 or 8: footprints of at least
  * 32*packet tiles are split into sub-tasks of 32*packet tiles, smaller ones
  * are lane-packed by the preprocess warps.  The tile shape and the bucket
  * size change images at the level of the T < 1e-4 stopping rule (which acts
- * per bucket); packet changes only the order in which pairs are emitted. */
+ * per bucket); packet changes only the order in which pairs are emitted.
+ * recompute 1: the forward keeps one running (colour, transmittance) prefix
+ * per tile instead of one per bucket (4 KB per bucket), and the backward
+ * rebuilds each bucket's prefix from it -- bit-identical prefixes, a
+ * workspace smaller by about 4 KB per bucket, one extra compositing pass over
+ * the needed buckets. */
 typedef struct {
   int bucket_size;
   int block_x, block_y;
   int packet;
+  int recompute;
 } fgs_tune_config;
 
 /* Workspace bytes (256-byte aligned base required) of a batched frame. */

@@ -352,3 +352,34 @@ def test_tuned_backward_matches_oracle_replay(setup, tune):
         b = ref[key].reshape(s.P, -1)
         errs[key] = _rel(a, b)
     assert max(errs.values()) <= 1e-4, errs
+
+
+@pytest.mark.parametrize("tune", [TuneConfig(128, 16, 16, 4, True), TuneConfig(32, 8, 32, 2, True)],
+                         ids=["b128_16x16", "b32_8x32"])
+def test_recompute_mode_matches_store_mode(setup, tune):
+    """Recompute mode keeps one running prefix per tile and rebuilds every
+    bucket's prefix in the backward: the same images (the forward folds the
+    same values) and the same gradients up to the order of float reductions,
+    from a workspace smaller by ~4 KB per bucket."""
+    s, T, cams, sets = setup
+    dev = T["means"].device
+    store_cfg = TuneConfig(tune.bucket_size, tune.block_x, tune.block_y, tune.packet, False)
+    r_store, _ = _batched(T, sets, tune=store_cfg)
+    ties = _flat_mask(r_store, _tie_masks(r_store))
+    dL = torch.randn(r_store.out_color.numel(), device=dev, generator=torch.Generator(device=dev).manual_seed(5))
+    dL[ties] = 0.0
+    st = [torch.zeros((s.P, 1), device=dev) for _ in range(4)]
+    rr = [torch.zeros((s.P, 1), device=dev) for _ in range(4)]
+    kw = lambda x: dict(xyz_gradient_accum=x[0], xyz_gradient_accum_abs=x[1], max_radii=x[2], denom=x[3])
+    g_store = r_store.backward(dL, T["means"], T["dc"], T["shs"], T["scales"], T["rotations"], 3, **kw(st))
+    img_store = r_store.out_color.clone()
+    r_rec, _ = _batched(T, sets, tune=tune)
+    assert r_rec.workspace.numel() < r_store.workspace.numel()
+    g_rec = r_rec.backward(dL, T["means"], T["dc"], T["shs"], T["scales"], T["rotations"], 3, **kw(rr))
+    torch.cuda.synchronize()
+    assert _C.device_errors(dev) == 0
+    assert (r_rec.out_color - img_store).abs()[~ties].max().item() == 0.0
+    for k in ("means3D", "opacities", "dc", "shs", "scales", "rotations"):
+        assert _rel(g_rec[k].cpu().numpy(), g_store[k].cpu().numpy()) <= 1e-5, k
+    for a, b in zip(rr, st):
+        assert _rel(a.cpu().numpy(), b.cpu().numpy()) <= 1e-5
