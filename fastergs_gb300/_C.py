@@ -242,3 +242,127 @@ def device_errors(dev: torch.device | None = None, clear: bool = True) -> int:
 ops = SimpleNamespace(preprocess=preprocess, sort_gaussian=sort_gaussian,
                       get_sort_buffer_size=get_sort_buffer_size, render_16x16=render_16x16, backward=backward,
                       adamUpdate=adamUpdate, render_simp=render_simp, render_depth=render_depth)
+
+
+# ---------------------------------------------------------------------------------------------------------
+# The vanilla 3DGS extension's entry points (gs_submodules/diff-gaussian-rasterization/ext.cpp:16-17,
+# rasterize_points.h:18-59) over the same C ABI: vanilla tensor layouts (sh (P, 16, 3) with the DC term
+# first, dL/dmeans2D (P, 3), dL/dsh (P, 16, 3)), FB's rasterization (bucket-granular stopping, ellipse tile
+# test).  The three opaque buffers carry the forward state to the backward:
+#   geomBuffer    float32 (P, 32): splat records;
+#   binningBuffer int32 [sorted record ids (R) | tile ranges (2 T)];
+#   imageBuffer   uint8 [image state | sample state | last contributor (H W) | final transmittance (H W)].
+_ALIAS_CAP: dict = {}
+
+
+def _align(v: int, a: int = 256) -> int:
+    return (v + a - 1) // a * a
+
+
+def _image_layout(R: int, W: int, H: int):
+    mb, ib, sb = state_sizes(R, W, H, TILE, TILE, BUCKET)
+    mb = max(mb, 1)
+    sbytes = (mb + 1) * _SAMPLE_ROW
+    off_smp = _align(ib)
+    off_lc = _align(off_smp + sbytes)
+    off_ts = _align(off_lc + 4 * W * H)
+    return mb, ib, sbytes, off_smp, off_lc, off_ts, off_ts + 4 * W * H
+
+
+def _split_sh(sh, dev):
+    if sh is None or sh.numel() == 0:
+        return torch.empty(0), torch.empty(0)
+    sh = _f32("sh", sh, dev)
+    return sh[:, :1].contiguous(), sh[:, 1:].contiguous()
+
+
+def rasterize_gaussians(background, means3D, colors, opacity, scales, rotations, scale_modifier, cov3D_precomp,
+                        viewmatrix, projmatrix, tan_fovx, tan_fovy, image_height, image_width, sh, degree, campos,
+                        prefiltered, debug):
+    """Vanilla RasterizeGaussiansCUDA (rasterize_points.h:18-37): returns
+    (num_rendered, color (3, H, W), radii (P,), geomBuffer, binningBuffer, imageBuffer)."""
+    if cov3D_precomp is not None and cov3D_precomp.numel():
+        raise NotImplementedError("precomputed 3D covariances are not supported (FB needs scales and rotations)")
+    dev = _device_of(means3D)
+    P, W, H = int(means3D.size(0)), int(image_width), int(image_height)
+    dc, rest = _split_sh(sh, dev)
+    T = ((W + TILE - 1) // TILE) * ((H + TILE - 1) // TILE)
+    geom = torch.empty((max(P, 1), 32), dtype=torch.float32, device=dev)
+    curr = torch.zeros(1, dtype=torch.int32, device=dev)
+    key = (dev.type, dev.index)
+    cap = _ALIAS_CAP.get(key, 1 << 22)
+    while True:
+        keys_u = torch.empty(cap, dtype=torch.int64, device=dev)
+        vals_u = torch.empty(cap, dtype=torch.int32, device=dev)
+        tasks = torch.empty(cap, dtype=torch.int32, device=dev)
+        curr.zero_()
+        radii = preprocess(int(degree), means3D, colors, dc, rest, opacity, scales, rotations, scale_modifier, W, H,
+                           TILE, TILE, campos, viewmatrix, projmatrix, tan_fovx, tan_fovy, 100.0, 0.01, keys_u,
+                           vals_u, tasks, curr, 1.0, geom, None)
+        R = int(curr.item())
+        errors = device_errors(dev)
+        if R < cap and not errors:
+            break
+        cap = max(2 * cap, 2 * R)  # pairs or large-footprint sub-tasks did not fit: grow and redo
+        _ALIAS_CAP[key] = cap
+    binning = torch.empty(R + 2 * T, dtype=torch.int32, device=dev)
+    keys_s = torch.empty(max(R, 1), dtype=torch.int64, device=dev)
+    tmp = torch.empty(int(_lib.load().fgs_sort_temp_bytes(max(R, 1))), dtype=torch.uint8, device=dev)
+    s = _stream(dev)
+    if R:
+        _lib.call("fgs_sort", R, W, H, TILE, TILE, _ptr(tmp), tmp.numel(), _ptr(keys_u), _ptr(vals_u), _ptr(keys_s),
+                  _ptr(binning), s)
+    mb, ib, sbytes, off_smp, off_lc, off_ts, total = _image_layout(R, W, H)
+    image = torch.empty(total, dtype=torch.uint8, device=dev)
+    bg = _f32("background", background, dev)
+    color = torch.empty((3, H, W), dtype=torch.float32, device=dev)
+    base = image.data_ptr()
+    _lib.call("fgs_render_fwd", P, R, W, H, TILE, TILE, BUCKET, _ptr(geom), _ptr(keys_s), _ptr(binning),
+              binning.data_ptr() + 4 * R, _ptr(bg), _ptr(color), base + off_lc, base + off_ts, base, ib,
+              base + off_smp, sbytes, mb, None, s)
+    return R, color, radii, geom, binning, image
+
+
+def rasterize_gaussians_backward(background, means3D, radii, colors, scales, rotations, scale_modifier,
+                                 cov3D_precomp, viewmatrix, projmatrix, tan_fovx, tan_fovy, dL_dout_color, sh, degree,
+                                 campos, geomBuffer, R, binningBuffer, imageBuffer, debug):
+    """Vanilla RasterizeGaussiansBackwardCUDA (rasterize_points.h:39-59): returns
+    (dL_dmeans2D (P, 3), dL_dcolors, dL_dopacity, dL_dmeans3D, dL_dcov3D, dL_dsh (P, 16, 3), dL_dscales,
+    dL_drotations)."""
+    if cov3D_precomp is not None and cov3D_precomp.numel():
+        raise NotImplementedError("precomputed 3D covariances are not supported (FB needs scales and rotations)")
+    dev = _device_of(means3D)
+    P, R = int(means3D.size(0)), int(R)
+    dL = _f32("dL_dout_color", dL_dout_color, dev)
+    H, W = int(dL.size(1)), int(dL.size(2))
+    dc, rest = _split_sh(sh, dev)
+    M = rest.size(1) if rest.numel() else 0
+    f = dict(dtype=torch.float32, device=dev)
+    out = dict(dmean2D=torch.empty((P, 4), **f), dconic=torch.empty((P, 4), **f), dopac=torch.empty((P, 1), **f),
+               dcolor=torch.empty((P, 3), **f), dmean3D=torch.empty((P, 3), **f), dcov3D=torch.empty((P, 6), **f),
+               ddc=torch.empty((P, 1, 3), **f), dsh=torch.empty((P, M, 3), **f), dscale=torch.empty((P, 3), **f),
+               drot=torch.empty((P, 4), **f))
+    if P:
+        mb, ib, sbytes, off_smp, off_lc, off_ts, total = _image_layout(R, W, H)
+        if imageBuffer.numel() < total or binningBuffer.numel() < R:
+            raise ValueError("imageBuffer / binningBuffer do not match num_rendered and the image size")
+        base = imageBuffer.data_ptr()
+        bg = _f32("background", background, dev)
+        grad = torch.empty((P, 12), **f)
+        s = _stream(dev)
+        _lib.call("fgs_render_bwd", P, W, H, TILE, TILE, BUCKET, _ptr(binningBuffer), binningBuffer.data_ptr() + 4 * R,
+                  _ptr(bg), _ptr(geomBuffer), base + off_ts, base + off_lc, base, base + off_smp, mb, _ptr(dL),
+                  _ptr(grad), s)
+        _lib.call("fgs_preprocess_bwd", P, int(degree), int(M), _ptr(_f32("means3D", means3D, dev)), _ptr(radii),
+                  _ptr(dc), _ptr(rest), _ptr(geomBuffer), _ptr(_f32("scales", scales, dev)),
+                  _ptr(_f32("rotations", rotations, dev)), float(scale_modifier),
+                  _ptr(_f32("viewmatrix", viewmatrix, dev)), _ptr(_f32("projmatrix", projmatrix, dev)), W, H,
+                  float(tan_fovx), float(tan_fovy), _ptr(_f32("campos", campos, dev)), _ptr(grad),
+                  _ptr(out["dmean2D"]), _ptr(out["dconic"]), _ptr(out["dopac"]), _ptr(out["dcolor"]),
+                  _ptr(out["dmean3D"]), _ptr(out["dcov3D"]), _ptr(out["ddc"]), _ptr(out["dsh"]),
+                  _ptr(out["dscale"]), _ptr(out["drot"]), 0, 0, 0, 0, s)
+    dmeans2D = torch.zeros((P, 3), **f)
+    dmeans2D[:, :2] = out["dmean2D"][:, :2]
+    has_sh = sh is not None and sh.numel() != 0
+    dsh = torch.cat([out["ddc"], out["dsh"]], dim=1) if has_sh else torch.empty(0, **f)
+    return (dmeans2D, out["dcolor"], out["dopac"], out["dmean3D"], out["dcov3D"], dsh, out["dscale"], out["drot"])

@@ -30,6 +30,7 @@ from . import _lib
 from ._C import _f32, _ptr, _stream
 
 MAX_VIEWS = 32
+MAX_PAIRS = (1 << 30) - 2  # the sort's look-back words carry 30-bit counts
 
 
 @dataclass(frozen=True)
@@ -124,7 +125,7 @@ class BatchedRasterizer:
     def _default_capacity(self) -> int:
         # about 4 pairs per Gaussian and camera at 1 MP, scaled by pixel count; fit() refines it
         mp = self.pix_off[-1] / 1e6
-        return int(max(1 << 20, min((1 << 31) - 1, 4 * self.P * max(mp, 1.0))))
+        return int(max(1 << 20, min(MAX_PAIRS, 4 * self.P * max(mp, 1.0))))
 
     def workspace_bytes(self, pair_capacity: int) -> int:
         out = C.c_size_t(0)
@@ -134,7 +135,7 @@ class BatchedRasterizer:
 
     def plan(self, pair_capacity: int) -> None:
         """(Re)allocate the workspace for up to pair_capacity pairs per frame."""
-        pair_capacity = int(min(max(pair_capacity, 1), (1 << 31) - 1))
+        pair_capacity = int(min(max(pair_capacity, 1), MAX_PAIRS))
         nbytes = self.workspace_bytes(pair_capacity)
         self.workspace = None
         self.workspace = torch.empty(nbytes, dtype=torch.uint8, device=self.device)

@@ -18,9 +18,8 @@
 namespace fgs {
 namespace {
 
-// Pair counts travel as uint32 on the device (the emission cursor) and
-// bucket counts as uint32 as well.
-constexpr int64_t kMaxBatchPairs = (int64_t)1 << 31;
+// Largest pair capacity: the sort's look-back words carry 30-bit counts.
+constexpr int64_t kMaxBatchPairs = ((int64_t)1 << 30) - 2;
 
 struct BatchLayout {
   size_t counters, curr, records, keys_u, vals_u, keys_s, vals_s, tasks, sort_tmp, ranges, image, sample, grad,

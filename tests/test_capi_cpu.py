@@ -58,3 +58,58 @@ def test_bad_arguments_are_rejected_without_touching_the_gpu(lib):
     assert lib.fgs_render_fwd(1, 10, 256, 256, 16, 8, 128, *([None] * 9), 0, None, 0, 10, None, None) == 1
     assert lib.fgs_render_bwd(1, 256, 256, 16, 16, 0, *([None] * 8), 0, None, None, None) == 1
     assert lib.fgs_adam_update(None, None, None, None, None, 0.1, 0.9, 0.999, 1e-8, 10, 0, None) == 1
+
+
+def _cams(sizes):
+    from fastergs_gb300 import _lib
+    arr = (_lib.Camera * len(sizes))()
+    for c, (w, h) in zip(arr, sizes):
+        # device pointers are never dereferenced by the sizing call; any non-null value will do
+        c.viewmatrix = c.projmatrix = c.campos = c.bg = 256
+        c.width, c.height = w, h
+        c.tan_fovx = c.tan_fovy = 0.5
+        c.scale_modifier = c.mult = 1.0
+    return arr
+
+
+def _ws(P, sizes, cfg, pairs):
+    import ctypes as C
+    from fastergs_gb300 import _lib
+    out = C.c_size_t(0)
+    st = _lib.load().fgs_batch_workspace_bytes(P, len(sizes), _cams(sizes), C.byref(cfg), pairs, C.byref(out))
+    return st, int(out.value)
+
+
+def test_batch_workspace_sizing_and_validation():
+    from fastergs_gb300 import _lib
+    sizes = [(1297, 840), (640, 360), (1920, 1080)]
+    fb = _lib.TuneConfig(128, 16, 16, 4, 0)
+    st, small = _ws(100_000, sizes, fb, 1 << 20)
+    assert st == 0 and small > 0
+    st, big = _ws(100_000, sizes, fb, 1 << 22)
+    assert st == 0 and big > small
+    st, rec = _ws(100_000, sizes, _lib.TuneConfig(128, 16, 16, 4, 1), 1 << 22)
+    assert st == 0 and rec < big  # one prefix per tile instead of per bucket
+    st, b16 = _ws(100_000, sizes, _lib.TuneConfig(16, 8, 32, 2, 0), 1 << 22)
+    assert st == 0 and b16 > big  # eight times the buckets
+    for cfg in (_lib.TuneConfig(0, 16, 16, 4, 0), _lib.TuneConfig(129, 16, 16, 4, 0),
+                _lib.TuneConfig(64, 8, 16, 4, 0), _lib.TuneConfig(64, 16, 16, 3, 0), _lib.TuneConfig(64, 16, 16, 4, 2)):
+        assert _ws(1000, sizes, cfg, 1 << 20)[0] == 1  # FGS_ERR_BAD_ARG
+    assert _ws(1000, [], fb, 1 << 20)[0] == 1
+    assert _ws(1000, [(64, 64)] * 33, fb, 1 << 20)[0] == 1
+    assert _ws(1000, sizes, fb, 1 << 30)[0] == 2  # FGS_ERR_CAPACITY: beyond the sort's 30-bit counts
+
+
+def test_tuner_search_space_and_cache_key():
+    from fastergs_gb300 import tune
+    from fastergs_gb300.batched import TuneConfig
+    space = tune.search_space()
+    assert len(space) == 18 and len(set(space)) == 18
+    assert {c.bucket_size for c in space} == {16, 32, 64}
+    assert {(c.block_x, c.block_y) for c in space} == {(16, 16), (8, 32)}
+    assert {c.packet for c in space} == {2, 4, 8}
+    assert TuneConfig() == TuneConfig(128, 16, 16, 4, False)  # FB's fixed choice
+    k1 = tune.cache_key(1_000_000, [(840, 1297), (360, 640)], 3, True)
+    assert k1 == tune.cache_key(600_000, [(840, 1297), (360, 640)], 3, True)  # same power-of-two range
+    assert k1 != tune.cache_key(1_000_000, [(840, 1297), (360, 640)], 3, False)
+    assert k1 != tune.cache_key(3_000_000, [(840, 1297), (360, 640)], 3, True)

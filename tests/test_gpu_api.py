@@ -163,3 +163,41 @@ def test_gradients_match_fp64_finite_differences(cuda_device):
         an = np.array([b for _, b in pairs])
         tol = 1e-4 * np.abs(fd) + 1e-4 * np.abs(fd).max()
         assert np.all(np.abs(an - fd) <= tol), (gi, np.max(np.abs(an - fd) / (np.abs(fd) + 1e-12)))
+
+
+def test_vanilla_rasterize_gaussians_alias(cuda_device):
+    """_C.rasterize_gaussians / rasterize_gaussians_backward take the vanilla
+    extension's layouts (sh (P, 1 + M, 3) with DC first, dL/dmeans2D (P, 3))
+    and give the drop-in path's image, radii and gradients."""
+    from fastergs_gb300 import _C
+    s = scenes.scene_c5a()
+    dev = cuda_device
+    st = settings_for(s.camera, dev, s.sh_degree, bg=(0.1, 0.2, 0.3))
+    m, sc, rot, op, dc, shs = s.activated()
+    t = lambda a: torch.tensor(np.ascontiguousarray(a), device=dev)
+    leaves = {k: t(v).requires_grad_(True) for k, v in dict(means=m, scales=sc, rotations=rot, opacities=op, dc=dc,
+                                                             shs=shs).items()}
+    img, radii = GaussianRasterizer(st)(means3D=leaves["means"], opacities=leaves["opacities"], dc=leaves["dc"],
+                                        shs=leaves["shs"], scales=leaves["scales"], rotations=leaves["rotations"])
+    dL = t(scenes.upstream_grad(3, s.camera.height, s.camera.width))
+    torch.autograd.backward(img, grad_tensors=dL)
+    empty = torch.empty(0, device=dev)
+    sh_full = torch.cat([t(dc), t(shs)], dim=1)
+    R, color, radii2, geom, binning, image = _C.rasterize_gaussians(
+        st.bg, t(m), empty, t(op), t(sc), t(rot), 1.0, empty, st.viewmatrix, st.projmatrix, st.tanfovx, st.tanfovy,
+        st.image_height, st.image_width, sh_full, s.sh_degree, st.campos, False, False)
+    assert R > 0 and color.shape == img.shape
+    assert torch.equal(radii2, radii)
+    assert (color - img.detach()).abs().max().item() <= 1e-5
+    g = _C.rasterize_gaussians_backward(st.bg, t(m), radii2, empty, t(sc), t(rot), 1.0, empty, st.viewmatrix,
+                                        st.projmatrix, st.tanfovx, st.tanfovy, dL, sh_full, s.sh_degree, st.campos,
+                                        geom, R, binning, image, False)
+    dmeans2D, dcolors, dop, dmean3D, dcov3D, dsh, dscale, drot = g
+    assert dmeans2D.shape == (s.P, 3) and dsh.shape == sh_full.shape and dop.shape == (s.P, 1)
+    rel = lambda a, b: ((a - b).abs().max() / b.abs().max().clamp_min(1e-30)).item()
+    assert rel(dmean3D, leaves["means"].grad) <= 1e-5
+    assert rel(dscale, leaves["scales"].grad) <= 1e-5
+    assert rel(drot, leaves["rotations"].grad) <= 1e-5
+    assert rel(dop, leaves["opacities"].grad) <= 1e-5
+    assert rel(dsh[:, :1], leaves["dc"].grad) <= 1e-5
+    assert rel(dsh[:, 1:], leaves["shs"].grad) <= 1e-5
