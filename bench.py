@@ -217,6 +217,8 @@ def gpu_bench(args, rank, local, world):
         step(dev_in)
     torch.cuda.synchronize()
     K = int(slot._buf.curr_offset.item())
+    W_eval = needed_evaluations(s, settings, dev_in, slot._buf, dev)
+    fp32_peak = ctypes_peak_fp32(dev)
 
     # timed region: device-resident inputs
     barrier(world)
@@ -302,7 +304,7 @@ def gpu_bench(args, rank, local, world):
         checkpoint = checkpoint_bench(args, dev)
     return dict(ms_step=ms_step_job, fwd_ms=fwd_ms, clocks=clocks, ktimes=ktimes, K=K,
                 launches_per_step=launches_per_step, e2e=e2e, P=s.P, W=cam.width, H=cam.height, batched=batched,
-                checkpoint=checkpoint)
+                checkpoint=checkpoint, W_eval=W_eval, fp32_peak=fp32_peak)
 
 
 def batched_bench(args, dev, s, dev_in, cams, label):
@@ -471,8 +473,57 @@ def checkpoint_bench(args, dev):
     return out
 
 
+def needed_evaluations(scene, settings, dev_in, buf, dev):
+    """Pixel-Gaussian evaluations FB's merge uses: the sum over pixels of the
+    last contributor count (every Gaussian of every bucket up to the one
+    after which the pixel stops).  This is the composite's algorithmic work."""
+    import torch
+    from fastergs_gb300 import _C
+    cam = scene.camera
+    buf.curr_offset.fill_(0)
+    e = torch.empty(0, device=dev)
+    _C.ops.preprocess(scene.sh_degree, dev_in["means"], e, dev_in["dc"], dev_in["shs"], dev_in["opacities"],
+                      dev_in["scales"], dev_in["rotations"], 1.0, cam.width, cam.height, 16, 16, settings.campos,
+                      settings.viewmatrix, settings.projmatrix, cam.tanfovx, cam.tanfovy, 100.0, 0.01,
+                      buf.gaussian_keys_unsorted, buf.gaussian_values_unsorted, buf.gaussian_values_sorted,
+                      buf.curr_offset, 1.0, buf.splat_buffer, None)
+    K = int(buf.curr_offset.item())
+    _C.ops.sort_gaussian(K, cam.width, cam.height, 16, 16, buf.list_sorting_space, buf.gaussian_keys_unsorted,
+                         buf.gaussian_values_unsorted, buf.gaussian_keys_sorted, buf.gaussian_values_sorted)
+    lc = torch.empty((cam.height, cam.width, 1), dtype=torch.int32, device=dev)
+    tf = torch.empty((cam.height, cam.width, 1), dtype=torch.float32, device=dev)
+    _C.ops.render_16x16(scene.P, K, cam.width, cam.height, buf.splat_buffer, buf.gaussian_keys_sorted,
+                        buf.gaussian_values_sorted, buf.ranges, settings.bg, lc, tf)
+    return int(lc.to(torch.int64).sum().item())
+
+
+def ctypes_peak_fp32(dev):
+    """Measured FP32 FMA throughput (TFLOP/s) of this GPU, via the library's microbenchmark."""
+    import ctypes
+    import torch
+    from fastergs_gb300 import _lib
+    out = ctypes.c_double(0.0)
+    _lib.call("fgs_peak_fp32", ctypes.byref(out), torch.cuda.current_stream(dev).cuda_stream)
+    return float(out.value)
+
+
+# FP32 FLOPs (FMA = 2) per pixel-Gaussian evaluation in the compositing
+# kernels, counted from their per-pixel formulas: forward = exponent (5),
+# exp2 + clamp + cut (3), blend (9); backward = alpha recomputation (8),
+# dL/dalpha and the un-blend (15), mean / conic / colour / opacity terms (27).
+FLOP_PER_EVAL = {"render_fwd": 17, "render_bwd": 50}
+
+# DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) from the
+# ncu captures summarised under profiles/, for this workload; None where no
+# capture of this workload exists.
+TRAFFIC_PER_LAUNCH: dict = {}
+
+
 def roofline(res, peaks):
-    """Roofline objects for the dominant kernel (by device time)."""
+    """Roofline of the dominant kernel (by device time) and a per-kernel table.
+    The compositing kernels are bound by FP32 issue: their roofline is
+    achieved FP32 TFLOP/s (needed evaluations x FLOPs per evaluation / time)
+    against the FFMA peak measured in this run; the rest are bound by HBM."""
     P, K = res["P"], res["K"]
     steps_ms = {k: v[0] for k, v in res["ktimes"].items()}
     launches = {k: v[1] for k, v in res["ktimes"].items()}
@@ -490,13 +541,26 @@ def roofline(res, peaks):
     }
     dom = max(steps_ms, key=lambda k: steps_ms[k])
     hbm = peaks.get("hbm_gbs", 6800.0)
+    hbm_src = "of measured (MEASURED_PEAKS.json hbm_gbs)" if "hbm_gbs" in peaks else "of fallback 6.8 TB/s"
+    fp32 = res["fp32_peak"]
+    W = res["W_eval"]
     per_launch_ms = steps_ms[dom] / max(launches[dom], 1)
-    b = algo.get(dom, 0)
-    achieved = b / (per_launch_ms * 1e-3) / 1e9 if per_launch_ms > 0 else 0.0
-    roof = {"kernel": dom, "bound": "hbm", "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
-            "frac": round(achieved / hbm, 4), "traffic": None,
-            "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if "hbm_gbs" in peaks else "fallback 6.8 TB/s",
-            "ms_per_launch": round(per_launch_ms, 4), "algorithmic_bytes": int(b)}
+    traffic = TRAFFIC_PER_LAUNCH.get(dom)
+    if dom in FLOP_PER_EVAL:
+        flops = W * FLOP_PER_EVAL[dom]
+        achieved = flops / (per_launch_ms * 1e-3) / 1e12
+        roof = {"kernel": dom, "bound": "fp32", "achieved": round(achieved, 2), "peak": round(fp32, 2),
+                "unit": "TFLOP/s", "frac": round(achieved / fp32, 4), "traffic": traffic,
+                "peak_source": "of measured (fgs_peak_fp32 FFMA microbenchmark, this run)",
+                "ms_per_launch": round(per_launch_ms, 4), "evaluations": int(W),
+                "flop_per_evaluation": FLOP_PER_EVAL[dom],
+                "hbm_frac": round(algo[dom] / (per_launch_ms * 1e-3) / 1e9 / hbm, 4)}
+    else:
+        b = algo.get(dom, 0)
+        achieved = b / (per_launch_ms * 1e-3) / 1e9 if per_launch_ms > 0 else 0.0
+        roof = {"kernel": dom, "bound": "hbm", "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
+                "frac": round(achieved / hbm, 4), "traffic": traffic, "peak_source": hbm_src,
+                "ms_per_launch": round(per_launch_ms, 4), "algorithmic_bytes": int(b)}
     table = {}
     for k in steps_ms:
         if launches[k]:
@@ -504,6 +568,8 @@ def roofline(res, peaks):
             entry = {"ms_per_launch": round(pl, 4), "launches": launches[k]}
             if k in algo and pl > 0:
                 entry["hbm_frac"] = round(algo[k] / (pl * 1e-3) / 1e9 / hbm, 4)
+            if k in FLOP_PER_EVAL and pl > 0:
+                entry["fp32_frac"] = round(W * FLOP_PER_EVAL[k] / (pl * 1e-3) / 1e12 / fp32, 4)
             table[k] = entry
     return roof, table
 

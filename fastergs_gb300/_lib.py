@@ -59,6 +59,7 @@ SIGNATURES = {
                                      vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp]),
     "fgs_batch_status": (i32, [i32, i32, camp, tunep, i64, vp, C.POINTER(C.c_int64), C.POINTER(C.c_int64), vp]),
     "fgs_batch_offsets": (i32, [i32, i32, camp, tunep, i64, C.POINTER(C.c_int64), i32]),
+    "fgs_peak_fp32": (i32, [C.POINTER(C.c_double), vp]),
     "fgs_kernel_timer": (i32, [i32, i32]),
     "fgs_kernel_timer_read": (i32, [i32, C.POINTER(C.c_double), C.POINTER(C.c_int)]),
 }

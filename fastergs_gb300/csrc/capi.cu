@@ -76,9 +76,53 @@ __global__ void __launch_bounds__(256) k_adam(float* __restrict__ param, const f
   m1[p] = a;
   m2[p] = b;
 }
+// FP32 issue ceiling for the compositing kernels' roofline: every thread runs
+// 8 independent FMA chains, so the FMA pipe, not latency, limits the rate.
+constexpr int kPeakChains = 8;
+constexpr int kPeakIters = 2048;
+__device__ float g_peak_sink;
+__global__ void __launch_bounds__(256) k_ffma_peak(float a, float b) {
+  float x[kPeakChains];
+#pragma unroll
+  for (int j = 0; j < kPeakChains; ++j) x[j] = a + (float)(threadIdx.x + j);
+#pragma unroll 4
+  for (int i = 0; i < kPeakIters; ++i)
+#pragma unroll
+    for (int j = 0; j < kPeakChains; ++j) x[j] = fmaf(x[j], b, a);
+  float s = 0.f;
+#pragma unroll
+  for (int j = 0; j < kPeakChains; ++j) s += x[j];
+  if (s == 12345.678f) g_peak_sink = s;  // never true; keeps the chains live
+}
+
 }  // namespace
 
 }  // namespace fgs
+
+extern "C" fgs_status fgs_peak_fp32(double* tflops, void* stream) {
+  if (!tflops) return FGS_ERR_BAD_ARG;
+  cudaStream_t s = (cudaStream_t)stream;
+  const int blocks = fgs::num_sms() * 8;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  FGS_TRY(cudaEventCreate(&e0));
+  FGS_TRY(cudaEventCreate(&e1));
+  float best = 1e30f;
+  for (int rep = 0; rep < 4; ++rep) {  // first launch warms up
+    cudaEventRecord(e0, s);
+    fgs::k_ffma_peak<<<blocks, 256, 0, s>>>(0.5f, 0.999f);
+    cudaEventRecord(e1, s);
+    FGS_TRY(cudaEventSynchronize(e1));
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    if (rep > 0) best = ms < best ? ms : best;
+  }
+  FGS_LAUNCH_CHECK();
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  const double flops = 2.0 * blocks * 256.0 * fgs::kPeakIters * fgs::kPeakChains;
+  *tflops = flops / (best * 1e-3) / 1e12;
+  return FGS_OK;
+}
 
 extern "C" const char* fgs_status_string(int status) {
   switch (status) {

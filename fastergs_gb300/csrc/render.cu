@@ -59,20 +59,24 @@ __global__ void __launch_bounds__(256) k_tile_ranges(const unsigned long long* _
 // Bucket bookkeeping (FB render.cu:418-433 counts buckets per tile, scans them
 // with CUB and copies the total to the host), plus the forward work queue.
 // Per tile: nb = ceil(n / bs) buckets, their inclusive offsets and the
-// bucket -> tile map.  Queue order: round k < kRounds holds bucket k of every
-// tile that has one, in tile order; buckets k >= kRounds follow, tile after
-// tile.  A tile's bucket k therefore always comes after its bucket k-1,
-// which is what the composite's per-tile chain waits on.  Both kernels scan
-// kScanValues per tile: [nb > 0], ..., [nb > kRounds-1], max(nb - kRounds, 0), nb.
+// bucket -> tile map.  Queue order: round k holds bucket k of every tile that
+// has one (k < kRounds; in any order inside the round), then buckets
+// k >= kRounds tile after tile.  A tile's bucket k therefore always comes
+// after its bucket k-1, which is what the composite's per-tile chain waits
+// on, and by the time a round starts the previous one is mostly folded.
+//   k_bucket_count  per-block scans of [max(nb - kRounds, 0), nb], histogram
+//                   of min(nb, kRounds);
+//   k_round_offsets one block: round sizes (tiles with nb > k) and their
+//                   exclusive offsets;
+//   k_bucket_fill   offsets, bucket -> tile map, queue slots (one atomic per
+//                   warp and round).
 __device__ __forceinline__ uint32_t tile_buckets(const uint32_t* __restrict__ ranges, int t, int bs) {
   return (ranges[2 * t + 1] - ranges[2 * t] + (uint32_t)bs - 1) / (uint32_t)bs;
 }
 
 __device__ __forceinline__ void scan_values(uint32_t nb, uint32_t (&v)[kScanValues]) {
-#pragma unroll
-  for (int j = 0; j < kRounds; ++j) v[j] = nb > (uint32_t)j ? 1u : 0u;
-  v[kRounds] = nb > (uint32_t)kRounds ? nb - kRounds : 0u;
-  v[kRounds + 1] = nb;
+  v[0] = nb > (uint32_t)kRounds ? nb - kRounds : 0u;
+  v[1] = nb;
 }
 
 // Inclusive block scan (kScanTiles threads) of every value; tot = block totals.
@@ -110,11 +114,18 @@ __device__ __forceinline__ void block_scan(uint32_t (&v)[kScanValues], uint32_t 
 }
 
 __global__ void __launch_bounds__(kScanTiles) k_bucket_count(int T, const uint32_t* __restrict__ ranges, int bs,
-                                                             uint32_t* __restrict__ block_sums) {
+                                                             uint32_t* __restrict__ block_sums,
+                                                             uint32_t* __restrict__ round_hist) {
   __shared__ uint32_t s_warp[kScanTiles / 32][kScanValues];
   const int t = blockIdx.x * kScanTiles + threadIdx.x;
+  const uint32_t nb = t < T ? tile_buckets(ranges, t, bs) : 0u;
+  if (t < T) {  // one atomic per distinct count in the warp
+    const uint32_t bin = min(nb, (uint32_t)kRounds);
+    const uint32_t peers = __match_any_sync(__activemask(), bin);
+    if ((peers & lanemask_lt()) == 0) atomicAdd(round_hist + bin, (uint32_t)__popc(peers));
+  }
   uint32_t v[kScanValues], tot[kScanValues];
-  scan_values(t < T ? tile_buckets(ranges, t, bs) : 0u, v);
+  scan_values(nb, v);
   block_scan(v, tot, s_warp);
   if (threadIdx.x < kScanValues) {
 #pragma unroll
@@ -123,8 +134,75 @@ __global__ void __launch_bounds__(kScanTiles) k_bucket_count(int T, const uint32
   }
 }
 
+// One block: round k has cnt[k] = #tiles with nb > k = sum_{n > k} hist[n]
+// slots; round_off[k] = sum_{j < k} cnt[j], round_off[kRounds] = first tail slot.
+__global__ void __launch_bounds__(1024) k_round_offsets(const uint32_t* __restrict__ round_hist,
+                                                        uint32_t* __restrict__ round_off,
+                                                        uint32_t* __restrict__ round_fill) {
+  constexpr int kPer = kRounds / 1024;
+  __shared__ uint32_t s_warp[32];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  // suffix sums of hist over n > k: thread tid owns k in [tid*kPer, tid*kPer + kPer), scanned from the top
+  uint32_t h[kPer];
+  uint32_t local = 0;
+#pragma unroll
+  for (int j = 0; j < kPer; ++j) {
+    h[j] = round_hist[tid * kPer + j + 1];  // hist[k + 1]
+    local += h[j];
+  }
+  // exclusive suffix over threads: sum of `local` of threads > tid
+  uint32_t incl = local;  // inclusive prefix over threads in reverse order
+  const int rlane = 31 - lane;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t u = __shfl_down_sync(0xffffffffu, incl, o);
+    if (rlane >= o) incl += u;
+  }
+  if (lane == 0) s_warp[warp] = incl;
+  __syncthreads();
+  uint32_t above = 0;
+  for (int w = warp + 1; w < 32; ++w) above += s_warp[w];
+  const uint32_t suffix = above + incl - local;  // hist entries owned by threads above this one
+  // cnt[k] = hist[k+1] + hist[k+2] + ... ; walk this thread's range downwards
+  uint32_t cnt[kPer];
+  uint32_t run = suffix;
+#pragma unroll
+  for (int j = kPer - 1; j >= 0; --j) {
+    run += h[j];
+    cnt[j] = run;
+  }
+  __syncthreads();
+  // exclusive prefix of cnt over k
+  uint32_t csum = 0;
+#pragma unroll
+  for (int j = 0; j < kPer; ++j) csum += cnt[j];
+  uint32_t pre = csum;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t u = __shfl_up_sync(0xffffffffu, pre, o);
+    if (lane >= o) pre += u;
+  }
+  if (lane == 31) s_warp[warp] = pre;
+  __syncthreads();
+  uint32_t wbase = 0, total = 0;
+  for (int w = 0; w < 32; ++w) {
+    if (w < warp) wbase += s_warp[w];
+    total += s_warp[w];
+  }
+  uint32_t off = wbase + pre - csum;
+#pragma unroll
+  for (int j = 0; j < kPer; ++j) {
+    round_off[tid * kPer + j] = off;
+    round_fill[tid * kPer + j] = 0;
+    off += cnt[j];
+  }
+  if (tid == 0) round_off[kRounds] = total;
+}
+
 __global__ void __launch_bounds__(kScanTiles) k_bucket_fill(int T, const uint32_t* __restrict__ ranges, int bs,
                                                             long long max_buckets, const uint32_t* __restrict__ block_sums,
+                                                            const uint32_t* __restrict__ round_off,
+                                                            uint32_t* __restrict__ round_fill,
                                                             uint32_t* __restrict__ bucket_off,
                                                             uint32_t* __restrict__ bucket_tile,
                                                             uint32_t* __restrict__ bucket_queue,
@@ -151,7 +229,7 @@ __global__ void __launch_bounds__(kScanTiles) k_bucket_fill(int T, const uint32_
   uint32_t v[kScanValues], tot[kScanValues];
   scan_values(nb, v);
   block_scan(v, tot, s_warp);  // its barriers also publish s_base / s_total
-  const uint32_t total = s_total[kRounds + 1];
+  const uint32_t total = s_total[1];
   const bool overflow = (long long)total > max_buckets;
   if (blockIdx.x == 0 && tid == 0) {
     bucket_sum[0] = overflow ? 0u : total;  // nothing is composited when the samples do not fit
@@ -159,21 +237,26 @@ __global__ void __launch_bounds__(kScanTiles) k_bucket_fill(int T, const uint32_
     bucket_sum[2] = 0;  // forward work cursor
     if (overflow) raise_error(kErrCapacity);
   }
-  if (t >= T) return;
-  tile_stage[t] = 0;
-  const uint32_t end = s_base[kRounds + 1] + v[kRounds + 1];
-  bucket_off[t] = end;
-  if (overflow) return;
+  const uint32_t end = s_base[1] + v[1];
   const uint32_t b0 = end - nb;
-  uint32_t round_off = 0;
-#pragma unroll
-  for (int k = 0; k < kRounds; ++k) {
-    if ((uint32_t)k < nb) {
-      bucket_queue[round_off + s_base[k] + v[k] - 1] = b0 + k;  // exclusive rank = inclusive - 1
-    }
-    round_off += s_total[k];
+  if (t < T) {
+    tile_stage[t] = 0;
+    bucket_off[t] = end;
   }
-  const uint32_t tail = round_off + s_base[kRounds] + v[kRounds] - (nb > kRounds ? nb - kRounds : 0u);
+  if (overflow) return;
+  // rounds: one slot request per warp and round
+  const uint32_t nr = min(nb, (uint32_t)kRounds);
+  for (uint32_t k = 0;; ++k) {
+    const uint32_t act = __ballot_sync(0xffffffffu, k < nr);
+    if (act == 0) break;
+    const int leader = __ffs(act) - 1;
+    uint32_t base = 0;
+    if (lane == leader) base = atomicAdd(round_fill + k, (uint32_t)__popc(act));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    if (k < nr) bucket_queue[round_off[k] + base + __popc(act & lanemask_lt())] = b0 + k;
+  }
+  if (t >= T) return;
+  const uint32_t tail = round_off[kRounds] + s_base[0] + v[0] - (nb > kRounds ? nb - kRounds : 0u);
   for (uint32_t k = kRounds; k < nb; ++k) bucket_queue[tail + (k - kRounds)] = b0 + k;
   for (uint32_t j = 0; j < nb; ++j) bucket_tile[b0 + j] = (uint32_t)t;
 }
@@ -355,10 +438,13 @@ fgs_status run_render_fwd(const Views& views, int64_t n_cap, const int32_t* n_de
   {
     KernelTimer kt__(FGS_K_BUCKET_SETUP, s);
     const unsigned nblk = (views.tiles + kScanTiles - 1) / kScanTiles;
-    k_bucket_count<<<nblk, kScanTiles, 0, s>>>((int)views.tiles, ranges, bucket_size, im.block_sums);
+    FGS_TRY(cudaMemsetAsync(im.round_hist, 0, sizeof(uint32_t) * (kRounds + 1), s));
+    k_bucket_count<<<nblk, kScanTiles, 0, s>>>((int)views.tiles, ranges, bucket_size, im.block_sums,
+                                               im.round_hist);
+    k_round_offsets<<<1, 1024, 0, s>>>(im.round_hist, im.round_off, im.round_fill);
     k_bucket_fill<<<nblk, kScanTiles, 0, s>>>((int)views.tiles, ranges, bucket_size, max_buckets, im.block_sums,
-                                              im.bucket_off, sm.bucket_tile, sm.bucket_queue, im.tile_stage,
-                                              im.bucket_sum);
+                                              im.round_off, im.round_fill, im.bucket_off, sm.bucket_tile,
+                                              sm.bucket_queue, im.tile_stage, im.bucket_sum);
     kt__.stop();
   }
   FGS_LAUNCH_CHECK();

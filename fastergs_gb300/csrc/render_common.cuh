@@ -20,8 +20,8 @@ constexpr int kMaxBucket = 128;    // largest supported bucket size
 // (number of buckets folded into the tile's running prefix, and which pixels
 // are still above the transmittance cut-off).
 constexpr int kScanTiles = 1024;  // tiles per bucket-setup scan block
-constexpr int kRounds = 8;        // leading bucket rounds of the forward work queue
-constexpr int kScanValues = kRounds + 2;
+constexpr int kRounds = 4096;     // bucket rounds of the forward work queue (local index < kRounds)
+constexpr int kScanValues = 2;    // per tile: buckets past the last round, buckets
 struct ImageState {
   float* pix_color;         // 3 * HW
   uint32_t* max_contrib;    // T
@@ -30,6 +30,9 @@ struct ImageState {
   uint32_t* block_sums;     // ceil(T / kScanTiles) x kScanValues
   uint32_t* tile_stage;     // T: buckets of the tile folded into its prefix
   uint32_t* tile_alive;     // T x 8: per 8x4 sub-block, lanes whose pixel is still compositing
+  uint32_t* round_hist;     // kRounds + 1: tiles by bucket count (capped at kRounds)
+  uint32_t* round_off;      // kRounds + 1: first queue slot of every round, then of the tail
+  uint32_t* round_fill;     // kRounds: slots handed out per round
   size_t bytes;
 };
 
@@ -59,6 +62,9 @@ inline ImageState carve_image(void* base, size_t pixels, size_t T) {
   s.block_sums = reinterpret_cast<uint32_t*>(p + off);  off = align_up(off + sizeof(uint32_t) * nblk * kScanValues, 256);
   s.tile_stage = reinterpret_cast<uint32_t*>(p + off);  off = align_up(off + sizeof(uint32_t) * T, 256);
   s.tile_alive = reinterpret_cast<uint32_t*>(p + off);  off = align_up(off + sizeof(uint32_t) * 8 * T, 256);
+  s.round_hist = reinterpret_cast<uint32_t*>(p + off);  off = align_up(off + sizeof(uint32_t) * (kRounds + 1), 256);
+  s.round_off = reinterpret_cast<uint32_t*>(p + off);   off = align_up(off + sizeof(uint32_t) * (kRounds + 1), 256);
+  s.round_fill = reinterpret_cast<uint32_t*>(p + off);  off = align_up(off + sizeof(uint32_t) * kRounds, 256);
   s.bytes = off;
   return s;
 }

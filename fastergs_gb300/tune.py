@@ -32,8 +32,12 @@ PACKETS = (2, 4, 8)
 _MEMO: dict = {}
 
 
-def search_space(buckets=BUCKETS, tiles=TILES, packets=PACKETS) -> list[TuneConfig]:
-    return [TuneConfig(b, bx, by, p) for b, (bx, by), p in itertools.product(buckets, tiles, packets)]
+def search_space(buckets=BUCKETS, tiles=TILES, packets=PACKETS, include_default: bool = True) -> list[TuneConfig]:
+    """bucket x tile x packet, plus FB's fixed choice (bucket 128, 16x16, packet 4)."""
+    space = [TuneConfig(b, bx, by, p) for b, (bx, by), p in itertools.product(buckets, tiles, packets)]
+    if include_default and TuneConfig() not in space:
+        space.append(TuneConfig())
+    return space
 
 
 def cache_key(P: int, sizes: Sequence[tuple[int, int]], sh_degree: int, backward: bool) -> str:

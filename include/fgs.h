@@ -293,6 +293,11 @@ enum {
 fgs_status fgs_kernel_timer(int kernel_id, int enable);
 fgs_status fgs_kernel_timer_read(int kernel_id, double* total_ms, int* launches);
 
+/* FP32 FMA throughput of this GPU in TFLOP/s (8 independent FMA chains per
+ * thread on every SM; synchronises the stream): the ceiling for the
+ * compositing kernels, which are bound by FP32 issue, not by HBM. */
+fgs_status fgs_peak_fp32(double* tflops, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -103,8 +103,9 @@ def test_batch_workspace_sizing_and_validation():
 def test_tuner_search_space_and_cache_key():
     from fastergs_gb300 import tune
     from fastergs_gb300.batched import TuneConfig
-    space = tune.search_space()
+    space = tune.search_space(include_default=False)
     assert len(space) == 18 and len(set(space)) == 18
+    assert TuneConfig() in tune.search_space() and len(tune.search_space()) == 19
     assert {c.bucket_size for c in space} == {16, 32, 64}
     assert {(c.block_x, c.block_y) for c in space} == {(16, 16), (8, 32)}
     assert {c.packet for c in space} == {2, 4, 8}
