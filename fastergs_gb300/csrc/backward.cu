@@ -292,15 +292,12 @@ __device__ __forceinline__ void sh_term(float B, float bx, float by, float bz, c
 
 // One thread per Gaussian; loops over the views and sums their gradients
 // (FB backward.cu:250-539, 892-918 for one view).
-__global__ void __launch_bounds__(256) k_preprocess_bwd(const PbwdArgs a) {
-  const int i = blockIdx.x * 256 + threadIdx.x;
-  if (i >= a.P) return;
-  float* gsh = a.dsh ? a.dsh + (size_t)i * a.M * 3 : nullptr;
-  const int used = (a.D + 1) * (a.D + 1) - 1;
+// One Gaussian: co / gsh are its SH row and its dL/dsh row (shared memory
+// when staged, else global); gsh starts at zero and is accumulated over views.
+__device__ __forceinline__ void pbwd_gaussian(const PbwdArgs& a, int i, const float* co, float* gsh) {
   float m3[3] = {0.f, 0.f, 0.f}, gc[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f}, gs[3] = {0.f, 0.f, 0.f};
   float gq[4] = {0.f, 0.f, 0.f, 0.f}, gdc[3] = {0.f, 0.f, 0.f};
   float4 gco_sum = make_float4(0.f, 0.f, 0.f, 0.f);
-  bool sh_written = false;
   const float3 p = make_float3(a.means[3 * (size_t)i], a.means[3 * (size_t)i + 1], a.means[3 * (size_t)i + 2]);
   // --- rotation of the raw quaternion (FB backward.cu:407-430)
   const float4 q = reinterpret_cast<const float4*>(a.rots)[i];
@@ -422,8 +419,7 @@ __global__ void __launch_bounds__(256) k_preprocess_bwd(const PbwdArgs a) {
       const float x = vx * inv_n, y = vy * inv_n, z = vz * inv_n;
       const float c0 = 0.28209479177387814f;
       gdc[0] += c0 * drgb.x; gdc[1] += c0 * drgb.y; gdc[2] += c0 * drgb.z;
-      const float* co = a.shs + (size_t)i * a.M * 3;
-      const bool add = sh_written;
+      const bool add = true;  // gsh starts at zero
       float3 dd = make_float3(0.f, 0.f, 0.f);
       if (a.D > 0) {
         const float c1 = 0.4886025119029199f;
@@ -458,7 +454,6 @@ __global__ void __launch_bounds__(256) k_preprocess_bwd(const PbwdArgs a) {
           }
         }
       }
-      sh_written = true;
       // d(v / |v|)/dv applied to the direction gradient
       const float vd = vx * dd.x + vy * dd.y + vz * dd.z;
       const float inv3 = inv_n * inv_n * inv_n;
@@ -494,9 +489,29 @@ __global__ void __launch_bounds__(256) k_preprocess_bwd(const PbwdArgs a) {
   a.ddc[3 * (size_t)i] = gdc[0]; a.ddc[3 * (size_t)i + 1] = gdc[1]; a.ddc[3 * (size_t)i + 2] = gdc[2];
   a.dscale[3 * (size_t)i] = gs[0]; a.dscale[3 * (size_t)i + 1] = gs[1]; a.dscale[3 * (size_t)i + 2] = gs[2];
   reinterpret_cast<float4*>(a.drot)[i] = make_float4(gq[0], gq[1], gq[2], gq[3]);
-  if (gsh) {
-    for (int k = sh_written ? 3 * used : 0; k < 3 * a.M; ++k) gsh[k] = 0.f;
+}
+
+__global__ void __launch_bounds__(256) k_preprocess_bwd(const PbwdArgs a) {
+  // sh_staged: [256 x M x 3] SH rows, then [256 x M x 3] dL/dsh accumulators
+  extern __shared__ __align__(16) float s_pb[];
+  const int first = blockIdx.x * 256, n = min(256, a.P - first), row = a.M * 3;
+  const int i = first + threadIdx.x;
+  if (a.sh_staged) {
+    float* s_co = s_pb;
+    float* s_g = s_pb + 256 * row;
+    block_copy_to_smem(s_co, a.shs, (size_t)first * row, n * row);
+    for (int j = threadIdx.x; j < n * row; j += 256) s_g[j] = 0.f;
+    __syncthreads();
+    if (i < a.P) pbwd_gaussian(a, i, s_co + threadIdx.x * row, s_g + threadIdx.x * row);
+    __syncthreads();
+    block_copy_from_smem(a.dsh, (size_t)first * row, s_g, n * row);
+    return;
   }
+  if (i >= a.P) return;
+  float* gsh = a.dsh ? a.dsh + (size_t)i * row : nullptr;
+  if (gsh)
+    for (int k = 0; k < row; ++k) gsh[k] = 0.f;
+  pbwd_gaussian(a, i, a.shs ? a.shs + (size_t)i * row : nullptr, gsh);
 }
 
 __global__ void __launch_bounds__(256) k_densify(int P, const int* radii, const float4* dm2, float* accum,
@@ -550,8 +565,11 @@ fgs_status run_render_bwd(const Views& views, int64_t records, int bucket_size, 
 }
 
 fgs_status run_preprocess_bwd(PbwdArgs& a, cudaStream_t s) {
+  a.sh_staged = (a.shs && a.dsh && a.M >= 1 && a.M <= kMaxStagedCoeffs) ? 1 : 0;
+  const int dyn = a.sh_staged ? 2 * 256 * a.M * 3 * (int)sizeof(float) : 0;
+  if (dyn) FGS_TRY(allow_dyn_smem(reinterpret_cast<const void*>(&k_preprocess_bwd), 2 * 256 * kMaxStagedCoeffs * 12));
   KernelTimer kt__(FGS_K_PREPROCESS_BWD, s);
-  k_preprocess_bwd<<<(a.P + 255) / 256, 256, 0, s>>>(a);
+  k_preprocess_bwd<<<(a.P + 255) / 256, 256, dyn, s>>>(a);
   kt__.stop();
   FGS_LAUNCH_CHECK();
   return FGS_OK;

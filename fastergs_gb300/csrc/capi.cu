@@ -1,5 +1,6 @@
 // Library-wide C entry points: status strings, device error word, SM count
 // cache, and the masked Adam step.
+#include <map>
 #include <mutex>
 #include <utility>
 #include <vector>
@@ -7,6 +8,20 @@
 #include "fgs_common.cuh"
 
 namespace fgs {
+
+cudaError_t allow_dyn_smem(const void* kernel, int bytes) {
+  static std::mutex mu;
+  static std::map<std::pair<const void*, int>, int> done;  // (kernel, device) -> bytes allowed
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  std::lock_guard<std::mutex> lk(mu);
+  int& have = done[{kernel, dev}];
+  if (have >= bytes) return cudaSuccess;
+  e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  if (e == cudaSuccess) have = bytes;
+  return e;
+}
 
 int num_sms() {
   // Cached per device; cudaDeviceGetAttribute is cheap but not free.

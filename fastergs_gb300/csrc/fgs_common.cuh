@@ -144,6 +144,36 @@ __device__ __forceinline__ void st_release_u32(uint32_t* p, uint32_t v) {
   asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 
+// Block-cooperative copy of n floats starting at src + first into shared
+// memory (16-byte aligned dst), with 16-byte loads when the source allows:
+// turns per-thread strided reads of a Gaussian's coefficient row (180 bytes
+// apart at SH degree 3) into coalesced ones.  No barrier; the caller syncs.
+__device__ __forceinline__ void block_copy_to_smem(float* dst, const float* src, size_t first, int n) {
+  const float* s = src + first;
+  if ((reinterpret_cast<uintptr_t>(s) & 15) == 0) {
+    const int n4 = n >> 2;
+    for (int j = threadIdx.x; j < n4; j += blockDim.x)
+      reinterpret_cast<float4*>(dst)[j] = __ldg(reinterpret_cast<const float4*>(s) + j);
+    for (int j = 4 * n4 + threadIdx.x; j < n; j += blockDim.x) dst[j] = __ldg(s + j);
+  } else {
+    for (int j = threadIdx.x; j < n; j += blockDim.x) dst[j] = __ldg(s + j);
+  }
+}
+// The reverse: n floats from shared memory to dst + first.
+__device__ __forceinline__ void block_copy_from_smem(float* dst, size_t first, const float* src, int n) {
+  float* d = dst + first;
+  if ((reinterpret_cast<uintptr_t>(d) & 15) == 0) {
+    const int n4 = n >> 2;
+    for (int j = threadIdx.x; j < n4; j += blockDim.x)
+      reinterpret_cast<float4*>(d)[j] = reinterpret_cast<const float4*>(src)[j];
+    for (int j = 4 * n4 + threadIdx.x; j < n; j += blockDim.x) d[j] = src[j];
+  } else {
+    for (int j = threadIdx.x; j < n; j += blockDim.x) d[j] = src[j];
+  }
+}
+// Largest SH coefficient count per Gaussian that is staged in shared memory.
+constexpr int kMaxStagedCoeffs = 16;
+
 // Column-major 4x4 transforms, as the 3DGS matrices are laid out.
 __device__ __forceinline__ float3 xform_point3(const float* m, float3 p) {
   return make_float3(m[0] * p.x + m[4] * p.y + m[8] * p.z + m[12], m[1] * p.x + m[5] * p.y + m[9] * p.z + m[13],
@@ -260,6 +290,9 @@ struct KernelTimer {
   KernelTimer(int id_, cudaStream_t s_) : id(id_), s(s_) { timer_begin(id, s); }
   void stop() { timer_end(id, s); }
 };
+// Opts a kernel into `bytes` of dynamic shared memory on the current device,
+// once per (kernel, device); the first launch happens before any capture.
+cudaError_t allow_dyn_smem(const void* kernel, int bytes);
 inline int tile_bits(uint32_t tiles) {
   int b = 0;
   while (b < 32 && (1u << b) < tiles) ++b;

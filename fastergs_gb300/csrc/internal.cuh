@@ -66,6 +66,7 @@ struct PbwdArgs {
   float* accum_abs;
   float* max_radii;
   float* denom;
+  int sh_staged;        // set by run_preprocess_bwd: SH rows and dL/dsh rows in shared memory
 };
 
 fgs_status run_preprocess_bwd(PbwdArgs& a, cudaStream_t s);

@@ -134,6 +134,7 @@ __global__ void __launch_bounds__(kPreThreads, 3) k_preprocess(const PreArgs a) 
   const int vi = (int)(blockIdx.x % (unsigned)a.views.V);
   const int chunk = (int)(blockIdx.x / (unsigned)a.views.V);
   const int i = chunk * kPreThreads + threadIdx.x;
+
   const ViewDesc& cam = a.views.v[vi];
   const int bx = a.views.bx, by = a.views.by;
   const size_t rbase = (size_t)vi * a.P;  // first record of this view
@@ -248,6 +249,7 @@ __global__ void __launch_bounds__(kPreThreads, 3) k_preprocess(const PreArgs a) 
         const float3 cpos = ld3(cam.campos);
         float dxv = p.x - cpos.x, dyv = p.y - cpos.y, dzv = p.z - cpos.z;
         const float inv = 1.0f / sqrtf(dxv * dxv + dyv * dyv + dzv * dzv);
+        // each thread reads its own contiguous SH row; consecutive loads hit the same L1 lines
         rgb = sh_colour(a.D, dxv * inv, dyv * inv, dzv * inv, a.dc + 3 * (size_t)i,
                         a.shs ? a.shs + (size_t)i * a.M * 3 : nullptr, rec + F_CLAMP);
       }
