@@ -1,12 +1,23 @@
-"""Benchmark: fwd+bwd ms/step and render FPS of the rasterizer at 1M Gaussians.
+"""Benchmark: fwd+bwd ms/step and render FPS of the rasterizer at 1M Gaussians,
+batched versus plain, on one GB300.
 
-Workload (default): 1,000,000 seeded synthetic Gaussians in a 10x10x10 box
-2-12 units ahead, heavy-tailed log-scales N(-4, 1), SH degree 3, one
-1297x840 view (FoV 50 deg), dL/dimage ~ N(0, 1) -- the configuration the
-reference's headline metric is quoted on, with synthetic data standing in for
-Mip-NeRF 360.  One step = forward + backward through the drop-in API
-(GaussianRasterizer + autograd).  Per-step inputs (~0.5 GB of parameters,
-records, pair lists and sample state) exceed the 129 MB L2.
+Headline (``value``): the drop-in path (GaussianRasterizer + autograd), one
+fwd+bwd step of 1,000,000 seeded synthetic Gaussians in a 10x10x10 box 2-12
+units ahead, heavy-tailed log-scales N(-4, 1), SH degree 3, one 1297x840 view
+(FoV 50 deg), dL/dimage ~ N(0, 1); synthetic data stands in for Mip-NeRF 360.
+Per-step inputs (parameters, records, pair lists, sample state) exceed the
+129 MB L2.  ``e2e`` repeats the step with pinned-host inputs and outputs copied
+inside the timed region.
+
+Also on the line:
+  batched     the same scene through 16 cameras of uneven resolution (and 16 at
+              1297x840): 16 sequential drop-in calls vs one batched step replayed
+              from a CUDA graph, with the autotuner's sweep (--tune sweep|default);
+  checkpoint  6M clustered Gaussians at 3840x2160: bucket prefixes stored vs
+              recomputed in the backward (step time, device memory held);
+  roofline    the dominant kernel against its bound: FP32 TFLOP/s vs a live FFMA
+              peak for the compositing kernels, GB/s vs MEASURED_PEAKS for the rest;
+  cpu_baseline the FP64 oracle on all host cores on 1/16 of the Gaussians, x16.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
@@ -513,10 +524,10 @@ def ctypes_peak_fp32(dev):
 # dL/dalpha and the un-blend (15), mean / conic / colour / opacity terms (27).
 FLOP_PER_EVAL = {"render_fwd": 17, "render_bwd": 50}
 
-# DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) from the
-# ncu captures summarised under profiles/, for this workload; None where no
-# capture of this workload exists.
-TRAFFIC_PER_LAUNCH: dict = {}
+# DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) of the
+# C2 workload, from the ncu captures summarised in profiles/ncu_c2_kernels.md.
+TRAFFIC_PER_LAUNCH = {"render_bwd": 55_832_320, "render_fwd": 50_232_320, "sort_pass": 38_462_720,
+                      "preprocess_bwd": 573_206_272, "preprocess": 200_908_544}
 
 
 def roofline(res, peaks):
@@ -545,7 +556,7 @@ def roofline(res, peaks):
     fp32 = res["fp32_peak"]
     W = res["W_eval"]
     per_launch_ms = steps_ms[dom] / max(launches[dom], 1)
-    traffic = TRAFFIC_PER_LAUNCH.get(dom)
+    traffic = TRAFFIC_PER_LAUNCH.get(dom) if res["P"] == 1_000_000 else None
     if dom in FLOP_PER_EVAL:
         flops = W * FLOP_PER_EVAL[dom]
         achieved = flops / (per_launch_ms * 1e-3) / 1e12
