@@ -132,8 +132,12 @@ def state_sizes(num_rendered, width, height, block_x=TILE, block_y=TILE, bucket_
 
 
 def render_16x16(P, num_rendered, width, height, splat_buffer, gaussian_keys_sorted, gaussian_values_sorted,
-                 ranges, bg_color, last_contributor, Ts_final, bucket_size=BUCKET):
-    """FB pybind.cpp:100-133.  Returns (bucket_sum, out_color (3,H,W), img_buffer, smp_buffer)."""
+                 ranges, bg_color, last_contributor, Ts_final, bucket_size=BUCKET, read_bucket_sum=True):
+    """FB pybind.cpp:100-133.  Returns (bucket_sum, out_color (3,H,W), img_buffer, smp_buffer).
+
+    read_bucket_sum=False skips FB's host read of the bucket count (and its
+    stream synchronisation) and returns the capacity the sample state was
+    sized for instead; this package's backward does not need the count."""
     dev = _device_of(splat_buffer)
     bg = _f32("bg", bg_color, dev)
     if bg.numel() != 3:
@@ -152,8 +156,8 @@ def render_16x16(P, num_rendered, width, height, splat_buffer, gaussian_keys_sor
     _lib.call("fgs_render_fwd", int(P), int(num_rendered), int(width), int(height), TILE, TILE, int(bucket_size),
               _ptr(splat_buffer), _ptr(gaussian_keys_sorted), _ptr(gaussian_values_sorted), _ptr(ranges),
               _ptr(bg), _ptr(out_color), _ptr(last_contributor), _ptr(Ts_final), _ptr(img_buffer), ib,
-              _ptr(smp_buffer), rows * _SAMPLE_ROW, mb, C.byref(bsum), _stream(dev))
-    return int(bsum.value), out_color, img_buffer, smp_buffer
+              _ptr(smp_buffer), rows * _SAMPLE_ROW, mb, C.byref(bsum) if read_bucket_sum else None, _stream(dev))
+    return (int(bsum.value) if read_bucket_sum else mb), out_color, img_buffer, smp_buffer
 
 
 def backward(degree, bucket_sum, means3D, radii, dc, sh, opacities, scales, rotations, scale_modifier, width,

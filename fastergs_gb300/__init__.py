@@ -49,6 +49,17 @@ class Buffer:
         self.device = device
 
 
+_HOST_COUNTS: dict = {}
+
+
+def _host_counts(dev) -> torch.Tensor:
+    """Pinned host words the forward reads the pair and task counts into."""
+    key = (dev.type, dev.index)
+    if key not in _HOST_COUNTS:
+        _HOST_COUNTS[key] = torch.zeros(2, dtype=torch.int32).pin_memory()
+    return _HOST_COUNTS[key]
+
+
 class _LazyBuffer:
     """Class attribute that allocates the shared Buffer on first access."""
 
@@ -91,11 +102,17 @@ class _RasterizeGaussians(torch.autograd.Function):
             raster_settings.tanfovx, raster_settings.tanfovy, zFar, zNear,
             buffer.gaussian_keys_unsorted, buffer.gaussian_values_unsorted, buffer.gaussian_values_sorted,
             buffer.curr_offset, raster_settings.mult, splat_buffer, culling)
-        num_rendered = int(buffer.curr_offset.cpu()[0])
-        device_errors = _C.device_errors(means3D.device)  # read and cleared either way
-        if num_rendered >= buffer.MAX_NUM_RENDERED:
-            raise RuntimeError("Too many k-v pairs!")
-        if device_errors:
+        # One host read per frame (FB's K read): the pair count and the
+        # large-footprint task count, copied together, one synchronisation.
+        counts = _host_counts(means3D.device)
+        counts[0].copy_(buffer.curr_offset[0], non_blocking=True)
+        counts[1].copy_(_C._counters(means3D.device)[0], non_blocking=True)
+        torch.cuda.current_stream(means3D.device).synchronize()
+        num_rendered, num_tasks = int(counts[0]), int(counts[1])
+        if num_rendered >= buffer.MAX_NUM_RENDERED or num_tasks > buffer.gaussian_values_sorted.numel() // 2:
+            _C.device_errors(means3D.device)  # clears the capacity bit the skipped writes latched
+            if num_rendered >= buffer.MAX_NUM_RENDERED:
+                raise RuntimeError("Too many k-v pairs!")
             raise RuntimeError("preprocess overflowed a device queue (too many large Gaussians)")
         _C.ops.sort_gaussian(num_rendered, raster_settings.image_width, raster_settings.image_height, 16, 16,
                              buffer.list_sorting_space, buffer.gaussian_keys_unsorted,
@@ -107,7 +124,7 @@ class _RasterizeGaussians(torch.autograd.Function):
         Ts_final = torch.empty((H, W, 1), device=means3D.device, dtype=torch.float)
         bucket_sum, out_color, img_buffer, smp_buffer = _C.ops.render_16x16(
             N, num_rendered, W, H, splat_buffer, buffer.gaussian_keys_sorted, buffer.gaussian_values_sorted,
-            buffer.ranges, raster_settings.bg, last_contributor, Ts_final)
+            buffer.ranges, raster_settings.bg, last_contributor, Ts_final, read_bucket_sum=False)
         ctx.raster_settings = raster_settings
         ctx.num_rendered = num_rendered
         ctx.buffer = buffer

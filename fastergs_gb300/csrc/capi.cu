@@ -96,6 +96,25 @@ __global__ void __launch_bounds__(256) k_adam(float* __restrict__ param, const f
 constexpr int kPeakChains = 8;
 constexpr int kPeakIters = 2048;
 __device__ float g_peak_sink;
+
+}  // namespace
+
+// Every translation unit's error word, gathered (and optionally cleared) by
+// one tiny kernel so that reading them costs one synchronisation.
+struct ErrorWords {
+  int* w[4];
+};
+__device__ int g_error_gather;
+__global__ void k_gather_errors(ErrorWords e, bool clear, int* out) {
+  if (threadIdx.x != 0) return;
+  int v = 0;
+  for (int j = 0; j < 4; ++j) {
+    v |= clear ? atomicExch(e.w[j], 0) : atomicOr(e.w[j], 0);
+  }
+  *out = v;
+}
+
+namespace {
 __global__ void __launch_bounds__(256) k_ffma_peak(float a, float b) {
   float x[kPeakChains];
 #pragma unroll
@@ -157,11 +176,30 @@ extern "C" fgs_status fgs_device_errors(int* flags, int clear, void* stream) {
   if (!flags) return FGS_ERR_BAD_ARG;
   *flags = 0;
   cudaStream_t s = (cudaStream_t)stream;
-  const bool c = clear != 0;
-  FGS_TRY(fgs::errors_preprocess(flags, c, s));
-  FGS_TRY(fgs::errors_sort(flags, c, s));
-  FGS_TRY(fgs::errors_render(flags, c, s));
-  FGS_TRY(fgs::errors_backward(flags, c, s));
+  int dev = 0;
+  FGS_TRY(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) return FGS_ERR_UNSUPPORTED;
+  static std::mutex mu;
+  static fgs::ErrorWords cache[64];
+  static bool have[64] = {false};
+  fgs::ErrorWords w;
+  {
+    std::lock_guard<std::mutex> lk(mu);
+    if (!have[dev]) {
+      cache[dev] = fgs::ErrorWords{{fgs::error_word_preprocess(), fgs::error_word_sort(), fgs::error_word_render(),
+                                    fgs::error_word_backward()}};
+      for (int* p : cache[dev].w)
+        if (!p) return FGS_ERR_CUDA;
+      have[dev] = true;
+    }
+    w = cache[dev];
+  }
+  int* out = nullptr;
+  FGS_TRY(cudaGetSymbolAddress(reinterpret_cast<void**>(&out), fgs::g_error_gather));
+  fgs::k_gather_errors<<<1, 32, 0, s>>>(w, clear != 0, out);
+  FGS_LAUNCH_CHECK();
+  FGS_TRY(cudaMemcpyAsync(flags, out, sizeof(int), cudaMemcpyDeviceToHost, s));
+  FGS_TRY(cudaStreamSynchronize(s));
   return FGS_OK;
 }
 

@@ -276,10 +276,11 @@ __device__ __forceinline__ void raise_error(int bits) { atomicOr(&g_error_word, 
 
 // Host helpers.
 int num_sms();
-cudaError_t errors_preprocess(int* out, bool clear, cudaStream_t s);
-cudaError_t errors_sort(int* out, bool clear, cudaStream_t s);
-cudaError_t errors_render(int* out, bool clear, cudaStream_t s);
-cudaError_t errors_backward(int* out, bool clear, cudaStream_t s);
+// Device address of each translation unit's error word (looked up once).
+int* error_word_preprocess();
+int* error_word_sort();
+int* error_word_render();
+int* error_word_backward();
 // Optional per-kernel event timing (fgs_kernel_timer).  Usage around a launch:
 //   KernelTimer kt(FGS_K_RENDER_FWD, stream); launch...; kt.stop();
 void timer_begin(int id, cudaStream_t s);
@@ -313,19 +314,12 @@ inline int tile_bits(uint32_t tiles) {
     if (e__ != cudaSuccess) return FGS_ERR_CUDA;      \
   } while (0)
 
-#define FGS_DEFINE_ERROR_ACCESSOR(name)                                                        \
-  namespace fgs {                                                                             \
-  cudaError_t errors_##name(int* out, bool clear, cudaStream_t s) {                           \
-    int v = 0;                                                                                \
-    cudaError_t e = cudaMemcpyFromSymbolAsync(&v, g_error_word, sizeof(int), 0,               \
-                                              cudaMemcpyDeviceToHost, s);                     \
-    if (e == cudaSuccess) e = cudaStreamSynchronize(s);                                       \
-    if (e == cudaSuccess && clear && v) {                                                     \
-      const int z = 0;                                                                        \
-      e = cudaMemcpyToSymbolAsync(g_error_word, &z, sizeof(int), 0, cudaMemcpyHostToDevice, s); \
-      if (e == cudaSuccess) e = cudaStreamSynchronize(s);                                     \
-    }                                                                                         \
-    *out |= v;                                                                                \
-    return e;                                                                                 \
-  }                                                                                           \
+#define FGS_DEFINE_ERROR_ACCESSOR(name)                                     \
+  namespace fgs {                                                          \
+  int* error_word_##name() {                                               \
+    void* p = nullptr;                                                     \
+    return cudaGetSymbolAddress(&p, g_error_word) == cudaSuccess           \
+               ? static_cast<int*>(p)                                      \
+               : nullptr;                                                  \
+  }                                                                        \
   }
