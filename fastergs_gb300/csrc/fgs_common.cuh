@@ -117,6 +117,34 @@ __device__ __forceinline__ ff ff_div(ff a, ff b) {
   return ff_fast_sum(q1, __fdiv_rn(r, b.hi));
 }
 
+// Packed FP32 pairs (sm_100+ f32x2 arithmetic): one instruction does the
+// work of two scalar ones with identical per-element IEEE rounding, which
+// halves the issue slots of the compositing kernels' FMA-heavy inner loops.
+typedef unsigned long long f2x;
+__device__ __forceinline__ f2x f2_pack(float lo, float hi) {
+  f2x r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
+  return r;
+}
+__device__ __forceinline__ void f2_unpack(f2x v, float& lo, float& hi) {
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
+}
+__device__ __forceinline__ f2x f2_fma(f2x a, f2x b, f2x c) {
+  f2x d;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+  return d;
+}
+__device__ __forceinline__ f2x f2_mul(f2x a, f2x b) {
+  f2x d;
+  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+__device__ __forceinline__ f2x f2_add(f2x a, f2x b) {
+  f2x d;
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+
 __device__ __forceinline__ uint32_t lanemask_lt() {
   uint32_t m;
   asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));

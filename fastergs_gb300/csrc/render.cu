@@ -309,7 +309,7 @@ struct FwdArgs {
 };
 
 template <int BX, bool RECOMPUTE>
-__global__ void __launch_bounds__(kFwdWarps * kWarp, 8) k_render_fwd(const FwdArgs a) {
+__global__ void __launch_bounds__(kFwdWarps * kWarp, 7) k_render_fwd(const FwdArgs a) {
   using M = TileMap<BX>;
   constexpr int BY = kTilePixels / BX;
   __shared__ BucketStage s_stage[kFwdWarps];

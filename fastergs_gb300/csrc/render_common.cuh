@@ -156,6 +156,12 @@ __device__ __forceinline__ float centre_offset(float whole, float frac, float pi
 // render.cu:285-391): alpha = min(0.99, o 2^e), dropped below 1/255.
 // Skipped (Gaussian, sub-block) pairs have alpha < 1/256 everywhere and would
 // leave C and T bit-for-bit unchanged.
+//
+// The 8 pixels are processed as 4 packed pairs (pixel slots 2j, 2j + 1, the
+// two halves of one 8x4 sub-block row pair) with f32x2 arithmetic.  The blend
+// runs on the negated alpha and colour, -wt = (-alpha) T and
+// C + (-c)(-wt), which are bit-identical to C + c (alpha T) and
+// T + (-alpha) T of the scalar form.
 template <int BX>
 __device__ __forceinline__ void composite_bucket(const BucketStage& st, int n, uint32_t live,
                                                  const float (&pxc)[TileMap<BX>::kCols],
@@ -163,40 +169,56 @@ __device__ __forceinline__ void composite_bucket(const BucketStage& st, int n, u
                                                  float (&Cr)[kPxPerThread], float (&Cg)[kPxPerThread],
                                                  float (&Cb)[kPxPerThread]) {
   using M = TileMap<BX>;
+  constexpr int kPairs = kPxPerThread / 2;
+  f2x T2[kPairs], R2[kPairs], G2[kPairs], B2[kPairs];
+  const f2x one2 = f2_pack(1.f, 1.f), zero2 = f2_pack(0.f, 0.f);
 #pragma unroll
-  for (int k = 0; k < kPxPerThread; ++k) { T[k] = 1.f; Cr[k] = 0.f; Cg[k] = 0.f; Cb[k] = 0.f; }
-  if (live == 0u) return;
-  for (int g = 0; g < n; ++g) {
-    const uint32_t mask = st.mask[g] & live;
-    if (mask == 0) continue;  // alpha < 1/256 on every live sub-block
-    const float4 pos = st.pos[g];
-    const float4 q4 = st.quad[g];   // A1, P, C1, log2 o
-    const float4 c = st.rgb[g];
-    float dx[M::kCols];
+  for (int j = 0; j < kPairs; ++j) { T2[j] = one2; R2[j] = zero2; G2[j] = zero2; B2[j] = zero2; }
+  if (live != 0u) {
+    for (int g = 0; g < n; ++g) {
+      const uint32_t mask = st.mask[g] & live;
+      if (mask == 0) continue;  // alpha < 1/256 on every live sub-block
+      const float4 pos = st.pos[g];
+      const float4 q4 = st.quad[g];   // A1, P, C1, log2 o
+      const float4 c = st.rgb[g];
+      const f2x A2 = f2_pack(q4.x, q4.x), P2 = f2_pack(q4.y, q4.y);
+      const f2x nr2 = f2_pack(-c.x, -c.x), ng2 = f2_pack(-c.y, -c.y), nb2 = f2_pack(-c.z, -c.z);
+      float dx[M::kCols];
 #pragma unroll
-    for (int cc = 0; cc < M::kCols; ++cc) dx[cc] = centre_offset(pos.x, pos.z, pxc[cc]);
+      for (int cc = 0; cc < M::kCols; ++cc) dx[cc] = centre_offset(pos.x, pos.z, pxc[cc]);
 #pragma unroll
-    for (int r = 0; r < M::kRows; ++r) {
-      const uint32_t rm = (mask >> (r * M::kCols)) & ((1u << M::kCols) - 1u);
-      if (rm == 0) continue;
-      const float dy = centre_offset(pos.y, pos.w, pyr[r]);
-      const float f = fmaf(q4.z * dy, dy, q4.w);  // log2 o + C1 dy^2
-#pragma unroll
-      for (int cc = 0; cc < M::kCols; ++cc) {
-        if (!((rm >> cc) & 1u)) continue;
-        const int k = r * M::kCols + cc;
+      for (int j = 0; j < kPairs; ++j) {
+        const int k0 = 2 * j, k1 = 2 * j + 1;  // pixel slots k = r * kCols + cc
+        if (((mask >> k0) & 3u) == 0u) continue;
+        const int r0 = k0 / M::kCols, c0 = k0 % M::kCols, r1 = k1 / M::kCols, c1 = k1 % M::kCols;
+        const float dy0 = centre_offset(pos.y, pos.w, pyr[r0]);
+        const float dy1 = r1 == r0 ? dy0 : centre_offset(pos.y, pos.w, pyr[r1]);
+        const float f0 = fmaf(q4.z * dy0, dy0, q4.w);  // log2 o + C1 dy^2
+        const float f1 = r1 == r0 ? f0 : fmaf(q4.z * dy1, dy1, q4.w);
         // alpha = o * exp(-q/2) = 2^(log2 o + A1 (dx + P dy)^2 + C1 dy^2)
-        const float w = fmaf(q4.y, dy, dx[cc]);
-        const float e = fmaf(q4.x * w, w, f);
-        float al = fminf(kAlphaMax, ex2_approx(e));
-        al = al < kAlphaCut ? 0.f : al;
-        const float wt = al * T[k];
-        Cr[k] = fmaf(c.x, wt, Cr[k]);
-        Cg[k] = fmaf(c.y, wt, Cg[k]);
-        Cb[k] = fmaf(c.z, wt, Cb[k]);
-        T[k] = fmaf(-al, T[k], T[k]);  // T (1 - alpha), rounded once
+        const f2x w2 = f2_fma(P2, f2_pack(dy0, dy1), f2_pack(dx[c0], dx[c1]));
+        const f2x e2 = f2_fma(f2_mul(A2, w2), w2, f2_pack(f0, f1));
+        float e0, e1;
+        f2_unpack(e2, e0, e1);
+        // -alpha: -min(0.99, 2^e), and 0 where alpha < 1/255
+        float n0 = fmaxf(-kAlphaMax, -ex2_approx(e0)), n1 = fmaxf(-kAlphaMax, -ex2_approx(e1));
+        n0 = n0 > -kAlphaCut ? 0.f : n0;
+        n1 = n1 > -kAlphaCut ? 0.f : n1;
+        const f2x na2 = f2_pack(n0, n1);
+        const f2x nwt2 = f2_mul(na2, T2[j]);  // -alpha T
+        R2[j] = f2_fma(nr2, nwt2, R2[j]);
+        G2[j] = f2_fma(ng2, nwt2, G2[j]);
+        B2[j] = f2_fma(nb2, nwt2, B2[j]);
+        T2[j] = f2_fma(na2, T2[j], T2[j]);    // T (1 - alpha), rounded once
       }
     }
+  }
+#pragma unroll
+  for (int j = 0; j < kPairs; ++j) {
+    f2_unpack(T2[j], T[2 * j], T[2 * j + 1]);
+    f2_unpack(R2[j], Cr[2 * j], Cr[2 * j + 1]);
+    f2_unpack(G2[j], Cg[2 * j], Cg[2 * j + 1]);
+    f2_unpack(B2[j], Cb[2 * j], Cb[2 * j + 1]);
   }
 }
 
