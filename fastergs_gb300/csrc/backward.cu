@@ -110,10 +110,12 @@ __global__ void __launch_bounds__(kBwdWarps * kWarp, 5) k_render_bwd(const BwdAr
     // Scale applied after the reduction to the value a lane ends up holding:
     // mean2D x/|x| need ln2 * W/2, y/|y| ln2 * H/2 (NDC), conic -0.5
     // (ln2 * -0.5 log2e), colour 1, opacity ln2 * log2e / o = 1 / o (per Gaussian).
+    // Colour (8..10) is accumulated negated.
     const float vscale = (vid == 0 || vid == 2)   ? kLn2 * 0.5f * (float)cam.W
                          : (vid == 1 || vid == 3) ? kLn2 * 0.5f * (float)cam.H
                          : (vid >= 4 && vid <= 7) ? -0.5f
-                                                  : 1.0f;
+                         : (vid >= 8 && vid <= 10) ? -1.0f
+                                                   : 1.0f;
     stage_bucket<BX>(st, a.splat, a.vals + bi.start, bi.n, lane, tx0, ty0);
     float pxc[M::kCols], pyr[M::kRows];
 #pragma unroll
@@ -169,30 +171,43 @@ __global__ void __launch_bounds__(kBwdWarps * kWarp, 5) k_render_bwd(const BwdAr
       publish_stage(a.tile_stage + bi.tile, (uint32_t)bi.local + 1u, lane);
     }
 
-    float T[kPxPerThread], Pd[kPxPerThread];
+    // Per pixel pair j (slots 2j, 2j + 1): transmittance and prefix . dL
+    // packed, and in shared memory (dL.r, dL.g | dL.b, K) of both pixels as
+    // two float4 so that every pair half lands in a register pair.
+    constexpr int kPairs = kPxPerThread / 2;
+    f2x T2[kPairs], Pd2[kPairs];
     float4* lk = s_lk[warp];
+    {
+      float Tk[kPxPerThread], Pk[kPxPerThread], lx[kPxPerThread], ly[kPxPerThread], lz[kPxPerThread],
+          kk[kPxPerThread];
 #pragma unroll
-    for (int r = 0; r < M::kRows; ++r)
+      for (int r = 0; r < M::kRows; ++r)
 #pragma unroll
-      for (int cc = 0; cc < M::kCols; ++cc) {
-        const int k = r * M::kCols + cc;
-        const int gxp = (int)pxc[cc], gyp = (int)pyr[r];
-        T[k] = 0.f; Pd[k] = 0.f;
-        float4 l4 = make_float4(0.f, 0.f, 0.f, 0.f);
-        if ((alive >> k) & 1u) {
-          const int pix = gyp * cam.W + gxp;
-          l4.x = dL[pix];
-          l4.y = dL[HW + pix];
-          l4.z = dL[2 * HW + pix];
-          T[k] = pre[k].w;
-          Pd[k] = pre[k].x * l4.x + pre[k].y * l4.y + pre[k].z * l4.z;
-          // K = C_final . dL + T_final * (bg . dL): everything behind a
-          // Gaussian is K - (prefix up to and including it) . dL.
-          l4.w = pcol[pix] * l4.x + pcol[HW + pix] * l4.y + pcol[2 * HW + pix] * l4.z +
-                 Tfin[pix] * (bgr * l4.x + bgg * l4.y + bgb * l4.z);
+        for (int cc = 0; cc < M::kCols; ++cc) {
+          const int k = r * M::kCols + cc;
+          const int gxp = (int)pxc[cc], gyp = (int)pyr[r];
+          Tk[k] = 0.f; Pk[k] = 0.f; lx[k] = 0.f; ly[k] = 0.f; lz[k] = 0.f; kk[k] = 0.f;
+          if ((alive >> k) & 1u) {
+            const int pix = gyp * cam.W + gxp;
+            lx[k] = dL[pix];
+            ly[k] = dL[HW + pix];
+            lz[k] = dL[2 * HW + pix];
+            Tk[k] = pre[k].w;
+            Pk[k] = pre[k].x * lx[k] + pre[k].y * ly[k] + pre[k].z * lz[k];
+            // K = C_final . dL + T_final * (bg . dL): everything behind a
+            // Gaussian is K - (prefix up to and including it) . dL.
+            kk[k] = pcol[pix] * lx[k] + pcol[HW + pix] * ly[k] + pcol[2 * HW + pix] * lz[k] +
+                    Tfin[pix] * (bgr * lx[k] + bgg * ly[k] + bgb * lz[k]);
+          }
         }
-        lk[k * kWarp + lane] = l4;
+#pragma unroll
+      for (int j = 0; j < kPairs; ++j) {
+        T2[j] = f2_pack(Tk[2 * j], Tk[2 * j + 1]);
+        Pd2[j] = f2_pack(Pk[2 * j], Pk[2 * j + 1]);
+        lk[(2 * j) * kWarp + lane] = make_float4(lx[2 * j], lx[2 * j + 1], ly[2 * j], ly[2 * j + 1]);
+        lk[(2 * j + 1) * kWarp + lane] = make_float4(lz[2 * j], lz[2 * j + 1], kk[2 * j], kk[2 * j + 1]);
       }
+    }
     // sub-blocks with at least one pixel that this bucket reaches
     uint32_t live_sb = 0;
 #pragma unroll
@@ -204,67 +219,96 @@ __global__ void __launch_bounds__(kBwdWarps * kWarp, 5) k_render_bwd(const BwdAr
       continue;
     }
 
+    const f2x one2 = f2_pack(1.f, 1.f);
     for (int g = 0; g < bi.n; ++g) {
       const uint32_t mask = st.mask[g] & live_sb;
       if (mask == 0) continue;  // alpha < 1/256 on every reached sub-block: no contribution
       const float4 pos = st.pos[g];
       const float4 q = st.quad[g];   // A1, P, C1, log2 o
       const float4 c = st.rgb[g];
-      const float A2 = 2.f * q.x, C2 = 2.f * q.z;
+      const f2x A12 = f2_pack(q.x, q.x), A22 = f2_pack(2.f * q.x, 2.f * q.x), P2 = f2_pack(q.y, q.y);
+      const f2x nr2 = f2_pack(-c.x, -c.x), ng2 = f2_pack(-c.y, -c.y), nb2 = f2_pack(-c.z, -c.z);
       float dx[M::kCols];
 #pragma unroll
       for (int cc = 0; cc < M::kCols; ++cc) dx[cc] = centre_offset(pos.x, pos.z, pxc[cc]);
-      float v[16];
-#pragma unroll
-      for (int j = 0; j < 16; ++j) v[j] = 0.f;
+      // Packed accumulators (the two halves are summed after the pixel loop):
+      // mean x, y; conic moments w^2, w dy, dy^2; -colour; opacity.
+      const f2x z2 = f2_pack(0.f, 0.f);
+      f2x V0 = z2, V1 = z2, V4 = z2, V5 = z2, V7 = z2, V8 = z2, V9 = z2, V10 = z2, V11 = z2;
+      float v2 = 0.f, v3 = 0.f;
       bool any = false;
 #pragma unroll
-      for (int r = 0; r < M::kRows; ++r) {
-        const uint32_t rm = (mask >> (r * M::kCols)) & ((1u << M::kCols) - 1u);
-        if (rm == 0) continue;
-        const float dy = centre_offset(pos.y, pos.w, pyr[r]);
-        const float f = fmaf(q.z * dy, dy, q.w);
-        const float c2dy = C2 * dy;
-#pragma unroll
-        for (int cc = 0; cc < M::kCols; ++cc) {
-          if (!((rm >> cc) & 1u)) continue;
-          const int k = r * M::kCols + cc;
-          const float w = fmaf(q.y, dy, dx[cc]);
-          const float e = fmaf(q.x * w, w, f);
-          const float al = fminf(kAlphaMax, ex2_approx(e));
-          if (((alive >> k) & 1u) && al >= kAlphaCut) {
-            any = true;
-            const float4 l4 = lk[k * kWarp + lane];  // dL rgb, K
-            const float wt = al * T[k];
-            const float cd = c.x * l4.x + c.y * l4.y + c.z * l4.z;
-            Pd[k] = fmaf(wt, cd, Pd[k]);
-            const float inv = rcp_approx(1.f - al);  // 1 - alpha >= 0.01
-            const float dLda = T[k] * cd - inv * (l4.w - Pd[k]);
-            T[k] = fmaf(-al, T[k], T[k]);
-            v[8] = fmaf(wt, l4.x, v[8]);
-            v[9] = fmaf(wt, l4.y, v[9]);
-            v[10] = fmaf(wt, l4.z, v[10]);
-            const float dp = dLda * al;  // dL/dexponent / ln2
-            // d exponent / d(centre x) = 2 A1 w, d / d(centre y) = 2 A1 P w + 2 C1 dy
-            const float gw = A2 * w;
-            const float tx = dp * gw;
-            const float ty = dp * fmaf(gw, q.y, c2dy);
-            v[0] += tx;
-            v[1] += ty;
-            v[2] += fabsf(tx);
-            v[3] += fabsf(ty);
-            // Conic-gradient moments in the exponent's own frame (w, dy),
-            // w = dx + P dy.  In pixel coordinates a thin footprint's
-            // cross-axis gradient is a small difference of large sums; here
-            // each frame axis is summed on its own.
-            v[4] = fmaf(dp, w * w, v[4]);
-            v[5] = fmaf(dp * w, dy, v[5]);
-            v[7] = fmaf(dp * dy, dy, v[7]);
-            v[11] += dp;
-          }
-        }
+      for (int j = 0; j < kPairs; ++j) {
+        const int k0 = 2 * j, k1 = 2 * j + 1;
+        if (((mask >> k0) & 3u) == 0u) continue;
+        const int r0 = k0 / M::kCols, c0 = k0 % M::kCols, r1 = k1 / M::kCols, c1 = k1 % M::kCols;
+        const float dy0 = centre_offset(pos.y, pos.w, pyr[r0]);
+        const float dy1 = r1 == r0 ? dy0 : centre_offset(pos.y, pos.w, pyr[r1]);
+        const float f0 = fmaf(q.z * dy0, dy0, q.w);
+        const float f1 = r1 == r0 ? f0 : fmaf(q.z * dy1, dy1, q.w);
+        const f2x dy2 = f2_pack(dy0, dy1);
+        const f2x w2 = f2_fma(P2, dy2, f2_pack(dx[c0], dx[c1]));
+        const f2x e2 = f2_fma(f2_mul(A12, w2), w2, f2_pack(f0, f1));
+        float e0, e1;
+        f2_unpack(e2, e0, e1);
+        // -alpha, 0 below the 1/255 cut (pixels this bucket does not reach
+        // have T = dL = K = 0 and contribute nothing either way)
+        float n0 = fmaxf(-kAlphaMax, -ex2_approx(e0)), n1 = fmaxf(-kAlphaMax, -ex2_approx(e1));
+        n0 = n0 > -kAlphaCut ? 0.f : n0;
+        n1 = n1 > -kAlphaCut ? 0.f : n1;
+        any |= (n0 != 0.f) | (n1 != 0.f);
+        const f2x na2 = f2_pack(n0, n1);
+        const float4 la = lk[(2 * j) * kWarp + lane], lb = lk[(2 * j + 1) * kWarp + lane];
+        const f2x Lx2 = f2_pack(la.x, la.y), Ly2 = f2_pack(la.z, la.w), Lz2 = f2_pack(lb.x, lb.y),
+                  K2 = f2_pack(lb.z, lb.w);
+        const f2x nwt2 = f2_mul(na2, T2[j]);                                   // -alpha T
+        const f2x ncd2 = f2_fma(nr2, Lx2, f2_fma(ng2, Ly2, f2_mul(nb2, Lz2)));  // -c . dL
+        Pd2[j] = f2_fma(nwt2, ncd2, Pd2[j]);
+        float o0, o1;
+        f2_unpack(f2_add(one2, na2), o0, o1);  // 1 - alpha >= 0.01
+        const f2x inv2 = f2_pack(rcp_approx(o0), rcp_approx(o1));
+        // -dL/dalpha = T (-c . dL) + (K - Pd) / (1 - alpha)
+        const f2x nd2 = f2_fma(inv2, f2_sub(K2, Pd2[j]), f2_mul(T2[j], ncd2));
+        T2[j] = f2_fma(na2, T2[j], T2[j]);
+        V8 = f2_fma(nwt2, Lx2, V8);
+        V9 = f2_fma(nwt2, Ly2, V9);
+        V10 = f2_fma(nwt2, Lz2, V10);
+        const f2x dp2 = f2_mul(nd2, na2);  // dL/dexponent / ln2
+        // d exponent / d(centre x) = 2 A1 w, d / d(centre y) = 2 A1 P w + 2 C1 dy
+        const f2x gw2 = f2_mul(A22, w2);
+        const f2x tx2 = f2_mul(dp2, gw2);
+        const f2x ty2 = f2_mul(dp2, f2_fma(gw2, P2, f2_pack(2.f * q.z * dy0, 2.f * q.z * dy1)));
+        V0 = f2_add(V0, tx2);
+        V1 = f2_add(V1, ty2);
+        float tx0, tx1, ty0, ty1;
+        f2_unpack(tx2, tx0, tx1);
+        f2_unpack(ty2, ty0, ty1);
+        v2 += fabsf(tx0) + fabsf(tx1);
+        v3 += fabsf(ty0) + fabsf(ty1);
+        // Conic-gradient moments in the exponent's own frame (w, dy),
+        // w = dx + P dy.  In pixel coordinates a thin footprint's cross-axis
+        // gradient is a small difference of large sums; here each frame
+        // axis is summed on its own.
+        V4 = f2_fma(dp2, f2_mul(w2, w2), V4);
+        V5 = f2_fma(f2_mul(dp2, w2), dy2, V5);
+        V7 = f2_fma(f2_mul(dp2, dy2), dy2, V7);
+        V11 = f2_add(V11, dp2);
       }
       if (__any_sync(0xffffffffu, any)) {
+        float v[16], a0, a1;
+        f2_unpack(V0, a0, a1); v[0] = a0 + a1;
+        f2_unpack(V1, a0, a1); v[1] = a0 + a1;
+        v[2] = v2;
+        v[3] = v3;
+        f2_unpack(V4, a0, a1); v[4] = a0 + a1;
+        f2_unpack(V5, a0, a1); v[5] = a0 + a1;
+        v[6] = 0.f;
+        f2_unpack(V7, a0, a1); v[7] = a0 + a1;
+        f2_unpack(V8, a0, a1); v[8] = a0 + a1;   // -dL/dcolour
+        f2_unpack(V9, a0, a1); v[9] = a0 + a1;
+        f2_unpack(V10, a0, a1); v[10] = a0 + a1;
+        f2_unpack(V11, a0, a1); v[11] = a0 + a1;
+        v[12] = v[13] = v[14] = v[15] = 0.f;
         const float tot = warp_transpose_reduce16(v, lane);
         if (!(lane & 1) && vid < FGS_GRAD_STRIDE && vid != 6) {
           const float s = (vid == 11) ? 1.0f / ex2_approx(q.w) : vscale;

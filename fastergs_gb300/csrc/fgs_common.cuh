@@ -144,6 +144,11 @@ __device__ __forceinline__ f2x f2_add(f2x a, f2x b) {
   asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
   return d;
 }
+__device__ __forceinline__ f2x f2_sub(f2x a, f2x b) {
+  f2x d;
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
 
 __device__ __forceinline__ uint32_t lanemask_lt() {
   uint32_t m;

@@ -33,6 +33,7 @@ constexpr int kMaxPasses = 8;
 constexpr uint32_t kFlagAgg = 1u << 30;
 constexpr uint32_t kFlagInc = 2u << 30;
 constexpr uint32_t kValueMask = (1u << 30) - 1;
+constexpr int kLookWindow = 8;  // predecessor words read per look-back round
 constexpr int kSortDynSmem = (int)((sizeof(unsigned long long) + sizeof(uint32_t)) * kSortTile);
 
 struct SortLayout {
@@ -182,22 +183,36 @@ __global__ void __launch_bounds__(kSortThreads, 2) k_onesweep(
       st_volatile_u32(lb + d, kFlagInc | real);
     } else {
       st_volatile_u32(lb + d, kFlagAgg | real);
+      // Windowed look-back: the words of the kLookWindow nearest unvisited
+      // predecessors are loaded together (independent loads, one latency),
+      // then summed newest first until an inclusive prefix; a word that is
+      // not published yet is re-polled (bounded) before the walk goes on.
       long long pred = (long long)tile - 1;
       int polls = 0;
-      while (pred >= 0) {
-        const uint32_t w = ld_volatile_u32(lookback + (size_t)pred * kRadix + d);
-        const uint32_t flag = w & ~kValueMask;
-        if (flag == 0) {
+      bool done = false;
+      while (!done && pred >= 0) {
+        uint32_t w[kLookWindow];
+#pragma unroll
+        for (int j = 0; j < kLookWindow; ++j)
+          w[j] = pred - j >= 0 ? ld_volatile_u32(lookback + (size_t)(pred - j) * kRadix + d) : 0u;
+        int used = 0;
+#pragma unroll
+        for (int j = 0; j < kLookWindow; ++j) {
+          if (done || used != j || pred - j < 0) continue;
+          const uint32_t flag = w[j] & ~kValueMask;
+          if (flag == 0) continue;  // not yet published: stop consuming here
+          excl += w[j] & kValueMask;
+          used = j + 1;
+          if (flag == kFlagInc) done = true;
+        }
+        pred -= used;
+        if (!done && used == 0) {  // the nearest unvisited predecessor has not published
           if (++polls > kSpinLimit) {
             raise_error(kErrTimeout);
             break;
           }
           __nanosleep(64);
-          continue;
         }
-        excl += w & kValueMask;
-        if (flag == kFlagInc) break;
-        --pred;
       }
       st_volatile_u32(lb + d, kFlagInc | (excl + real));
     }
