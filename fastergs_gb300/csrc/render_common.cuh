@@ -119,28 +119,36 @@ __device__ __forceinline__ void stage_bucket(BucketStage& st, const float* __res
     st.pos[j] = make_float4(X, Y, c.z, c.w);
     st.quad[j] = make_float4(b.z, b.w, c.x, c.y);
     st.rgb[j] = make_float4(a.z, a.w, b.x, __uint_as_float(id));
-    // Half-extents of the ellipse alpha >= 1/256, i.e. q <= 2 ln(256 o):
-    // |dx| <= sqrt(Q cov_xx), |dy| <= sqrt(Q cov_yy) with cov_yy = -0.5 log2e / C1
-    // and cov_xx = P^2 cov_yy + 1 / conic_a, 1 / conic_a = -0.5 log2e / A1.
-    // Outside it alpha < 1/256 < 1/255 even after FP32 rounding, so skipping
-    // those pixels changes nothing.
-    const float Q = 2.0f * kLn2 * (c.y + 8.0f);
-    const float cyy = -0.5f * kLog2e / c.x;
-    const float cxx = b.w * b.w * cyy - 0.5f * kLog2e / b.z;
-    const float rx = sqrtf(fmaxf(Q * cxx, 0.f)) + 1e-3f, ry = sqrtf(fmaxf(Q * cyy, 0.f)) + 1e-3f;
-    const float cx = (X - (float)tx0) + c.z, cy = (Y - (float)ty0) + c.w;
-    uint32_t cols = 0, rows = 0;
-#pragma unroll
-    for (int k = 0; k < M::kCols; ++k)
-      if (cx + rx >= 8.f * k && cx - rx <= 8.f * k + 7.f) cols |= 1u << k;
-#pragma unroll
-    for (int k = 0; k < M::kRows; ++k)
-      if (cy + ry >= 4.f * k && cy - ry <= 4.f * k + 3.f) rows |= 1u << k;
+    // Sub-blocks the ellipse alpha >= 1/256 reaches, from the exponent's own
+    // form e = log2 o + A1 w^2 + C1 dy^2, w = dx + P dy (A1, C1 < 0):
+    // e >= -8 needs |dy| <= sqrt(L / -C1) with L = log2 o + 8, and at a given
+    // dy, w within +-W(dy) = sqrt((L + C1 dy^2) / -A1), i.e. dx within
+    // -P dy +- W(dy).  Over a sub-block's 4 pixel rows that is a sheared
+    // interval, much tighter than the bounding box for rotated, elongated
+    // footprints.  Outside it alpha < 1/256 < 1/255 even after FP32 rounding
+    // (the 1e-3 px margins cover it), so skipping those pixels changes nothing.
+    const float L = c.y + 8.0f;
     uint32_t m = 0;
+    if (L > 0.f) {
+      const float inv_nA = -1.0f / b.z, nC = -c.x, P = b.w;
+      const float ry = sqrtf(L / nC) + 1e-3f;
+      const float cx = (X - (float)tx0) + c.z, cy = (Y - (float)ty0) + c.w;
 #pragma unroll
-    for (int k = 0; k < M::kRows; ++k)
-      if ((rows >> k) & 1u) m |= cols << (k * M::kCols);
-    st.mask[j] = (Q > 0.f) ? m : 0u;
+      for (int sr = 0; sr < M::kRows; ++sr) {
+        const float dlo = cy - (4.f * sr + 3.f), dhi = cy - 4.f * sr;  // dy over the sub-block's rows
+        if (dhi < -ry || dlo > ry) continue;
+        const float dys = fminf(fmaxf(0.f, dlo), dhi);  // the |dy|-smallest row offset
+        const float wm = sqrtf(fmaxf(0.f, (L - nC * dys * dys) * inv_nA)) + 1e-3f;
+        const float s0 = -P * dlo, s1 = -P * dhi;
+        const float lo = fminf(s0, s1) - wm, hi = fmaxf(s0, s1) + wm;
+#pragma unroll
+        for (int sc = 0; sc < M::kCols; ++sc) {
+          const float xr = cx - 8.f * sc;  // dx at the sub-block's first column
+          if (xr - 7.f <= hi && xr >= lo) m |= 1u << (sr * M::kCols + sc);
+        }
+      }
+    }
+    st.mask[j] = m;
   }
   __syncwarp();
 }
