@@ -130,7 +130,7 @@ extern "C" fgs_status fgs_render_batched_fwd(int P, int D, int M, const float* m
                                              size_t workspace_bytes, float* out_color, int32_t* radii,
                                              void* stream) {
   if (P < 0 || D < 0 || D > 3 || !cameras_ok(num_views, cams) || !config_ok(cfg) || pair_capacity < 1 ||
-      !workspace || !out_color || !radii)
+      !workspace || !out_color || (P > 0 && !radii))
     return FGS_ERR_BAD_ARG;
   if (pair_capacity > kMaxBatchPairs || (int64_t)num_views * P >= ((int64_t)1 << 32)) return FGS_ERR_CAPACITY;
   const int bucket_size = cfg->bucket_size;
@@ -186,7 +186,7 @@ extern "C" fgs_status fgs_render_batched_bwd(int P, int D, int M, const float* m
                                              float* xyz_gradient_accum, float* xyz_gradient_accum_abs,
                                              float* max_radii, float* denom, void* stream) {
   if (P < 0 || D < 0 || D > 3 || !cameras_ok(num_views, cams) || !config_ok(cfg) || pair_capacity < 1 ||
-      !workspace || !radii || !dL_dpixels)
+      !workspace || (P > 0 && !radii) || !dL_dpixels)
     return FGS_ERR_BAD_ARG;
   if (pair_capacity > kMaxBatchPairs || (int64_t)num_views * P >= ((int64_t)1 << 32)) return FGS_ERR_CAPACITY;
   const int bucket_size = cfg->bucket_size;

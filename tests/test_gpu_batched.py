@@ -383,3 +383,88 @@ def test_recompute_mode_matches_store_mode(setup, tune):
         assert _rel(g_rec[k].cpu().numpy(), g_store[k].cpu().numpy()) <= 1e-5, k
     for a, b in zip(rr, st):
         assert _rel(a.cpu().numpy(), b.cpu().numpy()) <= 1e-5
+
+
+def test_batched_colours_culling_and_per_camera_settings(cuda_device):
+    """Precomputed colours, a culling mask and a different scale modifier and
+    mult per camera: every camera must match the drop-in path with the same
+    settings, and the colour gradient must be the per-camera sum."""
+    dev = cuda_device
+    s = _scene(P=12000, seed=3)
+    T = tensors(s, dev)
+    cams = _cameras(sizes=[(200, 136), (97, 61), (256, 256)], seed=5)
+    smods, mults = [0.8, 1.0, 1.3], [1.0, 1.4, 0.7]
+    sets = [_settings(c, dev, bg, sh_degree=0, smod=sm, mult=mu)
+            for c, bg, sm, mu in zip(cams, _bgs(3), smods, mults)]
+    rng = np.random.default_rng(9)
+    colors = torch.tensor(rng.uniform(0.0, 1.5, size=(s.P, 3)).astype(np.float32), device=dev)
+    cull = torch.tensor(rng.random(s.P) < 0.2, device=dev)
+    dLs = [torch.tensor(scenes.upstream_grad(40 + k, st.image_height, st.image_width), device=dev)
+           for k, st in enumerate(sets)]
+    rast = BatchedRasterizer(sets, s.P)
+    rast.fit(T["means"], T["opacities"], None, None, colors, T["scales"], T["rotations"], cull, 0)
+    rast.forward(T["means"], T["opacities"], None, None, colors, T["scales"], T["rotations"], cull, 0)
+    ties = _tie_masks(rast)
+    for k in range(3):
+        dLs[k][:, torch.tensor(ties[k], device=dev)] = 0.0
+    g = rast.backward(torch.cat([d.reshape(-1) for d in dLs]), T["means"], None, None, T["scales"], T["rotations"], 0)
+    torch.cuda.synchronize()
+    assert _C.device_errors(dev) == 0
+    imgs = rast.images()
+    acc = None
+    for k, st in enumerate(sets):
+        leaves = {"means": T["means"].clone().requires_grad_(True), "colors": colors.clone().requires_grad_(True),
+                  "opacities": T["opacities"].clone().requires_grad_(True)}
+        img, radii = GaussianRasterizer(st)(means3D=leaves["means"], opacities=leaves["opacities"],
+                                            colors_precomp=leaves["colors"], scales=T["scales"],
+                                            rotations=T["rotations"], culling=cull)
+        assert torch.equal(rast.radii[k], radii), k
+        assert (radii[cull] == 0).all()
+        d = (imgs[k] - img.detach()).abs().amax(0).cpu().numpy()
+        assert d[~ties[k]].max(initial=0.0) <= 1e-6, k
+        torch.autograd.backward(img, grad_tensors=dLs[k])
+        gk = {n: v.grad.detach().clone() for n, v in leaves.items()}
+        acc = gk if acc is None else {n: acc[n] + gk[n] for n in acc}
+    assert _rel(g["colors"].cpu().numpy(), acc["colors"].cpu().numpy()) <= 1e-4
+    assert _rel(g["means3D"].cpu().numpy(), acc["means"].cpu().numpy()) <= 1e-4
+    assert _rel(g["opacities"].cpu().numpy(), acc["opacities"].cpu().numpy()) <= 1e-4
+
+
+def test_batched_many_tiny_and_ragged_cameras(cuda_device):
+    """32 cameras (the most one batch takes), down to 1x1 pixel images."""
+    dev = cuda_device
+    s = _scene(P=5000, seed=4)
+    T = tensors(s, dev)
+    sizes = [(1, 1), (17, 3), (5, 40), (33, 17), (64, 64), (15, 16), (16, 15), (129, 7)] * 4
+    cams = _cameras(sizes=sizes, seed=6)
+    sets = [_settings(c, dev) for c in cams]
+    rast, _ = _batched(T, sets)
+    imgs = rast.images()
+    ties = _tie_masks(rast)
+    assert len(imgs) == 32 and imgs[0].shape == (3, 1, 1)
+    for k, st in enumerate(sets):
+        img, radii = _plain(T, st)[:2]
+        assert torch.equal(rast.radii[k], radii), k
+        d = (imgs[k] - img).abs().amax(0).cpu().numpy()
+        assert d[~ties[k]].max(initial=0.0) <= 1e-6, k
+    with pytest.raises(ValueError):
+        BatchedRasterizer(sets + sets[:1], s.P)  # 33 cameras
+
+
+def test_batched_zero_gaussians_gives_background(cuda_device):
+    dev = cuda_device
+    cams = _cameras(sizes=[(40, 30), (16, 16)])
+    sets = [_settings(c, dev, bg) for c, bg in zip(cams, _bgs(2))]
+    e = torch.empty((0, 3), device=dev)
+    rast = BatchedRasterizer(sets, 0, pair_capacity=1024)
+    rast.forward(e, torch.empty((0, 1), device=dev), torch.empty((0, 1, 3), device=dev), torch.empty((0, 15, 3), device=dev),
+                 None, e, torch.empty((0, 4), device=dev), None, 3)
+    g = rast.backward(torch.ones(rast.out_color.numel(), device=dev), e, torch.empty((0, 1, 3), device=dev),
+                      torch.empty((0, 15, 3), device=dev), e, torch.empty((0, 4), device=dev), 3)
+    torch.cuda.synchronize()
+    assert _C.device_errors(dev) == 0
+    for k, im in enumerate(rast.images()):
+        bg = torch.tensor(_bgs(2)[k], device=dev, dtype=torch.float32).view(3, 1, 1)
+        assert torch.equal(im, bg.expand_as(im)), k
+    assert rast.status() == (0, 0)
+    assert g["means3D"].numel() == 0
