@@ -1,6 +1,6 @@
 """``_C`` of the rasterizer: the ``ops`` namespace FB's Python layer calls.
 
-Mirrors FB csrc/pybind.cpp:371-416 (``_C.ops.preprocess``, ``sort_gaussian``,
+Mirrors FB csrc/pybind.cpp:135-416 (``_C.ops.preprocess``, ``sort_gaussian``,
 ``get_sort_buffer_size``, ``render_16x16``, ``backward``, ``adamUpdate``,
 ``render_simp``, ``render_depth``) with the same argument order, tensor
 shapes and dtypes.  Each op validates its tensors, takes raw device pointers
@@ -225,14 +225,38 @@ def adamUpdate(param, param_grad, exp_avg, exp_avg_sq, visible, lr, b1, b2, eps,
               float(lr), float(b1), float(b2), float(eps), int(N), int(M), _stream(dev))
 
 
-def render_simp(*args, **kwargs):
-    """FB pybind.cpp:179-208 binds this importance pass; no FasterGS caller uses it through FB."""
-    raise NotImplementedError("render_simp is not implemented by the GB300 backend")
+def render_simp(P, num_rendered, width, height, splat_buffer, gaussian_keys_sorted, gaussian_values_sorted, ranges):
+    """FB pybind.cpp:179-208 (importance pass).  Returns (bucket_sum = 0, accum_weights_ptr (P,) f32,
+    accum_weights_count (P,) i32, accum_max_count (P,) f32)."""
+    dev = _device_of(splat_buffer)
+    f = dict(device=dev)
+    w = torch.empty(P, dtype=torch.float32, **f)
+    cnt = torch.empty(P, dtype=torch.int32, **f)
+    mx = torch.empty(P, dtype=torch.float32, **f)
+    _lib.call("fgs_render_simp", int(P), int(num_rendered), int(width), int(height), _ptr(splat_buffer),
+              _ptr(gaussian_keys_sorted), _ptr(gaussian_values_sorted), _ptr(ranges), _ptr(w), _ptr(cnt), _ptr(mx),
+              _stream(dev))
+    return 0, w, cnt, mx
 
 
-def render_depth(*args, **kwargs):
-    """FB pybind.cpp:135-176 binds this depth pass; no FasterGS caller uses it through FB."""
-    raise NotImplementedError("render_depth is not implemented by the GB300 backend")
+def render_depth(P, num_rendered, width, height, splat_buffer, gaussian_keys_sorted, gaussian_values_sorted, ranges,
+                 means3D, scales, rotations, proj_matrix, campos):
+    """FB pybind.cpp:135-176 (depth pass).  Returns (out_pts (3,H,W), out_depth (1,H,W), accum_alpha (1,H,W),
+    gidx (1,H,W) i32, discriminants (1,H,W))."""
+    dev = _device_of(splat_buffer)
+    H, W = int(height), int(width)
+    f = dict(dtype=torch.float32, device=dev)
+    out_pts = torch.empty((3, H, W), **f)
+    out_depth = torch.empty((1, H, W), **f)
+    accum_alpha = torch.empty((1, H, W), **f)
+    gidx = torch.empty((1, H, W), dtype=torch.int32, device=dev)
+    disc = torch.empty((1, H, W), **f)
+    _lib.call("fgs_render_depth", int(P), int(num_rendered), W, H, _ptr(splat_buffer), _ptr(gaussian_keys_sorted),
+              _ptr(gaussian_values_sorted), _ptr(ranges), _ptr(_f32("means3D", means3D, dev)),
+              _ptr(_f32("scales", scales, dev)), _ptr(_f32("rotations", rotations, dev)),
+              _ptr(_f32("proj_matrix", proj_matrix, dev)), _ptr(_f32("campos", campos, dev)), _ptr(out_pts),
+              _ptr(out_depth), _ptr(accum_alpha), _ptr(gidx), _ptr(disc), _stream(dev))
+    return out_pts, out_depth, accum_alpha, gidx, disc
 
 
 def device_errors(dev: torch.device | None = None, clear: bool = True) -> int:

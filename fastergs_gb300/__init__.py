@@ -60,6 +60,32 @@ def _host_counts(dev) -> torch.Tensor:
     return _HOST_COUNTS[key]
 
 
+def _bin(buffer, rs, means3D, dc, shs, colors_precomp, opacities, scales, rotations, culling):
+    """Preprocess and sort into the shared Buffer (FB __init__.py:96-119): returns (radii, num_rendered)."""
+    buffer.curr_offset.fill_(0)
+    radii = _C.ops.preprocess(
+        rs.sh_degree, means3D, colors_precomp, dc, shs, opacities, scales, rotations, rs.scale_modifier,
+        rs.image_width, rs.image_height, 16, 16, rs.campos, rs.viewmatrix, rs.projmatrix, rs.tanfovx, rs.tanfovy,
+        100.0, 0.01, buffer.gaussian_keys_unsorted, buffer.gaussian_values_unsorted, buffer.gaussian_values_sorted,
+        buffer.curr_offset, rs.mult, buffer.splat_buffer, culling)
+    # One host read per frame (FB's K read): the pair count and the
+    # large-footprint task count, copied together, one synchronisation.
+    counts = _host_counts(means3D.device)
+    counts[0].copy_(buffer.curr_offset[0], non_blocking=True)
+    counts[1].copy_(_C._counters(means3D.device)[0], non_blocking=True)
+    torch.cuda.current_stream(means3D.device).synchronize()
+    num_rendered, num_tasks = int(counts[0]), int(counts[1])
+    if num_rendered >= buffer.MAX_NUM_RENDERED or num_tasks > buffer.gaussian_values_sorted.numel() // 2:
+        _C.device_errors(means3D.device)  # clears the capacity bit the skipped writes latched
+        if num_rendered >= buffer.MAX_NUM_RENDERED:
+            raise RuntimeError("Too many k-v pairs!")
+        raise RuntimeError("preprocess overflowed a device queue (too many large Gaussians)")
+    _C.ops.sort_gaussian(num_rendered, rs.image_width, rs.image_height, 16, 16, buffer.list_sorting_space,
+                         buffer.gaussian_keys_unsorted, buffer.gaussian_values_unsorted, buffer.gaussian_keys_sorted,
+                         buffer.gaussian_values_sorted)
+    return radii, num_rendered
+
+
 class _LazyBuffer:
     """Class attribute that allocates the shared Buffer on first access."""
 
@@ -92,32 +118,9 @@ class _RasterizeGaussians(torch.autograd.Function):
                 raster_settings, culling, xyz_gradient_accum, xyz_gradient_accum_abs, max_radii, denom):
         buffer = _RasterizeGaussians.buffer
         splat_buffer = buffer.splat_buffer
-        zFar, zNear = 100.0, 0.01
         N = means3D.shape[0]
-        buffer.curr_offset.fill_(0)
-        radii = _C.ops.preprocess(
-            raster_settings.sh_degree, means3D, colors_precomp, dc, shs, opacities, scales, rotations,
-            raster_settings.scale_modifier, raster_settings.image_width, raster_settings.image_height, 16, 16,
-            raster_settings.campos, raster_settings.viewmatrix, raster_settings.projmatrix,
-            raster_settings.tanfovx, raster_settings.tanfovy, zFar, zNear,
-            buffer.gaussian_keys_unsorted, buffer.gaussian_values_unsorted, buffer.gaussian_values_sorted,
-            buffer.curr_offset, raster_settings.mult, splat_buffer, culling)
-        # One host read per frame (FB's K read): the pair count and the
-        # large-footprint task count, copied together, one synchronisation.
-        counts = _host_counts(means3D.device)
-        counts[0].copy_(buffer.curr_offset[0], non_blocking=True)
-        counts[1].copy_(_C._counters(means3D.device)[0], non_blocking=True)
-        torch.cuda.current_stream(means3D.device).synchronize()
-        num_rendered, num_tasks = int(counts[0]), int(counts[1])
-        if num_rendered >= buffer.MAX_NUM_RENDERED or num_tasks > buffer.gaussian_values_sorted.numel() // 2:
-            _C.device_errors(means3D.device)  # clears the capacity bit the skipped writes latched
-            if num_rendered >= buffer.MAX_NUM_RENDERED:
-                raise RuntimeError("Too many k-v pairs!")
-            raise RuntimeError("preprocess overflowed a device queue (too many large Gaussians)")
-        _C.ops.sort_gaussian(num_rendered, raster_settings.image_width, raster_settings.image_height, 16, 16,
-                             buffer.list_sorting_space, buffer.gaussian_keys_unsorted,
-                             buffer.gaussian_values_unsorted, buffer.gaussian_keys_sorted,
-                             buffer.gaussian_values_sorted)
+        radii, num_rendered = _bin(buffer, raster_settings, means3D, dc, shs, colors_precomp, opacities, scales,
+                                   rotations, culling)
         H, W = raster_settings.image_height, raster_settings.image_width
         # every pixel is written by the merge, so no zero-fill is needed
         last_contributor = torch.empty((H, W, 1), device=means3D.device, dtype=torch.int)
@@ -200,6 +203,56 @@ class GaussianRasterizer(nn.Module):
         return rasterize_gaussians(means3D, dc, shs, colors_precomp, opacities, scales, rotations, cov3D_precomp,
                                    self.raster_settings, culling, xyz_gradient_accum, xyz_gradient_accum_abs,
                                    max_radii, denom)
+
+
+def _inputs(means3D, opacities, dc, shs, colors_precomp, scales, rotations, culling):
+    empty = torch.tensor([])
+    return (empty if dc is None else dc, empty if shs is None else shs,
+            empty if colors_precomp is None else colors_precomp,
+            empty if scales is None else scales, empty if rotations is None else rotations,
+            torch.tensor([], dtype=torch.bool) if culling is None else culling)
+
+
+def _render_simp(self, means3D, opacities, dc=None, shs=None, colors_precomp=None, scales=None, rotations=None,
+                 cov3D_precomp=None, culling=None):
+    """Importance pass (FB _C.ops.render_simp, called as Mini-Splatting 2's faster renderer does,
+    mini-splatting2/gaussian_renderer/render_faster.py:181): returns (radii, accum_weights (P,),
+    accum_weights_count (P,), accum_max_count (P,))."""
+    if cov3D_precomp is not None:
+        raise NotImplementedError("precomputed 3D covariances are not supported (FB needs scales and rotations)")
+    dc, shs, colors_precomp, scales, rotations, culling = _inputs(means3D, opacities, dc, shs, colors_precomp,
+                                                                  scales, rotations, culling)
+    rs = self.raster_settings
+    buffer = _RasterizeGaussians.buffer
+    with torch.no_grad():
+        radii, K = _bin(buffer, rs, means3D, dc, shs, colors_precomp, opacities, scales, rotations, culling)
+        _, w, cnt, mx = _C.ops.render_simp(means3D.shape[0], K, rs.image_width, rs.image_height, buffer.splat_buffer,
+                                           buffer.gaussian_keys_sorted, buffer.gaussian_values_sorted, buffer.ranges)
+    return radii, w, cnt, mx
+
+
+def _render_depth(self, means3D, opacities, dc=None, shs=None, colors_precomp=None, scales=None, rotations=None,
+                  cov3D_precomp=None, culling=None):
+    """Depth pass (FB _C.ops.render_depth, called as Mini-Splatting 2's faster renderer does,
+    mini-splatting2/gaussian_renderer/render_faster.py:238): returns a dict with "out_pts" (3,H,W),
+    "rendered_depth", "accum_alpha", "gidx", "discriminants" (1,H,W) and "radii"."""
+    if cov3D_precomp is not None:
+        raise NotImplementedError("precomputed 3D covariances are not supported (FB needs scales and rotations)")
+    dc, shs, colors_precomp, scales, rotations, culling = _inputs(means3D, opacities, dc, shs, colors_precomp,
+                                                                  scales, rotations, culling)
+    rs = self.raster_settings
+    buffer = _RasterizeGaussians.buffer
+    with torch.no_grad():
+        radii, K = _bin(buffer, rs, means3D, dc, shs, colors_precomp, opacities, scales, rotations, culling)
+        pts, depth, alpha, gidx, disc = _C.ops.render_depth(
+            means3D.shape[0], K, rs.image_width, rs.image_height, buffer.splat_buffer, buffer.gaussian_keys_sorted,
+            buffer.gaussian_values_sorted, buffer.ranges, means3D, scales, rotations, rs.projmatrix, rs.campos)
+    return {"out_pts": pts, "rendered_depth": depth, "discriminants": disc, "gidx": gidx, "accum_alpha": alpha,
+            "radii": radii}
+
+
+GaussianRasterizer.render_simp = _render_simp
+GaussianRasterizer.render_depth = _render_depth
 
 
 class SparseGaussianAdam(torch.optim.Adam):

@@ -51,6 +51,8 @@ SIGNATURES = {
     "fgs_preprocess_bwd": (i32, [i32, i32, i32, vp, vp, vp, vp, vp, vp, vp, f32, vp, vp, i32, i32, f32, f32, vp,
                                  vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp]),
     "fgs_densify_stats": (i32, [i32, vp, vp, vp, vp, vp, vp, vp]),
+    "fgs_render_simp": (i32, [i32, i64, i32, i32, vp, vp, vp, vp, vp, vp, vp, vp]),
+    "fgs_render_depth": (i32, [i32, i64, i32, i32, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp]),
     "fgs_adam_update": (i32, [vp, vp, vp, vp, vp, f32, f32, f32, f32, C.c_uint32, C.c_uint32, vp]),
     "fgs_batch_workspace_bytes": (i32, [i32, i32, camp, tunep, i64, C.POINTER(C.c_size_t)]),
     "fgs_render_batched_fwd": (i32, [i32, i32, i32, vp, vp, vp, vp, vp, vp, vp, vp, i32, camp, tunep, i64, vp, sz,

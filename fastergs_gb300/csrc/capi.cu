@@ -101,14 +101,15 @@ __device__ float g_peak_sink;
 
 // Every translation unit's error word, gathered (and optionally cleared) by
 // one tiny kernel so that reading them costs one synchronisation.
+constexpr int kErrorUnits = 5;
 struct ErrorWords {
-  int* w[4];
+  int* w[kErrorUnits];
 };
 __device__ int g_error_gather;
 __global__ void k_gather_errors(ErrorWords e, bool clear, int* out) {
   if (threadIdx.x != 0) return;
   int v = 0;
-  for (int j = 0; j < 4; ++j) {
+  for (int j = 0; j < kErrorUnits; ++j) {
     v |= clear ? atomicExch(e.w[j], 0) : atomicOr(e.w[j], 0);
   }
   *out = v;
@@ -187,7 +188,7 @@ extern "C" fgs_status fgs_device_errors(int* flags, int clear, void* stream) {
     std::lock_guard<std::mutex> lk(mu);
     if (!have[dev]) {
       cache[dev] = fgs::ErrorWords{{fgs::error_word_preprocess(), fgs::error_word_sort(), fgs::error_word_render(),
-                                    fgs::error_word_backward()}};
+                                    fgs::error_word_backward(), fgs::error_word_aux()}};
       for (int* p : cache[dev].w)
         if (!p) return FGS_ERR_CUDA;
       have[dev] = true;

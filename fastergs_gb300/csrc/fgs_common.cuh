@@ -314,6 +314,7 @@ int* error_word_preprocess();
 int* error_word_sort();
 int* error_word_render();
 int* error_word_backward();
+int* error_word_aux();
 // Optional per-kernel event timing (fgs_kernel_timer).  Usage around a launch:
 //   KernelTimer kt(FGS_K_RENDER_FWD, stream); launch...; kt.stop();
 void timer_begin(int id, cudaStream_t s);

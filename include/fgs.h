@@ -179,6 +179,34 @@ fgs_status fgs_preprocess_bwd(
 fgs_status fgs_densify_stats(int P, const int32_t* radii, const float* dL_dmean2D, float* xyz_gradient_accum,
                              float* xyz_gradient_accum_abs, float* max_radii, float* denom, void* stream);
 
+/*
+ * Importance pass (FB render_16x16_simp, csrc/ops.h; pybind.cpp:179-208;
+ * render_simp.cu): per Gaussian the sum of blend weights alpha T over the
+ * pixels of its tiles, the number of pixels where alpha >= 1/255, and the
+ * number of pixels where it has the largest weight; each 16x16 tile composites
+ * its list in order and stops after a pair of Gaussians once all its pixels
+ * have T < 1e-4.  Computes the tile ranges first (like FB).  Outputs (P) are
+ * zeroed and fully written.
+ */
+fgs_status fgs_render_simp(int P, int64_t num_rendered, int width, int height, const float* splat_buffer,
+                           const uint64_t* keys_sorted, const uint32_t* values_sorted, uint32_t* ranges,
+                           float* accum_weights, int32_t* accum_count, float* accum_max_count, void* stream);
+
+/*
+ * Depth pass (FB render_16x16_depth; pybind.cpp:135-176; render_depth.cu):
+ * per pixel, along the ray through the pixel, the Gaussian of largest weight
+ * gives out_pts (3,H,W) (closest point of its 3-sigma ellipsoid to the ray),
+ * out_depth (H,W), discriminants (H,W) and gidx (H,W); accum_alpha (H,W) is
+ * the final transmittance.  means3D (P,3), scales (P,3) activated without
+ * the scale modifier, rotations (P,4), projmatrix the full projection,
+ * campos (3).
+ */
+fgs_status fgs_render_depth(int P, int64_t num_rendered, int width, int height, const float* splat_buffer,
+                            const uint64_t* keys_sorted, const uint32_t* values_sorted, uint32_t* ranges,
+                            const float* means3D, const float* scales, const float* rotations,
+                            const float* projmatrix, const float* campos, float* out_pts, float* out_depth,
+                            float* accum_alpha, int32_t* gidx, float* discriminants, void* stream);
+
 /* Masked Adam step over N rows of M floats; rows with visible[i]==0 are left
  * untouched.  Replaces ADAM::adamUpdate (FB adam.h, adam.cu:9-66). */
 fgs_status fgs_adam_update(float* param, const float* grad, float* exp_avg, float* exp_avg_sq,

@@ -65,6 +65,8 @@ def load():
             "orc_get_image": (None, [vp, vp, vp, vp, vp, vp, vp]),
             "orc_backward": (None, [vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp]),
             "orc_densify": (None, [vp, vp, vp, vp, vp, vp]),
+            "orc_render_simp": (None, [vp, f64, f64, f64, vp, vp, vp, vp]),
+            "orc_render_depth": (None, [vp, f64, f64, f64, vp, vp, vp, vp, vp, vp]),
             "orc_num_threads": (i32, []),
             "orc_set_threads": (None, [i32]),
             "orc_eval_sh": (None, [i32, i32, vp, vp, vp]),
@@ -199,6 +201,22 @@ class Oracle:
                                                                      "dmean3D", "dcov3D", "ddc", "dsh", "dscale",
                                                                      "drot")])
         return out
+
+    def render_simp(self, eps_alpha=1e-5, eps_T=1e-5, eps_w=1e-5):
+        """Importance pass on the current records and lists: per-Gaussian weight sums, counts, max counts."""
+        P = self.P
+        w, c, m, amb = np.empty(P), np.empty(P, np.int32), np.empty(P), np.empty(P, np.uint8)
+        self.lib.orc_render_simp(self.h, float(eps_alpha), float(eps_T), float(eps_w), _p(w), _p(c), _p(m), _p(amb))
+        return dict(weights=w, counts=c, max_counts=m, ambiguous=amb.astype(bool))
+
+    def render_depth(self, eps_alpha=1e-5, eps_T=1e-5, eps_w=1e-5):
+        """Depth pass on the current records and lists (per-pixel outputs, ambiguity flags)."""
+        H, W = self.H, self.W
+        pts, d, a, dsc = np.empty((3, H, W)), np.empty((H, W)), np.empty((H, W)), np.empty((H, W))
+        g, amb = np.empty((H, W), np.int32), np.empty((H, W), np.uint8)
+        self.lib.orc_render_depth(self.h, float(eps_alpha), float(eps_T), float(eps_w), _p(pts), _p(d), _p(a),
+                                  _p(g), _p(dsc), _p(amb))
+        return dict(out_pts=pts, out_depth=d, accum_alpha=a, gidx=g, discriminants=dsc, ambiguous=amb.astype(bool))
 
     def densify(self, dmean2D, grad_accum=None, grad_accum_abs=None, max_radii=None, denom=None):
         arrs = [_d(dmean2D), _d(grad_accum), _d(grad_accum_abs), _d(max_radii), _d(denom)]

@@ -28,6 +28,8 @@
 //   FB/csrc/cuda_rasterizer/backward.cu:250-403    conic/cov2D/cov3D/mean backward
 //   FB/csrc/cuda_rasterizer/backward.cu:121-245,407-539  SH, scale/rotation, projection backward
 //   FB/csrc/cuda_rasterizer/backward.cu:892-918    densification statistics
+//   FB/csrc/cuda_rasterizer/render_simp.cu:35-284  importance pass (per-tile, pairwise stop)
+//   FB/csrc/cuda_rasterizer/render_depth.cu:97-327 depth pass (per pixel, ray / 3-sigma ellipsoid)
 //
 // Build: g++ -O2 -fopenmp -shared -fPIC oracle/oracle.cpp -o oracle/liboracle.so
 #include <algorithm>
@@ -454,6 +456,174 @@ void composite(Scene& s) {
   s.n_clamped = n_cl;
 }
 
+// Importance pass (render_simp.cu:35-284): each tile walks its list in
+// order; a Gaussian with alpha >= 1/255 at a pixel adds its weight alpha T
+// (T -= weight) to the Gaussian's sum and 1 to its count, and the pixel keeps
+// the Gaussian of largest weight; after every pair of Gaussians (a lone
+// first one when the count is odd) the tile stops if every one of its 256
+// pixels has T < 1e-4 (pixels outside the image keep T = 1).  amb flags
+// Gaussians whose sums or counts are within rounding distance of a different
+// decision (alpha at the cut, a stop test at 1e-4, a near-tie for the
+// largest weight).
+void render_simp(const Scene& s, double eps_alpha, double eps_T, double eps_w, double* wsum, int* wcnt,
+                 double* wmaxcnt, uint8_t* amb) {
+  const Cam& c = s.cam;
+  const int T = s.T(), tp = 256;
+  const double cut = 1.0 / 255.0;
+  std::fill(wsum, wsum + s.P, 0.0);
+  std::fill(wcnt, wcnt + s.P, 0);
+  std::fill(wmaxcnt, wmaxcnt + s.P, 0.0);
+  std::fill(amb, amb + s.P, 0);
+  for (int t = 0; t < T; ++t) {
+    const int tx = t % c.gx, ty = t / c.gx, start = s.ranges[2 * t], end = s.ranges[2 * t + 1], n = end - start;
+    std::vector<double> Tp(tp, 1.0), wmax(tp, 0.0), wsecond(tp, 0.0);
+    std::vector<int> imax(tp, -1);
+    std::vector<uint8_t> inside(tp, 0);
+    for (int lp = 0; lp < tp; ++lp) {
+      const int px = tx * 16 + lp % 16, py = ty * 16 + lp / 16;
+      inside[lp] = px < c.W && py < c.H;
+    }
+    const int odd = n & 1;
+    bool tile_amb = false;
+    for (int i = 0; i < n; ++i) {
+      const int g = s.ids[start + i];
+      const double* r = &s.rec[(size_t)g * REC];
+      double sum = 0;
+      int cnt = 0;
+      for (int lp = 0; lp < tp; ++lp) {
+        if (!inside[lp]) continue;
+        const int px = tx * 16 + lp % 16, py = ty * 16 + lp / 16;
+        double a = std::min(0.99, alpha_of(r, px, py).a);
+        if (std::fabs(a - cut) <= eps_alpha * cut) amb[g] = 1;
+        if (a < cut) continue;
+        const double w = a * Tp[lp];
+        Tp[lp] -= w;
+        sum += w;
+        cnt += 1;
+        if (wmax[lp] < w) { wsecond[lp] = wmax[lp]; wmax[lp] = w; imax[lp] = g; }
+        else if (wsecond[lp] < w) wsecond[lp] = w;
+      }
+      if (g < s.P) { wsum[g] += sum; wcnt[g] += cnt; }
+      if (tile_amb) amb[g] = 1;
+      if (i >= odd && ((i - odd) & 1)) {
+        bool done = true, near = false;
+        for (int lp = 0; lp < tp; ++lp) {
+          done = done && inside[lp] && Tp[lp] < 1e-4;
+          if (inside[lp] && std::fabs(Tp[lp] - 1e-4) <= eps_T * 1e-4) near = true;
+        }
+        if (near) tile_amb = true;
+        if (done) break;
+      }
+    }
+    for (int lp = 0; lp < tp; ++lp) {
+      if (!inside[lp] || imax[lp] < 0) continue;
+      wmaxcnt[imax[lp]] += 1.0;
+      if (wmax[lp] - wsecond[lp] <= eps_w * wmax[lp]) amb[imax[lp]] = 1;
+    }
+    if (tile_amb)
+      for (int i = 0; i < n; ++i) amb[s.ids[start + i]] = 1;
+  }
+}
+
+// 4x4 inverse (column-major, cofactors).
+void invert4(const double* a, double* out) {
+  double inv[16];
+  inv[0] = a[5] * a[10] * a[15] - a[5] * a[11] * a[14] - a[9] * a[6] * a[15] + a[9] * a[7] * a[14] + a[13] * a[6] * a[11] - a[13] * a[7] * a[10];
+  inv[4] = -a[4] * a[10] * a[15] + a[4] * a[11] * a[14] + a[8] * a[6] * a[15] - a[8] * a[7] * a[14] - a[12] * a[6] * a[11] + a[12] * a[7] * a[10];
+  inv[8] = a[4] * a[9] * a[15] - a[4] * a[11] * a[13] - a[8] * a[5] * a[15] + a[8] * a[7] * a[13] + a[12] * a[5] * a[11] - a[12] * a[7] * a[9];
+  inv[12] = -a[4] * a[9] * a[14] + a[4] * a[10] * a[13] + a[8] * a[5] * a[14] - a[8] * a[6] * a[13] - a[12] * a[5] * a[10] + a[12] * a[6] * a[9];
+  inv[1] = -a[1] * a[10] * a[15] + a[1] * a[11] * a[14] + a[9] * a[2] * a[15] - a[9] * a[3] * a[14] - a[13] * a[2] * a[11] + a[13] * a[3] * a[10];
+  inv[5] = a[0] * a[10] * a[15] - a[0] * a[11] * a[14] - a[8] * a[2] * a[15] + a[8] * a[3] * a[14] + a[12] * a[2] * a[11] - a[12] * a[3] * a[10];
+  inv[9] = -a[0] * a[9] * a[15] + a[0] * a[11] * a[13] + a[8] * a[1] * a[15] - a[8] * a[3] * a[13] - a[12] * a[1] * a[11] + a[12] * a[3] * a[9];
+  inv[13] = a[0] * a[9] * a[14] - a[0] * a[10] * a[13] - a[8] * a[1] * a[14] + a[8] * a[2] * a[13] + a[12] * a[1] * a[10] - a[12] * a[2] * a[9];
+  inv[2] = a[1] * a[6] * a[15] - a[1] * a[7] * a[14] - a[5] * a[2] * a[15] + a[5] * a[3] * a[14] + a[13] * a[2] * a[7] - a[13] * a[3] * a[6];
+  inv[6] = -a[0] * a[6] * a[15] + a[0] * a[7] * a[14] + a[4] * a[2] * a[15] - a[4] * a[3] * a[14] - a[12] * a[2] * a[7] + a[12] * a[3] * a[6];
+  inv[10] = a[0] * a[5] * a[15] - a[0] * a[7] * a[13] - a[4] * a[1] * a[15] + a[4] * a[3] * a[13] + a[12] * a[1] * a[7] - a[12] * a[3] * a[5];
+  inv[14] = -a[0] * a[5] * a[14] + a[0] * a[6] * a[13] + a[4] * a[1] * a[14] - a[4] * a[2] * a[13] - a[12] * a[1] * a[6] + a[12] * a[2] * a[5];
+  inv[3] = -a[1] * a[6] * a[11] + a[1] * a[7] * a[10] + a[5] * a[2] * a[11] - a[5] * a[3] * a[10] - a[9] * a[2] * a[7] + a[9] * a[3] * a[6];
+  inv[7] = a[0] * a[6] * a[11] - a[0] * a[7] * a[10] - a[4] * a[2] * a[11] + a[4] * a[3] * a[10] + a[8] * a[2] * a[7] - a[8] * a[3] * a[6];
+  inv[11] = -a[0] * a[5] * a[11] + a[0] * a[7] * a[9] + a[4] * a[1] * a[11] - a[4] * a[3] * a[9] - a[8] * a[1] * a[7] + a[8] * a[3] * a[5];
+  inv[15] = a[0] * a[5] * a[10] - a[0] * a[6] * a[9] - a[4] * a[1] * a[10] + a[4] * a[2] * a[9] + a[8] * a[1] * a[6] - a[8] * a[2] * a[5];
+  const double det = a[0] * inv[0] + a[1] * inv[4] + a[2] * inv[8] + a[3] * inv[12];
+  for (int i = 0; i < 16; ++i) out[i] = det != 0 ? inv[i] / det : 0.0;
+}
+
+// Depth pass (render_depth.cu:97-327).  Per pixel: the ray from the camera
+// through the pixel's NDC point (2p+1)/S - 1, scaled by 1.0000001, at
+// z = 99/99.99, mapped by the inverse full projection without dividing by w;
+// Gaussians in list order: alpha < 1/255 skipped, stop before one that would
+// take T below 1e-4, then the closest approach of the ray to the Gaussian's
+// 3-sigma ellipsoid (raw quaternion, scales without the modifier); a
+// Gaussian behind the camera is skipped without changing T; the one of
+// largest weight alpha T gives point, depth, discriminant and index.  amb
+// flags pixels within rounding distance of a different decision.
+void render_depth(const Scene& s, double eps_alpha, double eps_T, double eps_w, double* out_pts, double* out_depth,
+                  double* accum_alpha, int* gidx, double* disc, uint8_t* amb) {
+  const Cam& c = s.cam;
+  const double cut = 1.0 / 255.0;
+  const size_t HW = (size_t)c.W * c.H;
+  double inv[16];
+  invert4(c.proj, inv);
+  const double* o = c.campos;
+#pragma omp parallel for schedule(dynamic, 8)
+  for (int pix = 0; pix < (int)HW; ++pix) {
+    const int px = pix % c.W, py = pix / c.W;
+    const int t = (py / 16) * c.gx + px / 16;
+    const double nx = ((2.0 * px + 1.0) / c.W - 1.0) * 1.0000001, ny = ((2.0 * py + 1.0) / c.H - 1.0) * 1.0000001;
+    const double nz = (100.0 - 100.0 * 0.01) / (100.0 - 0.01);
+    double rd[3];
+    for (int k = 0; k < 3; ++k) rd[k] = inv[k] * nx + inv[4 + k] * ny + inv[8 + k] * nz + inv[12 + k] - o[k];
+    const double rlen = std::sqrt(rd[0] * rd[0] + rd[1] * rd[1] + rd[2] * rd[2]);
+    const double dn[3] = {rd[0] / rlen, rd[1] / rlen, rd[2] / rlen};
+    double T = 1, wmax = 0, wsecond = 0, dmax = 0, dsc = 0, pr[3] = {0, 0, 0};
+    int im = 0;
+    bool a_flag = false;
+    for (int j = s.ranges[2 * t]; j < s.ranges[2 * t + 1]; ++j) {
+      const int g = s.ids[j];
+      const double* r = &s.rec[(size_t)g * REC];
+      const double a = std::min(0.99, alpha_of(r, px, py).a);
+      if (std::fabs(a - cut) <= eps_alpha * cut) a_flag = true;
+      if (a < cut) continue;
+      const double test_T = T * (1 - a);
+      if (std::fabs(test_T - 1e-4) <= eps_T * 1e-4) a_flag = true;
+      if (test_T < 1e-4) break;
+      const double* q = &s.rots[4 * (size_t)g];
+      const double qr = q[0], qx = q[1], qy = q[2], qz = q[3];
+      const double R[3][3] = {{1 - 2 * (qy * qy + qz * qz), 2 * (qx * qy - qr * qz), 2 * (qx * qz + qr * qy)},
+                              {2 * (qx * qy + qr * qz), 1 - 2 * (qx * qx + qz * qz), 2 * (qy * qz - qr * qx)},
+                              {2 * (qx * qz - qr * qy), 2 * (qy * qz + qr * qx), 1 - 2 * (qx * qx + qy * qy)}};
+      const double* m = &s.means[3 * (size_t)g];
+      const double* sc = &s.scales[3 * (size_t)g];
+      double lo[3], ld[3];
+      for (int k = 0; k < 3; ++k) {
+        lo[k] = (R[0][k] * (o[0] - m[0]) + R[1][k] * (o[1] - m[1]) + R[2][k] * (o[2] - m[2])) / (3 * sc[k]);
+        ld[k] = (R[0][k] * dn[0] + R[1][k] * dn[1] + R[2][k] * dn[2]) / (3 * sc[k]);
+      }
+      const double qa = ld[0] * ld[0] + ld[1] * ld[1] + ld[2] * ld[2];
+      const double qb = 2 * (ld[0] * lo[0] + ld[1] * lo[1] + ld[2] * lo[2]);
+      const double qc = lo[0] * lo[0] + lo[1] * lo[1] + lo[2] * lo[2] - 1;
+      const double tmin = -qb / 2 / qa;
+      const double depth = tmin / rlen;
+      if (std::fabs(depth) <= 1e-9) a_flag = true;
+      if (depth < 0) continue;
+      const double w = a * T;
+      if (wmax < w) {
+        wsecond = wmax; wmax = w; dmax = depth; dsc = qb * qb - 4 * qa * qc; im = g;
+        for (int k = 0; k < 3; ++k) pr[k] = o[k] + tmin * dn[k];
+      } else if (wsecond < w) {
+        wsecond = w;
+      }
+      T = test_T;
+    }
+    for (int k = 0; k < 3; ++k) out_pts[k * HW + pix] = pr[k];
+    out_depth[pix] = dmax;
+    accum_alpha[pix] = T;
+    disc[pix] = dsc;
+    gidx[pix] = im;
+    amb[pix] = (a_flag || (wmax > 0 && wmax - wsecond <= eps_w * wmax)) ? 1 : 0;
+  }
+}
+
 inline void atomic_add(double& dst, double v) {
 #pragma omp atomic
   dst += v;
@@ -818,6 +988,16 @@ void orc_get_decisions(void* h, int64_t* counts, uint8_t* gauss_clamped) {
   Scene& s = *static_cast<Scene*>(h);
   if (counts) { counts[0] = s.n_alpha_on; counts[1] = s.n_clamped; }
   if (gauss_clamped) std::memcpy(gauss_clamped, s.gauss_clamped.data(), s.gauss_clamped.size());
+}
+
+void orc_render_simp(void* h, double eps_alpha, double eps_T, double eps_w, double* wsum, int* wcnt,
+                     double* wmaxcnt, uint8_t* amb) {
+  render_simp(*static_cast<Scene*>(h), eps_alpha, eps_T, eps_w, wsum, wcnt, wmaxcnt, amb);
+}
+
+void orc_render_depth(void* h, double eps_alpha, double eps_T, double eps_w, double* out_pts, double* out_depth,
+                      double* accum_alpha, int* gidx, double* disc, uint8_t* amb) {
+  render_depth(*static_cast<Scene*>(h), eps_alpha, eps_T, eps_w, out_pts, out_depth, accum_alpha, gidx, disc, amb);
 }
 
 int orc_num_threads() {

@@ -38,11 +38,15 @@ def test_cpu_tensors_are_refused_not_emulated():
                           1.0, t, t)
 
 
-def test_unimplemented_ops_say_so():
-    with pytest.raises(NotImplementedError):
-        _C.ops.render_simp()
-    with pytest.raises(NotImplementedError):
-        _C.ops.render_depth()
+def test_auxiliary_passes_are_bound_with_fb_signatures():
+    import inspect
+    assert list(inspect.signature(_C.ops.render_simp).parameters) == [
+        "P", "num_rendered", "width", "height", "splat_buffer", "gaussian_keys_sorted", "gaussian_values_sorted",
+        "ranges"]
+    assert list(inspect.signature(_C.ops.render_depth).parameters)[-5:] == [
+        "means3D", "scales", "rotations", "proj_matrix", "campos"]
+    from fastergs_gb300 import GaussianRasterizer
+    assert callable(GaussianRasterizer.render_simp) and callable(GaussianRasterizer.render_depth)
 
 
 def test_scenes_are_seeded_and_shaped():
