@@ -62,6 +62,7 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-checkpoint", action="store_true")
+    ap.add_argument("--no-adam", action="store_true")
     ap.add_argument("--cameras", type=int, default=16)
     ap.add_argument("--tune", choices=["sweep", "default"], default="sweep",
                     help="batched launch config: autotuner sweep (18 configs) or FB's fixed choice")
@@ -297,6 +298,9 @@ def gpu_bench(args, rank, local, world):
         e2e_ms = max_over_ranks(ev0.elapsed_time(ev1) / args.steps, world, dev)
         e2e = {"value": e2e_ms / world, "unit": "ms/step", "h2d_bytes_per_step": int(in_bytes),
                "d2h_bytes_per_step": int(out_bytes), "wall_ms_per_step": (time.perf_counter() - t0) * 1e3 / args.steps}
+    fused_adam = None
+    if not args.no_adam and world == 1:
+        fused_adam = adam_bench(args, dev, s, rast, dL)
     batched = None
     if not args.no_batched and world == 1:
         batched = []
@@ -315,7 +319,69 @@ def gpu_bench(args, rank, local, world):
         checkpoint = checkpoint_bench(args, dev)
     return dict(ms_step=ms_step_job, fwd_ms=fwd_ms, clocks=clocks, ktimes=ktimes, K=K,
                 launches_per_step=launches_per_step, e2e=e2e, P=s.P, W=cam.width, H=cam.height, batched=batched,
-                checkpoint=checkpoint, W_eval=W_eval, fp32_peak=fp32_peak)
+                checkpoint=checkpoint, W_eval=W_eval, fp32_peak=fp32_peak, fused_adam=fused_adam)
+
+
+# Learning rates of FasterGS's sparse-Adam backbones (Taming / FastGS defaults;
+# f_rest at feature_lr / 20), for the training-step comparison.
+ADAM_LRS = {"xyz": 1.6e-4, "f_dc": 2.5e-3, "f_rest": 2.5e-3 / 20, "opacity": 2.5e-2, "scaling": 5e-3,
+            "rotation": 1e-3}
+
+
+def adam_bench(args, dev, s, rast, dL):
+    """C2 training step with FB's sparse Adam, unfused (gradients written, autograd through
+    sigmoid / exp / normalize, SparseGaussianAdam.step over the six groups) against the step
+    fused into the preprocess backward (no gradient in memory)."""
+    import torch
+    import torch.nn.functional as F
+    import fastergs_gb300 as fgs
+    from fastergs_gb300 import _lib
+    P = s.P
+    stream = torch.cuda.current_stream(dev)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    out = {"workload": "c2 training step: fwd + bwd + sparse Adam on the raw tensors (xyz, f_dc, f_rest, "
+                       "opacity, scaling, rotation), activations in the step"}
+    for mode in ("unfused", "fused"):
+        t = lambda a: torch.tensor(np.asarray(a, np.float32), device=dev).requires_grad_(True)
+        m = {"xyz": t(s.means), "f_dc": t(s.dc), "f_rest": t(s.shs), "opacity": t(s.opacity_logits),
+             "scaling": t(s.log_scales), "rotation": t(s.quats)}
+        opt = fgs.SparseGaussianAdam([{"params": [m[n]], "lr": ADAM_LRS[n], "name": n} for n in ADAM_LRS],
+                                     lr=0.0, eps=1e-15)
+        fused = mode == "fused"
+
+        def train_step():
+            img, radii = rast(means3D=m["xyz"], opacities=torch.sigmoid(m["opacity"]), dc=m["f_dc"], shs=m["f_rest"],
+                              scales=torch.exp(m["scaling"]), rotations=F.normalize(m["rotation"]),
+                              adam=opt if fused else None)
+            torch.autograd.backward(img, grad_tensors=dL)
+            if not fused:
+                opt.step(radii > 0, P)
+                opt.zero_grad(set_to_none=True)
+
+        for _ in range(max(args.warmup, 3)):
+            train_step()
+        torch.cuda.synchronize(dev)
+        ev0.record(stream)
+        for _ in range(args.steps):
+            train_step()
+        ev1.record(stream)
+        torch.cuda.synchronize(dev)
+        _lib.kernel_timers(True)
+        _lib.read_kernel_timers()
+        for _ in range(args.steps):
+            train_step()
+        torch.cuda.synchronize(dev)
+        kt = _lib.read_kernel_timers()
+        _lib.kernel_timers(False)
+        pb_ms, pb_n = kt.get("preprocess_bwd", (0.0, 0))
+        out[mode] = {"ms_per_step": round(ev0.elapsed_time(ev1) / args.steps, 4),
+                     "preprocess_bwd_ms": round(pb_ms / max(pb_n, 1), 4)}
+        del m, opt
+        torch.cuda.empty_cache()
+    out["saved_ms_per_step"] = round(out["unfused"]["ms_per_step"] - out["fused"]["ms_per_step"], 4)
+    # gradient tensors the fused step never writes nor reads back: 59 floats per Gaussian at SH 3
+    out["gradient_bytes_not_moved"] = int(2 * P * 59 * 4)
+    return out
 
 
 def batched_bench(args, dev, s, dev_in, cams, label):
@@ -526,8 +592,8 @@ FLOP_PER_EVAL = {"render_fwd": 17, "render_bwd": 50}
 
 # DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) of the
 # C2 workload, from the ncu captures summarised in profiles/ncu_c2_kernels.md.
-TRAFFIC_PER_LAUNCH = {"render_bwd": 55_832_320, "render_fwd": 50_232_320, "sort_pass": 38_462_720,
-                      "preprocess_bwd": 573_206_272, "preprocess": 200_908_544}
+TRAFFIC_PER_LAUNCH = {"render_bwd": 56_158_720, "render_fwd": 43_322_368, "sort_pass": 38_579_456,
+                      "preprocess_bwd": 572_444_928, "preprocess": 200_878_592}
 
 
 def roofline(res, peaks):
@@ -627,7 +693,7 @@ def main():
         "render_ms": round(res["fwd_ms"], 4),
         "e2e": res["e2e"], "gpu_launches": int(round(res["launches_per_step"] * args.steps)),
         "clocks": res["clocks"], "roofline": roof, "kernels": table, "cpu_baseline": cb,
-        "batched": res["batched"], "checkpoint": res["checkpoint"],
+        "batched": res["batched"], "checkpoint": res["checkpoint"], "fused_adam": res["fused_adam"],
     }
     print(json.dumps(line), flush=True)
     barrier(world)

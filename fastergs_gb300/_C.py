@@ -211,6 +211,45 @@ def backward(degree, bucket_sum, means3D, radii, dc, sh, opacities, scales, rota
     return dmean2D, dcolor, dopac, dmean3D, dcov3D, ddc, dsh, dscale, drot
 
 
+def backward_adam(degree, bucket_sum, means3D, radii, sh, opacities, scales, rotations, scale_modifier, width,
+                  height, block_x, block_y, tan_fovx, tan_fovy, campos, viewmatrix, projmatrix, img_func, smp_func,
+                  splat_buffer, point_list, ranges, background, last_contributor, Ts_final, dL_dout_color, adam,
+                  xyz_gradient_accum, xyz_gradient_accum_abs, max_radii, denom, bucket_size=BUCKET):
+    """``backward`` with the sparse Adam step fused into the preprocess backward: the raw parameters
+    and moments described by ``adam`` (an ``_lib.AdamFused``) are stepped in place and no gradient
+    tensor is produced (FB's step = backward + SparseGaussianAdam.step, __init__.py:267-298)."""
+    dev = _device_of(means3D)
+    P = means3D.size(0)
+    if P == 0:
+        return
+    M = sh.size(1) if sh.numel() and sh.size(0) != 0 else 0
+    grad_record = torch.empty((P, 12), dtype=torch.float32, device=dev)
+    means = _f32("means3D", means3D, dev)
+    shc = _f32("sh", sh, dev)
+    op = _f32("opacities", opacities, dev)
+    sc = _f32("scales", scales, dev)
+    ro = _f32("rotations", rotations, dev)
+    dL = _f32("dL_dout_color", dL_dout_color, dev)
+    bg = _f32("background", background, dev)
+    campos = _f32("campos", campos, dev)
+    viewmatrix = _f32("viewmatrix", viewmatrix, dev)
+    projmatrix = _f32("projmatrix", projmatrix, dev)
+    if dL.numel() != 3 * int(width) * int(height):
+        raise ValueError("dL_dout_color must be (3, H, W)")
+    mb = smp_func.size(0) - 1
+    s = _stream(dev)
+    _lib.call("fgs_render_bwd", int(P), int(width), int(height), int(block_x), int(block_y), int(bucket_size),
+              _ptr(point_list), _ptr(ranges), _ptr(bg), _ptr(splat_buffer), _ptr(Ts_final), _ptr(last_contributor),
+              _ptr(img_func), _ptr(smp_func), int(mb), _ptr(dL), _ptr(grad_record), s)
+    stats = xyz_gradient_accum is not None and xyz_gradient_accum.numel() != 0 and xyz_gradient_accum.size(0) != 0
+    _lib.call("fgs_preprocess_bwd_adam", int(P), int(degree), int(M), _ptr(means), _ptr(radii), _ptr(shc),
+              _ptr(splat_buffer), _ptr(op), _ptr(sc), _ptr(ro), float(scale_modifier), _ptr(viewmatrix),
+              _ptr(projmatrix), int(width), int(height), float(tan_fovx), float(tan_fovy), _ptr(campos),
+              _ptr(grad_record), C.byref(adam),
+              _ptr(xyz_gradient_accum) if stats else 0, _ptr(xyz_gradient_accum_abs) if stats else 0,
+              _ptr(max_radii) if stats else 0, _ptr(denom) if stats else 0, s)
+
+
 def adamUpdate(param, param_grad, exp_avg, exp_avg_sq, visible, lr, b1, b2, eps, N, M):
     """FB pybind.cpp:341-366 (masked Adam over N rows of M values)."""
     dev = _device_of(param)

@@ -24,7 +24,7 @@ from typing import NamedTuple
 import torch
 import torch.nn as nn
 
-from . import _C
+from . import _C, _lib
 
 __all__ = ["GaussianRasterizationSettings", "GaussianRasterizer", "rasterize_gaussians", "Buffer",
            "SparseGaussianAdam", "_RasterizeGaussians", "_C"]
@@ -102,10 +102,11 @@ class _LazyBuffer:
 
 
 def rasterize_gaussians(means3D, dc, shs, colors_precomp, opacities, scales, rotations, cov3Ds_precomp,
-                        raster_settings, culling, xyz_gradient_accum, xyz_gradient_accum_abs, max_radii, denom):
+                        raster_settings, culling, xyz_gradient_accum, xyz_gradient_accum_abs, max_radii, denom,
+                        adam=None):
     return _RasterizeGaussians.apply(means3D, dc, shs, colors_precomp, opacities, scales, rotations,
                                      cov3Ds_precomp, raster_settings, culling, xyz_gradient_accum,
-                                     xyz_gradient_accum_abs, max_radii, denom)
+                                     xyz_gradient_accum_abs, max_radii, denom, adam)
 
 
 class _RasterizeGaussians(torch.autograd.Function):
@@ -115,7 +116,9 @@ class _RasterizeGaussians(torch.autograd.Function):
 
     @staticmethod
     def forward(ctx, means3D, dc, shs, colors_precomp, opacities, scales, rotations, cov3Ds_precomp,
-                raster_settings, culling, xyz_gradient_accum, xyz_gradient_accum_abs, max_radii, denom):
+                raster_settings, culling, xyz_gradient_accum, xyz_gradient_accum_abs, max_radii, denom, adam=None):
+        if adam is not None:
+            adam._check_fused(means3D, dc, shs, colors_precomp)
         buffer = _RasterizeGaussians.buffer
         splat_buffer = buffer.splat_buffer
         N = means3D.shape[0]
@@ -129,6 +132,7 @@ class _RasterizeGaussians(torch.autograd.Function):
             N, num_rendered, W, H, splat_buffer, buffer.gaussian_keys_sorted, buffer.gaussian_values_sorted,
             buffer.ranges, raster_settings.bg, last_contributor, Ts_final, read_bucket_sum=False)
         ctx.raster_settings = raster_settings
+        ctx.adam = adam
         ctx.num_rendered = num_rendered
         ctx.buffer = buffer
         ctx.bucket_sum = bucket_sum
@@ -145,6 +149,17 @@ class _RasterizeGaussians(torch.autograd.Function):
         (means3D, scales, rotations, dc, shs, opacities, out_color, last_contributor, Ts_final, radii,
          splat_buffer, img_buffer, smp_buffer, xyz_gradient_accum, xyz_gradient_accum_abs, max_radii,
          denom) = ctx.saved_tensors
+        if ctx.adam is not None:
+            # sparse Adam fused into the backward: the raw parameters are stepped
+            # in place and autograd receives no gradient for them
+            fused, _keep, _ = ctx.adam._fused_args(means3D.shape[0], means3D.device)
+            _C.backward_adam(
+                rs.sh_degree, ctx.bucket_sum, means3D, radii, shs, opacities, scales, rotations, rs.scale_modifier,
+                rs.image_width, rs.image_height, 16, 16, rs.tanfovx, rs.tanfovy, rs.campos, rs.viewmatrix,
+                rs.projmatrix, img_buffer, smp_buffer, splat_buffer, buffer.gaussian_values_sorted, buffer.ranges,
+                rs.bg, last_contributor, Ts_final, grad_out_color.contiguous(), fused, xyz_gradient_accum,
+                xyz_gradient_accum_abs, max_radii, denom)
+            return (None,) * 15
         (grad_mean2D, grad_color, grad_opacity, grad_mean3D, grad_cov3D, grad_dc, grad_shs, grad_scales,
          grad_rotations) = _C.ops.backward(
             rs.sh_degree, ctx.bucket_sum, means3D, radii, dc, shs, opacities, scales, rotations,
@@ -153,7 +168,7 @@ class _RasterizeGaussians(torch.autograd.Function):
             buffer.gaussian_values_sorted, buffer.ranges, rs.bg, last_contributor, Ts_final,
             grad_out_color.contiguous(), xyz_gradient_accum, xyz_gradient_accum_abs, max_radii, denom)
         return (grad_mean3D, grad_dc, grad_shs, grad_color, grad_opacity, grad_scales, grad_rotations, grad_cov3D,
-                None, None, None, None, None, None)
+                None, None, None, None, None, None, None)
 
 
 class GaussianRasterizationSettings(NamedTuple):
@@ -182,7 +197,10 @@ class GaussianRasterizer(nn.Module):
 
     def forward(self, means3D, opacities, dc=None, shs=None, colors_precomp=None, scales=None, rotations=None,
                 cov3D_precomp=None, culling=None, xyz_gradient_accum=None, xyz_gradient_accum_abs=None,
-                max_radii=None, denom=None):
+                max_radii=None, denom=None, adam=None):
+        """FB's arguments, plus ``adam``: a SparseGaussianAdam whose step is fused into this frame's
+        backward (the raw parameters are stepped during ``loss.backward()``; do not call its
+        ``step`` for the frame).  Only the image loss reaches the parameters in that mode."""
         if (shs is None and colors_precomp is None) or (shs is not None and colors_precomp is not None):
             raise Exception('Please provide excatly one of either SHs or precomputed colors!')
         if ((scales is None or rotations is None) and cov3D_precomp is None) or \
@@ -202,7 +220,7 @@ class GaussianRasterizer(nn.Module):
         denom = empty if denom is None else denom
         return rasterize_gaussians(means3D, dc, shs, colors_precomp, opacities, scales, rotations, cov3D_precomp,
                                    self.raster_settings, culling, xyz_gradient_accum, xyz_gradient_accum_abs,
-                                   max_radii, denom)
+                                   max_radii, denom, adam)
 
 
 def _inputs(means3D, opacities, dc, shs, colors_precomp, scales, rotations, culling):
@@ -256,10 +274,91 @@ GaussianRasterizer.render_depth = _render_depth
 
 
 class SparseGaussianAdam(torch.optim.Adam):
-    """Adam that only steps the rows of visible Gaussians (FB __init__.py:267-298)."""
+    """Adam that only steps the rows of visible Gaussians (FB __init__.py:267-298).
 
-    def __init__(self, params, lr, eps):
+    ``step(visibility, N)`` is FB's.  Passed as ``adam=`` to the rasterizer, the
+    same step runs inside the frame's backward instead: the gradients of the
+    six named groups (xyz, f_dc, f_rest, opacity, scaling, rotation, as
+    FasterGS's backbones name them) never reach memory; the activations
+    opacity = sigmoid, scaling = exp, rotation = normalize are differentiated
+    in the kernel (``activations`` overrides them with "identity").
+    """
+
+    _DEFAULT_ACTS = {"opacity": "sigmoid", "scaling": "exp", "rotation": "normalize"}
+    _WIDTH = {"xyz": 3, "f_dc": 3, "opacity": 1, "scaling": 3, "rotation": 4}
+
+    def __init__(self, params, lr, eps, activations=None):
         super().__init__(params=params, lr=lr, eps=eps)
+        self.activations = dict(self._DEFAULT_ACTS, **(activations or {}))
+
+    def _named(self):
+        named = {}
+        for group in self.param_groups:
+            name = group.get("name")
+            if name in _lib.ADAM_GROUPS:
+                if len(group["params"]) != 1:
+                    raise ValueError(f"group {name!r} must hold exactly one tensor")
+                named[name] = group
+        return named
+
+    def _check_fused(self, means3D, dc, shs, colors_precomp):
+        """The fused step applies the rasterizer's gradients to the raw tensors: xyz, f_dc and f_rest
+        must be the tensors passed as means3D, dc and shs."""
+        if colors_precomp is not None and colors_precomp.numel():
+            raise ValueError("the fused Adam step needs SH colours (no precomputed colours)")
+        named = self._named()
+        if not named:
+            raise ValueError("no parameter group is named xyz, f_dc, f_rest, opacity, scaling or rotation")
+        for name, t in (("xyz", means3D), ("f_dc", dc), ("f_rest", shs)):
+            if name in named and (t is None or named[name]["params"][0].data_ptr() != t.data_ptr()):
+                raise ValueError(f"group {name!r} must be the tensor passed to the rasterizer")
+
+    @torch.no_grad()
+    def _fused_args(self, N, device, advance: bool = True, lr_device: torch.Tensor | None = None):
+        """One fused step's fgs_adam_fused: initialises the state lazily, advances each group's step
+        (unless advance=False) and sets FB's bias-compensated step sizes
+        (lr sqrt(1 - 0.999^t) / (1 - 0.9^t)) by value, or points the kernel at lr_device (6 device
+        floats the caller fills).  Returns (struct, tensors to keep alive, step sizes on the host)."""
+        fused = _lib.AdamFused()
+        lrs = torch.zeros(len(_lib.ADAM_GROUPS), dtype=torch.float32)
+        keep = []
+        named = self._named()
+        for gi, name in enumerate(_lib.ADAM_GROUPS):
+            group = named.get(name)
+            if group is None:
+                continue
+            param = group["params"][0]
+            if param.numel() == 0:
+                continue
+            width = self._WIDTH.get(name)
+            if (width is not None and param.numel() != N * width) or param.numel() % max(N, 1):
+                raise ValueError(f"group {name!r} does not hold {N} Gaussians")
+            if not (param.is_contiguous() and param.dtype == torch.float32 and param.device == device):
+                raise TypeError(f"group {name!r} must be a contiguous float32 tensor on {device}")
+            state = self.state[param]
+            if len(state) == 0:
+                state['step'] = torch.tensor(0.0, dtype=torch.float32)
+                state['exp_avg'] = torch.zeros_like(param, memory_format=torch.preserve_format)
+                state['exp_avg_sq'] = torch.zeros_like(param, memory_format=torch.preserve_format)
+            if advance:
+                state['step'] += 1
+            step = state['step']
+            if step > 0:
+                lrs[gi] = group["lr"] * (1 - 0.999 ** step) ** 0.5 / (1 - 0.9 ** step)
+            fused.param[gi] = param.data_ptr()
+            fused.exp_avg[gi] = state['exp_avg'].data_ptr()
+            fused.exp_avg_sq[gi] = state['exp_avg_sq'].data_ptr()
+            fused.eps[gi] = float(group["eps"])
+            keep.append(param)
+        for gi in range(len(_lib.ADAM_GROUPS)):
+            fused.lr_value[gi] = float(lrs[gi])
+        fused.lr = lr_device.data_ptr() if lr_device is not None else None
+        fused.b1, fused.b2 = 0.9, 0.999
+        acts = self.activations
+        fused.opacity_act = _lib.ACT[acts["opacity"]]
+        fused.scaling_act = _lib.ACT[acts["scaling"]]
+        fused.rotation_act = _lib.ACT[acts["rotation"]]
+        return fused, keep, lrs
 
     @torch.no_grad()
     def step(self, visibility, N):

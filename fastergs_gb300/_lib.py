@@ -30,7 +30,17 @@ class TuneConfig(C.Structure):
     _fields_ = [("bucket_size", i32), ("block_x", i32), ("block_y", i32), ("packet", i32), ("recompute", i32)]
 
 
-camp, tunep = C.POINTER(Camera), C.POINTER(TuneConfig)
+ADAM_GROUPS = ("xyz", "f_dc", "f_rest", "opacity", "scaling", "rotation")  # FGS_ADAM_* order
+ACT = {"identity": 0, "sigmoid": 1, "exp": 2, "normalize": 3}  # FGS_ACT_*
+
+
+class AdamFused(C.Structure):
+    """fgs_adam_fused: raw parameters, moments and step sizes of the fused sparse Adam."""
+    _fields_ = [("param", vp * 6), ("exp_avg", vp * 6), ("exp_avg_sq", vp * 6), ("lr", vp), ("lr_value", f32 * 6), ("eps", f32 * 6),
+                ("b1", f32), ("b2", f32), ("opacity_act", i32), ("scaling_act", i32), ("rotation_act", i32)]
+
+
+camp, tunep, adamp = C.POINTER(Camera), C.POINTER(TuneConfig), C.POINTER(AdamFused)
 
 # name: (restype, argtypes) -- mirrors include/fgs.h
 SIGNATURES = {
@@ -50,6 +60,8 @@ SIGNATURES = {
     "fgs_render_bwd": (i32, [i32, i32, i32, i32, i32, i32, vp, vp, vp, vp, vp, vp, vp, vp, i64, vp, vp, vp]),
     "fgs_preprocess_bwd": (i32, [i32, i32, i32, vp, vp, vp, vp, vp, vp, vp, f32, vp, vp, i32, i32, f32, f32, vp,
                                  vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp]),
+    "fgs_preprocess_bwd_adam": (i32, [i32, i32, i32, vp, vp, vp, vp, vp, vp, vp, f32, vp, vp, i32, i32, f32, f32,
+                                      vp, vp, adamp, vp, vp, vp, vp, vp]),
     "fgs_densify_stats": (i32, [i32, vp, vp, vp, vp, vp, vp, vp]),
     "fgs_render_simp": (i32, [i32, i64, i32, i32, vp, vp, vp, vp, vp, vp, vp, vp]),
     "fgs_render_depth": (i32, [i32, i64, i32, i32, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp]),
@@ -59,6 +71,8 @@ SIGNATURES = {
                                      vp, vp, vp]),
     "fgs_render_batched_bwd": (i32, [i32, i32, i32, vp, vp, vp, vp, vp, i32, camp, tunep, i64, vp, sz, vp, vp,
                                      vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp]),
+    "fgs_render_batched_bwd_adam": (i32, [i32, i32, i32, vp, vp, vp, vp, vp, i32, camp, tunep, i64, vp, sz, vp,
+                                          vp, adamp, vp, vp, vp, vp, vp]),
     "fgs_batch_status": (i32, [i32, i32, camp, tunep, i64, vp, C.POINTER(C.c_int64), C.POINTER(C.c_int64), vp]),
     "fgs_batch_offsets": (i32, [i32, i32, camp, tunep, i64, C.POINTER(C.c_int64), i32]),
     "fgs_peak_fp32": (i32, [C.POINTER(C.c_double), vp]),

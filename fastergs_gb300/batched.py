@@ -263,6 +263,30 @@ class BatchedRasterizer:
         return g
 
 
+    def backward_adam(self, dL_dpixels, means3D, shs, opacities, scales, rotations, sh_degree, fused,
+                      xyz_gradient_accum=None, xyz_gradient_accum_abs=None, max_radii=None, denom=None) -> None:
+        """Backward of the last forward with the sparse Adam step fused (``fused``: an
+        ``_lib.AdamFused`` from ``SparseGaussianAdam``): gradients summed over the cameras step the
+        raw parameters of every Gaussian some camera saw; no gradient tensor is written."""
+        self._check_points(means3D)
+        dev = self.device
+        dL = _f32("dL_dpixels", dL_dpixels, dev)
+        if dL.numel() != self.out_color.numel():
+            raise ValueError("dL_dpixels must match the flat colour buffer")
+        means = _f32("means3D", means3D, dev)
+        shc = _f32("shs", shs, dev)
+        op = _f32("opacities", opacities, dev)
+        sc = _f32("scales", scales, dev)
+        ro = _f32("rotations", rotations, dev)
+        M = shc.size(1) if shc.numel() else 0
+        stats = xyz_gradient_accum is not None and xyz_gradient_accum.numel() != 0
+        _lib.call("fgs_render_batched_bwd_adam", self.P, int(sh_degree), int(M), _ptr(means), _ptr(shc), _ptr(op),
+                  _ptr(sc), _ptr(ro), self.V, self._cams, C.byref(self._cfg), self.pair_capacity,
+                  _ptr(self.workspace), self.workspace.numel(), _ptr(self.radii), _ptr(dL), C.byref(fused),
+                  _ptr(xyz_gradient_accum) if stats else 0, _ptr(xyz_gradient_accum_abs) if stats else 0,
+                  _ptr(max_radii) if stats else 0, _ptr(denom) if stats else 0, _stream(dev))
+
+
 class _RasterizeBatched(torch.autograd.Function):
     """Autograd over one batched frame: returns the flat colour buffer and radii (V, P)."""
 
@@ -309,38 +333,114 @@ class CapturedStep:
     The parameter tensors, dL_dpixels and the statistics tensors are static:
     update them in place between ``replay()`` calls.  Gradients land in
     ``self.grads`` (summed over cameras), images in ``rast.out_color``.
+
+    With ``adam`` (a SparseGaussianAdam whose groups are named xyz, f_dc,
+    f_rest, opacity, scaling, rotation) the graph is a whole training step on
+    the optimiser's raw tensors: the activations (sigmoid, exp, normalize)
+    into static buffers, the forward, and the backward with the sparse Adam
+    step fused; ``params`` may then be None.  Each ``replay()`` advances the
+    optimiser's step counts and writes the new step sizes into the graph's
+    step-size table first.  Re-capture after densification (new tensors).
     """
 
-    def __init__(self, rast: BatchedRasterizer, params: dict, dL_dpixels: torch.Tensor, sh_degree: int = 0,
-                 stats: dict | None = None, with_backward: bool = True):
+    def __init__(self, rast: BatchedRasterizer, params: dict | None, dL_dpixels: torch.Tensor, sh_degree: int = 0,
+                 stats: dict | None = None, with_backward: bool = True, adam=None):
         self.rast = rast
-        self.params = params
         self.dL = dL_dpixels
         self.sh_degree = sh_degree
         self.stats = stats or {}
-        shs = params.get("shs")
-        self.grads = rast.alloc_grads(shs.size(1) if shs is not None and shs.numel() else 0)
         self.with_backward = with_backward
-        # Warm up on a side stream (first-call runtime setup must not be captured).
+        self.adam = adam
+        if adam is not None:
+            self._bind_adam(adam)
+        else:
+            self.params = params
+        shs = self.params.get("shs")
+        self.grads = rast.alloc_grads(shs.size(1) if shs is not None and shs.numel() else 0) if adam is None else {}
+        # Warm up on a side stream (first-call runtime setup must not be captured);
+        # the warm-up never steps the optimiser.
         side = torch.cuda.Stream(device=rast.device)
         side.wait_stream(torch.cuda.current_stream(rast.device))
         with torch.cuda.stream(side):
-            self._body()
+            self._body(warmup=True)
         torch.cuda.current_stream(rast.device).wait_stream(side)
         torch.cuda.synchronize(rast.device)
         self.graph = torch.cuda.CUDAGraph()
         with torch.cuda.graph(self.graph):
             self._body()
 
-    def _body(self):
+    def _bind_adam(self, adam):
+        named = adam._named()
+        missing = {"xyz", "opacity", "scaling", "rotation"} - set(named)
+        if missing:
+            raise ValueError(f"the optimiser has no group named {sorted(missing)}")
+        raw = {n: g["params"][0] for n, g in named.items()}
+        self._raw = raw
+        P, dev = self.rast.P, self.rast.device
+        self.params = dict(means3D=raw["xyz"], dc=raw.get("f_dc"), shs=raw.get("f_rest"),
+                           opacities=torch.empty((P, 1), dtype=torch.float32, device=dev),
+                           scales=torch.empty((P, 3), dtype=torch.float32, device=dev),
+                           rotations=torch.empty((P, 4), dtype=torch.float32, device=dev))
+        adam._check_fused(raw["xyz"], raw.get("f_dc"), raw.get("f_rest"), None)
+        # step sizes: pinned host slots copied into a device table the graph reads;
+        # a slot is rewritten only after its previous copy has completed
+        self._lr = torch.zeros(6, dtype=torch.float32, device=dev)
+        self._lr_host = [torch.zeros(6, dtype=torch.float32).pin_memory() for _ in range(4)]
+        self._lr_done = [None] * 4
+        self._replays = 0
+        self._fused = adam._fused_args(P, dev, advance=False, lr_device=self._lr)[0]
+
+    @torch.no_grad()
+    def _activations(self):
+        p, raw, acts = self.params, self._raw, self.adam.activations
+        op, sc, ro = raw["opacity"], raw["scaling"], raw["rotation"]
+        if acts["opacity"] == "sigmoid":
+            torch.sigmoid(op, out=p["opacities"])
+        else:
+            p["opacities"].copy_(op)
+        if acts["scaling"] == "exp":
+            torch.exp(sc, out=p["scales"])
+        else:
+            p["scales"].copy_(sc)
+        if acts["rotation"] == "normalize":
+            torch.nn.functional.normalize(ro, dim=-1, out=p["rotations"])
+        else:
+            p["rotations"].copy_(ro)
+
+    def _body(self, warmup: bool = False):
         p = self.params
+        if self.adam is not None:
+            self._activations()
         self.rast.forward(p["means3D"], p["opacities"], p.get("dc"), p.get("shs"), p.get("colors_precomp"),
                           p["scales"], p["rotations"], p.get("culling"), self.sh_degree)
-        if self.with_backward:
+        if not self.with_backward:
+            return
+        st = self.stats
+        if self.adam is None:
             self.rast.backward(self.dL, p["means3D"], p.get("dc"), p.get("shs"), p["scales"], p["rotations"],
-                               self.sh_degree, self.stats.get("xyz_gradient_accum"),
-                               self.stats.get("xyz_gradient_accum_abs"), self.stats.get("max_radii"),
-                               self.stats.get("denom"), out=self.grads)
+                               self.sh_degree, st.get("xyz_gradient_accum"), st.get("xyz_gradient_accum_abs"),
+                               st.get("max_radii"), st.get("denom"), out=self.grads)
+        elif warmup:  # the fused kernel with no group to step and no statistics: sets up, changes nothing
+            self.rast.backward_adam(self.dL, p["means3D"], p.get("shs"), p["opacities"], p["scales"],
+                                    p["rotations"], self.sh_degree, _lib.AdamFused())
+        else:
+            self.rast.backward_adam(self.dL, p["means3D"], p.get("shs"), p["opacities"], p["scales"],
+                                    p["rotations"], self.sh_degree, self._fused, st.get("xyz_gradient_accum"),
+                                    st.get("xyz_gradient_accum_abs"), st.get("max_radii"), st.get("denom"))
 
     def replay(self):
+        if self.adam is not None:
+            fused, _, lrs = self.adam._fused_args(self.rast.P, self.rast.device, lr_device=self._lr)
+            for g in range(6):
+                if fused.param[g] != self._fused.param[g] or fused.exp_avg[g] != self._fused.exp_avg[g]:
+                    raise RuntimeError("the optimiser's tensors changed since capture: build a new CapturedStep")
+            slot = self._replays % len(self._lr_host)
+            if self._lr_done[slot] is not None:
+                self._lr_done[slot].synchronize()
+            self._lr_host[slot].copy_(lrs)
+            self._lr.copy_(self._lr_host[slot], non_blocking=True)
+            ev = torch.cuda.Event()
+            ev.record(torch.cuda.current_stream(self.rast.device))
+            self._lr_done[slot] = ev
+            self._replays += 1
         self.graph.replay()

@@ -334,11 +334,18 @@ __device__ __forceinline__ void sh_term(float B, float bx, float by, float bz, c
   ddir.z = fmaf(bz, dot, ddir.z);
 }
 
+__device__ __forceinline__ float adam_lr(const fgs_adam_fused& ad, int g) {
+  return ad.lr ? ad.lr[g] : ad.lr_value[g];
+}
+
 // One thread per Gaussian; loops over the views and sums their gradients
 // (FB backward.cu:250-539, 892-918 for one view).
 // One Gaussian: co / gsh are its SH row and its dL/dsh row (shared memory
 // when staged, else global); gsh starts at zero and is accumulated over views.
-__device__ __forceinline__ void pbwd_gaussian(const PbwdArgs& a, int i, const float* co, float* gsh) {
+// Returns whether some view saw the Gaussian (radius > 0).
+template <bool ADAM>
+__device__ __forceinline__ bool pbwd_gaussian(const PbwdArgs& a, int i, const float* co, float* gsh) {
+  bool seen = false;
   float m3[3] = {0.f, 0.f, 0.f}, gc[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f}, gs[3] = {0.f, 0.f, 0.f};
   float gq[4] = {0.f, 0.f, 0.f, 0.f}, gdc[3] = {0.f, 0.f, 0.f};
   float4 gco_sum = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -373,6 +380,7 @@ __device__ __forceinline__ void pbwd_gaussian(const PbwdArgs& a, int i, const fl
     if (a.dconic) reinterpret_cast<float4*>(a.dconic)[rid] = make_float4(gx, gy, 0.f, gz);
     gco_sum.x += gco.x; gco_sum.y += gco.y; gco_sum.z += gco.z; gco_sum.w += gco.w;
     if (!(radius > 0)) continue;
+    seen = true;
     const float sv[3] = {cam.smod * a.scales[3 * (size_t)i], cam.smod * a.scales[3 * (size_t)i + 1],
                          cam.smod * a.scales[3 * (size_t)i + 2]};
     const float s2[3] = {sv[0] * sv[0], sv[1] * sv[1], sv[2] * sv[2]};
@@ -521,6 +529,67 @@ __device__ __forceinline__ void pbwd_gaussian(const PbwdArgs& a, int i, const fl
           4.f * qy * (dR[0][0] + dR[2][2]);
   gq[3] = 2.f * qr * (dR[1][0] - dR[0][1]) + 2.f * qx * (dR[0][2] + dR[2][0]) + 2.f * qy * (dR[1][2] + dR[2][1]) -
           4.f * qz * (dR[0][0] + dR[1][1]);
+  if constexpr (ADAM) {
+    // --- fused sparse Adam (FB adam.cu:26-37 on the autograd gradients of the
+    // raw parameters): only Gaussians some view saw take a step.  Every
+    // operand is loaded before the first store so the loads overlap.
+    if (!seen) return false;
+    const fgs_adam_fused& ad = a.adam;
+    constexpr int kE = 14;  // xyz 3, f_dc 3, opacity 1, scaling 3, rotation 4
+    constexpr int kGroup[kE] = {FGS_ADAM_XYZ, FGS_ADAM_XYZ, FGS_ADAM_XYZ, FGS_ADAM_F_DC, FGS_ADAM_F_DC,
+                                FGS_ADAM_F_DC, FGS_ADAM_OPACITY, FGS_ADAM_SCALING, FGS_ADAM_SCALING,
+                                FGS_ADAM_SCALING, FGS_ADAM_ROTATION, FGS_ADAM_ROTATION, FGS_ADAM_ROTATION,
+                                FGS_ADAM_ROTATION};
+    constexpr int kWidth[kE] = {3, 3, 3, 3, 3, 3, 1, 3, 3, 3, 4, 4, 4, 4};
+    constexpr int kCol[kE] = {0, 1, 2, 0, 1, 2, 0, 0, 1, 2, 0, 1, 2, 3};
+    float p[kE], m1[kE], m2[kE], g[kE];
+#pragma unroll
+    for (int e = 0; e < kE; ++e) {
+      p[e] = m1[e] = m2[e] = 0.f;
+      if (const float* prm = ad.param[kGroup[e]]) {
+        const size_t off = (size_t)kWidth[e] * i + kCol[e];
+        p[e] = prm[off];
+        m1[e] = ad.exp_avg[kGroup[e]][off];
+        m2[e] = ad.exp_avg_sq[kGroup[e]][off];
+      }
+    }
+    const bool sig = ad.param[FGS_ADAM_OPACITY] && ad.opacity_act == FGS_ACT_SIGMOID;
+    const float y = sig ? a.opac[i] : 0.f;
+    const bool ex = ad.param[FGS_ADAM_SCALING] && ad.scaling_act == FGS_ACT_EXP;
+    const float e0 = ex ? a.scales[3 * (size_t)i] : 1.f, e1 = ex ? a.scales[3 * (size_t)i + 1] : 1.f,
+                e2 = ex ? a.scales[3 * (size_t)i + 2] : 1.f;
+    g[0] = m3[0]; g[1] = m3[1]; g[2] = m3[2];
+    g[3] = gdc[0]; g[4] = gdc[1]; g[5] = gdc[2];
+    g[6] = sig ? gco_sum.w * (1.f - y) * y : gco_sum.w;  // sigmoid'(x) = (1 - y) y, in autograd's order
+    g[7] = ex ? gs[0] * e0 : gs[0];                        // exp'(x) = exp(x)
+    g[8] = ex ? gs[1] * e1 : gs[1];
+    g[9] = ex ? gs[2] * e2 : gs[2];
+    g[10] = gq[0]; g[11] = gq[1]; g[12] = gq[2]; g[13] = gq[3];
+    if (ad.param[FGS_ADAM_ROTATION] && ad.rotation_act == FGS_ACT_NORMALIZE) {
+      // q = x / max(|x|, 1e-12): dL/dx = g / d - x (g . x) / d^3 (the norm's
+      // term only where |x| > 1e-12, as the clamp passes it); x = raw row
+      const float x0 = p[10], x1 = p[11], x2 = p[12], x3 = p[13];
+      const float nrm = sqrtf(x0 * x0 + x1 * x1 + x2 * x2 + x3 * x3);
+      const float d = fmaxf(nrm, 1e-12f);
+      const float gx = gq[0] * x0 + gq[1] * x1 + gq[2] * x2 + gq[3] * x3;
+      const float c = nrm > 1e-12f ? gx / (d * d) / d : 0.f;
+      g[10] = gq[0] / d - x0 * c;
+      g[11] = gq[1] / d - x1 * c;
+      g[12] = gq[2] / d - x2 * c;
+      g[13] = gq[3] / d - x3 * c;
+    }
+#pragma unroll
+    for (int e = 0; e < kE; ++e) {
+      if (float* prm = ad.param[kGroup[e]]) {
+        adam_reg(p[e], m1[e], m2[e], g[e], adam_lr(ad, kGroup[e]), ad.b1, ad.b2, ad.eps[kGroup[e]]);
+        const size_t off = (size_t)kWidth[e] * i + kCol[e];
+        prm[off] = p[e];
+        ad.exp_avg[kGroup[e]][off] = m1[e];
+        ad.exp_avg_sq[kGroup[e]][off] = m2[e];
+      }
+    }
+    return true;
+  }
   // --- outputs (zeros where no view saw the Gaussian, as FB leaves them)
   a.dcolor[3 * (size_t)i] = gco_sum.x;
   a.dcolor[3 * (size_t)i + 1] = gco_sum.y;
@@ -533,11 +602,97 @@ __device__ __forceinline__ void pbwd_gaussian(const PbwdArgs& a, int i, const fl
   a.ddc[3 * (size_t)i] = gdc[0]; a.ddc[3 * (size_t)i + 1] = gdc[1]; a.ddc[3 * (size_t)i + 2] = gdc[2];
   a.dscale[3 * (size_t)i] = gs[0]; a.dscale[3 * (size_t)i + 1] = gs[1]; a.dscale[3 * (size_t)i + 2] = gs[2];
   reinterpret_cast<float4*>(a.drot)[i] = make_float4(gq[0], gq[1], gq[2], gq[3]);
+  return seen;
 }
 
-__global__ void __launch_bounds__(256) k_preprocess_bwd(const PbwdArgs a) {
+// f_rest rows of one block of Gaussians, [first, first + n), row floats each,
+// with their summed gradients in shared memory (s_g): the Adam step on the
+// rows of Gaussians some view saw, as float4 over the block's contiguous span
+// (kRestUnroll float4 per array in flight per thread; a float4 spans at most
+// two rows as row >= 3) when the arrays are 16-byte aligned there, else
+// element by element.  When the rasterizer's SH input is the f_rest tensor
+// itself, the parameter values come from the staged copy (s_co) instead of a
+// second read.
+constexpr int kRestUnroll = 4;
+__device__ __forceinline__ void adam_rest_rows(const PbwdArgs& a, int first, int n, int row, const float* s_co,
+                                               const float* s_g, const uint8_t* s_seen) {
+  const fgs_adam_fused& ad = a.adam;
+  const float lr = adam_lr(ad, FGS_ADAM_F_REST), eps = ad.eps[FGS_ADAM_F_REST], b1 = ad.b1, b2 = ad.b2;
+  const size_t base = (size_t)first * row;
+  float* prm = ad.param[FGS_ADAM_F_REST] + base;
+  float* pm1 = ad.exp_avg[FGS_ADAM_F_REST] + base;
+  float* pm2 = ad.exp_avg_sq[FGS_ADAM_F_REST] + base;
+  const bool staged = a.shs == ad.param[FGS_ADAM_F_REST];
+  const int total = n * row;
+  const bool vec = row >= 3 &&
+                   ((reinterpret_cast<uintptr_t>(prm) | reinterpret_cast<uintptr_t>(pm1) |
+                     reinterpret_cast<uintptr_t>(pm2)) & 15) == 0;
+  int done = 0;
+  if (vec) {
+    const int n4 = total >> 2;
+    float4* P4 = reinterpret_cast<float4*>(prm);
+    float4* A4 = reinterpret_cast<float4*>(pm1);
+    float4* B4 = reinterpret_cast<float4*>(pm2);
+    const float4* C4 = reinterpret_cast<const float4*>(s_co);
+    const float4* G4 = reinterpret_cast<const float4*>(s_g);
+    // Row of element j: floor((j + 1/2) / row) in FP32.  j < 256 row and
+    // 3 <= row <= 48, so the product is off by less than 5e-4 while the exact
+    // quotient stays at least 1 / (2 row) > 0.01 away from an integer
+    // (tests/test_capi_cpu.py checks every row and j).
+    const float inv_row = 1.f / (float)row;
+    for (int q0 = threadIdx.x; q0 < n4; q0 += 256 * kRestUnroll) {
+      float4 pv[kRestUnroll], av[kRestUnroll], bv[kRestUnroll];
+      int r0[kRestUnroll];
+      bool s0[kRestUnroll], s1[kRestUnroll];
+#pragma unroll
+      for (int u = 0; u < kRestUnroll; ++u) {
+        const int q = q0 + 256 * u, j = 4 * q;
+        r0[u] = (int)(((float)j + 0.5f) * inv_row);
+        const int r3 = (int)(((float)j + 3.5f) * inv_row);
+        s0[u] = q < n4 && s_seen[r0[u]] != 0;
+        s1[u] = q < n4 && s_seen[r3] != 0;
+        if (s0[u] || s1[u]) {
+          pv[u] = staged ? C4[q] : P4[q];
+          av[u] = A4[q];
+          bv[u] = B4[q];
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < kRestUnroll; ++u) {
+        if (!(s0[u] || s1[u])) continue;
+        const int q = q0 + 256 * u, j = 4 * q;
+        const int split = (r0[u] + 1) * row - j;  // elements [0, split) belong to row r0
+        const float4 gv = G4[q];
+        float* pp = &pv[u].x;
+        float* pa = &av[u].x;
+        float* pb = &bv[u].x;
+        const float gg[4] = {gv.x, gv.y, gv.z, gv.w};
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {  // branch-free: step all four, keep the seen rows' results
+          float p = pp[e], ma = pa[e], mb = pb[e];
+          adam_reg(p, ma, mb, gg[e], lr, b1, b2, eps);
+          const bool on = e < split ? s0[u] : s1[u];
+          pp[e] = on ? p : pp[e];
+          pa[e] = on ? ma : pa[e];
+          pb[e] = on ? mb : pb[e];
+        }
+        P4[q] = pv[u];
+        A4[q] = av[u];
+        B4[q] = bv[u];
+      }
+    }
+    done = n4 << 2;
+  }
+  for (int j = done + threadIdx.x; j < total; j += 256)
+    if (s_seen[j / row]) adam_step(prm, pm1, pm2, j, s_g[j], lr, b1, b2, eps);
+}
+
+// ADAM: the sparse Adam step fused in place of the gradient outputs.
+template <bool ADAM>
+__global__ void __launch_bounds__(256, 2) k_preprocess_bwd(const PbwdArgs a) {
   // sh_staged: [256 x M x 3] SH rows, then [256 x M x 3] dL/dsh accumulators
   extern __shared__ __align__(16) float s_pb[];
+  __shared__ uint8_t s_seen[256];
   const int first = blockIdx.x * 256, n = min(256, a.P - first), row = a.M * 3;
   const int i = first + threadIdx.x;
   if (a.sh_staged) {
@@ -546,16 +701,21 @@ __global__ void __launch_bounds__(256) k_preprocess_bwd(const PbwdArgs a) {
     block_copy_to_smem(s_co, a.shs, (size_t)first * row, n * row);
     for (int j = threadIdx.x; j < n * row; j += 256) s_g[j] = 0.f;
     __syncthreads();
-    if (i < a.P) pbwd_gaussian(a, i, s_co + threadIdx.x * row, s_g + threadIdx.x * row);
+    const bool seen = i < a.P && pbwd_gaussian<ADAM>(a, i, s_co + threadIdx.x * row, s_g + threadIdx.x * row);
+    s_seen[threadIdx.x] = seen ? 1 : 0;
     __syncthreads();
-    block_copy_from_smem(a.dsh, (size_t)first * row, s_g, n * row);
+    if constexpr (!ADAM) {
+      block_copy_from_smem(a.dsh, (size_t)first * row, s_g, n * row);
+    } else {
+      if (a.adam.param[FGS_ADAM_F_REST]) adam_rest_rows(a, first, n, row, s_co, s_g, s_seen);
+    }
     return;
   }
   if (i >= a.P) return;
   float* gsh = a.dsh ? a.dsh + (size_t)i * row : nullptr;
   if (gsh)
     for (int k = 0; k < row; ++k) gsh[k] = 0.f;
-  pbwd_gaussian(a, i, a.shs ? a.shs + (size_t)i * row : nullptr, gsh);
+  pbwd_gaussian<ADAM>(a, i, a.shs ? a.shs + (size_t)i * row : nullptr, gsh);
 }
 
 __global__ void __launch_bounds__(256) k_densify(int P, const int* radii, const float4* dm2, float* accum,
@@ -609,11 +769,16 @@ fgs_status run_render_bwd(const Views& views, int64_t records, int bucket_size, 
 }
 
 fgs_status run_preprocess_bwd(PbwdArgs& a, cudaStream_t s) {
-  a.sh_staged = (a.shs && a.dsh && a.M >= 1 && a.M <= kMaxStagedCoeffs) ? 1 : 0;
+  a.sh_staged = (a.shs && (a.dsh || a.adam_on) && a.M >= 1 && a.M <= kMaxStagedCoeffs) ? 1 : 0;
+  // the fused step keeps dL/dsh only in shared memory
+  if (a.adam_on && a.shs && a.D > 0 && !a.sh_staged) return FGS_ERR_BAD_ARG;
   const int dyn = a.sh_staged ? 2 * 256 * a.M * 3 * (int)sizeof(float) : 0;
-  if (dyn) FGS_TRY(allow_dyn_smem(reinterpret_cast<const void*>(&k_preprocess_bwd), 2 * 256 * kMaxStagedCoeffs * 12));
+  const void* kern = a.adam_on ? reinterpret_cast<const void*>(&k_preprocess_bwd<true>)
+                               : reinterpret_cast<const void*>(&k_preprocess_bwd<false>);
+  if (dyn) FGS_TRY(allow_dyn_smem(kern, 2 * 256 * kMaxStagedCoeffs * 12));
   KernelTimer kt__(FGS_K_PREPROCESS_BWD, s);
-  k_preprocess_bwd<<<(a.P + 255) / 256, 256, dyn, s>>>(a);
+  if (a.adam_on) k_preprocess_bwd<true><<<(a.P + 255) / 256, 256, dyn, s>>>(a);
+  else k_preprocess_bwd<false><<<(a.P + 255) / 256, 256, dyn, s>>>(a);
   kt__.stop();
   FGS_LAUNCH_CHECK();
   return FGS_OK;
@@ -672,6 +837,45 @@ extern "C" fgs_status fgs_preprocess_bwd(
   a.dmean3D = dL_dmean3D; a.dcov3D = dL_dcov3D; a.ddc = dL_ddc; a.dsh = (M > 0) ? dL_dsh : nullptr;
   a.dscale = dL_dscale; a.drot = dL_drot;
   a.accum = xyz_gradient_accum; a.accum_abs = xyz_gradient_accum_abs; a.max_radii = max_radii; a.denom = denom;
+  return run_preprocess_bwd(a, (cudaStream_t)stream);
+}
+
+bool fgs::adam_args_ok(const fgs_adam_fused* ad, const float* shs, const float* opacities) {
+  if (!ad) return false;
+  for (int g = 0; g < FGS_ADAM_GROUPS; ++g)
+    if (ad->param[g] && (!ad->exp_avg[g] || !ad->exp_avg_sq[g])) return false;
+  if (ad->opacity_act != FGS_ACT_IDENTITY && ad->opacity_act != FGS_ACT_SIGMOID) return false;
+  if (ad->scaling_act != FGS_ACT_IDENTITY && ad->scaling_act != FGS_ACT_EXP) return false;
+  if (ad->rotation_act != FGS_ACT_IDENTITY && ad->rotation_act != FGS_ACT_NORMALIZE) return false;
+  if (ad->param[FGS_ADAM_OPACITY] && ad->opacity_act == FGS_ACT_SIGMOID && !opacities) return false;
+  if (ad->param[FGS_ADAM_ROTATION] && ((uintptr_t)ad->param[FGS_ADAM_ROTATION] & 15)) return false;
+  if (ad->param[FGS_ADAM_F_REST] && !shs) return false;
+  return true;
+}
+
+extern "C" fgs_status fgs_preprocess_bwd_adam(
+    int P, int D, int M, const float* means3D, const int32_t* radii, const float* shs, const float* splat_buffer,
+    const float* opacities, const float* scales, const float* rotations, float scale_modifier,
+    const float* viewmatrix, const float* projmatrix, int width, int height, float tan_fovx, float tan_fovy,
+    const float* campos, const float* grad_record, const fgs_adam_fused* adam, float* xyz_gradient_accum,
+    float* xyz_gradient_accum_abs, float* max_radii, float* denom, void* stream) {
+  if (P < 0 || D < 0 || D > 3 || M < 0 || width <= 0 || height <= 0) return FGS_ERR_BAD_ARG;
+  if (P == 0) return FGS_OK;
+  if (!means3D || !radii || !splat_buffer || !scales || !rotations || !viewmatrix || !projmatrix || !grad_record ||
+      !adam_args_ok(adam, shs, opacities))
+    return FGS_ERR_BAD_ARG;
+  if (shs && (!campos || (D > 0 && M < (D + 1) * (D + 1) - 1))) return FGS_ERR_BAD_ARG;
+  if (((uintptr_t)grad_record & 15) || ((uintptr_t)rotations & 15)) return FGS_ERR_BAD_ARG;
+  PbwdArgs a;
+  a.views = single_view(width, height, 16, 16, viewmatrix, projmatrix, campos, nullptr, tan_fovx, tan_fovy, 1.f,
+                        scale_modifier);
+  a.P = P; a.D = D; a.M = M;
+  a.means = means3D; a.radii = radii; a.dc = nullptr; a.shs = shs; a.splat = splat_buffer;
+  a.scales = scales; a.rots = rotations; a.grad = grad_record;
+  a.dmean2D = nullptr; a.dconic = nullptr; a.dopac = nullptr; a.dcolor = nullptr;
+  a.dmean3D = nullptr; a.dcov3D = nullptr; a.ddc = nullptr; a.dsh = nullptr; a.dscale = nullptr; a.drot = nullptr;
+  a.accum = xyz_gradient_accum; a.accum_abs = xyz_gradient_accum_abs; a.max_radii = max_radii; a.denom = denom;
+  a.adam_on = 1; a.opac = opacities; a.adam = *adam;
   return run_preprocess_bwd(a, (cudaStream_t)stream);
 }
 

@@ -223,6 +223,48 @@ extern "C" fgs_status fgs_render_batched_bwd(int P, int D, int M, const float* m
   return run_preprocess_bwd(a, s);
 }
 
+extern "C" fgs_status fgs_render_batched_bwd_adam(int P, int D, int M, const float* means3D, const float* shs,
+                                                  const float* opacities, const float* scales,
+                                                  const float* rotations, int num_views, const fgs_camera* cams,
+                                                  const fgs_tune_config* cfg, int64_t pair_capacity, void* workspace,
+                                                  size_t workspace_bytes, const int32_t* radii,
+                                                  const float* dL_dpixels, const fgs_adam_fused* adam,
+                                                  float* xyz_gradient_accum, float* xyz_gradient_accum_abs,
+                                                  float* max_radii, float* denom, void* stream) {
+  if (P < 0 || D < 0 || D > 3 || !cameras_ok(num_views, cams) || !config_ok(cfg) || pair_capacity < 1 ||
+      !workspace || (P > 0 && !radii) || !dL_dpixels)
+    return FGS_ERR_BAD_ARG;
+  if (pair_capacity > kMaxBatchPairs || (int64_t)num_views * P >= ((int64_t)1 << 32)) return FGS_ERR_CAPACITY;
+  if (P == 0) return FGS_OK;
+  if (!means3D || !scales || !rotations || !adam_args_ok(adam, shs, opacities)) return FGS_ERR_BAD_ARG;
+  if (shs && D > 0 && M < (D + 1) * (D + 1) - 1) return FGS_ERR_BAD_ARG;
+  if (((uintptr_t)workspace & 255) || ((uintptr_t)rotations & 15)) return FGS_ERR_BAD_ARG;
+  const BatchLayout L = plan_for(P, num_views, cams, cfg, pair_capacity);
+  if (workspace_bytes < L.total) return FGS_ERR_CAPACITY;
+  char* ws = static_cast<char*>(workspace);
+  cudaStream_t s = (cudaStream_t)stream;
+  const Views views = make_views(num_views, cams, cfg->block_x, cfg->block_y);
+  const ImageState im = carve_image(ws + L.image, (size_t)L.pixels, L.tiles);
+  const SampleState sm = carve_sample(ws + L.sample, L.buckets, cfg->recompute ? (int64_t)L.tiles : L.buckets);
+  float* grad = reinterpret_cast<float*>(ws + L.grad);
+  fgs_status st = run_render_bwd(views, L.records_n, cfg->bucket_size, reinterpret_cast<uint32_t*>(ws + L.vals_s),
+                                 reinterpret_cast<uint32_t*>(ws + L.ranges), reinterpret_cast<float*>(ws + L.records),
+                                 reinterpret_cast<float*>(ws + L.ts_final),
+                                 reinterpret_cast<int32_t*>(ws + L.last_contrib), im, sm, dL_dpixels, grad,
+                                 cfg->recompute != 0, s);
+  if (st != FGS_OK) return st;
+  PbwdArgs a;
+  a.views = views;
+  a.P = P; a.D = D; a.M = M;
+  a.means = means3D; a.radii = radii; a.dc = nullptr; a.shs = shs; a.splat = reinterpret_cast<float*>(ws + L.records);
+  a.scales = scales; a.rots = rotations; a.grad = grad;
+  a.dmean2D = nullptr; a.dconic = nullptr; a.dopac = nullptr; a.dcolor = nullptr;
+  a.dmean3D = nullptr; a.dcov3D = nullptr; a.ddc = nullptr; a.dsh = nullptr; a.dscale = nullptr; a.drot = nullptr;
+  a.accum = xyz_gradient_accum; a.accum_abs = xyz_gradient_accum_abs; a.max_radii = max_radii; a.denom = denom;
+  a.adam_on = 1; a.opac = opacities; a.adam = *adam;
+  return run_preprocess_bwd(a, s);
+}
+
 extern "C" fgs_status fgs_batch_status(int P, int num_views, const fgs_camera* cams, const fgs_tune_config* cfg,
                                        int64_t pair_capacity, const void* workspace, int64_t* pairs,
                                        int64_t* buckets, void* stream) {

@@ -84,12 +84,7 @@ __global__ void __launch_bounds__(256) k_adam(float* __restrict__ param, const f
   const uint64_t row = p / M;
   if (row >= N) return;
   if (!visible[row]) return;
-  const float g = grad[p];
-  const float a = b1 * m1[p] + (1.0f - b1) * g;
-  const float b = b2 * m2[p] + (1.0f - b2) * g * g;
-  param[p] += -lr * a / (sqrtf(b) + eps);
-  m1[p] = a;
-  m2[p] = b;
+  adam_step(param, m1, m2, p, grad[p], lr, b1, b2, eps);
 }
 // FP32 issue ceiling for the compositing kernels' roofline: every thread runs
 // 8 independent FMA chains, so the FMA pipe, not latency, limits the rate.

@@ -207,6 +207,29 @@ __device__ __forceinline__ void block_copy_from_smem(float* dst, size_t first, c
 // Largest SH coefficient count per Gaussian that is staged in shared memory.
 constexpr int kMaxStagedCoeffs = 16;
 
+// One element of FB's masked Adam step (adam.cu:27-36); lr carries the bias
+// compensation.  Shared by the plain and the fused update so both round alike.
+// The moments are FB's to the bit; the step -lr m / (sqrt(v) + eps) uses the
+// hardware square root and reciprocal (relative error about 2^-22 of a step
+// of size ~lr) instead of the IEEE-rounded sequences, which cost the fused
+// preprocess backward a large share of its instructions.
+__device__ __forceinline__ void adam_reg(float& param, float& m1, float& m2, float g, float lr, float b1, float b2,
+                                         float eps) {
+  const float a = b1 * m1 + (1.0f - b1) * g;
+  const float b = b2 * m2 + (1.0f - b2) * g * g;
+  param += (-lr * a) * rcp_approx(sqrt_approx(b) + eps);
+  m1 = a;
+  m2 = b;
+}
+__device__ __forceinline__ void adam_step(float* param, float* m1, float* m2, size_t k, float g, float lr, float b1,
+                                          float b2, float eps) {
+  float p = param[k], a = m1[k], b = m2[k];
+  adam_reg(p, a, b, g, lr, b1, b2, eps);
+  param[k] = p;
+  m1[k] = a;
+  m2[k] = b;
+}
+
 // Column-major 4x4 transforms, as the 3DGS matrices are laid out.
 __device__ __forceinline__ float3 xform_point3(const float* m, float3 p) {
   return make_float3(m[0] * p.x + m[4] * p.y + m[8] * p.z + m[12], m[1] * p.x + m[5] * p.y + m[9] * p.z + m[13],

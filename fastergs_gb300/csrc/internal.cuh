@@ -66,8 +66,17 @@ struct PbwdArgs {
   float* accum_abs;
   float* max_radii;
   float* denom;
-  int sh_staged;        // set by run_preprocess_bwd: SH rows and dL/dsh rows in shared memory
+  int sh_staged = 0;    // set by run_preprocess_bwd: SH rows and dL/dsh rows in shared memory
+  // Fused sparse Adam (adam_on): the gradient outputs above are unused; the
+  // activation backward and the Adam step update the raw parameters instead.
+  int adam_on = 0;
+  const float* opac = nullptr;  // activated opacities (P), for the sigmoid backward
+  fgs_adam_fused adam{};
 };
+
+// Host check of a fused Adam description (moments for every stepped group,
+// step sizes, known activations, 16-byte rotation rows, f_rest only with SH).
+bool adam_args_ok(const fgs_adam_fused* ad, const float* shs, const float* opacities);
 
 fgs_status run_preprocess_bwd(PbwdArgs& a, cudaStream_t s);
 fgs_status run_tile_ranges(int64_t n_cap, const int32_t* n_dev, uint32_t tiles, const uint64_t* keys_sorted,

@@ -214,6 +214,57 @@ fgs_status fgs_adam_update(float* param, const float* grad, float* exp_avg, floa
                            uint32_t N, uint32_t M, void* stream);
 
 /*
+ * Sparse Adam fused into the preprocess backward.  FB's training step writes
+ * every per-Gaussian gradient (dL/dmean3D, dc, sh, opacity, scale, rotation:
+ * 59 floats per Gaussian at SH degree 3), lets autograd push them through the
+ * activations (sigmoid, exp, normalize), and reads them back in
+ * SparseGaussianAdam.step (FB __init__.py:267-298, adam.cu:9-38).  The fused
+ * form applies the activation backward and FB's masked Adam step to the raw
+ * parameters in the kernel that produces the gradients; no gradient reaches
+ * memory.  A Gaussian is stepped when its radius is > 0 in at least one view
+ * (FB: visible = radii > 0).
+ *
+ * Groups (the names FasterGS's optimisers give their parameter groups):
+ * xyz (P,3), f_dc (P,1,3), f_rest (P,M,3), opacity (P,1), scaling (P,3),
+ * rotation (P,4); a group whose param is NULL is not stepped.  Step sizes are
+ * already multiplied by FB's bias compensation sqrt(1 - b2^t) / (1 - b1^t):
+ * lr_value by value, or, when lr is not NULL, FGS_ADAM_GROUPS device floats
+ * at lr, so that a captured CUDA graph picks up step sizes written between
+ * replays.  Activations: opacities =
+ * sigmoid(raw), scales = exp(raw), rotations = raw / |raw| (FGS_ACT_*), or
+ * identity where the rasterizer is given the raw tensor itself.
+ */
+enum {
+  FGS_ADAM_XYZ = 0, FGS_ADAM_F_DC = 1, FGS_ADAM_F_REST = 2, FGS_ADAM_OPACITY = 3, FGS_ADAM_SCALING = 4,
+  FGS_ADAM_ROTATION = 5, FGS_ADAM_GROUPS = 6
+};
+enum { FGS_ACT_IDENTITY = 0, FGS_ACT_SIGMOID = 1, FGS_ACT_EXP = 2, FGS_ACT_NORMALIZE = 3 };
+typedef struct {
+  float* param[FGS_ADAM_GROUPS];
+  float* exp_avg[FGS_ADAM_GROUPS];
+  float* exp_avg_sq[FGS_ADAM_GROUPS];
+  const float* lr;                /* device step sizes, or NULL: lr_value */
+  float lr_value[FGS_ADAM_GROUPS];
+  float eps[FGS_ADAM_GROUPS];
+  float b1, b2;
+  int opacity_act;                /* FGS_ACT_SIGMOID or FGS_ACT_IDENTITY */
+  int scaling_act;                /* FGS_ACT_EXP or FGS_ACT_IDENTITY */
+  int rotation_act;               /* FGS_ACT_NORMALIZE or FGS_ACT_IDENTITY */
+} fgs_adam_fused;
+
+/* fgs_preprocess_bwd with the sparse Adam step in place of the gradient
+ * outputs.  opacities (P) are the activated opacities the forward used
+ * (needed for FGS_ACT_SIGMOID).  f_rest rows are staged in shared memory:
+ * M <= 16 when shs is given and D > 0.  Densification statistics as in
+ * fgs_preprocess_bwd. */
+fgs_status fgs_preprocess_bwd_adam(
+    int P, int D, int M, const float* means3D, const int32_t* radii, const float* shs,
+    const float* splat_buffer, const float* opacities, const float* scales, const float* rotations,
+    float scale_modifier, const float* viewmatrix, const float* projmatrix, int width, int height,
+    float tan_fovx, float tan_fovy, const float* campos, const float* grad_record, const fgs_adam_fused* adam,
+    float* xyz_gradient_accum, float* xyz_gradient_accum_abs, float* max_radii, float* denom, void* stream);
+
+/*
  * Batched multi-camera rendering.  No counterpart in FB, which renders one
  * camera per call and reads the pair and bucket counts back to the host
  * three times per step (FB __init__.py:106-132, rasterizer_imp.cu:141-147),
@@ -288,6 +339,17 @@ fgs_status fgs_render_batched_bwd(int P, int D, int M, const float* means3D, con
                                   float* dL_dopacity, float* dL_dscale, float* dL_drot, float* dL_dcolor,
                                   float* dL_dcov3D, float* xyz_gradient_accum, float* xyz_gradient_accum_abs,
                                   float* max_radii, float* denom, void* stream);
+
+/* fgs_render_batched_bwd with the sparse Adam step fused into its preprocess
+ * backward (see fgs_adam_fused): gradients summed over the cameras step the
+ * raw parameters of every Gaussian that some camera saw. */
+fgs_status fgs_render_batched_bwd_adam(int P, int D, int M, const float* means3D, const float* shs,
+                                       const float* opacities, const float* scales, const float* rotations,
+                                       int num_views, const fgs_camera* cams, const fgs_tune_config* cfg,
+                                       int64_t pair_capacity, void* workspace, size_t workspace_bytes,
+                                       const int32_t* radii, const float* dL_dpixels, const fgs_adam_fused* adam,
+                                       float* xyz_gradient_accum, float* xyz_gradient_accum_abs,
+                                       float* max_radii, float* denom, void* stream);
 
 /* Reads the pair and bucket counts of the last batched forward on this
  * workspace (synchronises the stream).  Returns FGS_ERR_CAPACITY when the

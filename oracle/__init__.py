@@ -246,3 +246,46 @@ def cov3d(scales, quats, scale_modifier: float = 1.0):
     out = np.empty((scales.shape[0], 6))
     load().orc_cov3d(scales.shape[0], _p(scales), _p(quats), float(scale_modifier), _p(out))
     return out
+
+
+def sparse_adam(param, grad, exp_avg, exp_avg_sq, visible, lr: float, step: int, eps: float, b1: float = 0.9,
+                b2: float = 0.999):
+    """FB's SparseGaussianAdam.step for one parameter group, in FP32 as FB computes it.
+
+    FB __init__.py:288-298: the step count t is advanced first and the kernel is
+    given lr sqrt(1 - 0.999^t) / (1 - 0.9^t); adam.cu:26-37: for rows with
+    visible[i], m = b1 m + (1 - b1) g, v = b2 v + (1 - b2) g g,
+    p += -lr m / (sqrt(v) + eps); other rows are untouched.  Returns new
+    (param, exp_avg, exp_avg_sq) arrays of param's shape.
+    """
+    f = np.float32
+    t = f(step)
+    lr_t = f(f(lr) * np.sqrt(f(1) - f(0.999) ** t) / (f(1) - f(0.9) ** t))
+    N = len(visible)
+    p, g = np.asarray(param, f).reshape(N, -1), np.asarray(grad, f).reshape(N, -1)
+    m, v = np.asarray(exp_avg, f).reshape(N, -1), np.asarray(exp_avg_sq, f).reshape(N, -1)
+    b1, b2, eps = f(b1), f(b2), f(eps)
+    m_new = b1 * m + (f(1) - b1) * g
+    v_new = b2 * v + (f(1) - b2) * g * g
+    p_new = p + (-lr_t) * m_new / (np.sqrt(v_new) + eps)
+    vis = np.asarray(visible, bool)[:, None]
+    shape = np.shape(param)
+    return (np.where(vis, p_new, p).reshape(shape), np.where(vis, m_new, m).reshape(shape),
+            np.where(vis, v_new, v).reshape(shape))
+
+
+def activation_grad(kind: str, raw, grad_out):
+    """dL/draw from dL/dactivated for the 3DGS activations (FP64): sigmoid (y' = (1 - y) y),
+    exp (y' = y) and normalize along the last axis (dL/dx = g / |x| - x (g . x) / |x|^3)."""
+    raw, g = np.asarray(raw, np.float64), np.asarray(grad_out, np.float64)
+    if kind == "sigmoid":
+        y = 1.0 / (1.0 + np.exp(-raw))
+        return g * (1.0 - y) * y
+    if kind == "exp":
+        return g * np.exp(raw)
+    if kind == "normalize":
+        n = np.linalg.norm(raw, axis=-1, keepdims=True)
+        return g / n - raw * (g * raw).sum(-1, keepdims=True) / n ** 3
+    if kind == "identity":
+        return g
+    raise ValueError(kind)

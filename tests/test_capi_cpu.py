@@ -114,3 +114,65 @@ def test_tuner_search_space_and_cache_key():
     assert k1 == tune.cache_key(600_000, [(840, 1297), (360, 640)], 3, True)  # same power-of-two range
     assert k1 != tune.cache_key(1_000_000, [(840, 1297), (360, 640)], 3, False)
     assert k1 != tune.cache_key(3_000_000, [(840, 1297), (360, 640)], 3, True)
+
+
+def test_ctypes_structs_match_the_header(tmp_path):
+    """The ctypes mirrors of fgs_camera, fgs_tune_config and fgs_adam_fused have the C layout."""
+    import shutil
+    import subprocess
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    probe = tmp_path / "layout.c"
+    fields = {"fgs_camera": (_lib.Camera, ["viewmatrix", "bg", "width", "mult"]),
+              "fgs_tune_config": (_lib.TuneConfig, ["bucket_size", "recompute"]),
+              "fgs_adam_fused": (_lib.AdamFused, ["param", "exp_avg", "exp_avg_sq", "lr", "lr_value", "eps", "b1",
+                                                  "b2", "opacity_act", "scaling_act", "rotation_act"])}
+    lines = ["#include <stdio.h>", "#include <stddef.h>", '#include "fgs.h"', "int main(void) {"]
+    for name, (_, fs) in fields.items():
+        lines.append(f'  printf("%zu\\n", sizeof({name}));')
+        lines += [f'  printf("%zu\\n", offsetof({name}, {f}));' for f in fs]
+    lines += ["  return 0;", "}"]
+    probe.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    subprocess.run([cc, "-I", str(HEADER.parent), str(probe), "-o", str(exe)], check=True)
+    got = [int(v) for v in subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split()]
+    want = []
+    for name, (cls, fs) in fields.items():
+        want.append(C.sizeof(cls))
+        want += [getattr(cls, f).offset for f in fs]
+    assert got == want
+
+
+def test_fused_adam_entries_reject_bad_arguments(lib):
+    a = _lib.AdamFused()
+    s = None
+    # P == 0 is a no-op; a missing description, moments or an unknown activation is BAD_ARG
+    assert lib.fgs_preprocess_bwd_adam(0, 0, 0, None, None, None, None, None, None, None, 1.0, None, None, 8, 8, 0.5,
+                                       0.5, None, None, C.byref(a), None, None, None, None, s) == 0
+    dummy = C.c_void_p(256)
+    args = [8, 0, 0, dummy, dummy, None, dummy, dummy, dummy, dummy, 1.0, dummy, dummy, 8, 8, 0.5, 0.5, dummy, dummy]
+    assert lib.fgs_preprocess_bwd_adam(*args, None, None, None, None, None, s) == 1
+    a.param[0] = 256  # xyz without moments
+    assert lib.fgs_preprocess_bwd_adam(*args, C.byref(a), None, None, None, None, s) == 1
+    a.exp_avg[0] = a.exp_avg_sq[0] = 512
+    a.opacity_act = 7
+    assert lib.fgs_preprocess_bwd_adam(*args, C.byref(a), None, None, None, None, s) == 1
+    a.opacity_act = _lib.ACT["sigmoid"]
+    a.param[3], a.exp_avg[3], a.exp_avg_sq[3] = 256, 512, 768  # sigmoid opacity without the activated opacities
+    assert lib.fgs_preprocess_bwd_adam(*args[:7], None, *args[8:], C.byref(a), None, None, None, None, s) == 1
+    a.param[5], a.exp_avg[5], a.exp_avg_sq[5] = 260, 512, 768  # misaligned rotation rows
+    assert lib.fgs_preprocess_bwd_adam(*args, C.byref(a), None, None, None, None, s) == 1
+
+
+def test_fused_adam_row_index_in_fp32_is_exact():
+    """The fused step finds the Gaussian of f_rest element j of a 256-Gaussian block as
+    floor((j + 1/2) / row) and floor((j + 7/2) / row) in FP32 (row = 3 M, M <= 16): equal to
+    integer division for every row and element."""
+    import numpy as np
+    for row in range(3, 49):
+        inv = np.float32(1) / np.float32(row)
+        j = np.arange(256 * row, dtype=np.int64)
+        for off in (0, 3):
+            got = ((j.astype(np.float32) + np.float32(off + 0.5)) * inv).astype(np.int64)
+            assert np.array_equal(got, (j + off) // row), row
