@@ -63,6 +63,7 @@ def parse():
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-checkpoint", action="store_true")
     ap.add_argument("--no-adam", action="store_true")
+    ap.add_argument("--no-loss", action="store_true")
     ap.add_argument("--cameras", type=int, default=16)
     ap.add_argument("--tune", choices=["sweep", "default"], default="sweep",
                     help="batched launch config: autotuner sweep (18 configs) or FB's fixed choice")
@@ -176,6 +177,73 @@ def cpu_baseline(steps: int, warmup: int, n_gauss: int):
 
 
 # --------------------------------------------------------------------------- GPU path
+def loss_bench(args, dev, H, W):
+    """The training loss right after the image on the C2 frame (3 x 840 x 1297):
+    (1 - 0.2) L1 + 0.2 (1 - SSIM) with dL/dimage, fused (fgs_l1_dssim), against
+    the same loss from the fused-ssim mirror (map + partials, then the
+    backward) plus torch's L1, as the training loops compose it; and the FP64
+    oracle on the host for one frame."""
+    import torch
+    from fastergs_gb300.ssim import fused_ssim, l1_dssim_loss
+    rng = np.random.default_rng(11)
+    img = rng.uniform(0.0, 1.0, size=(3, H, W)).astype(np.float32)
+    gt = np.clip(img + rng.normal(0.0, 0.1, size=img.shape), 0.0, 1.0).astype(np.float32)
+    x = torch.tensor(img, device=dev, requires_grad=True)
+    y = torch.tensor(gt, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    # a buffer larger than L2, written between timed steps so every step reads from HBM
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+
+    def timed(fn, reps):
+        for _ in range(3):
+            fn()
+        torch.cuda.synchronize(dev)
+        tot = 0.0
+        for _ in range(reps):
+            flush.fill_(1)
+            ev0.record(stream)
+            fn()
+            ev1.record(stream)
+            torch.cuda.synchronize(dev)
+            tot += ev0.elapsed_time(ev1)
+        return tot / reps
+
+    def fused():
+        x.grad = None
+        loss, _ = l1_dssim_loss(x, y, 0.2)
+        loss.backward()
+
+    def composed():
+        x.grad = None
+        loss = 0.8 * (x - y).abs().mean() + 0.2 * (1.0 - fused_ssim(x.unsqueeze(0), y.unsqueeze(0)))
+        loss.backward()
+
+    reps = max(5, args.steps)
+    from fastergs_gb300 import _lib
+    _lib.kernel_timers(True, ["loss"])
+    _lib.read_kernel_timers(["loss"])
+    ms_fused = timed(fused, reps)
+    k_ms, k_n = _lib.read_kernel_timers(["loss"])["loss"]
+    _lib.kernel_timers(False, ["loss"])
+    kernel_ms = k_ms / max(k_n, 1)
+    ms_composed = timed(composed, reps)
+    t0 = time.perf_counter()
+    oracle_mod = __import__("oracle")
+    oracle_mod.l1_dssim(img, gt, 0.2)
+    cpu_ms = (time.perf_counter() - t0) * 1e3
+    px = 3 * H * W
+    algo = 12 * px  # image and target read, dL/dimage written, 4 B each
+    pk = ROOT / "MEASURED_PEAKS.json"
+    hbm = json.loads(pk.read_text()).get("hbm_gbs", 6800.0) if pk.exists() else 6800.0
+    achieved = algo / (kernel_ms * 1e-3) / 1e9
+    return {"workload": f"c2 frame 3x{H}x{W}: (1 - 0.2) L1 + 0.2 (1 - SSIM) and dL/dimage, L2 flushed per step",
+            "fused_ms": round(ms_fused, 4), "fused_kernel_ms": round(kernel_ms, 4),
+            "fused_ssim_plus_torch_l1_ms": round(ms_composed, 4),
+            "algorithmic_bytes": int(algo), "hbm_frac_of_measured": round(achieved / hbm, 4),
+            "cpu_fp64_oracle_ms": round(cpu_ms, 1)}
+
+
 def gpu_bench(args, rank, local, world):
     import torch
     import fastergs_gb300 as fgs
@@ -277,6 +345,9 @@ def gpu_bench(args, rank, local, world):
     fused_adam = None
     if not args.no_adam and world == 1:
         fused_adam = adam_bench(args, dev, s, rast, dL)
+    loss = None
+    if not args.no_loss and world == 1:
+        loss = loss_bench(args, dev, cam.height, cam.width)
     batched = None
     if not args.no_batched and world == 1:
         batched = []
@@ -295,7 +366,7 @@ def gpu_bench(args, rank, local, world):
         checkpoint = checkpoint_bench(args, dev)
     return dict(ms_step=ms_step_job, fwd_ms=fwd_ms, clocks=clocks, ktimes=ktimes, K=K,
                 launches_per_step=launches_per_step, e2e=e2e, P=s.P, W=cam.width, H=cam.height, batched=batched,
-                checkpoint=checkpoint, W_eval=W_eval, fp32_peak=fp32_peak, fused_adam=fused_adam)
+                checkpoint=checkpoint, W_eval=W_eval, fp32_peak=fp32_peak, fused_adam=fused_adam, loss=loss)
 
 
 def e2e_bench(args, dev, stream, host, dL_host, dev_in, dL, rast, world):
@@ -741,6 +812,7 @@ def main():
         "e2e": res["e2e"], "gpu_launches": int(round(res["launches_per_step"] * args.steps)),
         "clocks": res["clocks"], "roofline": roof, "kernels": table, "cpu_baseline": cb,
         "batched": res["batched"], "checkpoint": res["checkpoint"], "fused_adam": res["fused_adam"],
+        "loss": res["loss"],
     }
     print(json.dumps(line), flush=True)
     barrier(world)

@@ -63,6 +63,10 @@ SIGNATURES = {
     "fgs_preprocess_bwd_adam": (i32, [i32, i32, i32, vp, vp, vp, vp, vp, vp, vp, f32, vp, vp, i32, i32, f32, f32,
                                       vp, vp, adamp, vp, vp, vp, vp, vp]),
     "fgs_densify_stats": (i32, [i32, vp, vp, vp, vp, vp, vp, vp]),
+    "fgs_ssim_fwd": (i32, [i32, i32, i32, f32, f32, vp, vp, vp, vp, vp, vp, vp]),
+    "fgs_ssim_bwd": (i32, [i32, i32, i32, vp, vp, vp, vp, vp, vp, vp, vp]),
+    "fgs_l1_dssim_scratch_bytes": (sz, [i32, i32, i32]),
+    "fgs_l1_dssim": (i32, [i32, i32, i32, f32, vp, vp, vp, sz, vp, vp, vp, vp]),
     "fgs_render_simp": (i32, [i32, i64, i32, i32, vp, vp, vp, vp, vp, vp, vp, vp]),
     "fgs_render_depth": (i32, [i32, i64, i32, i32, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp]),
     "fgs_adam_update": (i32, [vp, vp, vp, vp, vp, f32, f32, f32, f32, C.c_uint32, C.c_uint32, vp]),
@@ -82,7 +86,8 @@ SIGNATURES = {
 
 # Kernel ids of fgs_kernel_timer (include/fgs.h).
 KERNELS = {"preprocess": 0, "preprocess_large": 1, "sort_hist": 2, "sort_pass": 3, "tile_ranges": 4,
-           "bucket_setup": 5, "render_fwd": 6, "empty_tiles": 7, "render_bwd": 8, "preprocess_bwd": 9}
+           "bucket_setup": 5, "render_fwd": 6, "empty_tiles": 7, "render_bwd": 8, "preprocess_bwd": 9,
+           "loss": 10}
 
 
 class FgsError(RuntimeError):

@@ -18,7 +18,8 @@ CSRC = PKG / "csrc"
 OBJ = PKG / "_build"
 LIB = PKG / "libfgs.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["preprocess.cu", "sort.cu", "render.cu", "backward.cu", "batched.cu", "aux_passes.cu", "capi.cu"]
+SOURCES = ["preprocess.cu", "sort.cu", "render.cu", "backward.cu", "batched.cu", "aux_passes.cu", "ssim.cu",
+           "capi.cu"]
 
 
 def nvcc() -> str:

@@ -265,6 +265,35 @@ fgs_status fgs_preprocess_bwd_adam(
     float* xyz_gradient_accum, float* xyz_gradient_accum_abs, float* max_radii, float* denom, void* stream);
 
 /*
+ * SSIM (the fused-ssim extension FasterGS's backbones train with,
+ * gs_submodules/fused-ssim/ssim.cu; the SSIM of 3DGS/utils/loss_utils.py:33-63):
+ * 11-tap Gaussian window of sigma 1.5, zero padding.  Images are `planes`
+ * contiguous H x W float planes (batch x channels).
+ *
+ * fgs_ssim_fwd: the SSIM map, and, when dm_dmu1 / dm_dsigma1_sq / dm_dsigma12
+ * are given (all or none), the map's partial derivatives w.r.t. mu1, E[x^2]
+ * and E[xy] that fgs_ssim_bwd needs (fusedssim, ssim.cu:185-285).
+ * fgs_ssim_bwd: dL/dimg1 from dL/dmap (fusedssim_backward, ssim.cu:287-365).
+ */
+fgs_status fgs_ssim_fwd(int planes, int H, int W, float C1, float C2, const float* img1, const float* img2,
+                        float* ssim_map, float* dm_dmu1, float* dm_dsigma1_sq, float* dm_dsigma12, void* stream);
+fgs_status fgs_ssim_bwd(int planes, int H, int W, const float* img1, const float* img2, const float* dL_dmap,
+                        const float* dm_dmu1, const float* dm_dsigma1_sq, const float* dm_dsigma12,
+                        float* dL_dimg1, void* stream);
+
+/*
+ * The training loss of FasterGS's backbones in one pass with its gradient
+ * (taming-3dgs/train_faster.py:121-125, FastGS/train_faster.py:105-109):
+ *   loss = (1 - lambda) mean|img - gt| + lambda (1 - mean SSIM(img, gt)),
+ * C1 = 0.01^2, C2 = 0.03^2, "same" padding.  Writes *loss, *ssim_mean
+ * (optional) and dL_dimg = dloss/dimg (device), never the SSIM map.  scratch:
+ * fgs_l1_dssim_scratch_bytes(planes, H, W) bytes, 8-byte aligned.
+ */
+size_t fgs_l1_dssim_scratch_bytes(int planes, int H, int W);
+fgs_status fgs_l1_dssim(int planes, int H, int W, float lambda, const float* img, const float* gt, void* scratch,
+                        size_t scratch_bytes, float* loss, float* ssim_mean, float* dL_dimg, void* stream);
+
+/*
  * Batched multi-camera rendering.  No counterpart in FB, which renders one
  * camera per call and reads the pair and bucket counts back to the host
  * three times per step (FB __init__.py:106-132, rasterizer_imp.cu:141-147),
@@ -378,7 +407,7 @@ fgs_status fgs_batch_offsets(int P, int num_views, const fgs_camera* cams, const
 enum {
   FGS_K_PREPROCESS = 0, FGS_K_PREPROCESS_LARGE = 1, FGS_K_SORT_HIST = 2, FGS_K_SORT_PASS = 3,
   FGS_K_TILE_RANGES = 4, FGS_K_BUCKET_SETUP = 5, FGS_K_RENDER_FWD = 6, FGS_K_EMPTY_TILES = 7,
-  FGS_K_RENDER_BWD = 8, FGS_K_PREPROCESS_BWD = 9, FGS_K_COUNT = 10
+  FGS_K_RENDER_BWD = 8, FGS_K_PREPROCESS_BWD = 9, FGS_K_LOSS = 10, FGS_K_COUNT = 11
 };
 fgs_status fgs_kernel_timer(int kernel_id, int enable);
 fgs_status fgs_kernel_timer_read(int kernel_id, double* total_ms, int* launches);

@@ -289,3 +289,59 @@ def activation_grad(kind: str, raw, grad_out):
     if kind == "identity":
         return g
     raise ValueError(kind)
+
+
+def ssim_window() -> np.ndarray:
+    """11-tap Gaussian of sigma 1.5, normalised (3DGS utils/loss_utils.py:23-25), FP64."""
+    t = np.arange(11, dtype=np.float64) - 5.0
+    g = np.exp(-t * t / (2.0 * 1.5 * 1.5))
+    return g / g.sum()
+
+
+def _window_sum(a):
+    """Separable 11x11 window sum of the last two axes with zero padding ("same"),
+    the F.conv2d(..., padding=5) of 3DGS utils/loss_utils.py:44-52."""
+    w = ssim_window()
+    H, W = a.shape[-2:]
+    p = np.zeros(a.shape[:-2] + (H + 10, W + 10))
+    p[..., 5:5 + H, 5:5 + W] = a
+    h = sum(w[t] * p[..., :, t:t + W] for t in range(11))
+    return sum(w[t] * h[..., t:t + H, :] for t in range(11))
+
+
+def ssim_map(img1, img2, C1: float = 0.01 ** 2, C2: float = 0.03 ** 2):
+    """SSIM map and its partials w.r.t. mu1, E[x^2], E[xy] (FP64), as fused-ssim returns them
+    (ssim.cu:262-283; the map of 3DGS loss_utils.py:44-60).  Arrays (..., H, W)."""
+    x, y = np.asarray(img1, np.float64), np.asarray(img2, np.float64)
+    return ssim_from_moments(_window_sum(x), _window_sum(y), _window_sum(x * x), _window_sum(y * y),
+                             _window_sum(x * y), C1, C2)
+
+
+def ssim_from_moments(mu1, mu2, e11, e22, e12, C1: float = 0.01 ** 2, C2: float = 0.03 ** 2):
+    """SSIM and its partials w.r.t. mu1, E[x^2], E[xy] from the five window moments (FP64)."""
+    s1, s2, s12 = e11 - mu1 * mu1, e22 - mu2 * mu2, e12 - mu1 * mu2
+    C = 2 * mu1 * mu2 + C1
+    D = 2 * s12 + C2
+    A = mu1 * mu1 + mu2 * mu2 + C1
+    B = s1 + s2 + C2
+    m = C * D / (A * B)
+    d_mu1 = (2 * mu2 * D - 2 * mu2 * C) / (A * B) - 2 * mu1 * C * D / (A * A * B) + 2 * mu1 * C * D / (A * B * B)
+    return m, d_mu1, -C * D / (A * B * B), 2 * C / (A * B)
+
+
+def ssim_backward(img1, img2, dL_dmap, d_mu1, d_e11, d_e12):
+    """dL/dimg1 = G * (g dm/dmu1) + 2 x G * (g dm/dE[x^2]) + y G * (g dm/dE[xy]) (fused-ssim
+    ssim.cu:287-365; the window is symmetric, so its transpose is itself)."""
+    g = np.asarray(dL_dmap, np.float64)
+    x, y = np.asarray(img1, np.float64), np.asarray(img2, np.float64)
+    return _window_sum(g * d_mu1) + 2 * x * _window_sum(g * d_e11) + y * _window_sum(g * d_e12)
+
+
+def l1_dssim(img, gt, lam: float):
+    """The backbones' training loss (1 - lam) mean|img - gt| + lam (1 - mean SSIM) and its
+    gradient w.r.t. img (taming-3dgs/train_faster.py:121-125), FP64: (loss, ssim_mean, grad)."""
+    x, y = np.asarray(img, np.float64), np.asarray(gt, np.float64)
+    n = x.size
+    m, a, b, c = ssim_map(x, y)
+    grad = (1.0 - lam) * np.sign(x - y) / n + ssim_backward(x, y, np.full_like(m, -lam / n), a, b, c)
+    return (1.0 - lam) * np.abs(x - y).mean() + lam * (1.0 - m.mean()), m.mean(), grad

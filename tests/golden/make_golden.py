@@ -9,6 +9,10 @@ stores inputs and outputs in tests/golden/*.npz:
                       L L^T -> strip_symmetric (the 3DGS covariance path)
   camera_golden.npz   3DGS/utils/graphics_utils.py getWorld2View2 /
                       getProjectionMatrix composed as 3DGS/scene/cameras.py:54-57
+  ssim_golden.npz     3DGS/utils/loss_utils.py ssim (per-image means) and the
+                      training loss (1 - lambda) l1_loss + lambda (1 - ssim),
+                      with their gradients w.r.t. the rendered image by
+                      autograd, in FP64 (the window is the module's own)
 
 build_rotation / build_scaling_rotation allocate with device='cuda'; the
 script runs them on CPU by handing the module a torch proxy whose zeros()
@@ -98,6 +102,27 @@ def make_cameras(rng):
                         world_view=arr(4), proj=arr(5), full_proj=arr(6), center=arr(7))
 
 
+def make_ssim(rng):
+    lu = _load("3DGS/utils/loss_utils.py", "ref_loss_utils")
+    out = {}
+    for k, (B, C, H, W) in enumerate([(1, 3, 37, 53), (2, 1, 64, 40)]):
+        img = rng.uniform(0.0, 1.0, size=(B, C, H, W))
+        gt = np.clip(img + rng.normal(0.0, 0.15, size=img.shape), 0.0, 1.0)
+        x = torch.tensor(img, dtype=torch.float64, requires_grad=True)
+        y = torch.tensor(gt, dtype=torch.float64)
+        per_image = lu.ssim(x, y, size_average=False)          # mean SSIM per image
+        g_ssim, = torch.autograd.grad(per_image.sum(), x)      # d sum of image means / d img
+        x2 = torch.tensor(img, dtype=torch.float64, requires_grad=True)
+        lam = 0.2
+        loss = (1.0 - lam) * lu.l1_loss(x2, y) + lam * (1.0 - lu.ssim(x2, y))
+        g_loss, = torch.autograd.grad(loss, x2)
+        out.update({f"img{k}": img, f"gt{k}": gt, f"ssim{k}": per_image.detach().numpy(),
+                    f"grad_ssim{k}": g_ssim.numpy(), f"loss{k}": np.float64(loss.item()),
+                    f"grad_loss{k}": g_loss.numpy()})
+    out["lam"] = np.float64(0.2)
+    np.savez_compressed(HERE / "ssim_golden.npz", **out)
+
+
 def main():
     if not REF.exists():
         sys.exit(f"reference checkout not found at {REF}")
@@ -105,6 +130,7 @@ def main():
     make_sh(rng)
     make_cov(rng)
     make_cameras(rng)
+    make_ssim(np.random.default_rng(20241204))
     print("wrote", sorted(p.name for p in HERE.glob("*.npz")))
 
 
