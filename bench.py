@@ -177,6 +177,23 @@ def cpu_baseline(steps: int, warmup: int, n_gauss: int):
 
 
 # --------------------------------------------------------------------------- GPU path
+def ply_bench(s):
+    """Writing and reading the C2 scene as a 3DGS PLY file (host I/O, page cache)."""
+    from fastergs_gb300 import ply
+    params = {"xyz": s.means, "f_dc": s.dc, "f_rest": s.shs, "opacity": s.opacity_logits, "scaling": s.log_scales,
+              "rotation": s.quats}
+    with tempfile.TemporaryDirectory() as d:
+        path = os.path.join(d, "point_cloud.ply")
+        t0 = time.perf_counter()
+        ply.save_ply(path, params)
+        t1 = time.perf_counter()
+        ply.load_ply(path)
+        t2 = time.perf_counter()
+        nbytes = os.path.getsize(path)
+    return {"gaussians": int(s.P), "file_bytes": int(nbytes), "save_ms": round((t1 - t0) * 1e3, 1),
+            "load_ms": round((t2 - t1) * 1e3, 1)}
+
+
 def loss_bench(args, dev, H, W):
     """The training loss right after the image on the C2 frame (3 x 840 x 1297):
     (1 - 0.2) L1 + 0.2 (1 - SSIM) with dL/dimage, fused (fgs_l1_dssim), against
@@ -348,6 +365,7 @@ def gpu_bench(args, rank, local, world):
     loss = None
     if not args.no_loss and world == 1:
         loss = loss_bench(args, dev, cam.height, cam.width)
+        loss["ply"] = ply_bench(s)
     batched = None
     if not args.no_batched and world == 1:
         batched = []

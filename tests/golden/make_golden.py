@@ -9,6 +9,11 @@ stores inputs and outputs in tests/golden/*.npz:
                       L L^T -> strip_symmetric (the 3DGS covariance path)
   camera_golden.npz   3DGS/utils/graphics_utils.py getWorld2View2 /
                       getProjectionMatrix composed as 3DGS/scene/cameras.py:54-57
+  ply_golden.npz      3DGS/scene/gaussian_model.py save_ply (the vertex array it
+                      hands plyfile: property names and values) and load_ply
+                      (the tensors it builds from that array), SH degrees 1, 3
+  camera_ts_golden.npz  getWorld2View2 with a translate / scale, composed as
+                      3DGS/scene/cameras.py:54-57
   ssim_golden.npz     3DGS/utils/loss_utils.py ssim (per-image means) and the
                       training loss (1 - lambda) l1_loss + lambda (1 - ssim),
                       with their gradients w.r.t. the rendered image by
@@ -16,7 +21,10 @@ stores inputs and outputs in tests/golden/*.npz:
 
 build_rotation / build_scaling_rotation allocate with device='cuda'; the
 script runs them on CPU by handing the module a torch proxy whose zeros()
-drops the device argument.  Nothing else of the reference is changed.
+(and, for load_ply, tensor()) drops the device argument.  gaussian_model.py
+imports plyfile and simple_knn, absent here: it gets stand-ins whose PlyData /
+PlyElement capture the array save_ply writes and hand it back to load_ply.
+Nothing else of the reference is changed.
 
 Usage:  python tests/golden/make_golden.py
 """
@@ -123,6 +131,122 @@ def make_ssim(rng):
     np.savez_compressed(HERE / "ssim_golden.npz", **out)
 
 
+class _PlyCapture:
+    """Stand-in for the plyfile module: keeps the vertex array save_ply describes."""
+
+    def __init__(self):
+        self.elements = None
+        cap = self
+
+        class PlyElement:
+            @staticmethod
+            def describe(arr, name):
+                return (name, arr)
+
+        class _Props:
+            def __init__(self, name):
+                self.name = name
+
+        class _Element:
+            def __init__(self, arr):
+                self.arr = arr
+                self.properties = [_Props(n) for n in arr.dtype.names]
+
+            def __getitem__(self, k):
+                return self.arr[k]
+
+        class PlyData:
+            def __init__(self, els=None):
+                self.els = els or []
+                self.elements = [_Element(a) for _, a in self.els]
+
+            def write(self, path):
+                cap.elements = self.els
+
+            @staticmethod
+            def read(path):
+                return PlyData(cap.elements)
+
+        self.module = types.SimpleNamespace(PlyData=PlyData, PlyElement=PlyElement)
+
+
+def make_ply(rng):
+    import tempfile
+    cap = _PlyCapture()
+    saved = {k: sys.modules.get(k) for k in ("plyfile", "simple_knn", "simple_knn._C")}
+    sys.modules["plyfile"] = cap.module
+    sys.modules["simple_knn"] = types.ModuleType("simple_knn")
+    sys.modules["simple_knn._C"] = types.SimpleNamespace(distCUDA2=None)
+    sys.path.insert(0, str(REF / "3DGS"))
+    try:
+        gm = _load("3DGS/scene/gaussian_model.py", "ref_gaussian_model")
+        proxy = _cpu_torch_proxy()
+        tensor = torch.tensor
+
+        def tensor_cpu(*args, **kwargs):
+            kwargs.pop("device", None)
+            return tensor(*args, **kwargs)
+
+        proxy.tensor = tensor_cpu
+        gm.torch = proxy
+        out = {}
+        for deg in (1, 3):
+            P, M = 37, (deg + 1) ** 2 - 1
+            model = object.__new__(gm.GaussianModel)
+            model.max_sh_degree = deg
+            f = lambda *shape: torch.tensor(rng.normal(size=shape), dtype=torch.float32)
+            model._xyz, model._features_dc, model._features_rest = f(P, 3), f(P, 1, 3), f(P, M, 3)
+            model._opacity, model._scaling, model._rotation = f(P, 1), f(P, 3), f(P, 4)
+            with tempfile.TemporaryDirectory() as d:
+                model.save_ply(os.path.join(d, "point_cloud.ply"))
+                (_, arr), = cap.elements
+                loaded = object.__new__(gm.GaussianModel)
+                loaded.max_sh_degree = deg
+                loaded.load_ply(os.path.join(d, "point_cloud.ply"))
+            out[f"names{deg}"] = np.array(arr.dtype.names)
+            out[f"vertex{deg}"] = np.stack([arr[n] for n in arr.dtype.names], axis=1).astype(np.float32)
+            for k, t in (("xyz", model._xyz), ("f_dc", model._features_dc), ("f_rest", model._features_rest),
+                         ("opacity", model._opacity), ("scaling", model._scaling), ("rotation", model._rotation)):
+                out[f"{k}{deg}"] = t.numpy()
+            for k, t in (("xyz", loaded._xyz), ("f_dc", loaded._features_dc), ("f_rest", loaded._features_rest),
+                         ("opacity", loaded._opacity), ("scaling", loaded._scaling),
+                         ("rotation", loaded._rotation)):
+                out[f"loaded_{k}{deg}"] = t.detach().numpy()
+        np.savez_compressed(HERE / "ply_golden.npz", **out)
+    finally:
+        sys.path.remove(str(REF / "3DGS"))
+        for k, v in saved.items():
+            if v is None:
+                sys.modules.pop(k, None)
+            else:
+                sys.modules[k] = v
+
+
+def make_cameras_ts(rng):
+    gr = _load("3DGS/utils/graphics_utils.py", "ref_graphics_utils_ts")
+    out = {k: [] for k in ("R", "T", "translate", "scale", "fovx", "fovy", "world_view", "full_proj", "center")}
+    for k in range(4):
+        q = rng.normal(size=4)
+        q /= np.linalg.norm(q)
+        r, x, y, z = q
+        R = np.array([[1 - 2 * (y * y + z * z), 2 * (x * y - r * z), 2 * (x * z + r * y)],
+                      [2 * (x * y + r * z), 1 - 2 * (x * x + z * z), 2 * (y * z - r * x)],
+                      [2 * (x * z - r * y), 2 * (y * z + r * x), 1 - 2 * (x * x + y * y)]])
+        T = rng.normal(size=3) * 2
+        tr = rng.normal(size=3)
+        sc = float(rng.uniform(0.5, 2.0))
+        fovx = math.radians(float(rng.uniform(40, 80)))
+        fovy = math.radians(float(rng.uniform(30, 70)))
+        wv = torch.tensor(gr.getWorld2View2(R, T, tr, sc)).transpose(0, 1)
+        pm = gr.getProjectionMatrix(znear=0.01, zfar=100.0, fovX=fovx, fovY=fovy).transpose(0, 1)
+        full = wv.unsqueeze(0).bmm(pm.unsqueeze(0)).squeeze(0)
+        for key, val in (("R", R), ("T", T), ("translate", tr), ("scale", sc), ("fovx", fovx), ("fovy", fovy),
+                         ("world_view", wv.numpy()), ("full_proj", full.numpy()),
+                         ("center", wv.inverse()[3, :3].numpy())):
+            out[key].append(val)
+    np.savez_compressed(HERE / "camera_ts_golden.npz", **{k: np.stack(v) for k, v in out.items()})
+
+
 def main():
     if not REF.exists():
         sys.exit(f"reference checkout not found at {REF}")
@@ -131,6 +255,8 @@ def main():
     make_cov(rng)
     make_cameras(rng)
     make_ssim(np.random.default_rng(20241204))
+    make_ply(np.random.default_rng(7))
+    make_cameras_ts(np.random.default_rng(8))
     print("wrote", sorted(p.name for p in HERE.glob("*.npz")))
 
 

@@ -201,3 +201,22 @@ def test_vanilla_rasterize_gaussians_alias(cuda_device):
     assert rel(dop, leaves["opacities"].grad) <= 1e-5
     assert rel(dsh[:, :1], leaves["dc"].grad) <= 1e-5
     assert rel(dsh[:, 1:], leaves["shs"].grad) <= 1e-5
+
+
+def test_render_from_ply_file_matches_direct_render(cuda_device, tmp_path):
+    """A scene written as a 3DGS PLY, read back and rasterized with settings from
+    fastergs_gb300.cameras gives the direct render's radii and image."""
+    from fastergs_gb300 import cameras, ply
+    s = scenes.scene_c1()
+    params = {"xyz": s.means, "f_dc": s.dc, "f_rest": s.shs, "opacity": s.opacity_logits, "scaling": s.log_scales,
+              "rotation": s.quats}
+    ply.save_ply(tmp_path / "point_cloud.ply", params)
+    loaded = ply.load_ply(tmp_path / "point_cloud.ply")  # 15 coefficients stored, rendered at the scene's degree
+    assert loaded["f_rest"].shape == s.shs.shape
+    model = ply.to_device(loaded, cuda_device)
+    rs = cameras.raster_settings(s.camera, sh_degree=s.sh_degree, device=cuda_device)
+    with torch.no_grad():
+        img, radii = GaussianRasterizer(rs)(**ply.activated(model))
+        img_ref, radii_ref = render(s, raw_params(s, cuda_device), cuda_device)
+    assert torch.equal(radii, radii_ref)
+    assert float((img - img_ref).abs().max()) < 1e-6
