@@ -119,7 +119,7 @@ __device__ __forceinline__ float3 sh_colour(int D, float x, float y, float z, co
   return f3(fmaxf(r.x, 0.0f), fmaxf(r.y, 0.0f), fmaxf(r.z, 0.0f));
 }
 
-__global__ void __launch_bounds__(kPreThreads, 3) k_preprocess(const PreArgs a) {
+__global__ void __launch_bounds__(kPreThreads, 4) k_preprocess(const PreArgs a) {
   __shared__ float2 s_xy[kPreWarps][kWarp];
   __shared__ float4 s_cp[kPreWarps][kWarp];    // conic a, b, c, power
   __shared__ int4 s_geo[kPreWarps][kWarp];     // rect min x, min y, width, candidate start

@@ -409,10 +409,25 @@ __global__ void __launch_bounds__(kFwdWarps * kWarp, 7) k_render_fwd(const FwdAr
   }
 }
 
+// Self-check of the bounded waits: one warp waits, as a bucket of the chain
+// does, for a stage that nothing publishes; the wait gives up after
+// kSpinLimit polls, raises the timeout bit and the warp returns.
+__global__ void k_selftest_wait(uint32_t* flag) { wait_stage(flag, 1u, threadIdx.x & 31); }
+
 }  // namespace
 }  // namespace fgs
 
 FGS_DEFINE_ERROR_ACCESSOR(render)
+
+extern "C" fgs_status fgs_selftest_wait(uint32_t* flag, void* stream) {
+  using namespace fgs;
+  if (!flag) return FGS_ERR_BAD_ARG;
+  cudaStream_t s = (cudaStream_t)stream;
+  FGS_TRY(cudaMemsetAsync(flag, 0, sizeof(uint32_t), s));
+  k_selftest_wait<<<1, kWarp, 0, s>>>(flag);
+  FGS_LAUNCH_CHECK();
+  return FGS_OK;
+}
 
 namespace fgs {
 fgs_status run_tile_ranges(int64_t n_cap, const int32_t* n_dev, uint32_t tiles, const uint64_t* keys_sorted,

@@ -39,14 +39,34 @@ struct Taps {
   float w[kTaps];
 };
 
-// rows x cols region of a plane whose top-left is (y0, x0), zero outside
-// the image, into dst with row stride ld.
-__device__ __forceinline__ void stage_region(float* dst, int ld, const float* plane, int H, int W, int y0, int x0,
-                                             int rows, int cols) {
-  for (int i = threadIdx.x; i < rows * cols; i += kSsimThreads) {
-    const int r = i / cols, c = i - r * cols;
-    const int y = y0 + r, x = x0 + c;
-    dst[r * ld + c] = (y >= 0 && y < H && x >= 0 && x < W) ? __ldg(plane + (size_t)y * W + x) : 0.f;
+// N x N regions of two planes whose top-left is (y0, x0), zero outside the
+// image, into da / db (row stride N): four elements of each per thread and
+// round, all eight loads issued before the shared-memory stores.
+template <int N>
+__device__ __forceinline__ void stage_two(float* __restrict__ da, float* __restrict__ db,
+                                          const float* __restrict__ pa, const float* __restrict__ pb, int H, int W,
+                                          int y0, int x0) {
+  constexpr int kU = 4;
+  for (int base = threadIdx.x; base < N * N; base += kU * kSsimThreads) {
+    float va[kU], vb[kU];
+#pragma unroll
+    for (int u = 0; u < kU; ++u) {
+      const int i = base + u * kSsimThreads;
+      const int r = i / N, c = i - r * N;
+      const int y = y0 + r, x = x0 + c;
+      const bool in = i < N * N && y >= 0 && y < H && x >= 0 && x < W;
+      const size_t at = in ? (size_t)y * W + x : 0;
+      va[u] = in ? __ldg(pa + at) : 0.f;
+      vb[u] = in ? __ldg(pb + at) : 0.f;
+    }
+#pragma unroll
+    for (int u = 0; u < kU; ++u) {
+      const int i = base + u * kSsimThreads;
+      if (i < N * N) {
+        da[i] = va[u];
+        db[i] = vb[u];
+      }
+    }
   }
 }
 
@@ -183,8 +203,7 @@ __global__ void __launch_bounds__(kSsimThreads) k_ssim_fwd(int H, int W, float C
   FwdShared& sh = *reinterpret_cast<FwdShared*>(s_raw);
   const int x0 = blockIdx.x * kT, y0 = blockIdx.y * kT;
   const size_t poff = (size_t)blockIdx.z * H * W;
-  stage_region(sh.sx, kFwdRows, img1 + poff, H, W, y0 - kRad, x0 - kRad, kFwdRows, kFwdRows);
-  stage_region(sh.sy, kFwdRows, img2 + poff, H, W, y0 - kRad, x0 - kRad, kFwdRows, kFwdRows);
+  stage_two<kFwdRows>(sh.sx, sh.sy, img1 + poff, img2 + poff, H, W, y0 - kRad, x0 - kRad);
   __syncthreads();
   hpass_moments<4>(sh.sx, sh.sy, kFwdRows, sh.h, kFwdRows * kT, kT, kFwdRows, kT, w);
   __syncthreads();
@@ -281,8 +300,7 @@ __global__ void __launch_bounds__(kSsimThreads) k_l1_dssim(int H, int W, float C
   const size_t poff = (size_t)blockIdx.z * H * W;
   const float* px = img + poff;
   const float* py = gt + poff;
-  stage_region(sh.a.in.sx, kInRows, px, H, W, y0 - 2 * kRad, x0 - 2 * kRad, kInRows, kInRows);
-  stage_region(sh.a.in.sy, kInRows, py, H, W, y0 - 2 * kRad, x0 - 2 * kRad, kInRows, kInRows);
+  stage_two<kInRows>(sh.a.in.sx, sh.a.in.sy, px, py, H, W, y0 - 2 * kRad, x0 - 2 * kRad);
   __syncthreads();
   // moments for the tile plus a 5-pixel halo: 52 staged rows x 42 columns
   hpass_moments<6>(sh.a.in.sx, sh.a.in.sy, kInRows, sh.b.h1, kInRows * kFwdRows, kFwdRows, kInRows, kFwdRows, w);
@@ -329,16 +347,23 @@ __global__ void __launch_bounds__(kSsimThreads) k_l1_dssim(int H, int W, float C
   vsums<4, 3>(sh.b.h2, kFwdRows * kT, kT, r0, c, w, s);
   float l1 = 0.f;
   const float wl1 = (1.f - lambda) * inv_n;
+  float xv[4], yv[4];
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {  // loads first, then the stores
+    const int y = y0 + r0 + k, x = x0 + c;
+    const bool in = y < H && x < W;
+    const size_t i = in ? (size_t)y * W + x : 0;
+    xv[k] = in ? __ldg(px + i) : 0.f;
+    yv[k] = in ? __ldg(py + i) : 0.f;
+  }
 #pragma unroll
   for (int k = 0; k < 4; ++k) {
     const int y = y0 + r0 + k, x = x0 + c;
     if (y < H && x < W) {
-      const size_t i = (size_t)y * W + x;
-      const float xv = __ldg(px + i), yv = __ldg(py + i);
-      const float d = xv - yv;
+      const float d = xv[k] - yv[k];
       l1 += fabsf(d);
       const float sg = d > 0.f ? 1.f : (d < 0.f ? -1.f : 0.f);  // d|d|/dd as torch.abs (0 at 0)
-      dL_dimg[poff + i] = s[k][0] + 2.f * xv * s[k][1] + yv * s[k][2] + wl1 * sg;
+      dL_dimg[poff + (size_t)y * W + x] = s[k][0] + 2.f * xv[k] * s[k][1] + yv[k] * s[k][2] + wl1 * sg;
     }
   }
   // per-tile sums of m and |x - y|

@@ -53,6 +53,13 @@ const char* fgs_version(void);
  * Synchronises the stream.  *flags receives the word. */
 fgs_status fgs_device_errors(int* flags, int clear, void* stream);
 
+/* Self-check of the bounded device waits: one warp runs the wait of the
+ * compositing chain on `flag` (one device u32, zeroed here), which nothing
+ * sets; the wait gives up after its bounded spin (about a second), raises the
+ * timeout bit (bit 0) in the device error word and the kernel returns, so
+ * the context stays usable.  Read the bit with fgs_device_errors. */
+fgs_status fgs_selftest_wait(uint32_t* flag, void* stream);
+
 /*
  * Per-Gaussian preprocess and (tile, Gaussian) key emission.
  * Replaces faster::preprocess (FB csrc/ops.h:71-85, body

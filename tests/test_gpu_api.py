@@ -7,7 +7,7 @@ import torch
 
 import oracle
 from fastergs_gb300 import (Buffer, GaussianRasterizationSettings, GaussianRasterizer, SparseGaussianAdam,
-                            _RasterizeGaussians, scenes)
+                            _C, _RasterizeGaussians, scenes)
 
 pytestmark = pytest.mark.gpu
 
@@ -220,3 +220,22 @@ def test_render_from_ply_file_matches_direct_render(cuda_device, tmp_path):
         img_ref, radii_ref = render(s, raw_params(s, cuda_device), cuda_device)
     assert torch.equal(radii, radii_ref)
     assert float((img - img_ref).abs().max()) < 1e-6
+
+
+def test_expired_wait_reports_timeout_and_context_survives(cuda_device):
+    """A bounded device wait on a flag nothing sets gives up, raises the timeout bit that the
+    host reads, and the context keeps working (no fault, no hang)."""
+    import time
+    from fastergs_gb300 import _lib
+    assert _C.device_errors(cuda_device) == 0
+    flag = torch.zeros(1, dtype=torch.int32, device=cuda_device)
+    t0 = time.perf_counter()
+    _lib.call("fgs_selftest_wait", flag.data_ptr(), torch.cuda.current_stream(cuda_device).cuda_stream)
+    errs = _C.device_errors(cuda_device)  # synchronises, reads and clears
+    assert errs & 1, errs
+    assert time.perf_counter() - t0 < 30.0
+    assert _C.device_errors(cuda_device) == 0
+    s = scenes.scene_c1(P=2000)
+    img, radii = render(s, raw_params(s, cuda_device), cuda_device)
+    assert torch.isfinite(img).all() and int((radii > 0).sum()) > 0
+    assert _C.device_errors(cuda_device) == 0
