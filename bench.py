@@ -421,6 +421,11 @@ def e2e_bench(args, dev, stream, host, dL_host, dev_in, dL, rast, world):
         ready[0] = upload(0, start)
         for t in range(steps):
             st = t % 2
+            # Step t+1's upload goes out first: the forward below blocks the host
+            # (one read of the pair count) until step t's inputs are in, and the
+            # other input set is free once step t-1, its previous user, is done.
+            if t + 1 < steps:
+                ready[(t + 1) % 2] = upload(t + 1, done[(t + 1) % 2])
             stream.wait_event(ready[st])
             leaves = {k: v.detach().requires_grad_(True) for k, v in dev_sets[st].items()}
             img, _ = rast(means3D=leaves["means"], opacities=leaves["opacities"], dc=leaves["dc"], shs=leaves["shs"],
@@ -428,8 +433,6 @@ def e2e_bench(args, dev, stream, host, dL_host, dev_in, dL, rast, world):
             torch.autograd.backward(img, grad_tensors=dL_sets[st])
             ev_done = torch.cuda.Event()
             ev_done.record(stream)
-            if t + 1 < steps:  # the other input set is free once step t-1 is done with it
-                ready[(t + 1) % 2] = upload(t + 1, done[(t + 1) % 2])
             done[st] = ev_done
             with torch.cuda.stream(copy_out):
                 copy_out.wait_event(ev_done)

@@ -69,11 +69,13 @@ def _bin(buffer, rs, means3D, dc, shs, colors_precomp, opacities, scales, rotati
         100.0, 0.01, buffer.gaussian_keys_unsorted, buffer.gaussian_values_unsorted, buffer.gaussian_values_sorted,
         buffer.curr_offset, rs.mult, buffer.splat_buffer, culling)
     # One host read per frame (FB's K read): the pair count and the
-    # large-footprint task count, copied together, one synchronisation.
+    # large-footprint task count, stored into pinned memory by a kernel (no
+    # copy-engine queueing behind the caller's own transfers), one synchronisation.
     counts = _host_counts(means3D.device)
-    counts[0].copy_(buffer.curr_offset[0], non_blocking=True)
-    counts[1].copy_(_C._counters(means3D.device)[0], non_blocking=True)
-    torch.cuda.current_stream(means3D.device).synchronize()
+    stream = torch.cuda.current_stream(means3D.device)
+    _lib.call("fgs_read_counts", buffer.curr_offset.data_ptr(), _C._counters(means3D.device).data_ptr(),
+              counts.data_ptr(), stream.cuda_stream)
+    stream.synchronize()
     num_rendered, num_tasks = int(counts[0]), int(counts[1])
     if num_rendered >= buffer.MAX_NUM_RENDERED or num_tasks > buffer.gaussian_values_sorted.numel() // 2:
         _C.device_errors(means3D.device)  # clears the capacity bit the skipped writes latched

@@ -48,6 +48,7 @@ SIGNATURES = {
     "fgs_version": (C.c_char_p, []),
     "fgs_device_errors": (i32, [C.POINTER(C.c_int), i32, vp]),
     "fgs_selftest_wait": (i32, [vp, vp]),
+    "fgs_read_counts": (i32, [vp, vp, vp, vp]),
     "fgs_preprocess": (i32, [i32, i32, i32, vp, vp, vp, vp, vp, vp, vp, f32, i32, i32, i32, i32, vp, vp, vp,
                              f32, f32, f32, f32, f32, vp, vp, i64, vp, vp, i64, vp, i64, vp, vp, vp, vp]),
     "fgs_sort_temp_bytes": (sz, [i64]),

@@ -212,6 +212,32 @@ extern "C" fgs_status fgs_adam_update(float* param, const float* grad, float* ex
   return FGS_OK;
 }
 
+namespace fgs {
+namespace {
+// Two device words into mapped host memory, stored by the GPU itself.
+__global__ void k_store_counts(const int32_t* a, const int32_t* b, int32_t* out) {
+  out[0] = a ? *a : 0;
+  out[1] = b ? *b : 0;
+}
+}  // namespace
+}  // namespace fgs
+
+extern "C" fgs_status fgs_read_counts(const int32_t* curr_offset, const int32_t* counters, int32_t* host_out,
+                                      void* stream) {
+  if (!host_out || (!curr_offset && !counters)) return FGS_ERR_BAD_ARG;
+  cudaStream_t s = (cudaStream_t)stream;
+  void* dptr = nullptr;
+  if (cudaHostGetDevicePointer(&dptr, host_out, 0) == cudaSuccess && dptr) {
+    fgs::k_store_counts<<<1, 1, 0, s>>>(curr_offset, counters, static_cast<int32_t*>(dptr));
+    FGS_LAUNCH_CHECK();
+    return FGS_OK;
+  }
+  (void)cudaGetLastError();  // not mapped host memory: copy instead
+  if (curr_offset) FGS_TRY(cudaMemcpyAsync(host_out, curr_offset, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+  if (counters) FGS_TRY(cudaMemcpyAsync(host_out + 1, counters, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+  return FGS_OK;
+}
+
 extern "C" fgs_status fgs_kernel_timer(int kernel_id, int enable) {
   if (kernel_id < 0 || kernel_id >= FGS_K_COUNT) return FGS_ERR_BAD_ARG;
   fgs::g_timers[kernel_id].enabled = enable != 0;

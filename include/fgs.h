@@ -53,6 +53,14 @@ const char* fgs_version(void);
  * Synchronises the stream.  *flags receives the word. */
 fgs_status fgs_device_errors(int* flags, int clear, void* stream);
 
+/* Writes [*curr_offset, counters[0]] (either may be NULL: 0) into host_out,
+ * two int32 of page-locked host memory, with a one-thread kernel that stores
+ * through the buffer's mapped device address: the read of a frame's pair and
+ * task counts then never queues behind large copies on the copy engines.
+ * Falls back to cudaMemcpyAsync when host_out is not mapped.  The caller
+ * synchronises the stream before reading host_out. */
+fgs_status fgs_read_counts(const int32_t* curr_offset, const int32_t* counters, int32_t* host_out, void* stream);
+
 /* Self-check of the bounded device waits: one warp runs the wait of the
  * compositing chain on `flag` (one device u32, zeroed here), which nothing
  * sets; the wait gives up after its bounded spin (about a second), raises the
