@@ -64,6 +64,7 @@ def parse():
     ap.add_argument("--no-checkpoint", action="store_true")
     ap.add_argument("--no-adam", action="store_true")
     ap.add_argument("--no-loss", action="store_true")
+    ap.add_argument("--no-aux", action="store_true")
     ap.add_argument("--cameras", type=int, default=16)
     ap.add_argument("--tune", choices=["sweep", "default"], default="sweep",
                     help="batched launch config: autotuner sweep (18 configs) or FB's fixed choice")
@@ -177,6 +178,36 @@ def cpu_baseline(steps: int, warmup: int, n_gauss: int):
 
 
 # --------------------------------------------------------------------------- GPU path
+def aux_bench(args, dev, rast, dev_in, K):
+    """FB's importance and depth passes (render_simp / render_depth, as Mini-Splatting 2 calls them)
+    on the C2 scene: the whole call (preprocess, sort, pass) and the pass kernel alone."""
+    import torch
+    from fastergs_gb300 import _lib
+    stream = torch.cuda.current_stream(dev)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    kw = dict(means3D=dev_in["means"], opacities=dev_in["opacities"], dc=dev_in["dc"], shs=dev_in["shs"],
+              scales=dev_in["scales"], rotations=dev_in["rotations"])
+    out = {"workload": f"c2 scene, {K} pairs"}
+    for name, fn, timer in (("render_simp", rast.render_simp, "render_simp"),
+                            ("render_depth", rast.render_depth, "render_depth")):
+        with torch.no_grad():
+            for _ in range(3):
+                fn(**kw)
+            torch.cuda.synchronize(dev)
+            _lib.kernel_timers(True, [timer])
+            _lib.read_kernel_timers([timer])
+            ev0.record(stream)
+            for _ in range(args.steps):
+                fn(**kw)
+            ev1.record(stream)
+            torch.cuda.synchronize(dev)
+            k_ms, k_n = _lib.read_kernel_timers([timer])[timer]
+            _lib.kernel_timers(False, [timer])
+        out[name] = {"call_ms": round(ev0.elapsed_time(ev1) / args.steps, 4),
+                     "kernel_ms": round(k_ms / max(k_n, 1), 4)}
+    return out
+
+
 def ply_bench(s):
     """Writing and reading the C2 scene as a 3DGS PLY file (host I/O, page cache)."""
     from fastergs_gb300 import ply
@@ -359,6 +390,9 @@ def gpu_bench(args, rank, local, world):
     e2e = None
     if not args.no_e2e:
         e2e = e2e_bench(args, dev, stream, host, dL_host, dev_in, dL, rast, world)
+    aux = None
+    if not args.no_aux and world == 1:
+        aux = aux_bench(args, dev, rast, dev_in, K)
     fused_adam = None
     if not args.no_adam and world == 1:
         fused_adam = adam_bench(args, dev, s, rast, dL)
@@ -384,7 +418,8 @@ def gpu_bench(args, rank, local, world):
         checkpoint = checkpoint_bench(args, dev)
     return dict(ms_step=ms_step_job, fwd_ms=fwd_ms, clocks=clocks, ktimes=ktimes, K=K,
                 launches_per_step=launches_per_step, e2e=e2e, P=s.P, W=cam.width, H=cam.height, batched=batched,
-                checkpoint=checkpoint, W_eval=W_eval, fp32_peak=fp32_peak, fused_adam=fused_adam, loss=loss)
+                checkpoint=checkpoint, W_eval=W_eval, fp32_peak=fp32_peak, fused_adam=fused_adam, loss=loss,
+                aux=aux)
 
 
 def e2e_bench(args, dev, stream, host, dL_host, dev_in, dL, rast, world):
@@ -833,7 +868,7 @@ def main():
         "e2e": res["e2e"], "gpu_launches": int(round(res["launches_per_step"] * args.steps)),
         "clocks": res["clocks"], "roofline": roof, "kernels": table, "cpu_baseline": cb,
         "batched": res["batched"], "checkpoint": res["checkpoint"], "fused_adam": res["fused_adam"],
-        "loss": res["loss"],
+        "loss": res["loss"], "aux": res["aux"],
     }
     print(json.dumps(line), flush=True)
     barrier(world)

@@ -281,8 +281,10 @@ extern "C" fgs_status fgs_render_simp(int P, int64_t num_rendered, int width, in
   }
   fgs_status st = run_tile_ranges(num_rendered, nullptr, (uint32_t)(gx * gy), keys_sorted, ranges, s);
   if (st != FGS_OK) return st;
+  KernelTimer kt__(FGS_K_SIMP, s);
   k_render_simp<<<gx * gy, kWarp, 0, s>>>(P, width, height, gx, splat_buffer, values_sorted, ranges, accum_weights,
                                           accum_count, accum_max_count);
+  kt__.stop();
   FGS_LAUNCH_CHECK();
   return FGS_OK;
 }
@@ -303,9 +305,11 @@ extern "C" fgs_status fgs_render_depth(int P, int64_t num_rendered, int width, i
   const int gx = (width + 15) / 16, gy = (height + 15) / 16;
   fgs_status st = run_tile_ranges(num_rendered, nullptr, (uint32_t)(gx * gy), keys_sorted, ranges, s);
   if (st != FGS_OK) return st;
+  KernelTimer kt__(FGS_K_DEPTH, s);
   k_render_depth<<<gx * gy, kDepthThreads, 0, s>>>(width, height, gx, splat_buffer, values_sorted, ranges, means3D,
                                                     scales, rotations, projmatrix, campos, out_pts, out_depth,
                                                     accum_alpha, gidx, discriminants);
+  kt__.stop();
   FGS_LAUNCH_CHECK();
   return FGS_OK;
 }

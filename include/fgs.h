@@ -422,7 +422,8 @@ fgs_status fgs_batch_offsets(int P, int num_views, const fgs_camera* cams, const
 enum {
   FGS_K_PREPROCESS = 0, FGS_K_PREPROCESS_LARGE = 1, FGS_K_SORT_HIST = 2, FGS_K_SORT_PASS = 3,
   FGS_K_TILE_RANGES = 4, FGS_K_BUCKET_SETUP = 5, FGS_K_RENDER_FWD = 6, FGS_K_EMPTY_TILES = 7,
-  FGS_K_RENDER_BWD = 8, FGS_K_PREPROCESS_BWD = 9, FGS_K_LOSS = 10, FGS_K_COUNT = 11
+  FGS_K_RENDER_BWD = 8, FGS_K_PREPROCESS_BWD = 9, FGS_K_LOSS = 10, FGS_K_SIMP = 11, FGS_K_DEPTH = 12,
+  FGS_K_COUNT = 13
 };
 fgs_status fgs_kernel_timer(int kernel_id, int enable);
 fgs_status fgs_kernel_timer_read(int kernel_id, double* total_ms, int* launches);
