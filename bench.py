@@ -65,6 +65,7 @@ def parse():
     ap.add_argument("--no-adam", action="store_true")
     ap.add_argument("--no-loss", action="store_true")
     ap.add_argument("--no-aux", action="store_true")
+    ap.add_argument("--no-c3", action="store_true")
     ap.add_argument("--cameras", type=int, default=16)
     ap.add_argument("--tune", choices=["sweep", "default"], default="sweep",
                     help="batched launch config: autotuner sweep (18 configs) or FB's fixed choice")
@@ -178,6 +179,64 @@ def cpu_baseline(steps: int, warmup: int, n_gauss: int):
 
 
 # --------------------------------------------------------------------------- GPU path
+def c3_bench(args, dev):
+    """C3: 3M Gaussians in 64 Zipf-weighted anisotropic clusters, 1920x1080, SH degree 3, forward
+    only through the drop-in rasterizer: render ms, FPS and the per-kernel device time."""
+    import torch
+    import fastergs_gb300 as fgs
+    from fastergs_gb300 import _lib, cameras, scenes
+    s = scenes.scene_c3(seed=0)
+    m, sc, rot, op, dc, shs = s.activated()
+    d = {k: torch.from_numpy(np.ascontiguousarray(v)).to(dev)
+         for k, v in dict(means=m, scales=sc, rotations=rot, opacities=op, dc=dc, shs=shs).items()}
+    rast = fgs.GaussianRasterizer(cameras.raster_settings(s.camera, sh_degree=s.sh_degree, device=dev))
+    slot = fgs._RasterizeGaussians.__dict__["buffer"]
+    old = slot._buf
+    cap = 1 << 23
+    kw = dict(means3D=d["means"], opacities=d["opacities"], dc=d["dc"], shs=d["shs"], scales=d["scales"],
+              rotations=d["rotations"])
+    try:
+        while True:
+            slot._buf = None
+            torch.cuda.empty_cache()
+            slot._buf = fgs.Buffer(device=dev, MAX_NUM_RENDERED=cap)
+            try:
+                with torch.no_grad():
+                    rast(**kw)
+                break
+            except RuntimeError as e:
+                if "Too many k-v pairs" not in str(e):
+                    raise
+                cap *= 2
+        K = int(slot._buf.curr_offset.item())
+        stream = torch.cuda.current_stream(dev)
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with torch.no_grad():
+            for _ in range(max(args.warmup, 3)):
+                rast(**kw)
+            torch.cuda.synchronize(dev)
+            ev0.record(stream)
+            for _ in range(args.steps):
+                rast(**kw)
+            ev1.record(stream)
+            torch.cuda.synchronize(dev)
+            ms = ev0.elapsed_time(ev1) / args.steps
+            _lib.kernel_timers(True)
+            _lib.read_kernel_timers()
+            for _ in range(args.steps):
+                rast(**kw)
+            torch.cuda.synchronize(dev)
+            kt = _lib.read_kernel_timers()
+            _lib.kernel_timers(False)
+    finally:
+        slot._buf = old
+        del d
+        torch.cuda.empty_cache()
+    return {"workload": "c3: 3M Gaussians, 64 Zipf(1.2) clusters, 1920x1080, SH degree 3, forward only",
+            "gaussians": int(s.P), "pairs": K, "render_ms": round(ms, 4), "render_fps": round(1000.0 / ms, 1),
+            "kernels_ms_per_frame": {k: round(v[0] / args.steps, 4) for k, v in kt.items() if v[1]}}
+
+
 def aux_bench(args, dev, rast, dev_in, K):
     """FB's importance and depth passes (render_simp / render_depth, as Mini-Splatting 2 calls them)
     on the C2 scene: the whole call (preprocess, sort, pass) and the pass kernel alone."""
@@ -347,6 +406,7 @@ def gpu_bench(args, rank, local, world):
     K = int(slot._buf.curr_offset.item())
     W_eval = needed_evaluations(s, settings, dev_in, slot._buf, dev)
     fp32_peak = ctypes_peak_fp32(dev)
+    ex2_peak = ctypes_peak_ex2(dev)
 
     # timed region: device-resident inputs
     barrier(world)
@@ -410,6 +470,9 @@ def gpu_bench(args, rank, local, world):
                                    target=(0.0, 0.0, 7.0)) for c in c4]
         batched.append(batched_bench(args, dev, s, dev_in, same, f"{args.cameras} cameras at 1297x840 on the same "
                                      "circle"))
+    c3 = None
+    if not args.no_c3 and world == 1:
+        c3 = c3_bench(args, dev)
     checkpoint = None
     if not args.no_checkpoint and world == 1:
         del dev_in
@@ -418,8 +481,9 @@ def gpu_bench(args, rank, local, world):
         checkpoint = checkpoint_bench(args, dev)
     return dict(ms_step=ms_step_job, fwd_ms=fwd_ms, clocks=clocks, ktimes=ktimes, K=K,
                 launches_per_step=launches_per_step, e2e=e2e, P=s.P, W=cam.width, H=cam.height, batched=batched,
-                checkpoint=checkpoint, W_eval=W_eval, fp32_peak=fp32_peak, fused_adam=fused_adam, loss=loss,
-                aux=aux)
+                checkpoint=checkpoint, W_eval=W_eval, fp32_peak=fp32_peak, ex2_peak=ex2_peak, fused_adam=fused_adam,
+                loss=loss,
+                aux=aux, c3=c3)
 
 
 def e2e_bench(args, dev, stream, host, dL_host, dev_in, dL, rast, world):
@@ -748,6 +812,16 @@ def needed_evaluations(scene, settings, dev_in, buf, dev):
     return int(lc.to(torch.int64).sum().item())
 
 
+def ctypes_peak_ex2(dev):
+    """MUFU ex2 Gop/s of this GPU (fgs_peak_ex2)."""
+    import ctypes
+    import torch
+    from fastergs_gb300 import _lib
+    out = ctypes.c_double(0.0)
+    _lib.call("fgs_peak_ex2", ctypes.byref(out), torch.cuda.current_stream(dev).cuda_stream)
+    return float(out.value)
+
+
 def ctypes_peak_fp32(dev):
     """Measured FP32 FMA throughput (TFLOP/s) of this GPU, via the library's microbenchmark."""
     import ctypes
@@ -763,6 +837,9 @@ def ctypes_peak_fp32(dev):
 # exp2 + clamp + cut (3), blend (9); backward = alpha recomputation (8),
 # dL/dalpha and the un-blend (15), mean / conic / colour / opacity terms (27).
 FLOP_PER_EVAL = {"render_fwd": 17, "render_bwd": 50}
+# MUFU operations per evaluation: the alpha's ex2 (forward); ex2 and the
+# 1 / (1 - alpha) reciprocal (backward).  Against fgs_peak_ex2.
+MUFU_PER_EVAL = {"render_fwd": 1, "render_bwd": 2}
 
 # DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) of the
 # C2 workload, from the ncu captures summarised in profiles/ncu_c2_kernels.md.
@@ -805,7 +882,9 @@ def roofline(res, peaks):
                 "peak_source": "of measured (fgs_peak_fp32 FFMA microbenchmark, this run)",
                 "ms_per_launch": round(per_launch_ms, 4), "evaluations": int(W),
                 "flop_per_evaluation": FLOP_PER_EVAL[dom],
-                "hbm_frac": round(algo[dom] / (per_launch_ms * 1e-3) / 1e9 / hbm, 4)}
+                "hbm_frac": round(algo[dom] / (per_launch_ms * 1e-3) / 1e9 / hbm, 4),
+                "ex2_peak_gops": round(res["ex2_peak"], 1),
+                "mufu_frac": round(W * MUFU_PER_EVAL[dom] / (per_launch_ms * 1e-3) / 1e9 / res["ex2_peak"], 4)}
     else:
         b = algo.get(dom, 0)
         achieved = b / (per_launch_ms * 1e-3) / 1e9 if per_launch_ms > 0 else 0.0
@@ -821,6 +900,7 @@ def roofline(res, peaks):
                 entry["hbm_frac"] = round(algo[k] / (pl * 1e-3) / 1e9 / hbm, 4)
             if k in FLOP_PER_EVAL and pl > 0:
                 entry["fp32_frac"] = round(W * FLOP_PER_EVAL[k] / (pl * 1e-3) / 1e12 / fp32, 4)
+                entry["mufu_frac"] = round(W * MUFU_PER_EVAL[k] / (pl * 1e-3) / 1e9 / res["ex2_peak"], 4)
             table[k] = entry
     return roof, table
 
@@ -868,7 +948,7 @@ def main():
         "e2e": res["e2e"], "gpu_launches": int(round(res["launches_per_step"] * args.steps)),
         "clocks": res["clocks"], "roofline": roof, "kernels": table, "cpu_baseline": cb,
         "batched": res["batched"], "checkpoint": res["checkpoint"], "fused_adam": res["fused_adam"],
-        "loss": res["loss"], "aux": res["aux"],
+        "loss": res["loss"], "aux": res["aux"], "c3": res["c3"],
     }
     print(json.dumps(line), flush=True)
     barrier(world)

@@ -79,9 +79,13 @@ SIGNATURES = {
                                      vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp]),
     "fgs_render_batched_bwd_adam": (i32, [i32, i32, i32, vp, vp, vp, vp, vp, i32, camp, tunep, i64, vp, sz, vp,
                                           vp, adamp, vp, vp, vp, vp, vp]),
+    "fgs_tune_grad_bytes": (sz, [i32, i32]),
+    "fgs_tune": (i32, [i32, i32, i32, vp, vp, vp, vp, vp, vp, vp, vp, i32, camp, tunep, i32, i64, vp, sz, vp, vp, vp,
+                       vp, sz, i32, C.POINTER(C.c_int), C.POINTER(C.c_float), vp]),
     "fgs_batch_status": (i32, [i32, i32, camp, tunep, i64, vp, C.POINTER(C.c_int64), C.POINTER(C.c_int64), vp]),
     "fgs_batch_offsets": (i32, [i32, i32, camp, tunep, i64, C.POINTER(C.c_int64), i32]),
     "fgs_peak_fp32": (i32, [C.POINTER(C.c_double), vp]),
+    "fgs_peak_ex2": (i32, [C.POINTER(C.c_double), vp]),
     "fgs_kernel_timer": (i32, [i32, i32]),
     "fgs_kernel_timer_read": (i32, [i32, C.POINTER(C.c_double), C.POINTER(C.c_int)]),
 }

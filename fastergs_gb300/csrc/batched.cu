@@ -298,3 +298,97 @@ extern "C" fgs_status fgs_batch_offsets(int P, int num_views, const fgs_camera* 
   for (int i = 0; i < 10; ++i) offsets[i] = v[i];
   return FGS_OK;
 }
+
+// ---------------------------------------------------------------------------
+// Autotuner (C entry of fastergs_gb300.tune.autotune).
+namespace {
+constexpr size_t kTuneAlign = 256;
+size_t tune_up(size_t v) { return (v + kTuneAlign - 1) & ~(kTuneAlign - 1); }
+// Float counts of the gradient arrays carved from the tuner's arena, in order:
+// dmean3D, ddc, dsh, dopacity, dscale, drot, dcolor, dcov3D.
+void tune_grad_sizes(int64_t P, int M, size_t (&n)[8]) {
+  n[0] = 3 * P; n[1] = 3 * P; n[2] = 3 * (size_t)M * P; n[3] = P;
+  n[4] = 3 * P; n[5] = 4 * P; n[6] = 3 * P; n[7] = 6 * P;
+}
+}  // namespace
+
+extern "C" size_t fgs_tune_grad_bytes(int P, int M) {
+  if (P < 0 || M < 0) return 0;
+  size_t n[8];
+  tune_grad_sizes(P, M, n);
+  size_t total = 0;
+  for (size_t v : n) total += tune_up(sizeof(float) * v);
+  return total;
+}
+
+extern "C" fgs_status fgs_tune(int P, int D, int M, const float* means3D, const float* colors_precomp,
+                               const float* dc, const float* shs, const float* opacities, const float* scales,
+                               const float* rotations, const uint8_t* culling, int num_views, const fgs_camera* cams,
+                               const fgs_tune_config* candidates, int n_candidates, int64_t pair_capacity,
+                               void* workspace, size_t workspace_bytes, float* out_color, int32_t* radii,
+                               const float* dL_dpixels, void* grad_arena, size_t grad_arena_bytes, int reps,
+                               int* best, float* ms, void* stream) {
+  if (!candidates || n_candidates < 1 || !best || !ms || reps < 1 || !workspace) return FGS_ERR_BAD_ARG;
+  if (dL_dpixels && (!grad_arena || grad_arena_bytes < fgs_tune_grad_bytes(P, M) ||
+                     ((uintptr_t)grad_arena & (kTuneAlign - 1))))
+    return FGS_ERR_BAD_ARG;
+  cudaStream_t s = (cudaStream_t)stream;
+  float* g[8] = {nullptr};
+  if (dL_dpixels) {
+    size_t n[8];
+    tune_grad_sizes(P, M, n);
+    char* p = static_cast<char*>(grad_arena);
+    for (int k = 0; k < 8; ++k) {
+      g[k] = reinterpret_cast<float*>(p);
+      p += tune_up(sizeof(float) * n[k]);
+    }
+  }
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  FGS_TRY(cudaEventCreate(&e0));
+  if (cudaEventCreate(&e1) != cudaSuccess) {
+    cudaEventDestroy(e0);
+    return FGS_ERR_CUDA;
+  }
+  auto step = [&](const fgs_tune_config* cfg) -> fgs_status {
+    fgs_status st = fgs_render_batched_fwd(P, D, M, means3D, colors_precomp, dc, shs, opacities, scales, rotations,
+                                           culling, num_views, cams, cfg, pair_capacity, workspace, workspace_bytes,
+                                           out_color, radii, stream);
+    if (st != FGS_OK || !dL_dpixels) return st;
+    return fgs_render_batched_bwd(P, D, M, means3D, dc, shs, scales, rotations, num_views, cams, cfg, pair_capacity,
+                                  workspace, workspace_bytes, radii, dL_dpixels, g[0], g[1], g[2],
+                                  g[3], g[4], g[5], g[6], g[7], nullptr, nullptr, nullptr, nullptr, stream);
+  };
+  int chosen = -1;
+  fgs_status result = FGS_OK;
+  for (int i = 0; i < n_candidates; ++i) {
+    ms[i] = -1.f;  // does not fit the workspace, is not a valid config, or failed
+    size_t need = 0;
+    if (fgs_batch_workspace_bytes(P, num_views, cams, candidates + i, pair_capacity, &need) != FGS_OK ||
+        need > workspace_bytes)
+      continue;
+    if (step(candidates + i) != FGS_OK) continue;  // warm-up
+    int64_t pairs = 0, buckets = 0;
+    const fgs_status st = fgs_batch_status(P, num_views, cams, candidates + i, pair_capacity, workspace, &pairs,
+                                           &buckets, stream);
+    if (st == FGS_ERR_CAPACITY) {
+      ms[i] = -2.f;  // the frame outgrew pair_capacity
+      continue;
+    }
+    if (st != FGS_OK) continue;
+    bool ok = cudaEventRecord(e0, s) == cudaSuccess;
+    for (int r = 0; ok && r < reps; ++r) ok = step(candidates + i) == FGS_OK;
+    ok = ok && cudaEventRecord(e1, s) == cudaSuccess && cudaEventSynchronize(e1) == cudaSuccess;
+    float t = 0.f;
+    if (!ok || cudaEventElapsedTime(&t, e0, e1) != cudaSuccess) {
+      result = FGS_ERR_CUDA;
+      break;
+    }
+    ms[i] = t / (float)reps;
+    if (chosen < 0 || ms[i] < ms[chosen]) chosen = i;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  *best = chosen;
+  if (result != FGS_OK) return result;
+  return chosen < 0 ? FGS_ERR_CAPACITY : FGS_OK;
+}

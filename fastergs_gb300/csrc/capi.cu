@@ -125,9 +125,58 @@ __global__ void __launch_bounds__(256) k_ffma_peak(float a, float b) {
   if (s == 12345.678f) g_peak_sink = s;  // never true; keeps the chains live
 }
 
+// MUFU ex2 issue ceiling (the alpha of every pixel-Gaussian evaluation is one
+// ex2.approx): 8 independent chains x = ex2(x) * -0.5 per thread, values
+// bounded in (-0.5, 0]; the multiply runs on the FMA pipe, beside the MUFU.
+__global__ void __launch_bounds__(256) k_ex2_peak(float a) {
+  float x[kPeakChains];
+#pragma unroll
+  for (int j = 0; j < kPeakChains; ++j) x[j] = -a * (float)(1 + ((threadIdx.x + j) & 7));
+#pragma unroll 4
+  for (int i = 0; i < kPeakIters; ++i)
+#pragma unroll
+    for (int j = 0; j < kPeakChains; ++j) x[j] = ex2_approx(x[j]) * -0.5f;
+  float s = 0.f;
+#pragma unroll
+  for (int j = 0; j < kPeakChains; ++j) s += x[j];
+  if (s == 12345.678f) g_peak_sink = s;
+}
+
+template <typename Launch>
+cudaError_t best_ms(Launch launch, cudaStream_t s, float* out) {
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  cudaError_t err = cudaEventCreate(&e0);
+  if (err == cudaSuccess) err = cudaEventCreate(&e1);
+  float best = 1e30f;
+  for (int rep = 0; err == cudaSuccess && rep < 4; ++rep) {  // first launch warms up
+    cudaEventRecord(e0, s);
+    launch();
+    cudaEventRecord(e1, s);
+    err = cudaEventSynchronize(e1);
+    float ms = 0.f;
+    if (err == cudaSuccess) err = cudaEventElapsedTime(&ms, e0, e1);
+    if (rep > 0) best = ms < best ? ms : best;
+  }
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  *out = best;
+  return err == cudaSuccess ? cudaGetLastError() : err;
+}
+
 }  // namespace
 
 }  // namespace fgs
+
+extern "C" fgs_status fgs_peak_ex2(double* gops, void* stream) {
+  if (!gops) return FGS_ERR_BAD_ARG;
+  cudaStream_t s = (cudaStream_t)stream;
+  const int blocks = fgs::num_sms() * 8;
+  float best = 0.f;
+  FGS_TRY(fgs::best_ms([&] { fgs::k_ex2_peak<<<blocks, 256, 0, s>>>(0.25f); }, s, &best));
+  const double ops = (double)blocks * 256.0 * fgs::kPeakIters * fgs::kPeakChains;
+  *gops = ops / (best * 1e-3) / 1e9;
+  return FGS_OK;
+}
 
 extern "C" fgs_status fgs_peak_fp32(double* tflops, void* stream) {
   if (!tflops) return FGS_ERR_BAD_ARG;

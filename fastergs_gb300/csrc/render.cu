@@ -351,7 +351,17 @@ __global__ void __launch_bounds__(kFwdWarps * kWarp, 7) k_render_fwd(const FwdAr
     // and in bucket order): C += T_prefix * C_b, T_prefix *= T_b; a pixel
     // stops after the bucket that takes T below 1e-4, or at the tile's last
     // bucket, and then writes its outputs.
-    if (bi.local > 0) wait_stage(stage_word, (uint32_t)bi.local, lane);
+    if (bi.local > 0) {
+      wait_stage(stage_word, (uint32_t)bi.local, lane);
+      // Every pixel of the tile has stopped: nothing to fold, write or publish
+      // (kStageDead already satisfies the waits of every later bucket).
+      uint32_t sw = lane == 0 ? ld_acquire_u32(stage_word) : 0u;
+      sw = __shfl_sync(0xffffffffu, sw, 0);
+      if (sw == kStageDead) {
+        q = q_next;
+        continue;
+      }
+    }
     const int nb_tile = (int)a.bucket_off[bi.tile] - (bi.tile ? (int)a.bucket_off[bi.tile - 1] : 0);
     const bool last_bucket = bi.local == nb_tile - 1;
     const int ntile = (int)(a.ranges[2 * bi.tile + 1] - a.ranges[2 * bi.tile]);
@@ -404,7 +414,9 @@ __global__ void __launch_bounds__(kFwdWarps * kWarp, 7) k_render_fwd(const FwdAr
       }
     if (lane < kPxPerThread) st_volatile_u32(alive_words + lane, my_word);
     if (lane == 0 && any_before && !any_after) a.max_contrib[bi.tile] = (uint32_t)contrib;
-    publish_stage(stage_word, (uint32_t)bi.local + 1u, lane);
+    // The bucket that stops the tile's last pixel ends the chain: its later
+    // buckets skip their waits instead of handing an empty prefix along.
+    publish_stage(stage_word, any_after ? (uint32_t)bi.local + 1u : kStageDead, lane);
     q = q_next;
   }
 }

@@ -230,6 +230,10 @@ __device__ __forceinline__ void composite_bucket(const BucketStage& st, int n, u
   }
 }
 
+// tile_stage value of a tile whose pixels have all stopped: it satisfies every
+// wait, and the buckets that read it do nothing.
+constexpr uint32_t kStageDead = 0xffffffffu;
+
 // Waits until a tile's first `stage` buckets are folded into its prefix.
 // Lane 0 polls (bounded); the bucket it waits for was handed out earlier and
 // its warp is running, so the wait ends unless something is broken, in which

@@ -126,3 +126,49 @@ def autotune(settings, params: dict, sh_degree: int = 3, candidates: Iterable[Tu
         disk[key] = dict(config=best["config"], ms=best["ms"], seconds=time.time() - t0)
         _store(path, disk)
     return cfg, table
+
+
+def autotune_native(settings, params: dict, sh_degree: int = 3, candidates: Iterable[TuneConfig] | None = None,
+                    backward: bool = True, reps: int = 5, headroom: float = 1.15) -> tuple[TuneConfig, list[dict]]:
+    """The same search through the library's own tuner (fgs_tune): plain launches timed with CUDA
+    events instead of graph replays, for callers that drive the C ABI without Python.  Returns
+    (best config, table of {config, ms}); ms is -1 for a config whose workspace did not fit and -2
+    for one whose frame outgrew the planned pair capacity."""
+    import ctypes as C
+
+    from . import _lib
+    from ._C import _f32, _ptr, _stream
+
+    cands = list(candidates) if candidates is not None else search_space()
+    P = params["means3D"].shape[0]
+    probe = BatchedRasterizer(settings, P, tune=TuneConfig())
+    pairs = probe.fit(params["means3D"], params["opacities"], params.get("dc"), params.get("shs"),
+                      params.get("colors_precomp"), params["scales"], params["rotations"], params.get("culling"),
+                      sh_degree, headroom=headroom)
+    dev = probe.device
+    cap = int(pairs * headroom) + (1 << 16)
+    need = 0
+    for cfg in cands:
+        out = C.c_size_t(0)
+        if _lib.load().fgs_batch_workspace_bytes(P, probe.V, probe._cams, C.byref(cfg.as_c()), cap, C.byref(out)) == 0:
+            need = max(need, int(out.value))
+    probe.workspace = None
+    workspace = torch.empty(max(need, 256), dtype=torch.uint8, device=dev)
+    dev_ = lambda k: _f32(k, params.get(k), dev)
+    shs = dev_("shs")
+    M = shs.size(1) if shs.numel() else 0
+    dL = torch.ones(probe.out_color.numel(), device=dev) if backward else None
+    gbytes = int(_lib.load().fgs_tune_grad_bytes(P, M))
+    arena = torch.empty(max(gbytes, 256), dtype=torch.uint8, device=dev) if backward else None
+    arr = (_lib.TuneConfig * len(cands))(*[c.as_c() for c in cands])
+    ms = (C.c_float * len(cands))()
+    best = C.c_int(-1)
+    cull = params.get("culling")
+    cull_t = cull.to(device=dev, dtype=torch.uint8).contiguous() if cull is not None and cull.numel() else None
+    _lib.call("fgs_tune", P, int(sh_degree), int(M), _ptr(dev_("means3D")), _ptr(dev_("colors_precomp")),
+              _ptr(dev_("dc")), _ptr(shs), _ptr(dev_("opacities")), _ptr(dev_("scales")), _ptr(dev_("rotations")),
+              _ptr(cull_t), probe.V, probe._cams, arr, len(cands), cap, workspace.data_ptr(), workspace.numel(),
+              probe.out_color.data_ptr(), probe.radii.data_ptr(), _ptr(dL), _ptr(arena), gbytes, int(reps),
+              C.byref(best), ms, _stream(dev))
+    table = [dict(config=dataclasses.asdict(c), ms=float(ms[i])) for i, c in enumerate(cands)]
+    return cands[best.value], table

@@ -395,6 +395,27 @@ fgs_status fgs_render_batched_bwd_adam(int P, int D, int M, const float* means3D
                                        float* xyz_gradient_accum, float* xyz_gradient_accum_abs,
                                        float* max_radii, float* denom, void* stream);
 
+/*
+ * Autotuner over launch configurations (the C entry of
+ * fastergs_gb300.tune.autotune; FB fixes bucket 128, 16x16 tiles and the
+ * 128-tile sub-task size at compile time).  For every candidate: skipped
+ * (ms = -1) unless its fgs_batch_workspace_bytes fits workspace_bytes; one
+ * warm-up frame, skipped (ms = -2) if it overflows pair_capacity; then `reps`
+ * frames timed with CUDA events on the stream, ms = mean per frame.  A frame
+ * is the batched forward, plus the backward when dL_dpixels is given (its
+ * gradients go to grad_arena, fgs_tune_grad_bytes(P, M) bytes, 256-byte
+ * aligned; densification statistics are not touched).  *best receives the
+ * index of the fastest candidate; FGS_ERR_CAPACITY when none ran.
+ * Synchronises the stream.
+ */
+size_t fgs_tune_grad_bytes(int P, int M);
+fgs_status fgs_tune(int P, int D, int M, const float* means3D, const float* colors_precomp, const float* dc,
+                    const float* shs, const float* opacities, const float* scales, const float* rotations,
+                    const uint8_t* culling, int num_views, const fgs_camera* cams, const fgs_tune_config* candidates,
+                    int n_candidates, int64_t pair_capacity, void* workspace, size_t workspace_bytes,
+                    float* out_color, int32_t* radii, const float* dL_dpixels, void* grad_arena,
+                    size_t grad_arena_bytes, int reps, int* best, float* ms, void* stream);
+
 /* Reads the pair and bucket counts of the last batched forward on this
  * workspace (synchronises the stream).  Returns FGS_ERR_CAPACITY when the
  * frame overflowed pair_capacity (or its bucket bound); the counts are then
@@ -432,6 +453,10 @@ fgs_status fgs_kernel_timer_read(int kernel_id, double* total_ms, int* launches)
  * thread on every SM; synchronises the stream): the ceiling for the
  * compositing kernels, which are bound by FP32 issue, not by HBM. */
 fgs_status fgs_peak_fp32(double* tflops, void* stream);
+/* MUFU ex2.approx throughput in Gop/s (8 independent chains per thread on
+ * every SM; synchronises the stream): one ex2 per pixel-Gaussian evaluation
+ * in both compositing kernels. */
+fgs_status fgs_peak_ex2(double* gops, void* stream);
 
 #ifdef __cplusplus
 }

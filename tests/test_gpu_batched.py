@@ -468,3 +468,37 @@ def test_batched_zero_gaussians_gives_background(cuda_device):
         assert torch.equal(im, bg.expand_as(im)), k
     assert rast.status() == (0, 0)
     assert g["means3D"].numel() == 0
+
+
+def test_native_autotuner_times_candidates_and_picks_the_fastest(setup):
+    """fgs_tune (through tune.autotune_native): every candidate that fits is timed, the fastest
+    is returned; a pair capacity too small for the frame marks every candidate -2 and reports
+    FGS_ERR_CAPACITY without touching memory past the buffers."""
+    import ctypes as C
+    from fastergs_gb300 import _lib
+    from fastergs_gb300.tune import autotune_native
+    s, T, cams, sets = setup
+    params = {"means3D": T["means"], "opacities": T["opacities"], "dc": T["dc"], "shs": T["shs"],
+              "scales": T["scales"], "rotations": T["rotations"]}
+    cands = [TuneConfig(), TuneConfig(32, 16, 16, 4), TuneConfig(64, 8, 32, 2), TuneConfig(16, 16, 16, 8, True)]
+    for backward in (False, True):
+        best, table = autotune_native(sets, params, sh_degree=3, candidates=cands, backward=backward, reps=2)
+        ms = [r["ms"] for r in table]
+        assert all(m > 0 for m in ms), ms
+        assert best == cands[int(np.argmin(ms))]
+    assert _C.device_errors(T["means"].device) == 0
+    # capacity far below the frame's pairs: every candidate overflows
+    rast = BatchedRasterizer(sets, T["means"].shape[0], pair_capacity=1 << 10)
+    arr = (_lib.TuneConfig * 2)(cands[0].as_c(), cands[1].as_c())
+    ms = (C.c_float * 2)()
+    best = C.c_int(5)
+    st = _lib.load().fgs_tune(T["means"].shape[0], 3, T["shs"].shape[1], T["means"].data_ptr(), None,
+                              T["dc"].data_ptr(), T["shs"].data_ptr(), T["opacities"].data_ptr(),
+                              T["scales"].data_ptr(), T["rotations"].data_ptr(), None, rast.V, rast._cams, arr, 2,
+                              rast.pair_capacity, rast.workspace.data_ptr(), rast.workspace.numel(),
+                              rast.out_color.data_ptr(), rast.radii.data_ptr(), None, None, 0, 1, C.byref(best),
+                              ms, torch.cuda.current_stream().cuda_stream)
+    assert st == 2 and best.value == -1
+    assert ms[0] == -2.0 or ms[0] == -1.0
+    _C.device_errors(T["means"].device)  # clears the capacity bit the skipped writes latched
+    assert _C.device_errors(T["means"].device) == 0
