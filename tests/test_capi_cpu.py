@@ -176,3 +176,37 @@ def test_fused_adam_row_index_in_fp32_is_exact():
         for off in (0, 3):
             got = ((j.astype(np.float32) + np.float32(off + 0.5)) * inv).astype(np.int64)
             assert np.array_equal(got, (j + off) // row), row
+
+
+def _declarations():
+    """{name: (return type, [parameter declarations])} of every function include/fgs.h declares."""
+    text = re.sub(r"/\*.*?\*/", "", HEADER.read_text(), flags=re.S)
+    text = re.sub(r"#[^\n]*", "", text)
+    out = {}
+    for m in re.finditer(r"([A-Za-z_][\w\s\*]*?)\b(fgs_[a-z0-9_]+)\s*\(([^;{]*?)\)\s*;", text):
+        params = [p.strip() for p in m.group(3).split(",") if p.strip() and p.strip() != "void"]
+        out[m.group(2)] = (" ".join(m.group(1).split()), params)
+    return out
+
+
+def test_ctypes_signatures_match_the_header_arity():
+    decls = _declarations()
+    assert set(decls) == set(_lib.SIGNATURES), set(decls) ^ set(_lib.SIGNATURES)
+    for name, (ret, params) in decls.items():
+        restype, argtypes = _lib.SIGNATURES[name]
+        assert len(argtypes) == len(params), (name, len(argtypes), len(params))
+        for p, a in zip(params, argtypes):
+            ptr = "*" in p
+            if ptr:
+                assert a in (C.c_void_p, C.c_char_p) or hasattr(a, "_type_") and not isinstance(a._type_, str), \
+                    (name, p, a)
+            else:
+                assert a not in (C.c_void_p,) or "void*" in p.replace(" ", ""), (name, p, a)
+        if ret.endswith("*"):
+            assert restype in (C.c_char_p, C.c_void_p), (name, ret)
+        elif "size_t" in ret:
+            assert restype == C.c_size_t, (name, ret)
+        elif "int64_t" in ret:
+            assert restype == C.c_int64, (name, ret)
+        else:
+            assert restype == C.c_int, (name, ret)
