@@ -41,37 +41,47 @@ struct BwdArgs {
   int bs;
 };
 
-// Sum 16 per-lane values over the warp.  On return lane l holds the total of
-// value (l >> 1) & 15 (lanes 2j and 2j+1 both hold value j).
-__device__ __forceinline__ float warp_transpose_reduce16(float (&v)[16], int lane) {
-#pragma unroll
-  for (int j = 0; j < 8; ++j) {
+// Sum 12 per-lane values over the warp by recursive halving with a
+// transpose (exchanges of 6, 3, 2, 1 and 1 values).  On return lane l holds
+// the total of value (d + 2c) + 3b + 6a, with a, b, c, d bits 4, 3, 2, 1 of
+// l; lanes with c = d = 1 hold a zero pad (warp_value_of).
+__device__ __forceinline__ float warp_transpose_reduce12(float (&v)[12], int lane) {
+  {
     const bool hi = lane & 16;
-    const float send = hi ? v[j] : v[j + 8];
-    const float keep = hi ? v[j + 8] : v[j];
-    v[j] = keep + __shfl_xor_sync(0xffffffffu, send, 16);
-  }
 #pragma unroll
-  for (int j = 0; j < 4; ++j) {
-    const bool hi = lane & 8;
-    const float send = hi ? v[j] : v[j + 4];
-    const float keep = hi ? v[j + 4] : v[j];
-    v[j] = keep + __shfl_xor_sync(0xffffffffu, send, 8);
-  }
-#pragma unroll
-  for (int j = 0; j < 2; ++j) {
-    const bool hi = lane & 4;
-    const float send = hi ? v[j] : v[j + 2];
-    const float keep = hi ? v[j + 2] : v[j];
-    v[j] = keep + __shfl_xor_sync(0xffffffffu, send, 4);
+    for (int j = 0; j < 6; ++j) {
+      const float send = hi ? v[j] : v[j + 6];
+      const float keep = hi ? v[j + 6] : v[j];
+      v[j] = keep + __shfl_xor_sync(0xffffffffu, send, 16);
+    }
   }
   {
-    const bool hi = lane & 2;
-    const float send = hi ? v[0] : v[1];
-    const float keep = hi ? v[1] : v[0];
-    v[0] = keep + __shfl_xor_sync(0xffffffffu, send, 2);
+    const bool hi = lane & 8;
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      const float send = hi ? v[j] : v[j + 3];
+      const float keep = hi ? v[j + 3] : v[j];
+      v[j] = keep + __shfl_xor_sync(0xffffffffu, send, 8);
+    }
   }
-  return v[0] + __shfl_xor_sync(0xffffffffu, v[0], 1);
+  {
+    const bool hi = lane & 4;
+    const float s0 = hi ? v[0] : v[2], k0 = hi ? v[2] : v[0];
+    const float s1 = hi ? v[1] : 0.f, k1 = hi ? 0.f : v[1];  // slot 3 is the pad
+    v[0] = k0 + __shfl_xor_sync(0xffffffffu, s0, 4);
+    v[1] = k1 + __shfl_xor_sync(0xffffffffu, s1, 4);
+  }
+  const bool hi = lane & 2;
+  const float send = hi ? v[0] : v[1];
+  const float keep = hi ? v[1] : v[0];
+  const float r = keep + __shfl_xor_sync(0xffffffffu, send, 2);
+  return r + __shfl_xor_sync(0xffffffffu, r, 1);
+}
+
+// The value warp_transpose_reduce12 leaves in `lane`, or -1 for a pad lane.
+__device__ __forceinline__ int warp_value_of(int lane) {
+  const int a = (lane >> 4) & 1, b = (lane >> 3) & 1, c = (lane >> 2) & 1, d = (lane >> 1) & 1;
+  return (c && d) ? -1 : (d + 2 * c) + 3 * b + 6 * a;
 }
 
 template <int BX, bool RECOMPUTE>
@@ -85,7 +95,7 @@ __global__ void __launch_bounds__(kBwdWarps * kWarp, 5) k_render_bwd(const BwdAr
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   BucketStage& st = s_stage[warp];
   const int B = (int)a.bucket_sum[0];
-  const int vid = (lane >> 1) & 15;  // value a lane holds after the transpose reduction
+  const int vid = warp_value_of(lane);  // value a lane holds after the transpose reduction
 
   // Buckets in the forward's queue order (round by round), so that in
   // recompute mode a tile's bucket k is always handed out after bucket k-1.
@@ -295,7 +305,7 @@ __global__ void __launch_bounds__(kBwdWarps * kWarp, 5) k_render_bwd(const BwdAr
         V11 = f2_add(V11, dp2);
       }
       if (__any_sync(0xffffffffu, any)) {
-        float v[16], a0, a1;
+        float v[12], a0, a1;
         f2_unpack(V0, a0, a1); v[0] = a0 + a1;
         f2_unpack(V1, a0, a1); v[1] = a0 + a1;
         v[2] = v2;
@@ -308,9 +318,8 @@ __global__ void __launch_bounds__(kBwdWarps * kWarp, 5) k_render_bwd(const BwdAr
         f2_unpack(V9, a0, a1); v[9] = a0 + a1;
         f2_unpack(V10, a0, a1); v[10] = a0 + a1;
         f2_unpack(V11, a0, a1); v[11] = a0 + a1;
-        v[12] = v[13] = v[14] = v[15] = 0.f;
-        const float tot = warp_transpose_reduce16(v, lane);
-        if (!(lane & 1) && vid < FGS_GRAD_STRIDE && vid != 6) {
+        const float tot = warp_transpose_reduce12(v, lane);
+        if (!(lane & 1) && vid >= 0 && vid != 6) {
           const float s = (vid == 11) ? 1.0f / ex2_approx(q.w) : vscale;
           atomicAdd(a.grad + (size_t)__float_as_uint(c.w) * FGS_GRAD_STRIDE + vid, tot * s);
         }
