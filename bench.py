@@ -835,8 +835,11 @@ def ctypes_peak_fp32(dev):
 # FP32 FLOPs (FMA = 2) per pixel-Gaussian evaluation in the compositing
 # kernels, counted from their per-pixel formulas: forward = exponent (5),
 # exp2 + clamp + cut (3), blend (9); backward = alpha recomputation (8),
-# dL/dalpha and the un-blend (15), mean / conic / colour / opacity terms (27).
-FLOP_PER_EVAL = {"render_fwd": 17, "render_bwd": 50}
+# dL/dalpha and the un-blend (15), mean / conic / colour / opacity terms (25),
+# plus 2 for the |dL/dmean2D| sums when the caller asks for the
+# xyz_gradient_accum_abs statistic (the bench step, like 3DGS and Taming,
+# does not, and the kernel then skips them).
+FLOP_PER_EVAL = {"render_fwd": 17, "render_bwd": 48}
 # MUFU operations per evaluation: the alpha's ex2 (forward); ex2 and the
 # 1 / (1 - alpha) reciprocal (backward).  Against fgs_peak_ex2.
 MUFU_PER_EVAL = {"render_fwd": 1, "render_bwd": 2}

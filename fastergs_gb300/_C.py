@@ -59,6 +59,10 @@ def _counters(dev: torch.device) -> torch.Tensor:
     return _COUNTERS[key]
 
 
+def _nonempty(t) -> bool:
+    return t is not None and t.numel() != 0
+
+
 def _device_of(t: torch.Tensor) -> torch.device:
     if not t.is_cuda:
         raise ValueError("the rasterizer runs on CUDA tensors only (no CPU fallback)")
@@ -163,9 +167,10 @@ def render_16x16(P, num_rendered, width, height, splat_buffer, gaussian_keys_sor
 def backward(degree, bucket_sum, means3D, radii, dc, sh, opacities, scales, rotations, scale_modifier, width,
              height, block_x, block_y, tan_fovx, tan_fovy, zFar, zNear, campos, viewmatrix, projmatrix, img_func,
              smp_func, splat_buffer, point_list, ranges, background, last_contributor, Ts_final, dL_dout_color,
-             xyz_gradient_accum, xyz_gradient_accum_abs, max_radii, denom, bucket_size=BUCKET):
+             xyz_gradient_accum, xyz_gradient_accum_abs, max_radii, denom, bucket_size=BUCKET, abs_grad=True):
     """FB pybind.cpp:210-339.  Returns (dL_dmean2D, dL_dcolor, dL_dopacity, dL_dmean3D, dL_dcov3D, dL_ddc,
-    dL_dsh, dL_dscale, dL_drot)."""
+    dL_dsh, dL_dscale, dL_drot).  abs_grad=False leaves dL_dmean2D[:, 2:] (the |dL/dmean2D| sums,
+    read only by the xyz_gradient_accum_abs statistic) at zero and skips their work."""
     dev = _device_of(means3D)
     P = means3D.size(0)
     M = sh.size(1) if sh.numel() and sh.size(0) != 0 else 0
@@ -199,7 +204,7 @@ def backward(degree, bucket_sum, means3D, radii, dc, sh, opacities, scales, rota
     s = _stream(dev)
     _lib.call("fgs_render_bwd", int(P), int(width), int(height), int(block_x), int(block_y), int(bucket_size),
               _ptr(point_list), _ptr(ranges), _ptr(bg), _ptr(splat_buffer), _ptr(Ts_final), _ptr(last_contributor),
-              _ptr(img_func), _ptr(smp_func), int(mb), _ptr(dL), _ptr(grad_record), s)
+              _ptr(img_func), _ptr(smp_func), int(mb), _ptr(dL), _ptr(grad_record), 0 if abs_grad else 1, s)
     stats = xyz_gradient_accum is not None and xyz_gradient_accum.numel() != 0 and xyz_gradient_accum.size(0) != 0
     _lib.call("fgs_preprocess_bwd", int(P), int(degree), int(M), _ptr(means), _ptr(radii), _ptr(dcc), _ptr(shc),
               _ptr(splat_buffer), _ptr(sc), _ptr(ro), float(scale_modifier), _ptr(viewmatrix), _ptr(projmatrix),
@@ -240,7 +245,8 @@ def backward_adam(degree, bucket_sum, means3D, radii, sh, opacities, scales, rot
     s = _stream(dev)
     _lib.call("fgs_render_bwd", int(P), int(width), int(height), int(block_x), int(block_y), int(bucket_size),
               _ptr(point_list), _ptr(ranges), _ptr(bg), _ptr(splat_buffer), _ptr(Ts_final), _ptr(last_contributor),
-              _ptr(img_func), _ptr(smp_func), int(mb), _ptr(dL), _ptr(grad_record), s)
+              _ptr(img_func), _ptr(smp_func), int(mb), _ptr(dL), _ptr(grad_record),
+              0 if _nonempty(xyz_gradient_accum_abs) else 1, s)
     stats = xyz_gradient_accum is not None and xyz_gradient_accum.numel() != 0 and xyz_gradient_accum.size(0) != 0
     _lib.call("fgs_preprocess_bwd_adam", int(P), int(degree), int(M), _ptr(means), _ptr(radii), _ptr(shc),
               _ptr(splat_buffer), _ptr(op), _ptr(sc), _ptr(ro), float(scale_modifier), _ptr(viewmatrix),
@@ -419,7 +425,7 @@ def rasterize_gaussians_backward(background, means3D, radii, colors, scales, rot
         s = _stream(dev)
         _lib.call("fgs_render_bwd", P, W, H, TILE, TILE, BUCKET, _ptr(binningBuffer), binningBuffer.data_ptr() + 4 * R,
                   _ptr(bg), _ptr(geomBuffer), base + off_ts, base + off_lc, base, base + off_smp, mb, _ptr(dL),
-                  _ptr(grad), s)
+                  _ptr(grad), 0, s)
         _lib.call("fgs_preprocess_bwd", P, int(degree), int(M), _ptr(_f32("means3D", means3D, dev)), _ptr(radii),
                   _ptr(dc), _ptr(rest), _ptr(geomBuffer), _ptr(_f32("scales", scales, dev)),
                   _ptr(_f32("rotations", rotations, dev)), float(scale_modifier),

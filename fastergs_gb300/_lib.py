@@ -59,7 +59,7 @@ SIGNATURES = {
     "fgs_state_bytes": (i32, [i32, i32, i32, i32, i64, C.POINTER(C.c_size_t), C.POINTER(C.c_size_t)]),
     "fgs_render_fwd": (i32, [i32, i64, i32, i32, i32, i32, i32, vp, vp, vp, vp, vp, vp, vp, vp, vp, sz, vp, sz,
                              i64, u32p, vp]),
-    "fgs_render_bwd": (i32, [i32, i32, i32, i32, i32, i32, vp, vp, vp, vp, vp, vp, vp, vp, i64, vp, vp, vp]),
+    "fgs_render_bwd": (i32, [i32, i32, i32, i32, i32, i32, vp, vp, vp, vp, vp, vp, vp, vp, i64, vp, vp, i32, vp]),
     "fgs_preprocess_bwd": (i32, [i32, i32, i32, vp, vp, vp, vp, vp, vp, vp, f32, vp, vp, i32, i32, f32, f32, vp,
                                  vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp]),
     "fgs_preprocess_bwd_adam": (i32, [i32, i32, i32, vp, vp, vp, vp, vp, vp, vp, f32, vp, vp, i32, i32, f32, f32,

@@ -14,6 +14,8 @@
 //   * the preprocess backward is one kernel (FB launches two) that also
 //     scatters the record into FB's output tensors and accumulates the
 //     densification statistics.
+#include <type_traits>
+
 #include "render_common.cuh"
 
 namespace fgs {
@@ -84,7 +86,9 @@ __device__ __forceinline__ int warp_value_of(int lane) {
   return (c && d) ? -1 : (d + 2 * c) + 3 * b + 6 * a;
 }
 
-template <int BX, bool RECOMPUTE>
+// ABS: also sum |dL/dmean2D| per Gaussian (dmean2D.zw, for the
+// xyz_gradient_accum_abs statistic); without it those two slots stay zero.
+template <int BX, bool RECOMPUTE, bool ABS>
 __global__ void __launch_bounds__(kBwdWarps * kWarp, 5) k_render_bwd(const BwdArgs a) {
   using M = TileMap<BX>;
   constexpr int BY = kTilePixels / BX;
@@ -290,11 +294,13 @@ __global__ void __launch_bounds__(kBwdWarps * kWarp, 5) k_render_bwd(const BwdAr
         const f2x ty2 = f2_mul(dp2, f2_fma(gw2, P2, f2_pack(2.f * q.z * dy0, 2.f * q.z * dy1)));
         V0 = f2_add(V0, tx2);
         V1 = f2_add(V1, ty2);
-        float tx0, tx1, ty0, ty1;
-        f2_unpack(tx2, tx0, tx1);
-        f2_unpack(ty2, ty0, ty1);
-        v2 += fabsf(tx0) + fabsf(tx1);
-        v3 += fabsf(ty0) + fabsf(ty1);
+        if constexpr (ABS) {
+          float tx0, tx1, ty0, ty1;
+          f2_unpack(tx2, tx0, tx1);
+          f2_unpack(ty2, ty0, ty1);
+          v2 += fabsf(tx0) + fabsf(tx1);
+          v3 += fabsf(ty0) + fabsf(ty1);
+        }
         // Conic-gradient moments in the exponent's own frame (w, dy),
         // w = dx + P dy.  In pixel coordinates a thin footprint's cross-axis
         // gradient is a small difference of large sums; here each frame
@@ -319,7 +325,7 @@ __global__ void __launch_bounds__(kBwdWarps * kWarp, 5) k_render_bwd(const BwdAr
         f2_unpack(V10, a0, a1); v[10] = a0 + a1;
         f2_unpack(V11, a0, a1); v[11] = a0 + a1;
         const float tot = warp_transpose_reduce12(v, lane);
-        if (!(lane & 1) && vid >= 0 && vid != 6) {
+        if (!(lane & 1) && vid >= 0 && vid != 6 && (ABS || (vid != 2 && vid != 3))) {
           const float s = (vid == 11) ? 1.0f / ex2_approx(q.w) : vscale;
           atomicAdd(a.grad + (size_t)__float_as_uint(c.w) * FGS_GRAD_STRIDE + vid, tot * s);
         }
@@ -747,7 +753,8 @@ namespace fgs {
 fgs_status run_render_bwd(const Views& views, int64_t records, int bucket_size, const uint32_t* values_sorted,
                           const uint32_t* ranges, const float* splat, const float* Ts_final,
                           const int32_t* last_contributor, const ImageState& im, const SampleState& sm,
-                          const float* dL_dpixels, float* grad_record, bool recompute, cudaStream_t s) {
+                          const float* dL_dpixels, float* grad_record, bool recompute, bool abs_grad,
+                          cudaStream_t s) {
   FGS_TRY(cudaMemsetAsync(grad_record, 0, sizeof(float) * FGS_GRAD_STRIDE * (size_t)records, s));
   // backward work cursor (word 3 of the image-state header); reset on every call
   FGS_TRY(cudaMemsetAsync(im.bucket_sum + 3, 0, sizeof(uint32_t), s));
@@ -762,14 +769,20 @@ fgs_status run_render_bwd(const Views& views, int64_t records, int bucket_size, 
     auto launch = [&](auto kernel) {
       kernel<<<num_sms() * resident_blocks(kernel, nt, 0), nt, 0, s>>>(a);
     };
+    auto by_tile = [&](auto rc, auto ab) {
+      constexpr bool R = decltype(rc)::value, A = decltype(ab)::value;
+      if (views.bx == 8) launch(k_render_bwd<8, R, A>);
+      else if (views.bx == 16) launch(k_render_bwd<16, R, A>);
+      else launch(k_render_bwd<32, R, A>);
+    };
+    using T_ = std::true_type;
+    using F_ = std::false_type;
     if (recompute) {
-      if (views.bx == 8) launch(k_render_bwd<8, true>);
-      else if (views.bx == 16) launch(k_render_bwd<16, true>);
-      else launch(k_render_bwd<32, true>);
+      if (abs_grad) by_tile(T_{}, T_{});
+      else by_tile(T_{}, F_{});
     } else {
-      if (views.bx == 8) launch(k_render_bwd<8, false>);
-      else if (views.bx == 16) launch(k_render_bwd<16, false>);
-      else launch(k_render_bwd<32, false>);
+      if (abs_grad) by_tile(F_{}, T_{});
+      else by_tile(F_{}, F_{});
     }
     kt__.stop();
   }
@@ -801,7 +814,7 @@ extern "C" fgs_status fgs_render_bwd(int P, int width, int height, int block_x, 
                                      const float* splat_buffer, const float* Ts_final,
                                      const int32_t* last_contributor, const void* image_state,
                                      const void* sample_state, int64_t max_buckets, const float* dL_dpixels,
-                                     float* grad_record, void* stream) {
+                                     float* grad_record, int flags, void* stream) {
   if (P < 0 || width <= 0 || height <= 0 || !tile_shape_ok(block_x, block_y) || bucket_size < 1 ||
       bucket_size > kMaxBucket || max_buckets < 0)
     return FGS_ERR_BAD_ARG;
@@ -815,7 +828,7 @@ extern "C" fgs_status fgs_render_bwd(int P, int width, int height, int block_x, 
   const int64_t mb = max_buckets > 0 ? max_buckets : 1;
   const SampleState sm = carve_sample(const_cast<void*>(sample_state), mb, mb);
   return run_render_bwd(views, P, bucket_size, values_sorted, ranges, splat_buffer, Ts_final, last_contributor, im,
-                        sm, dL_dpixels, grad_record, false, (cudaStream_t)stream);
+                        sm, dL_dpixels, grad_record, false, (flags & FGS_BWD_NO_ABS) == 0, (cudaStream_t)stream);
 }
 
 extern "C" fgs_status fgs_preprocess_bwd(

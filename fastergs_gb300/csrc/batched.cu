@@ -209,7 +209,7 @@ extern "C" fgs_status fgs_render_batched_bwd(int P, int D, int M, const float* m
                                  reinterpret_cast<uint32_t*>(ws + L.ranges), reinterpret_cast<float*>(ws + L.records),
                                  reinterpret_cast<float*>(ws + L.ts_final),
                                  reinterpret_cast<int32_t*>(ws + L.last_contrib), im, sm, dL_dpixels, grad,
-                                 cfg->recompute != 0, s);
+                                 cfg->recompute != 0, xyz_gradient_accum_abs != nullptr, s);
   if (st != FGS_OK) return st;
   PbwdArgs a;
   a.views = views;
@@ -251,7 +251,7 @@ extern "C" fgs_status fgs_render_batched_bwd_adam(int P, int D, int M, const flo
                                  reinterpret_cast<uint32_t*>(ws + L.ranges), reinterpret_cast<float*>(ws + L.records),
                                  reinterpret_cast<float*>(ws + L.ts_final),
                                  reinterpret_cast<int32_t*>(ws + L.last_contrib), im, sm, dL_dpixels, grad,
-                                 cfg->recompute != 0, s);
+                                 cfg->recompute != 0, xyz_gradient_accum_abs != nullptr, s);
   if (st != FGS_OK) return st;
   PbwdArgs a;
   a.views = views;

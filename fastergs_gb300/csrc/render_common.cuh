@@ -323,6 +323,7 @@ fgs_status run_render_fwd(const Views& views, int64_t n_cap, const int32_t* n_de
 fgs_status run_render_bwd(const Views& views, int64_t records, int bucket_size, const uint32_t* values_sorted,
                           const uint32_t* ranges, const float* splat, const float* Ts_final,
                           const int32_t* last_contributor, const ImageState& im, const SampleState& sm,
-                          const float* dL_dpixels, float* grad_record, bool recompute, cudaStream_t s);
+                          const float* dL_dpixels, float* grad_record, bool recompute, bool abs_grad,
+                          cudaStream_t s);
 
 }  // namespace fgs

@@ -162,13 +162,16 @@ fgs_status fgs_render_fwd(int P, int64_t num_rendered, int width, int height, in
  * Backward composite, bucket-parallel, front-to-back inside each bucket.
  * Replaces faster::render_backward (FB csrc/ops.h:123-135,
  * backward.cu:956-977).  grad_record (P, FGS_GRAD_STRIDE) is zeroed here and
- * accumulated with vector reductions.
+ * accumulated with vector reductions.  flags = 0 computes every slot, as FB
+ * does; FGS_BWD_NO_ABS skips the |dL/dmean2D| sums, whose only consumer is
+ * the xyz_gradient_accum_abs statistic.
  */
+#define FGS_BWD_NO_ABS 1  /* flags: leave dmean2D.zw (the sums of |dL/dmean2D|) at zero */
 fgs_status fgs_render_bwd(int P, int width, int height, int block_x, int block_y, int bucket_size,
                           const uint32_t* values_sorted, const uint32_t* ranges, const float* bg,
                           const float* splat_buffer, const float* Ts_final, const int32_t* last_contributor,
                           const void* image_state, const void* sample_state, int64_t max_buckets,
-                          const float* dL_dpixels, float* grad_record, void* stream);
+                          const float* dL_dpixels, float* grad_record, int flags, void* stream);
 
 /*
  * Per-Gaussian backward of projection, EWA covariance, SH and 3D covariance;

@@ -56,7 +56,7 @@ def test_bad_arguments_are_rejected_without_touching_the_gpu(lib):
     assert lib.fgs_sort(-5, 256, 256, 16, 16, None, 0, None, None, None, None, None) == 1
     assert lib.fgs_sort(0, 256, 256, 16, 16, None, 0, None, None, None, None, None) == 0
     assert lib.fgs_render_fwd(1, 10, 256, 256, 16, 8, 128, *([None] * 9), 0, None, 0, 10, None, None) == 1
-    assert lib.fgs_render_bwd(1, 256, 256, 16, 16, 0, *([None] * 8), 0, None, None, None) == 1
+    assert lib.fgs_render_bwd(1, 256, 256, 16, 16, 0, *([None] * 8), 0, None, None, 0, None) == 1
     assert lib.fgs_adam_update(None, None, None, None, None, 0.1, 0.9, 0.999, 1e-8, 10, 0, None) == 1
 
 
