@@ -167,26 +167,30 @@ def render_16x16(P, num_rendered, width, height, splat_buffer, gaussian_keys_sor
 def backward(degree, bucket_sum, means3D, radii, dc, sh, opacities, scales, rotations, scale_modifier, width,
              height, block_x, block_y, tan_fovx, tan_fovy, zFar, zNear, campos, viewmatrix, projmatrix, img_func,
              smp_func, splat_buffer, point_list, ranges, background, last_contributor, Ts_final, dL_dout_color,
-             xyz_gradient_accum, xyz_gradient_accum_abs, max_radii, denom, bucket_size=BUCKET, abs_grad=True):
+             xyz_gradient_accum, xyz_gradient_accum_abs, max_radii, denom, bucket_size=BUCKET, abs_grad=True,
+             minimal=False):
     """FB pybind.cpp:210-339.  Returns (dL_dmean2D, dL_dcolor, dL_dopacity, dL_dmean3D, dL_dcov3D, dL_ddc,
     dL_dsh, dL_dscale, dL_drot).  abs_grad=False leaves dL_dmean2D[:, 2:] (the |dL/dmean2D| sums,
-    read only by the xyz_gradient_accum_abs statistic) at zero and skips their work."""
+    read only by the xyz_gradient_accum_abs statistic) at zero and skips their work.  minimal=True
+    (the autograd step) returns empty dL_dmean2D and dL_dcov3D, and an empty dL_dcolor when SH
+    coefficients are given, without writing them."""
     dev = _device_of(means3D)
     P = means3D.size(0)
     M = sh.size(1) if sh.numel() and sh.size(0) != 0 else 0
     f = dict(dtype=torch.float32, device=dev)
-    dmean2D = torch.empty((P, 4), **f)
-    dcolor = torch.empty((P, 3), **f)
+    none = torch.empty(0, **f)
+    dmean2D = none if minimal else torch.empty((P, 4), **f)
+    dcolor = none if (minimal and sh.numel()) else torch.empty((P, 3), **f)
     dopac = torch.empty((P, 1), **f)
     dmean3D = torch.empty((P, 3), **f)
-    dcov3D = torch.empty((P, 6), **f)
+    dcov3D = none if minimal else torch.empty((P, 6), **f)
     ddc = torch.empty((P, 1, 3), **f)
     dsh = torch.empty((P, M, 3), **f)
     dscale = torch.empty((P, 3), **f)
     drot = torch.empty((P, 4), **f)
     if P == 0:
         return dmean2D, dcolor, dopac, dmean3D, dcov3D, ddc, dsh, dscale, drot
-    dconic = torch.empty((P, 2, 2), **f)
+    dconic = none if minimal else torch.empty((P, 2, 2), **f)
     grad_record = torch.empty((P, 12), **f)
     means = _f32("means3D", means3D, dev)
     dcc = _f32("dc", dc, dev)

@@ -169,7 +169,10 @@ class _RasterizeGaussians(torch.autograd.Function):
             rs.campos, rs.viewmatrix, rs.projmatrix, img_buffer, smp_buffer, splat_buffer,
             buffer.gaussian_values_sorted, buffer.ranges, rs.bg, last_contributor, Ts_final,
             grad_out_color.contiguous(), xyz_gradient_accum, xyz_gradient_accum_abs, max_radii, denom,
-            abs_grad=_C._nonempty(xyz_gradient_accum_abs))  # dmean2D is not returned to autograd
+            abs_grad=_C._nonempty(xyz_gradient_accum_abs),  # dmean2D is not returned to autograd
+            minimal=True)
+        grad_color = grad_color if grad_color.numel() else None      # only precomputed colours need it
+        grad_cov3D = None                                             # covariances are never precomputed here
         return (grad_mean3D, grad_dc, grad_shs, grad_color, grad_opacity, grad_scales, grad_rotations, grad_cov3D,
                 None, None, None, None, None, None, None)
 

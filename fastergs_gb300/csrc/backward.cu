@@ -605,15 +605,20 @@ __device__ __forceinline__ bool pbwd_gaussian(const PbwdArgs& a, int i, const fl
     }
     return true;
   }
-  // --- outputs (zeros where no view saw the Gaussian, as FB leaves them)
-  a.dcolor[3 * (size_t)i] = gco_sum.x;
-  a.dcolor[3 * (size_t)i + 1] = gco_sum.y;
-  a.dcolor[3 * (size_t)i + 2] = gco_sum.z;
+  // --- outputs (zeros where no view saw the Gaussian, as FB leaves them);
+  // dcolor and dcov3D are optional (only precomputed colours / covariances need them)
+  if (a.dcolor) {
+    a.dcolor[3 * (size_t)i] = gco_sum.x;
+    a.dcolor[3 * (size_t)i + 1] = gco_sum.y;
+    a.dcolor[3 * (size_t)i + 2] = gco_sum.z;
+  }
   a.dopac[i] = gco_sum.w;
   float* gm = a.dmean3D + 3 * (size_t)i;
   gm[0] = m3[0]; gm[1] = m3[1]; gm[2] = m3[2];
+  if (a.dcov3D) {
 #pragma unroll
-  for (int k = 0; k < 6; ++k) a.dcov3D[6 * (size_t)i + k] = gc[k];
+    for (int k = 0; k < 6; ++k) a.dcov3D[6 * (size_t)i + k] = gc[k];
+  }
   a.ddc[3 * (size_t)i] = gdc[0]; a.ddc[3 * (size_t)i + 1] = gdc[1]; a.ddc[3 * (size_t)i + 2] = gdc[2];
   a.dscale[3 * (size_t)i] = gs[0]; a.dscale[3 * (size_t)i + 1] = gs[1]; a.dscale[3 * (size_t)i + 2] = gs[2];
   reinterpret_cast<float4*>(a.drot)[i] = make_float4(gq[0], gq[1], gq[2], gq[3]);
@@ -842,8 +847,7 @@ extern "C" fgs_status fgs_preprocess_bwd(
   if (P < 0 || D < 0 || D > 3 || M < 0 || width <= 0 || height <= 0) return FGS_ERR_BAD_ARG;
   if (P == 0) return FGS_OK;
   if (!means3D || !radii || !splat_buffer || !scales || !rotations || !viewmatrix || !projmatrix || !grad_record ||
-      !dL_dmean2D || !dL_dconic || !dL_dopacity || !dL_dcolor || !dL_dmean3D || !dL_dcov3D || !dL_ddc ||
-      !dL_dscale || !dL_drot)
+      !dL_dopacity || !dL_dmean3D || !dL_ddc || !dL_dscale || !dL_drot)
     return FGS_ERR_BAD_ARG;
   if (shs && (!dc || !campos || (D > 0 && M < (D + 1) * (D + 1) - 1) || !dL_dsh)) return FGS_ERR_BAD_ARG;
   if (((uintptr_t)grad_record & 15) || ((uintptr_t)dL_dmean2D & 15) || ((uintptr_t)dL_dconic & 15) ||

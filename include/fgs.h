@@ -180,7 +180,9 @@ fgs_status fgs_render_bwd(int P, int width, int height, int block_x, int block_y
  * Replaces faster::preprocess_backward + add_densification_stats
  * (FB csrc/ops.h:108-121,137-145; backward.cu:922-954,980-999) and the
  * output allocation of backward_torch (FB csrc/pybind.cpp:258-267).
- * All outputs are fully written (zeros where FB leaves zeros).
+ * All outputs are fully written (zeros where FB leaves zeros).  dL_dmean2D,
+ * dL_dconic, dL_dcolor and dL_dcov3D may be NULL: an autograd step needs
+ * none of them unless colours or covariances are precomputed.
  */
 fgs_status fgs_preprocess_bwd(
     int P, int D, int M, const float* means3D, const int32_t* radii, const float* dc, const float* shs,
