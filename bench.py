@@ -6,18 +6,30 @@ fwd+bwd step of 1,000,000 seeded synthetic Gaussians in a 10x10x10 box 2-12
 units ahead, heavy-tailed log-scales N(-4, 1), SH degree 3, one 1297x840 view
 (FoV 50 deg), dL/dimage ~ N(0, 1); synthetic data stands in for Mip-NeRF 360.
 Per-step inputs (parameters, records, pair lists, sample state) exceed the
-129 MB L2.  ``e2e`` repeats the step with pinned-host inputs and outputs copied
-inside the timed region.
+129 MB L2.  ``e2e`` repeats the step with pinned-host inputs (parameters and
+dL/dimage) uploaded and its outputs (image and every parameter gradient)
+downloaded inside the timed region, on copy streams that overlap the
+neighbouring steps' kernels.
 
 Also on the line:
+  kernels     every kernel's per-launch device time (CUDA events on the launch
+              stream) with its HBM, FP32 and MUFU fractions;
+  roofline    the dominant kernel against its bound: FP32 TFLOP/s vs a live FFMA
+              peak for the compositing kernels (MUFU vs a live ex2 peak beside it),
+              GB/s vs MEASURED_PEAKS for the rest;
+  aux         the importance and depth passes on the same scene;
+  fused_adam  the training step with sparse Adam, unfused vs fused into the
+              preprocess backward;
+  loss        (1 - 0.2) L1 + 0.2 (1 - SSIM) and dL/dimage on the C2 frame, fused
+              vs fused_ssim + torch L1, and PLY save / load of the scene;
   batched     the same scene through 16 cameras of uneven resolution (and 16 at
               1297x840): 16 sequential drop-in calls vs one batched step replayed
               from a CUDA graph, with the autotuner's sweep (--tune sweep|default);
+  c3          3M clustered Gaussians at 1920x1080, forward only;
   checkpoint  6M clustered Gaussians at 3840x2160: bucket prefixes stored vs
               recomputed in the backward (step time, device memory held);
-  roofline    the dominant kernel against its bound: FP32 TFLOP/s vs a live FFMA
-              peak for the compositing kernels, GB/s vs MEASURED_PEAKS for the rest;
   cpu_baseline the FP64 oracle on all host cores on 1/16 of the Gaussians, x16.
+Each section has a --no-<section> switch (--no-cpu-baseline, --no-e2e, ...).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
