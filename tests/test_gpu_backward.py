@@ -112,3 +112,22 @@ def test_zero_gaussians(cuda_device):
     g = run_backward(s, fw, scenes.upstream_grad(0, 256, 256), cuda_device)
     for k in KEYS:
         assert np.all(g[k] == 0), k
+
+
+@pytest.mark.parametrize("WH", [(1, 1), (5, 3), (17, 33), (1031, 9), (640, 480)],
+                         ids=lambda wh: f"{wh[0]}x{wh[1]}")
+def test_backward_huge_gaussians_and_odd_image_sizes(cuda_device, WH):
+    from test_gpu_forward import huge_and_odd
+    s = huge_and_odd(*WH)
+    fw = run_forward(s, cuda_device, bg=(0.25, 0.5, 0.75))
+    o = replay_oracle(s, fw, bg=(0.25, 0.5, 0.75))
+    amb = o.image()["ambiguous"]
+    dL = scenes.upstream_grad(3, s.camera.height, s.camera.width)
+    dL[:, amb] = 0.0
+    g = run_backward(s, fw, dL, cuda_device, stats=True)
+    r = o.backward(dL.astype(np.float64))
+    _compare(g, r)
+    # a Gaussian that no pixel saw has exactly zero gradients
+    unseen = ~np.isin(np.arange(s.P), fw["vals_sorted"])
+    for k in ("dmean3D", "dopacity", "ddc", "dscale", "drot"):
+        assert np.all(g[k][unseen] == 0.0), k

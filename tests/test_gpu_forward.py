@@ -234,3 +234,62 @@ def test_everything_culled_gives_background(cuda_device):
     img = fw["out_color"].cpu().numpy()
     np.testing.assert_allclose(img[:, 0, 0], [0.1, 0.2, 0.3], rtol=1e-7)
     assert np.all(fw["Ts_final"].cpu().numpy() == 1.0)
+
+
+def huge_and_odd(W, H, seed=7, P=600, n_huge=20):
+    """C1-like scene on a W x H image with n_huge Gaussians large enough
+    (tile rectangle of 128 tiles or more on the larger images) to take the
+    large-footprint sub-task path of the preprocess."""
+    s = scenes.scene_c1(seed=seed, P=P)
+    rng = np.random.default_rng(seed + 1)
+    s.means[:n_huge] = np.stack([rng.uniform(-0.6, 0.6, n_huge), rng.uniform(-0.4, 0.4, n_huge),
+                                 rng.uniform(3.0, 5.0, n_huge)], axis=1).astype(np.float32)
+    s.log_scales[:n_huge] = np.log(rng.uniform(0.25, 0.5, (n_huge, 3))).astype(np.float32)
+    s.opacity_logits[:n_huge] = rng.uniform(-3.0, -1.0, (n_huge, 1)).astype(np.float32)
+    s.camera = scenes.make_camera(W, H, 60.0)
+    return s
+
+
+ODD_SIZES = [(1, 1), (5, 3), (17, 33), (1031, 9), (640, 480)]
+
+
+@pytest.mark.parametrize("WH", ODD_SIZES, ids=lambda wh: f"{wh[0]}x{wh[1]}")
+def test_huge_gaussians_and_odd_image_sizes(cuda_device, WH):
+    W, H = WH
+    s = huge_and_odd(W, H)
+    fw = run_forward(s, cuda_device, bg=(0.25, 0.5, 0.75))
+    tiles = ((W + 15) // 16) * ((H + 15) // 16)
+    rect = fw["rec"].view(np.int32)[:, 12:16].astype(np.int64)
+    radii = fw["radii"].cpu().numpy()
+    area = np.where(radii > 0, (rect[:, 2] - rect[:, 0]) * (rect[:, 3] - rect[:, 1]), 0)
+    if tiles >= 128:
+        assert (area >= 128).sum() >= 5  # the sub-task path is exercised
+    # (tile, Gaussian) pairs: the large-footprint sub-tasks emit exactly the
+    # pairs the oracle's per-tile test emits, once each
+    oe = oracle_scene(s)
+    rec, _, _ = gpu_records_as_oracle(fw)
+    oe.set_records(rec, radii, radii > 0)
+    oe.emit_sort(eps_pair=1e-5)
+    pr = oe.pairs()
+    gtile = (fw["keys_unsorted"].view(np.uint64) >> np.uint64(32)).astype(np.int64)
+    gpu = set(zip(gtile.tolist(), fw["vals_unsorted"].tolist()))
+    assert len(gpu) == fw["K"], "duplicate pairs emitted"
+    otile = (pr["keys"] >> np.uint64(32)).astype(np.int64)
+    orc = set(zip(otile.tolist(), pr["ids"].tolist()))
+    amb = set(zip(otile[pr["ambiguous"]].tolist(), pr["ids"][pr["ambiguous"]].tolist()))
+    assert (gpu ^ orc) <= amb, f"{len(gpu - orc)} extra / {len(orc - gpu)} missing pairs"
+    o2 = oracle_scene(s).preprocess()
+    r = o2.records()
+    a = r["ambiguous"]
+    np.testing.assert_array_equal(radii[~a], r["radii"][~a])
+    o = replay_oracle(s, fw, bg=(0.25, 0.5, 0.75))
+    im = o.image()
+    ok = ~im["ambiguous"]
+    gimg = fw["out_color"].cpu().numpy().astype(np.float64)
+    assert gimg.shape == (3, H, W)
+    if ok.any():
+        assert np.abs(gimg - im["out_color"])[:, ok].max() <= 1e-5
+    lc = fw["last_contrib"].cpu().numpy()[..., 0]
+    np.testing.assert_array_equal(lc[ok], im["last_contributor"][ok])
+    assert fw["bucket_sum"] == im["num_buckets"]
+    np.testing.assert_array_equal(fw["ranges"].shape, (tiles, 2))
