@@ -41,6 +41,7 @@ struct TimerSlot {
   std::mutex mu;
   bool enabled = false;
   std::vector<std::pair<cudaEvent_t, cudaEvent_t>> pairs;  // recorded since the last read
+  int kernels = 0;                                         // launches inside those pairs
   cudaEvent_t open = nullptr;
 };
 TimerSlot g_timers[FGS_K_COUNT];
@@ -61,7 +62,7 @@ void timer_begin(int id, cudaStream_t s) {
   t.open = e;
 }
 
-void timer_end(int id, cudaStream_t s) {
+void timer_end(int id, cudaStream_t s, int kernels) {
   if (id < 0 || id >= FGS_K_COUNT) return;
   TimerSlot& t = g_timers[id];
   if (!t.enabled) return;
@@ -71,6 +72,7 @@ void timer_end(int id, cudaStream_t s) {
   cudaEventCreate(&e);
   cudaEventRecord(e, s);
   t.pairs.emplace_back(t.open, e);
+  t.kernels += kernels;
   t.open = nullptr;
 }
 
@@ -277,7 +279,9 @@ extern "C" fgs_status fgs_read_counts(const int32_t* curr_offset, const int32_t*
   cudaStream_t s = (cudaStream_t)stream;
   void* dptr = nullptr;
   if (cudaHostGetDevicePointer(&dptr, host_out, 0) == cudaSuccess && dptr) {
+    fgs::KernelTimer kt__(FGS_K_READ_COUNTS, s);
     fgs::k_store_counts<<<1, 1, 0, s>>>(curr_offset, counters, static_cast<int32_t*>(dptr));
+    kt__.stop();
     FGS_LAUNCH_CHECK();
     return FGS_OK;
   }
@@ -307,7 +311,8 @@ extern "C" fgs_status fgs_kernel_timer_read(int kernel_id, double* total_ms, int
     cudaEventDestroy(pr.second);
   }
   *total_ms = sum;
-  *launches = (int)t.pairs.size();
+  *launches = t.kernels;
+  t.kernels = 0;
   t.pairs.clear();
   return FGS_OK;
 }

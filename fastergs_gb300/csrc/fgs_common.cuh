@@ -340,13 +340,15 @@ int* error_word_backward();
 int* error_word_aux();
 // Optional per-kernel event timing (fgs_kernel_timer).  Usage around a launch:
 //   KernelTimer kt(FGS_K_RENDER_FWD, stream); launch...; kt.stop();
+// `kernels`: how many kernel launches the timed region holds.
 void timer_begin(int id, cudaStream_t s);
-void timer_end(int id, cudaStream_t s);
+void timer_end(int id, cudaStream_t s, int kernels);
 struct KernelTimer {
   int id;
   cudaStream_t s;
-  KernelTimer(int id_, cudaStream_t s_) : id(id_), s(s_) { timer_begin(id, s); }
-  void stop() { timer_end(id, s); }
+  int kernels;
+  KernelTimer(int id_, cudaStream_t s_, int kernels_ = 1) : id(id_), s(s_), kernels(kernels_) { timer_begin(id, s); }
+  void stop() { timer_end(id, s, kernels); }
 };
 // Opts a kernel into `bytes` of dynamic shared memory on the current device,
 // once per (kernel, device); the first launch happens before any capture.

@@ -463,7 +463,7 @@ fgs_status run_render_fwd(const Views& views, int64_t n_cap, const int32_t* n_de
   fgs_status st = run_tile_ranges(n_cap, n_dev, views.tiles, keys_sorted, ranges, s);
   if (st != FGS_OK) return st;
   {
-    KernelTimer kt__(FGS_K_BUCKET_SETUP, s);
+    KernelTimer kt__(FGS_K_BUCKET_SETUP, s, 3);
     const unsigned nblk = (views.tiles + kScanTiles - 1) / kScanTiles;
     FGS_TRY(cudaMemsetAsync(im.round_hist, 0, sizeof(uint32_t) * (kRounds + 1), s));
     k_bucket_count<<<nblk, kScanTiles, 0, s>>>((int)views.tiles, ranges, bucket_size, im.block_sums,

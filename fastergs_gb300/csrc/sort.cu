@@ -4,22 +4,22 @@
 // (csrc/cuda_rasterizer/sort.cu:28-44) with a single-pass-per-digit
 // ("onesweep") sort written for this GPU:
 //   * one upfront kernel builds the 8-bit digit histograms of every pass in a
-//     single read of the keys;
+//     single read of the keys and turns them into global digit bases;
 //   * each pass is one kernel: a CTA of 512 threads (8 keys each, few enough
-//     registers for 2 CTAs = 32 warps per SM) ranks a 4096-key tile in shared memory
-//     (warp match + per-warp digit counters, so ranks are stable), publishes its
-//     per-digit counts, obtains the exclusive prefix of all earlier tiles by a
-//     decoupled look-back, and scatters through shared memory so that global
-//     writes form contiguous runs per digit;
+//     registers for 2 CTAs = 32 warps per SM) ranks a 4096-key tile in shared
+//     memory (ballot digit masks + per-warp digit counters, so ranks are
+//     stable), publishes its per-digit counts, sorts the tile locally, obtains
+//     the exclusive prefix of all earlier tiles by a decoupled look-back, and
+//     scatters so that global writes form contiguous runs per digit;
 //   * only the key bits that can differ are sorted: 32 depth bits plus
 //     ceil(log2(tiles)) tile bits, i.e. 5-6 passes for 256..32768 tiles.
 // Every look-back wait is bounded (kSpinLimit polls); on expiry the kernel
 // records kErrTimeout in the error word and continues, so it never hangs.
-#include <atomic>
 #include <algorithm>
 #include <mutex>
 
 #include "internal.cuh"
+
 
 namespace fgs {
 namespace {
@@ -33,7 +33,7 @@ constexpr int kMaxPasses = 8;
 constexpr uint32_t kFlagAgg = 1u << 30;
 constexpr uint32_t kFlagInc = 2u << 30;
 constexpr uint32_t kValueMask = (1u << 30) - 1;
-constexpr int kLookWindow = 8;  // predecessor words read per look-back round
+constexpr int kLookWindow = 32;  // predecessor words read per look-back round
 constexpr int kSortDynSmem = (int)((sizeof(unsigned long long) + sizeof(uint32_t)) * kSortTile);
 
 struct SortLayout {
@@ -49,7 +49,7 @@ constexpr SortLayout layout_for(int64_t n) {
   L.tiles = (n + kSortTile - 1) / kSortTile;
   size_t off = 0;
   L.hist = off;      off = up(off + sizeof(uint32_t) * kMaxPasses * kRadix);
-  L.counters = off;  off = up(off + sizeof(uint32_t) * kMaxPasses);
+  L.counters = off;  off = up(off + sizeof(uint32_t) * (kMaxPasses + 1));  // tile counters, histogram done count
   L.lookback = off;  off = up(off + sizeof(uint32_t) * kMaxPasses * (size_t)L.tiles * kRadix);
   L.alt_keys = off;  off = up(off + sizeof(uint64_t) * (size_t)n);
   L.alt_vals = off;  off = up(off + sizeof(uint32_t) * (size_t)n);
@@ -57,7 +57,23 @@ constexpr SortLayout layout_for(int64_t n) {
   return L;
 }
 
-// All pass histograms in one read of the keys.
+// All pass histograms in one read of the keys; the last block to finish turns
+// them into exclusive digit offsets (the global base of every digit of every
+// pass), so the pass kernels read their bases instead of scanning.
+// Lanes of the warp whose 8-bit digit equals this lane's: one ballot per
+// digit bit (ALU votes; a warp match instruction on this GPU queues on the
+// same pipe as shared and global memory accesses and throttled the passes).
+__device__ __forceinline__ uint32_t digit_peers(uint32_t d) {
+  uint32_t m = 0xffffffffu;
+#pragma unroll
+  for (int b = 0; b < 8; ++b) {
+    const bool bit = (d >> b) & 1u;
+    const uint32_t bal = __ballot_sync(0xffffffffu, bit);
+    m &= bit ? bal : ~bal;
+  }
+  return m;
+}
+
 // Pair count: the host bound, or min(bound, *n_dev) when the count lives on
 // the device (batched / graph-captured frames).
 __device__ __forceinline__ long long pair_count(long long n_cap, const int* n_dev) {
@@ -65,8 +81,10 @@ __device__ __forceinline__ long long pair_count(long long n_cap, const int* n_de
 }
 
 __global__ void __launch_bounds__(kSortThreads) k_histogram(const unsigned long long* keys, long long n_cap,
-                                                            const int* n_dev, int passes, uint32_t* hist) {
+                                                            const int* n_dev, int passes, uint32_t* hist,
+                                                            uint32_t* done) {
   __shared__ uint32_t s_h[kMaxPasses][kRadix];
+  __shared__ bool s_last;
   const long long n = pair_count(n_cap, n_dev);
   for (int j = threadIdx.x; j < kMaxPasses * kRadix; j += kSortThreads) (&s_h[0][0])[j] = 0;
   __syncthreads();
@@ -80,36 +98,48 @@ __global__ void __launch_bounds__(kSortThreads) k_histogram(const unsigned long 
     const uint32_t v = (&s_h[0][0])[j];
     if (v) atomicAdd(&hist[j], v);
   }
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) s_last = atomicAdd(done, 1u) == gridDim.x - 1;
+  __syncthreads();
+  if (!s_last) return;
+  __threadfence();
+  // One warp per pass: exclusive scan of its 256 counts, 8 per lane.
+  const int lane = threadIdx.x & 31, p = threadIdx.x >> 5;
+  if (p < passes) {
+    uint32_t c[8], sum = 0;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      c[j] = ld_volatile_u32(hist + p * kRadix + lane * 8 + j);
+      sum += c[j];
+    }
+    uint32_t incl = sum;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t u = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += u;
+    }
+    uint32_t run = incl - sum;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      hist[p * kRadix + lane * 8 + j] = run;
+      run += c[j];
+    }
+  }
 }
 
-// Exclusive scan of one value per thread (kSortThreads); returns the
-// exclusive prefix, *total receives the sum.  Uses s_tmp[kSortWarps].
-__device__ __forceinline__ uint32_t block_excl_scan(uint32_t v, uint32_t* s_tmp, uint32_t* total) {
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  uint32_t incl = v;
-#pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    const uint32_t u = __shfl_up_sync(0xffffffffu, incl, o);
-    if (lane >= o) incl += u;
-  }
-  if (lane == 31) s_tmp[warp] = incl;
-  __syncthreads();
-  uint32_t wbase = 0, tot = 0;
-#pragma unroll
-  for (int w = 0; w < kSortWarps; ++w) {
-    const uint32_t x = s_tmp[w];
-    if (w < warp) wbase += x;
-    tot += x;
-  }
-  __syncthreads();
-  *total = tot;
-  return wbase + incl - v;
-}
-
+// One digit pass.  Per tile of kSortTile keys:
+//   1. rank every key within its warp's digit counters (warp match: stable);
+//   2. per digit: counts of the warps, tile count published for look-back;
+//   3. tile-local digit offsets (block scan) and a local sort of the tile into
+//      shared memory;
+//   4. per digit: decoupled look-back over a window of kLookWindow
+//      predecessors per round, with no key registers live;
+//   5. global scatter from shared memory, contiguous per digit run.
 __global__ void __launch_bounds__(kSortThreads, 2) k_onesweep(
     const unsigned long long* __restrict__ keys_in, const uint32_t* __restrict__ vals_in,
     unsigned long long* __restrict__ keys_out, uint32_t* __restrict__ vals_out, long long n_cap, const int* n_dev,
-    int shift, const uint32_t* __restrict__ hist, uint32_t* lookback, uint32_t* tile_counter) {
+    int shift, const uint32_t* __restrict__ digit_base, uint32_t* lookback, uint32_t* tile_counter) {
   extern __shared__ __align__(16) unsigned char s_dyn[];  // kSortDynSmem bytes
   unsigned long long* s_keys = reinterpret_cast<unsigned long long*>(s_dyn);
   uint32_t* s_vals = reinterpret_cast<uint32_t*>(s_dyn + sizeof(unsigned long long) * kSortTile);
@@ -127,13 +157,13 @@ __global__ void __launch_bounds__(kSortThreads, 2) k_onesweep(
   const long long tile_base = (long long)tile * kSortTile;
   const long long n = pair_count(n_cap, n_dev);
   if (tile_base >= n) return;  // grid sized for the capacity; this tile is empty
+  const int valid = (int)min((long long)kSortTile, n - tile_base);
 
-  // Load: warp w owns keys [tile_base + w*256, +256), 32 consecutive per step,
-  // so (warp, step, lane) is the input order and the ranks below are stable.
+  // Load: warp w owns keys [tile_base + w*32*items, ...), 32 consecutive per
+  // step, so (warp, step, lane) is the input order and the ranks are stable.
   unsigned long long k[kSortItems];
   uint32_t v[kSortItems];
   uint32_t rank[kSortItems];
-  int n_invalid = 0;
 #pragma unroll
   for (int r = 0; r < kSortItems; ++r) {
     const long long idx = tile_base + warp * (kWarp * kSortItems) + r * kWarp + lane;
@@ -143,33 +173,24 @@ __global__ void __launch_bounds__(kSortThreads, 2) k_onesweep(
     } else {
       k[r] = ~0ull;  // digit 255, ranked after every real key of the tile
       v[r] = 0;
-      ++n_invalid;
     }
   }
 #pragma unroll
   for (int r = 0; r < kSortItems; ++r) {
     const uint32_t d = (uint32_t)(k[r] >> shift) & 0xff;
-    const uint32_t peers = __match_any_sync(0xffffffffu, d);
+    const uint32_t peers = digit_peers(d);
     const uint32_t before = s_whist[warp][d];
     __syncwarp();
     if ((peers & lanemask_lt()) == 0) s_whist[warp][d] = before + __popc(peers);
     __syncwarp();
     rank[r] = before + __popc(peers & lanemask_lt());
   }
-  // Padding keys only exist in the last tile and all sit in digit 255.
-  int pad = n_invalid;
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) pad += __shfl_xor_sync(0xffffffffu, pad, o);
-  if (lane == 0) s_tmp[warp] = (uint32_t)pad;
-  __syncthreads();
-  uint32_t pad_total = 0;
-#pragma unroll
-  for (int w = 0; w < kSortWarps; ++w) pad_total += s_tmp[w];
   __syncthreads();
 
-  // Per digit (threads 0..255): warp offsets, tile count, look-back.
+  // Per digit (threads 0..255, warps 0..7): warp offsets, tile count, publish.
   const uint32_t d = (uint32_t)tid;
-  uint32_t cnt = 0, excl = 0;
+  uint32_t cnt = 0, incl = 0;
+  uint32_t* lb = lookback + (size_t)tile * kRadix;
   if (tid < kRadix) {
 #pragma unroll
     for (int w = 0; w < kSortWarps; ++w) {
@@ -177,12 +198,38 @@ __global__ void __launch_bounds__(kSortThreads, 2) k_onesweep(
       s_whist[w][d] = cnt;
       cnt += x;
     }
-    const uint32_t real = (d == 255) ? cnt - pad_total : cnt;
-    uint32_t* lb = lookback + (size_t)tile * kRadix;
-    if (tile == 0) {
-      st_volatile_u32(lb + d, kFlagInc | real);
-    } else {
-      st_volatile_u32(lb + d, kFlagAgg | real);
+    // padding keys (last tile only) all sit in digit 255
+    const uint32_t real = (d == 255) ? cnt - (uint32_t)(kSortTile - valid) : cnt;
+    st_volatile_u32(lb + d, (tile == 0 ? kFlagInc : kFlagAgg) | real);
+    incl = cnt;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t u = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += u;
+    }
+    if (lane == 31) s_tmp[warp] = incl;
+  }
+  __syncthreads();
+  uint32_t toff = 0;
+  if (tid < kRadix) {
+    for (int w = 0; w < warp; ++w) toff += s_tmp[w];
+    toff += incl - cnt;
+    s_toff[d] = toff;
+  }
+  __syncthreads();
+
+  // Local sort of the tile into shared memory.
+#pragma unroll
+  for (int r = 0; r < kSortItems; ++r) {
+    const uint32_t dd = (uint32_t)(k[r] >> shift) & 0xff;
+    const uint32_t slot = s_toff[dd] + s_whist[warp][dd] + rank[r];
+    s_keys[slot] = k[r];
+    s_vals[slot] = v[r];
+  }
+
+  if (tid < kRadix) {
+    uint32_t excl = 0;
+    if (tile != 0) {
       // Windowed look-back: the words of the kLookWindow nearest unvisited
       // predecessors are loaded together (independent loads, one latency),
       // then summed newest first until an inclusive prefix; a word that is
@@ -190,15 +237,15 @@ __global__ void __launch_bounds__(kSortThreads, 2) k_onesweep(
       long long pred = (long long)tile - 1;
       int polls = 0;
       bool done = false;
-      while (!done && pred >= 0) {
+      while (!done) {
         uint32_t w[kLookWindow];
 #pragma unroll
         for (int j = 0; j < kLookWindow; ++j)
-          w[j] = pred - j >= 0 ? ld_volatile_u32(lookback + (size_t)(pred - j) * kRadix + d) : 0u;
+          w[j] = pred - j >= 0 ? ld_volatile_u32(lookback + (size_t)(pred - j) * kRadix + d) : kFlagInc;
         int used = 0;
 #pragma unroll
         for (int j = 0; j < kLookWindow; ++j) {
-          if (done || used != j || pred - j < 0) continue;
+          if (done || used != j) continue;
           const uint32_t flag = w[j] & ~kValueMask;
           if (flag == 0) continue;  // not yet published: stop consuming here
           excl += w[j] & kValueMask;
@@ -214,29 +261,13 @@ __global__ void __launch_bounds__(kSortThreads, 2) k_onesweep(
           __nanosleep(64);
         }
       }
+      const uint32_t real = (d == 255) ? cnt - (uint32_t)(kSortTile - valid) : cnt;
       st_volatile_u32(lb + d, kFlagInc | (excl + real));
     }
-  }
-
-  // Global digit base of this pass, tile-local digit offsets.
-  uint32_t gtot, ttot;
-  const uint32_t gbase = block_excl_scan(tid < kRadix ? hist[d] : 0u, s_tmp, &gtot);
-  const uint32_t toff = block_excl_scan(cnt, s_tmp, &ttot);
-  if (tid < kRadix) {
-    s_toff[d] = toff;
-    s_dst[d] = gbase + excl - toff;  // global position of shared slot i = s_dst[digit] + i
+    s_dst[d] = digit_base[d] + excl - toff;  // global position of shared slot i = s_dst[digit] + i
   }
   __syncthreads();
 
-#pragma unroll
-  for (int r = 0; r < kSortItems; ++r) {
-    const uint32_t dd = (uint32_t)(k[r] >> shift) & 0xff;
-    const uint32_t slot = s_toff[dd] + s_whist[warp][dd] + rank[r];
-    s_keys[slot] = k[r];
-    s_vals[slot] = v[r];
-  }
-  __syncthreads();
-  const int valid = (int)min((long long)kSortTile, n - tile_base);
   for (int j = tid; j < valid; j += kSortThreads) {
     const unsigned long long kk = s_keys[j];
     const uint32_t pos = s_dst[(uint32_t)(kk >> shift) & 0xff] + (uint32_t)j;
@@ -247,6 +278,7 @@ __global__ void __launch_bounds__(kSortThreads, 2) k_onesweep(
       raise_error(kErrTimeout);  // only reachable after an expired look-back
     }
   }
+  __syncthreads();
 }
 
 }  // namespace
@@ -281,20 +313,11 @@ fgs_status run_sort(int64_t n_cap, const int32_t* n_dev, uint32_t tiles, void* t
   {
     KernelTimer kt__(FGS_K_SORT_HIST, s);
     k_histogram<<<hist_blocks, kSortThreads, 0, s>>>(reinterpret_cast<const unsigned long long*>(keys_in), n_cap,
-                                                     n_dev, passes, hist);
+                                                     n_dev, passes, hist, counters + kMaxPasses);
     kt__.stop();
   }
   FGS_LAUNCH_CHECK();
-  // The dynamic shared-memory opt-in is a per-device function attribute; set
-  // once per device (before any capture, by the first call).
-  static std::atomic<bool> smem_set[64];
-  int dev = 0;
-  FGS_TRY(cudaGetDevice(&dev));
-  if (dev < 0 || dev >= 64) return FGS_ERR_UNSUPPORTED;
-  if (!smem_set[dev].load()) {
-    FGS_TRY(cudaFuncSetAttribute(k_onesweep, cudaFuncAttributeMaxDynamicSharedMemorySize, kSortDynSmem));
-    smem_set[dev].store(true);
-  }
+  FGS_TRY(allow_dyn_smem(reinterpret_cast<const void*>(&k_onesweep), kSortDynSmem));
   const unsigned long long* src_k = reinterpret_cast<const unsigned long long*>(keys_in);
   const uint32_t* src_v = values_in;
   for (int p = 0; p < passes; ++p) {
