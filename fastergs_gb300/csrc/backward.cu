@@ -767,7 +767,7 @@ fgs_status run_render_bwd(const Views& views, int64_t records, int bucket_size, 
   if (recompute) FGS_TRY(cudaMemsetAsync(im.tile_stage, 0, sizeof(uint32_t) * views.tiles, s));
   BwdArgs a{views, splat, values_sorted, ranges, sm.bucket_tile, sm.bucket_queue, im.bucket_off, im.bucket_sum,
             im.max_contrib, sm.samples, im.tile_stage, im.pix_color, Ts_final, last_contributor, dL_dpixels,
-            grad_record, bucket_size};
+            grad_record, sub_bucket_size(bucket_size)};
   {
     KernelTimer kt__(FGS_K_RENDER_BWD, s);
     const int nt = kBwdWarps * kWarp;

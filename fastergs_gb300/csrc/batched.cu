@@ -39,7 +39,8 @@ BatchLayout plan(int P, int V, const int* W, const int* H, int bx, int by, int64
     L.tiles += (uint32_t)(((W[v] + bx - 1) / bx) * ((H[v] + by - 1) / by));
     L.pixels += (int64_t)W[v] * H[v];
   }
-  L.buckets = (pairs + bucket_size - 1) / bucket_size + std::min<int64_t>((int64_t)L.tiles, pairs);
+  const int64_t sub = sub_bucket_size(bucket_size);  // sample state is per sub-bucket
+  L.buckets = (pairs + sub - 1) / sub + std::min<int64_t>((int64_t)L.tiles, pairs);
   if (L.buckets < 1) L.buckets = 1;
   L.records_n = (int64_t)V * P;
   L.sort_bytes = sort_temp_bytes(pairs);

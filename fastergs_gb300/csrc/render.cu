@@ -115,10 +115,12 @@ __device__ __forceinline__ void block_scan(uint32_t (&v)[kScanValues], uint32_t 
 
 __global__ void __launch_bounds__(kScanTiles) k_bucket_count(int T, const uint32_t* __restrict__ ranges, int bs,
                                                              uint32_t* __restrict__ block_sums,
-                                                             uint32_t* __restrict__ round_hist) {
+                                                             uint32_t* __restrict__ round_hist,
+                                                             uint32_t* __restrict__ bucket_sum) {
   __shared__ uint32_t s_warp[kScanTiles / 32][kScanValues];
   const int t = blockIdx.x * kScanTiles + threadIdx.x;
   const uint32_t nb = t < T ? tile_buckets(ranges, t, bs) : 0u;
+  if (t == 0) bucket_sum[4] = 0;  // buckets of the stop granularity, summed by k_bucket_fill
   if (t < T) {  // one atomic per distinct count in the warp
     const uint32_t bin = min(nb, (uint32_t)kRounds);
     const uint32_t peers = __match_any_sync(__activemask(), bin);
@@ -200,7 +202,8 @@ __global__ void __launch_bounds__(1024) k_round_offsets(const uint32_t* __restri
 }
 
 __global__ void __launch_bounds__(kScanTiles) k_bucket_fill(int T, const uint32_t* __restrict__ ranges, int bs,
-                                                            long long max_buckets, const uint32_t* __restrict__ block_sums,
+                                                            int split, long long max_buckets,
+                                                            const uint32_t* __restrict__ block_sums,
                                                             const uint32_t* __restrict__ round_off,
                                                             uint32_t* __restrict__ round_fill,
                                                             uint32_t* __restrict__ bucket_off,
@@ -226,6 +229,12 @@ __global__ void __launch_bounds__(kScanTiles) k_bucket_fill(int T, const uint32_
   }
   const int t = blockIdx.x * kScanTiles + tid;
   const uint32_t nb = t < T ? tile_buckets(ranges, t, bs) : 0u;
+  {  // buckets of the stop granularity (FB's count): one atomic per warp
+    uint32_t nf = t < T ? tile_buckets(ranges, t, bs * split) : 0u;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) nf += __shfl_xor_sync(0xffffffffu, nf, o);
+    if (lane == 0 && nf) atomicAdd(bucket_sum + 4, nf);
+  }
   uint32_t v[kScanValues], tot[kScanValues];
   scan_values(nb, v);
   block_scan(v, tot, s_warp);  // its barriers also publish s_base / s_total
@@ -305,7 +314,8 @@ struct FwdArgs {
   int* last_contrib;    // per view (H, W), view k at pix_off
   float* Ts_final;
   uint32_t* max_contrib;
-  int bs;
+  int bs;      // Gaussians per (sub-)bucket
+  int split;   // sub-buckets per bucket of the stop granularity
 };
 
 template <int BX, bool RECOMPUTE>
@@ -349,8 +359,9 @@ __global__ void __launch_bounds__(kFwdWarps * kWarp, 7) k_render_fwd(const FwdAr
 
     // Fold into the tile's prefix (FB's merge, render.cu:285-391, per pixel
     // and in bucket order): C += T_prefix * C_b, T_prefix *= T_b; a pixel
-    // stops after the bucket that takes T below 1e-4, or at the tile's last
-    // bucket, and then writes its outputs.
+    // stops after the bucket of the stop granularity that takes T below 1e-4
+    // (tested after its last sub-bucket only), or at the tile's last bucket,
+    // and then writes its outputs.
     if (bi.local > 0) {
       wait_stage(stage_word, (uint32_t)bi.local, lane);
       // Every pixel of the tile has stopped: nothing to fold, write or publish
@@ -364,6 +375,7 @@ __global__ void __launch_bounds__(kFwdWarps * kWarp, 7) k_render_fwd(const FwdAr
     }
     const int nb_tile = (int)a.bucket_off[bi.tile] - (bi.tile ? (int)a.bucket_off[bi.tile - 1] : 0);
     const bool last_bucket = bi.local == nb_tile - 1;
+    const bool stop_point = (bi.local + 1) % a.split == 0;  // end of a bucket of the stop granularity
     const int ntile = (int)(a.ranges[2 * bi.tile + 1] - a.ranges[2 * bi.tile]);
     const int contrib = min(ntile, (bi.local + 1) * a.bs);
     const uint32_t prev_w = (bi.local > 0 && lane < kPxPerThread) ? ld_volatile_u32(alive_words + lane) : 0u;
@@ -393,7 +405,7 @@ __global__ void __launch_bounds__(kFwdWarps * kWarp, 7) k_render_fwd(const FwdAr
           const float nbl = fmaf(pre.w, Cb[k], pre.z);
           const float nt = pre.w * T[k];
           out[p] = make_float4(nr, ng, nbl, nt);
-          if (nt < kTMin || last_bucket) {
+          if ((stop_point && nt < kTMin) || last_bucket) {
             alive = false;
             const size_t pix = (size_t)py * cam.W + px;
             float* oc = a.out_color + 3 * (size_t)cam.pix_off;
@@ -462,14 +474,15 @@ fgs_status run_render_fwd(const Views& views, int64_t n_cap, const int32_t* n_de
                           cudaStream_t s) {
   fgs_status st = run_tile_ranges(n_cap, n_dev, views.tiles, keys_sorted, ranges, s);
   if (st != FGS_OK) return st;
+  const int split = bucket_split(bucket_size), sub = sub_bucket_size(bucket_size);
   {
     KernelTimer kt__(FGS_K_BUCKET_SETUP, s, 3);
     const unsigned nblk = (views.tiles + kScanTiles - 1) / kScanTiles;
     FGS_TRY(cudaMemsetAsync(im.round_hist, 0, sizeof(uint32_t) * (kRounds + 1), s));
-    k_bucket_count<<<nblk, kScanTiles, 0, s>>>((int)views.tiles, ranges, bucket_size, im.block_sums,
-                                               im.round_hist);
+    k_bucket_count<<<nblk, kScanTiles, 0, s>>>((int)views.tiles, ranges, sub, im.block_sums, im.round_hist,
+                                               im.bucket_sum);
     k_round_offsets<<<1, 1024, 0, s>>>(im.round_hist, im.round_off, im.round_fill);
-    k_bucket_fill<<<nblk, kScanTiles, 0, s>>>((int)views.tiles, ranges, bucket_size, max_buckets, im.block_sums,
+    k_bucket_fill<<<nblk, kScanTiles, 0, s>>>((int)views.tiles, ranges, sub, split, max_buckets, im.block_sums,
                                               im.round_off, im.round_fill, im.bucket_off, sm.bucket_tile,
                                               sm.bucket_queue, im.tile_stage, im.bucket_sum);
     kt__.stop();
@@ -477,7 +490,7 @@ fgs_status run_render_fwd(const Views& views, int64_t n_cap, const int32_t* n_de
   FGS_LAUNCH_CHECK();
   FwdArgs fa{views, splat, values_sorted, ranges, sm.bucket_tile, sm.bucket_queue, im.bucket_off, im.bucket_sum,
              sm.samples, im.tile_stage, im.tile_alive, out_color, im.pix_color, last_contributor, Ts_final,
-             im.max_contrib, bucket_size};
+             im.max_contrib, sub, split};
   {
     KernelTimer kt__(FGS_K_RENDER_FWD, s);
     const int nt = kFwdWarps * kWarp;
@@ -521,8 +534,10 @@ extern "C" int64_t fgs_max_buckets(int64_t num_rendered, int width, int height, 
                                    int bucket_size) {
   if (width <= 0 || height <= 0 || block_x <= 0 || block_y <= 0 || bucket_size <= 0 || num_rendered < 0) return -1;
   const int64_t T = (int64_t)((width + block_x - 1) / block_x) * ((height + block_y - 1) / block_y);
-  // Every tile wastes at most one partially filled bucket.
-  return (num_rendered + bucket_size - 1) / bucket_size + std::min<int64_t>(T, num_rendered);
+  // Sub-buckets (the units of the sample state); every tile wastes at most
+  // one partially filled one.
+  const int64_t sub = bucket_size > kMaxBucket ? bucket_size : sub_bucket_size(bucket_size);
+  return (num_rendered + sub - 1) / sub + std::min<int64_t>(T, num_rendered);
 }
 
 extern "C" fgs_status fgs_state_bytes(int width, int height, int block_x, int block_y, int64_t max_buckets,
@@ -562,10 +577,10 @@ extern "C" fgs_status fgs_render_fwd(int P, int64_t num_rendered, int width, int
                                        max_buckets, false, s);
   if (st != FGS_OK) return st;
   if (bucket_sum_host) {
-    uint32_t hs[2] = {0, 0};
+    uint32_t hs[5] = {0, 0, 0, 0, 0};
     FGS_TRY(cudaMemcpyAsync(hs, im.bucket_sum, sizeof(hs), cudaMemcpyDeviceToHost, s));
     FGS_TRY(cudaStreamSynchronize(s));
-    *bucket_sum_host = hs[1];
+    *bucket_sum_host = hs[4];
     if ((int64_t)hs[1] > max_buckets) return FGS_ERR_CAPACITY;
   }
   return FGS_OK;

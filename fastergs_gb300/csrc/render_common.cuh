@@ -12,6 +12,20 @@ constexpr int kTilePixels = 256;   // block_x * block_y must equal this
 constexpr int kPxPerThread = 8;    // pixels per lane: one warp covers a tile
 constexpr int kMaxBucket = 128;    // largest supported bucket size
 
+// A bucket of bucket_size Gaussians is the merge's stop granularity (FB's
+// BUCKET_SIZE: a pixel stops after the bucket that takes its transmittance
+// below 1e-4).  Buckets larger than kSubBucket are composited as
+// bucket_size / kSubBucket sub-buckets, each with its own prefix sample, and
+// the stop test runs only after a bucket's last sub-bucket, so the outputs
+// keep the bucket's stop semantics while a tile's chain has twice as many
+// links to spread over the GPU.  "Bucket" in the composite kernels, the
+// bookkeeping and the sample state means the sub-bucket.
+constexpr int kSubBucket = 64;
+inline int bucket_split(int bucket_size) {
+  return (bucket_size > kSubBucket && bucket_size % kSubBucket == 0) ? bucket_size / kSubBucket : 1;
+}
+inline int sub_bucket_size(int bucket_size) { return bucket_size / bucket_split(bucket_size); }
+
 // Per-image state (FB ImageState, rasterizer_imp.h:76-88), carved from one
 // caller buffer:  pixel colour planes (3, H*W) without background,
 // per-tile max contributor count, per-tile inclusive bucket offsets, a
@@ -26,7 +40,8 @@ struct ImageState {
   float* pix_color;         // 3 * HW
   uint32_t* max_contrib;    // T
   uint32_t* bucket_off;     // T (inclusive scan of bucket counts)
-  uint32_t* bucket_sum;     // [0] buckets to render, [1] buckets needed, [2], [3] work cursors
+  uint32_t* bucket_sum;     // [0] sub-buckets to render, [1] sub-buckets needed, [2], [3] work
+                            // cursors, [4] buckets of bucket_size (the count FB reports)
   uint32_t* block_sums;     // ceil(T / kScanTiles) x kScanValues
   uint32_t* tile_stage;     // T: buckets of the tile folded into its prefix
   uint32_t* tile_alive;     // T x 8: per 8x4 sub-block, lanes whose pixel is still compositing
@@ -55,7 +70,7 @@ inline ImageState carve_image(void* base, size_t pixels, size_t T) {
   ImageState s;
   size_t off = 0;
   const size_t nblk = (T + kScanTiles - 1) / kScanTiles;
-  s.bucket_sum = reinterpret_cast<uint32_t*>(p + off);  off = align_up(off + 16, 256);
+  s.bucket_sum = reinterpret_cast<uint32_t*>(p + off);  off = align_up(off + 32, 256);
   s.pix_color = reinterpret_cast<float*>(p + off);      off = align_up(off + sizeof(float) * 3 * pixels, 256);
   s.max_contrib = reinterpret_cast<uint32_t*>(p + off); off = align_up(off + sizeof(uint32_t) * T, 256);
   s.bucket_off = reinterpret_cast<uint32_t*>(p + off);  off = align_up(off + sizeof(uint32_t) * T, 256);

@@ -133,7 +133,11 @@ fgs_status fgs_sort_noalloc(int64_t num_rendered, int width, int height, int blo
 fgs_status fgs_tile_ranges(int64_t num_rendered, int num_tiles, const uint64_t* keys_sorted,
                            uint32_t* ranges, void* stream);
 
-/* Upper bound on the bucket count of a frame with num_rendered pairs. */
+/* Upper bound on the composited bucket count of a frame with num_rendered
+ * pairs: the units of the sample state.  bucket_size is the merge's stop
+ * granularity (FB's BUCKET_SIZE, 128); buckets larger than 64 Gaussians are
+ * composited as 64-Gaussian sub-buckets, each with its own prefix sample, and
+ * the transmittance stop is tested only at the end of a full bucket. */
 int64_t fgs_max_buckets(int64_t num_rendered, int width, int height, int block_x, int block_y,
                         int bucket_size);
 
@@ -149,7 +153,8 @@ fgs_status fgs_state_bytes(int width, int height, int block_x, int block_y, int6
  * Replaces faster::render_16x16 (FB csrc/ops.h:96-106, render.cu:393-470).
  * out_color (3,H,W), last_contributor (H,W), Ts_final (H,W) are written.
  * If bucket_sum_host is non-NULL the stream is synchronised at the end and
- * the bucket count is stored there (FB returns it to Python).
+ * the count of buckets of bucket_size Gaussians is stored there (FB returns
+ * it to Python; it does not count sub-buckets).
  */
 fgs_status fgs_render_fwd(int P, int64_t num_rendered, int width, int height, int block_x, int block_y,
                           int bucket_size, const float* splat_buffer, const uint64_t* keys_sorted,

@@ -41,8 +41,11 @@ def test_status_strings_and_version(lib):
 def test_sizing_helpers(lib):
     assert lib.fgs_sort_temp_bytes(0) > 0
     assert lib.fgs_sort_temp_bytes(1 << 20) > 12 * (1 << 20)
-    # one partially filled bucket per tile at most
-    assert lib.fgs_max_buckets(1000, 256, 256, 16, 16, 128) == 8 + 256
+    # counted in composited sub-buckets (64 Gaussians for FB's 128), one
+    # partially filled one per tile at most
+    assert lib.fgs_max_buckets(1000, 256, 256, 16, 16, 128) == 16 + 256
+    assert lib.fgs_max_buckets(1000, 256, 256, 16, 16, 64) == 16 + 256
+    assert lib.fgs_max_buckets(1000, 256, 256, 16, 16, 32) == 32 + 256
     assert lib.fgs_max_buckets(10, 256, 256, 16, 16, 128) == 1 + 10
     ib, sb = C.c_size_t(0), C.c_size_t(0)
     assert lib.fgs_state_bytes(256, 256, 16, 16, 100, C.byref(ib), C.byref(sb)) == 0
