@@ -362,68 +362,83 @@ __global__ void __launch_bounds__(kFwdWarps * kWarp, 7) k_render_fwd(const FwdAr
     // stops after the bucket of the stop granularity that takes T below 1e-4
     // (tested after its last sub-bucket only), or at the tile's last bucket,
     // and then writes its outputs.
-    if (bi.local > 0) {
-      wait_stage(stage_word, (uint32_t)bi.local, lane);
-      // Every pixel of the tile has stopped: nothing to fold, write or publish
-      // (kStageDead already satisfies the waits of every later bucket).
-      uint32_t sw = lane == 0 ? ld_acquire_u32(stage_word) : 0u;
-      sw = __shfl_sync(0xffffffffu, sw, 0);
-      if (sw == kStageDead) {
-        q = q_next;
-        continue;
-      }
-    }
+    // Independent of the chain: read before the wait.
     const int nb_tile = (int)a.bucket_off[bi.tile] - (bi.tile ? (int)a.bucket_off[bi.tile - 1] : 0);
     const bool last_bucket = bi.local == nb_tile - 1;
     const bool stop_point = (bi.local + 1) % a.split == 0;  // end of a bucket of the stop granularity
     const int ntile = (int)(a.ranges[2 * bi.tile + 1] - a.ranges[2 * bi.tile]);
     const int contrib = min(ntile, (bi.local + 1) * a.bs);
-    const uint32_t prev_w = (bi.local > 0 && lane < kPxPerThread) ? ld_volatile_u32(alive_words + lane) : 0u;
     const size_t HW = (size_t)cam.W * cam.H;
     float4* out = a.samples + (size_t)(RECOMPUTE ? bi.tile : b) * kTilePixels;
     const float4* prev = RECOMPUTE ? out : a.samples + (size_t)(b - 1) * kTilePixels;
+    // The link of the tile's chain: wait for bucket k-1's fold, then load the
+    // alive words with the first half of the prefix samples, and the second
+    // half after the first is folded (two round trips; the samples of pixels
+    // that stopped are read and ignored).
+    uint32_t prev_w = 0u;
+    if (bi.local > 0) {
+      // Every pixel of the tile has stopped: nothing to fold, write or publish
+      // (kStageDead already satisfies the waits of every later bucket).
+      if (wait_stage(stage_word, (uint32_t)bi.local, lane) == kStageDead) {
+        q = q_next;
+        continue;
+      }
+      if (lane < kPxPerThread) prev_w = ld_volatile_u32(alive_words + lane);
+    }
     bool any_before = false, any_after = false;
     uint32_t my_word = 0;
+    constexpr int kHalfRows = M::kRows / 2;
 #pragma unroll
-    for (int r = 0; r < M::kRows; ++r)
+    for (int h = 0; h < 2; ++h) {
+      float4 pre[kHalfRows * M::kCols];
 #pragma unroll
-      for (int cc = 0; cc < M::kCols; ++cc) {
-        const int k = r * M::kCols + cc;
-        const int p = M::pix(r, cc, lane);
-        const int px = tx0 + 8 * cc + (lane & 7), py = ty0 + 4 * r + (lane >> 3);
-        bool alive;
-        if (bi.local == 0) {
-          alive = px < cam.W && py < cam.H;
-        } else {
-          alive = (__shfl_sync(0xffffffffu, prev_w, k) >> lane) & 1u;
-        }
-        any_before |= __any_sync(0xffffffffu, alive);
-        if (alive) {
-          const float4 pre = bi.local > 0 ? __ldcg(prev + p) : make_float4(0.f, 0.f, 0.f, 1.f);
-          const float nr = fmaf(pre.w, Cr[k], pre.x);
-          const float ng = fmaf(pre.w, Cg[k], pre.y);
-          const float nbl = fmaf(pre.w, Cb[k], pre.z);
-          const float nt = pre.w * T[k];
-          out[p] = make_float4(nr, ng, nbl, nt);
-          if ((stop_point && nt < kTMin) || last_bucket) {
-            alive = false;
-            const size_t pix = (size_t)py * cam.W + px;
-            float* oc = a.out_color + 3 * (size_t)cam.pix_off;
-            float* pc = a.pix_color + 3 * (size_t)cam.pix_off;
-            oc[pix] = nr + nt * cam.bg[0];
-            oc[HW + pix] = ng + nt * cam.bg[1];
-            oc[2 * HW + pix] = nbl + nt * cam.bg[2];
-            pc[pix] = nr;
-            pc[HW + pix] = ng;
-            pc[2 * HW + pix] = nbl;
-            a.last_contrib[cam.pix_off + pix] = contrib;
-            a.Ts_final[cam.pix_off + pix] = nt;
+      for (int rr = 0; rr < kHalfRows; ++rr)
+#pragma unroll
+        for (int cc = 0; cc < M::kCols; ++cc)
+          pre[rr * M::kCols + cc] = bi.local > 0 ? __ldcg(prev + M::pix(h * kHalfRows + rr, cc, lane))
+                                                 : make_float4(0.f, 0.f, 0.f, 1.f);
+#pragma unroll
+      for (int rr = 0; rr < kHalfRows; ++rr)
+#pragma unroll
+        for (int cc = 0; cc < M::kCols; ++cc) {
+          const int r = h * kHalfRows + rr;
+          const int k = r * M::kCols + cc;
+          const float4 pk = pre[rr * M::kCols + cc];
+          const int p = M::pix(r, cc, lane);
+          const int px = tx0 + 8 * cc + (lane & 7), py = ty0 + 4 * r + (lane >> 3);
+          bool alive;
+          if (bi.local == 0) {
+            alive = px < cam.W && py < cam.H;
+          } else {
+            alive = (__shfl_sync(0xffffffffu, prev_w, k) >> lane) & 1u;
           }
+          any_before |= __any_sync(0xffffffffu, alive);
+          if (alive) {
+            const float nr = fmaf(pk.w, Cr[k], pk.x);
+            const float ng = fmaf(pk.w, Cg[k], pk.y);
+            const float nbl = fmaf(pk.w, Cb[k], pk.z);
+            const float nt = pk.w * T[k];
+            out[p] = make_float4(nr, ng, nbl, nt);
+            if ((stop_point && nt < kTMin) || last_bucket) {
+              alive = false;
+              const size_t pix = (size_t)py * cam.W + px;
+              float* oc = a.out_color + 3 * (size_t)cam.pix_off;
+              float* pc = a.pix_color + 3 * (size_t)cam.pix_off;
+              oc[pix] = nr + nt * cam.bg[0];
+              oc[HW + pix] = ng + nt * cam.bg[1];
+              oc[2 * HW + pix] = nbl + nt * cam.bg[2];
+              pc[pix] = nr;
+              pc[HW + pix] = ng;
+              pc[2 * HW + pix] = nbl;
+              a.last_contrib[cam.pix_off + pix] = contrib;
+              a.Ts_final[cam.pix_off + pix] = nt;
+            }
+          }
+          const uint32_t word = __ballot_sync(0xffffffffu, alive);
+          any_after |= word != 0u;
+          if (lane == k) my_word = word;
         }
-        const uint32_t word = __ballot_sync(0xffffffffu, alive);
-        any_after |= word != 0u;
-        if (lane == k) my_word = word;
-      }
+    }
     if (lane < kPxPerThread) st_volatile_u32(alive_words + lane, my_word);
     if (lane == 0 && any_before && !any_after) a.max_contrib[bi.tile] = (uint32_t)contrib;
     // The bucket that stops the tile's last pixel ends the chain: its later

@@ -253,7 +253,9 @@ constexpr uint32_t kStageDead = 0xffffffffu;
 // Lane 0 polls (bounded); the bucket it waits for was handed out earlier and
 // its warp is running, so the wait ends unless something is broken, in which
 // case the timeout bit is raised and the warp carries on.
-__device__ __forceinline__ void wait_stage(const uint32_t* tile_stage, uint32_t stage, int lane) {
+// Returns the stage every lane acquired (>= stage unless the wait expired;
+// kStageDead when the tile's last pixel has stopped).
+__device__ __forceinline__ uint32_t wait_stage(const uint32_t* tile_stage, uint32_t stage, int lane) {
   if (lane == 0) {
     int spins = 0;
     while (ld_acquire_u32(tile_stage) < stage) {
@@ -265,7 +267,7 @@ __device__ __forceinline__ void wait_stage(const uint32_t* tile_stage, uint32_t 
     }
   }
   __syncwarp();
-  (void)ld_acquire_u32(tile_stage);  // every lane acquires the folded prefix
+  return ld_acquire_u32(tile_stage);  // every lane acquires the folded prefix
 }
 
 // Publishes that the tile's first `stage` buckets are folded (after every
