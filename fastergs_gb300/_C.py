@@ -25,7 +25,7 @@ TILE = 16
 BUCKET = 128
 # Sample-state rows are sized so the buffer's first dimension encodes the
 # bucket capacity the forward reserved: rows = max_buckets + 1.
-_SAMPLE_ROW = 4104  # per bucket: 256 x 16-byte samples, owner tile, queue slot
+_SAMPLE_ROW = 4120  # per bucket: 256 x 16-byte samples, owner tile, queue slot, live-list entry
 
 
 def _ptr(t: torch.Tensor | None) -> int:

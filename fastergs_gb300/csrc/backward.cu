@@ -30,6 +30,7 @@ struct BwdArgs {
   const uint32_t* ranges;
   const uint32_t* bucket_tile;
   const uint32_t* bucket_queue;
+  const uint4* live;
   const uint32_t* bucket_off;
   uint32_t* bucket_sum;
   const uint32_t* max_contrib;
@@ -86,6 +87,36 @@ __device__ __forceinline__ int warp_value_of(int lane) {
   return (c && d) ? -1 : (d + 2 * c) + 3 * b + 6 * a;
 }
 
+// The backward's work list in store mode: the forward's queue without the
+// buckets that no pixel reaches (past the tile's last contributor; ~3 in 4 at
+// C2), each entry holding what the backward needs to start the bucket, so a
+// warp pays one prefetched load per bucket instead of a chain of dependent
+// reads per queue slot.  Order: the queue's, warp by warp.
+__global__ void __launch_bounds__(256) k_live_buckets(uint32_t* bucket_sum, const uint32_t* __restrict__ queue,
+                                                      const uint32_t* __restrict__ bucket_tile,
+                                                      const uint32_t* __restrict__ bucket_off,
+                                                      const uint32_t* __restrict__ ranges,
+                                                      const uint32_t* __restrict__ max_contrib, int bs,
+                                                      uint4* __restrict__ live) {
+  const int q = blockIdx.x * 256 + threadIdx.x, lane = threadIdx.x & 31;
+  const int B = (int)bucket_sum[0];
+  bool keep = false;
+  uint4 e = make_uint4(0u, 0u, 0u, 0u);
+  if (q < B) {
+    const int b = (int)queue[q];
+    const BucketInfo bi = bucket_info(b, bucket_tile, bucket_off, ranges, bs);
+    keep = (uint32_t)(bi.local * bs) < max_contrib[bi.tile];
+    e = make_uint4((uint32_t)b, (uint32_t)bi.tile, (uint32_t)bi.start, ((uint32_t)bi.local << 8) | (uint32_t)bi.n);
+  }
+  const uint32_t m = __ballot_sync(0xffffffffu, keep);
+  if (m == 0u) return;  // warp-uniform
+  const int leader = __ffs(m) - 1;
+  uint32_t base = 0;
+  if (lane == leader) base = atomicAdd(bucket_sum + 5, (uint32_t)__popc(m));
+  base = __shfl_sync(0xffffffffu, base, leader);
+  if (keep) live[base + __popc(m & lanemask_lt())] = e;
+}
+
 // ABS: also sum |dL/dmean2D| per Gaussian (dmean2D.zw, for the
 // xyz_gradient_accum_abs statistic); without it those two slots stay zero.
 template <int BX, bool RECOMPUTE, bool ABS>
@@ -98,17 +129,33 @@ __global__ void __launch_bounds__(kBwdWarps * kWarp, 5) k_render_bwd(const BwdAr
   __shared__ float4 s_lk[kBwdWarps][kTilePixels];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   BucketStage& st = s_stage[warp];
-  const int B = (int)a.bucket_sum[0];
+  const int B = (int)a.bucket_sum[RECOMPUTE ? 0 : 5];
   const int vid = warp_value_of(lane);  // value a lane holds after the transpose reduction
 
-  // Buckets in the forward's queue order (round by round), so that in
-  // recompute mode a tile's bucket k is always handed out after bucket k-1.
-  for (int q = next_bucket(a.bucket_sum + 3, lane); q < B;) {
-    const int q_next = next_bucket(a.bucket_sum + 3, lane);
-    const int b = (int)a.bucket_queue[q];
-    const BucketInfo bi = bucket_info(b, a.bucket_tile, a.bucket_off, a.ranges, a.bs);
+  // Store mode: the live-bucket list (k_live_buckets), one 16-byte entry per
+  // bucket, the next entry loaded while the current bucket is processed.
+  // Recompute mode: the forward's queue order (round by round), so that a
+  // tile's bucket k is always handed out after bucket k-1.
+  int q = next_bucket(a.bucket_sum + 3, lane), q_next = 0;
+  uint4 e_cur = make_uint4(0u, 0u, 0u, 0u), e_next = e_cur;
+  if (!RECOMPUTE && q < B) e_cur = a.live[q];
+  for (; q < B; q = q_next, e_cur = e_next) {
+    q_next = next_bucket(a.bucket_sum + 3, lane);
+    if (!RECOMPUTE && q_next < B) e_next = a.live[q_next];
+    int b;
+    BucketInfo bi;
+    if (RECOMPUTE) {
+      b = (int)a.bucket_queue[q];
+      bi = bucket_info(b, a.bucket_tile, a.bucket_off, a.ranges, a.bs);
+    } else {
+      b = (int)e_cur.x;
+      bi.tile = (int)e_cur.y;
+      bi.start = (int)e_cur.z;
+      bi.local = (int)(e_cur.w >> 8);
+      bi.n = (int)(e_cur.w & 0xffu);
+    }
     const uint32_t thres = (uint32_t)(bi.local * a.bs);
-    if (thres >= a.max_contrib[bi.tile]) {  // no pixel of the tile reaches this bucket
+    if (RECOMPUTE && thres >= a.max_contrib[bi.tile]) {  // no pixel of the tile reaches this bucket
       q = q_next;
       continue;
     }
@@ -761,13 +808,23 @@ fgs_status run_render_bwd(const Views& views, int64_t records, int bucket_size, 
                           const float* dL_dpixels, float* grad_record, bool recompute, bool abs_grad,
                           cudaStream_t s) {
   FGS_TRY(cudaMemsetAsync(grad_record, 0, sizeof(float) * FGS_GRAD_STRIDE * (size_t)records, s));
-  // backward work cursor (word 3 of the image-state header); reset on every call
-  FGS_TRY(cudaMemsetAsync(im.bucket_sum + 3, 0, sizeof(uint32_t), s));
+  // backward work cursor and live-list count (words 3 and 5 of the
+  // image-state header); reset on every call
+  FGS_TRY(cudaMemsetAsync(im.bucket_sum + 3, 0, 3 * sizeof(uint32_t), s));
   // recompute mode rebuilds every tile's prefix from the start
   if (recompute) FGS_TRY(cudaMemsetAsync(im.tile_stage, 0, sizeof(uint32_t) * views.tiles, s));
-  BwdArgs a{views, splat, values_sorted, ranges, sm.bucket_tile, sm.bucket_queue, im.bucket_off, im.bucket_sum,
-            im.max_contrib, sm.samples, im.tile_stage, im.pix_color, Ts_final, last_contributor, dL_dpixels,
-            grad_record, sub_bucket_size(bucket_size)};
+  const int sub = sub_bucket_size(bucket_size);
+  if (!recompute) {
+    KernelTimer kt__(FGS_K_BWD_LIST, s);
+    const unsigned blocks = (unsigned)((std::max<int64_t>(sm.max_buckets, 1) + 255) / 256);
+    k_live_buckets<<<blocks, 256, 0, s>>>(im.bucket_sum, sm.bucket_queue, sm.bucket_tile, im.bucket_off, ranges,
+                                          im.max_contrib, sub, sm.live);
+    kt__.stop();
+    FGS_LAUNCH_CHECK();
+  }
+  BwdArgs a{views, splat, values_sorted, ranges, sm.bucket_tile, sm.bucket_queue, sm.live, im.bucket_off,
+            im.bucket_sum, im.max_contrib, sm.samples, im.tile_stage, im.pix_color, Ts_final, last_contributor,
+            dL_dpixels, grad_record, sub};
   {
     KernelTimer kt__(FGS_K_RENDER_BWD, s);
     const int nt = kBwdWarps * kWarp;

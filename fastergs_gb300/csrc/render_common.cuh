@@ -41,7 +41,8 @@ struct ImageState {
   uint32_t* max_contrib;    // T
   uint32_t* bucket_off;     // T (inclusive scan of bucket counts)
   uint32_t* bucket_sum;     // [0] sub-buckets to render, [1] sub-buckets needed, [2], [3] work
-                            // cursors, [4] buckets of bucket_size (the count FB reports)
+                            // cursors, [4] buckets of bucket_size (the count FB reports),
+                            // [5] entries of the backward's live-bucket list
   uint32_t* block_sums;     // ceil(T / kScanTiles) x kScanValues
   uint32_t* tile_stage;     // T: buckets of the tile folded into its prefix
   uint32_t* tile_alive;     // T x 8: per 8x4 sub-block, lanes whose pixel is still compositing
@@ -58,7 +59,10 @@ struct ImageState {
 struct SampleState {
   uint32_t* bucket_tile;    // max_buckets
   uint32_t* bucket_queue;   // max_buckets: forward processing order
+  uint4* live;              // max_buckets: the backward's work list (store mode), one entry per
+                            // bucket that some pixel reaches: bucket, tile, first pair, local << 8 | n
   float4* samples;          // max_buckets * 256
+  int64_t max_buckets;
   size_t bytes;
 };
 
@@ -92,7 +96,9 @@ inline SampleState carve_sample(void* base, int64_t max_buckets, int64_t slots) 
   size_t off = 0;
   s.bucket_tile = reinterpret_cast<uint32_t*>(p + off); off = align_up(off + sizeof(uint32_t) * (size_t)max_buckets, 256);
   s.bucket_queue = reinterpret_cast<uint32_t*>(p + off); off = align_up(off + sizeof(uint32_t) * (size_t)max_buckets, 256);
+  s.live = reinterpret_cast<uint4*>(p + off);           off = align_up(off + sizeof(uint4) * (size_t)max_buckets, 256);
   s.samples = reinterpret_cast<float4*>(p + off);       off = align_up(off + sizeof(float4) * kTilePixels * (size_t)slots, 256);
+  s.max_buckets = max_buckets;
   s.bytes = off;
   return s;
 }
