@@ -28,8 +28,7 @@ struct BwdArgs {
   const float* splat;
   const uint32_t* vals;
   const uint32_t* ranges;
-  const uint32_t* bucket_tile;
-  const uint32_t* bucket_queue;
+  const uint2* bucket_queue;
   const uint4* live;
   const uint32_t* bucket_off;
   uint32_t* bucket_sum;
@@ -92,8 +91,7 @@ __device__ __forceinline__ int warp_value_of(int lane) {
 // C2), each entry holding what the backward needs to start the bucket, so a
 // warp pays one prefetched load per bucket instead of a chain of dependent
 // reads per queue slot.  Order: the queue's, warp by warp.
-__global__ void __launch_bounds__(256) k_live_buckets(uint32_t* bucket_sum, const uint32_t* __restrict__ queue,
-                                                      const uint32_t* __restrict__ bucket_tile,
+__global__ void __launch_bounds__(256) k_live_buckets(uint32_t* bucket_sum, const uint2* __restrict__ queue,
                                                       const uint32_t* __restrict__ bucket_off,
                                                       const uint32_t* __restrict__ ranges,
                                                       const uint32_t* __restrict__ max_contrib, int bs,
@@ -103,10 +101,9 @@ __global__ void __launch_bounds__(256) k_live_buckets(uint32_t* bucket_sum, cons
   bool keep = false;
   uint4 e = make_uint4(0u, 0u, 0u, 0u);
   if (q < B) {
-    const int b = (int)queue[q];
-    const BucketInfo bi = bucket_info(b, bucket_tile, bucket_off, ranges, bs);
+    const BucketInfo bi = bucket_info(queue[q], bucket_off, ranges, bs);
     keep = (uint32_t)(bi.local * bs) < max_contrib[bi.tile];
-    e = make_uint4((uint32_t)b, (uint32_t)bi.tile, (uint32_t)bi.start, ((uint32_t)bi.local << 8) | (uint32_t)bi.n);
+    e = make_uint4((uint32_t)bi.b, (uint32_t)bi.tile, (uint32_t)bi.start, ((uint32_t)bi.local << 8) | (uint32_t)bi.n);
   }
   const uint32_t m = __ballot_sync(0xffffffffu, keep);
   if (m == 0u) return;  // warp-uniform
@@ -145,8 +142,8 @@ __global__ void __launch_bounds__(kBwdWarps * kWarp, 5) k_render_bwd(const BwdAr
     int b;
     BucketInfo bi;
     if (RECOMPUTE) {
-      b = (int)a.bucket_queue[q];
-      bi = bucket_info(b, a.bucket_tile, a.bucket_off, a.ranges, a.bs);
+      bi = bucket_info(a.bucket_queue[q], a.bucket_off, a.ranges, a.bs);
+      b = bi.b;
     } else {
       b = (int)e_cur.x;
       bi.tile = (int)e_cur.y;
@@ -817,12 +814,12 @@ fgs_status run_render_bwd(const Views& views, int64_t records, int bucket_size, 
   if (!recompute) {
     KernelTimer kt__(FGS_K_BWD_LIST, s);
     const unsigned blocks = (unsigned)((std::max<int64_t>(sm.max_buckets, 1) + 255) / 256);
-    k_live_buckets<<<blocks, 256, 0, s>>>(im.bucket_sum, sm.bucket_queue, sm.bucket_tile, im.bucket_off, ranges,
-                                          im.max_contrib, sub, sm.live);
+    k_live_buckets<<<blocks, 256, 0, s>>>(im.bucket_sum, sm.bucket_queue, im.bucket_off, ranges, im.max_contrib,
+                                          sub, sm.live);
     kt__.stop();
     FGS_LAUNCH_CHECK();
   }
-  BwdArgs a{views, splat, values_sorted, ranges, sm.bucket_tile, sm.bucket_queue, sm.live, im.bucket_off,
+  BwdArgs a{views, splat, values_sorted, ranges, sm.bucket_queue, sm.live, im.bucket_off,
             im.bucket_sum, im.max_contrib, sm.samples, im.tile_stage, im.pix_color, Ts_final, last_contributor,
             dL_dpixels, grad_record, sub};
   {

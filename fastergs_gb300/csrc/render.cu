@@ -207,8 +207,7 @@ __global__ void __launch_bounds__(kScanTiles) k_bucket_fill(int T, const uint32_
                                                             const uint32_t* __restrict__ round_off,
                                                             uint32_t* __restrict__ round_fill,
                                                             uint32_t* __restrict__ bucket_off,
-                                                            uint32_t* __restrict__ bucket_tile,
-                                                            uint32_t* __restrict__ bucket_queue,
+                                                            uint2* __restrict__ bucket_queue,
                                                             uint32_t* __restrict__ tile_stage, uint32_t* bucket_sum) {
   __shared__ uint32_t s_warp[kScanTiles / 32][kScanValues];
   __shared__ uint32_t s_base[kScanValues], s_total[kScanValues];
@@ -247,7 +246,6 @@ __global__ void __launch_bounds__(kScanTiles) k_bucket_fill(int T, const uint32_
     if (overflow) raise_error(kErrCapacity);
   }
   const uint32_t end = s_base[1] + v[1];
-  const uint32_t b0 = end - nb;
   if (t < T) {
     tile_stage[t] = 0;
     bucket_off[t] = end;
@@ -262,12 +260,11 @@ __global__ void __launch_bounds__(kScanTiles) k_bucket_fill(int T, const uint32_
     uint32_t base = 0;
     if (lane == leader) base = atomicAdd(round_fill + k, (uint32_t)__popc(act));
     base = __shfl_sync(0xffffffffu, base, leader);
-    if (k < nr) bucket_queue[round_off[k] + base + __popc(act & lanemask_lt())] = b0 + k;
+    if (k < nr) bucket_queue[round_off[k] + base + __popc(act & lanemask_lt())] = make_uint2((uint32_t)t, k);
   }
   if (t >= T) return;
   const uint32_t tail = round_off[kRounds] + s_base[0] + v[0] - (nb > kRounds ? nb - kRounds : 0u);
-  for (uint32_t k = kRounds; k < nb; ++k) bucket_queue[tail + (k - kRounds)] = b0 + k;
-  for (uint32_t j = 0; j < nb; ++j) bucket_tile[b0 + j] = (uint32_t)t;
+  for (uint32_t k = kRounds; k < nb; ++k) bucket_queue[tail + (k - kRounds)] = make_uint2((uint32_t)t, k);
 }
 
 // Tiles without buckets (and every tile when the buckets did not fit): the
@@ -302,8 +299,7 @@ struct FwdArgs {
   const float* splat;
   const uint32_t* vals;
   const uint32_t* ranges;
-  const uint32_t* bucket_tile;
-  const uint32_t* bucket_queue;
+  const uint2* bucket_queue;
   const uint32_t* bucket_off;
   uint32_t* bucket_sum;
   float4* samples;
@@ -326,10 +322,16 @@ __global__ void __launch_bounds__(kFwdWarps * kWarp, 7) k_render_fwd(const FwdAr
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   BucketStage& st = s_stage[warp];
   const int B = (int)a.bucket_sum[0];
-  for (int q = next_bucket(a.bucket_sum + 2, lane); q < B;) {
-    const int q_next = next_bucket(a.bucket_sum + 2, lane);
-    const int b = (int)a.bucket_queue[q];
-    const BucketInfo bi = bucket_info(b, a.bucket_tile, a.bucket_off, a.ranges, a.bs);
+  // Queue entries are prefetched one ahead; a bucket's own reads (offsets,
+  // tile range, stage and alive words) are independent of one another.
+  int q = next_bucket(a.bucket_sum + 2, lane), q_next = 0;
+  uint2 e_cur = make_uint2(0u, 0u), e_next = e_cur;
+  if (q < B) e_cur = a.bucket_queue[q];
+  for (; q < B; q = q_next, e_cur = e_next) {
+    q_next = next_bucket(a.bucket_sum + 2, lane);
+    if (q_next < B) e_next = a.bucket_queue[q_next];
+    const BucketInfo bi = bucket_info(e_cur, a.bucket_off, a.ranges, a.bs);
+    const int b = bi.b;
     const ViewDesc& cam = a.views.v[a.views.of_tile((uint32_t)bi.tile)];
     const int lt = bi.tile - (int)cam.tile_off;  // tile index inside its view
     const int tx0 = (lt % cam.gx) * BX, ty0 = (lt / cam.gx) * BY;
@@ -337,11 +339,17 @@ __global__ void __launch_bounds__(kFwdWarps * kWarp, 7) k_render_fwd(const FwdAr
     uint32_t* alive_words = a.tile_alive + (size_t)bi.tile * kPxPerThread;
 
     // Sub-blocks that may still need this bucket: from whatever prefix state
-    // the tile has published so far (a superset of the state after bucket k-1).
+    // the tile has published so far (a superset of the state after bucket k-1;
+    // the alive words are read together with the stage and used once it shows
+    // that some bucket was folded).
     uint32_t spec = (1u << kPxPerThread) - 1u;
     if (bi.local > 0) {
       uint32_t w = 0u;
-      if (lane < kPxPerThread) w = ld_acquire_u32(stage_word) > 0 ? ld_volatile_u32(alive_words + lane) : ~0u;
+      if (lane < kPxPerThread) {
+        const uint32_t sw = ld_acquire_u32(stage_word);
+        const uint32_t aw = ld_volatile_u32(alive_words + lane);
+        w = sw > 0 ? aw : ~0u;
+      }
       spec = __ballot_sync(0xffffffffu, w != 0u);
     }
 
@@ -362,9 +370,7 @@ __global__ void __launch_bounds__(kFwdWarps * kWarp, 7) k_render_fwd(const FwdAr
     // stops after the bucket of the stop granularity that takes T below 1e-4
     // (tested after its last sub-bucket only), or at the tile's last bucket,
     // and then writes its outputs.
-    // Independent of the chain: read before the wait.
-    const int nb_tile = (int)a.bucket_off[bi.tile] - (bi.tile ? (int)a.bucket_off[bi.tile - 1] : 0);
-    const bool last_bucket = bi.local == nb_tile - 1;
+    const bool last_bucket = bi.local == bi.nb_tile - 1;
     const bool stop_point = (bi.local + 1) % a.split == 0;  // end of a bucket of the stop granularity
     const int ntile = (int)(a.ranges[2 * bi.tile + 1] - a.ranges[2 * bi.tile]);
     const int contrib = min(ntile, (bi.local + 1) * a.bs);
@@ -498,12 +504,12 @@ fgs_status run_render_fwd(const Views& views, int64_t n_cap, const int32_t* n_de
                                                im.bucket_sum);
     k_round_offsets<<<1, 1024, 0, s>>>(im.round_hist, im.round_off, im.round_fill);
     k_bucket_fill<<<nblk, kScanTiles, 0, s>>>((int)views.tiles, ranges, sub, split, max_buckets, im.block_sums,
-                                              im.round_off, im.round_fill, im.bucket_off, sm.bucket_tile,
-                                              sm.bucket_queue, im.tile_stage, im.bucket_sum);
+                                              im.round_off, im.round_fill, im.bucket_off, sm.bucket_queue,
+                                              im.tile_stage, im.bucket_sum);
     kt__.stop();
   }
   FGS_LAUNCH_CHECK();
-  FwdArgs fa{views, splat, values_sorted, ranges, sm.bucket_tile, sm.bucket_queue, im.bucket_off, im.bucket_sum,
+  FwdArgs fa{views, splat, values_sorted, ranges, sm.bucket_queue, im.bucket_off, im.bucket_sum,
              sm.samples, im.tile_stage, im.tile_alive, out_color, im.pix_color, last_contributor, Ts_final,
              im.max_contrib, sub, split};
   {

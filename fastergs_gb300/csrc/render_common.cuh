@@ -52,13 +52,12 @@ struct ImageState {
   size_t bytes;
 };
 
-// Per-bucket state (FB SampleState, rasterizer_imp.h:91-102): the owning tile
-// of each bucket, the forward work queue, and per (bucket, pixel) a float4
+// Per-bucket state (FB SampleState, rasterizer_imp.h:91-102): the forward work
+// queue (each entry names its tile), the backward's live list, and per (bucket, pixel) a float4
 // (C.rgb, T) holding the running prefix after the bucket, which is all the
 // backward needs (16 bytes per pixel and bucket instead of FB's 40).
 struct SampleState {
-  uint32_t* bucket_tile;    // max_buckets
-  uint32_t* bucket_queue;   // max_buckets: forward processing order
+  uint2* bucket_queue;      // max_buckets: forward processing order, entries (tile, local index)
   uint4* live;              // max_buckets: the backward's work list (store mode), one entry per
                             // bucket that some pixel reaches: bucket, tile, first pair, local << 8 | n
   float4* samples;          // max_buckets * 256
@@ -94,8 +93,7 @@ inline SampleState carve_sample(void* base, int64_t max_buckets, int64_t slots) 
   char* p = static_cast<char*>(base);
   SampleState s;
   size_t off = 0;
-  s.bucket_tile = reinterpret_cast<uint32_t*>(p + off); off = align_up(off + sizeof(uint32_t) * (size_t)max_buckets, 256);
-  s.bucket_queue = reinterpret_cast<uint32_t*>(p + off); off = align_up(off + sizeof(uint32_t) * (size_t)max_buckets, 256);
+  s.bucket_queue = reinterpret_cast<uint2*>(p + off);   off = align_up(off + sizeof(uint2) * (size_t)max_buckets, 256);
   s.live = reinterpret_cast<uint4*>(p + off);           off = align_up(off + sizeof(uint4) * (size_t)max_buckets, 256);
   s.samples = reinterpret_cast<float4*>(p + off);       off = align_up(off + sizeof(float4) * kTilePixels * (size_t)slots, 256);
   s.max_buckets = max_buckets;
@@ -316,15 +314,20 @@ inline int resident_blocks(K kernel, int threads, size_t smem) {
 // Bucket b -> (tile, first pair, pair count, index of the bucket in its tile).
 struct BucketInfo {
   int tile, start, n, local;
+  int b;        // global bucket index (sample slot)
+  int nb_tile;  // buckets of the tile
 };
-__device__ __forceinline__ BucketInfo bucket_info(int b, const uint32_t* __restrict__ bucket_tile,
-                                                  const uint32_t* __restrict__ bucket_off,
+// The bucket of queue entry (tile, local): the four reads are independent.
+__device__ __forceinline__ BucketInfo bucket_info(uint2 qe, const uint32_t* __restrict__ bucket_off,
                                                   const uint32_t* __restrict__ ranges, int bs) {
   BucketInfo bi;
-  bi.tile = (int)bucket_tile[b];
+  bi.tile = (int)qe.x;
+  bi.local = (int)qe.y;
   const int first = bi.tile ? (int)bucket_off[bi.tile - 1] : 0;
-  bi.local = b - first;
+  const int last = (int)bucket_off[bi.tile];
   const int rs = (int)ranges[2 * bi.tile], re = (int)ranges[2 * bi.tile + 1];
+  bi.b = first + bi.local;
+  bi.nb_tile = last - first;
   bi.start = rs + bi.local * bs;
   bi.n = min(bs, re - bi.start);
   return bi;
