@@ -22,6 +22,10 @@ namespace fgs {
 namespace {
 
 constexpr int kBwdWarps = 4;
+// Preprocess backward: Gaussians per block and blocks per SM (128 registers
+// a thread; SH rows and dL/dsh staged in 2 x 24 KB of shared memory a block).
+constexpr int kPbwdThreads = 128;
+constexpr int kPbwdBlocks = 4;
 
 struct BwdArgs {
   Views views;
@@ -699,18 +703,18 @@ __device__ __forceinline__ void adam_rest_rows(const PbwdArgs& a, int first, int
     float4* B4 = reinterpret_cast<float4*>(pm2);
     const float4* C4 = reinterpret_cast<const float4*>(s_co);
     const float4* G4 = reinterpret_cast<const float4*>(s_g);
-    // Row of element j: floor((j + 1/2) / row) in FP32.  j < 256 row and
+    // Row of element j: floor((j + 1/2) / row) in FP32.  j < kPbwdThreads row and
     // 3 <= row <= 48, so the product is off by less than 5e-4 while the exact
     // quotient stays at least 1 / (2 row) > 0.01 away from an integer
     // (tests/test_capi_cpu.py checks every row and j).
     const float inv_row = 1.f / (float)row;
-    for (int q0 = threadIdx.x; q0 < n4; q0 += 256 * kRestUnroll) {
+    for (int q0 = threadIdx.x; q0 < n4; q0 += kPbwdThreads * kRestUnroll) {
       float4 pv[kRestUnroll], av[kRestUnroll], bv[kRestUnroll];
       int r0[kRestUnroll];
       bool s0[kRestUnroll], s1[kRestUnroll];
 #pragma unroll
       for (int u = 0; u < kRestUnroll; ++u) {
-        const int q = q0 + 256 * u, j = 4 * q;
+        const int q = q0 + kPbwdThreads * u, j = 4 * q;
         r0[u] = (int)(((float)j + 0.5f) * inv_row);
         const int r3 = (int)(((float)j + 3.5f) * inv_row);
         s0[u] = q < n4 && s_seen[r0[u]] != 0;
@@ -724,7 +728,7 @@ __device__ __forceinline__ void adam_rest_rows(const PbwdArgs& a, int first, int
 #pragma unroll
       for (int u = 0; u < kRestUnroll; ++u) {
         if (!(s0[u] || s1[u])) continue;
-        const int q = q0 + 256 * u, j = 4 * q;
+        const int q = q0 + kPbwdThreads * u, j = 4 * q;
         const int split = (r0[u] + 1) * row - j;  // elements [0, split) belong to row r0
         const float4 gv = G4[q];
         float* pp = &pv[u].x;
@@ -747,23 +751,23 @@ __device__ __forceinline__ void adam_rest_rows(const PbwdArgs& a, int first, int
     }
     done = n4 << 2;
   }
-  for (int j = done + threadIdx.x; j < total; j += 256)
+  for (int j = done + threadIdx.x; j < total; j += kPbwdThreads)
     if (s_seen[j / row]) adam_step(prm, pm1, pm2, j, s_g[j], lr, b1, b2, eps);
 }
 
 // ADAM: the sparse Adam step fused in place of the gradient outputs.
 template <bool ADAM>
-__global__ void __launch_bounds__(256, 2) k_preprocess_bwd(const PbwdArgs a) {
-  // sh_staged: [256 x M x 3] SH rows, then [256 x M x 3] dL/dsh accumulators
+__global__ void __launch_bounds__(kPbwdThreads, kPbwdBlocks) k_preprocess_bwd(const PbwdArgs a) {
+  // sh_staged: [kPbwdThreads x M x 3] SH rows, then as many dL/dsh accumulators
   extern __shared__ __align__(16) float s_pb[];
-  __shared__ uint8_t s_seen[256];
-  const int first = blockIdx.x * 256, n = min(256, a.P - first), row = a.M * 3;
+  __shared__ uint8_t s_seen[kPbwdThreads];
+  const int first = blockIdx.x * kPbwdThreads, n = min(kPbwdThreads, a.P - first), row = a.M * 3;
   const int i = first + threadIdx.x;
   if (a.sh_staged) {
     float* s_co = s_pb;
-    float* s_g = s_pb + 256 * row;
+    float* s_g = s_pb + kPbwdThreads * row;
     block_copy_to_smem(s_co, a.shs, (size_t)first * row, n * row);
-    for (int j = threadIdx.x; j < n * row; j += 256) s_g[j] = 0.f;
+    for (int j = threadIdx.x; j < n * row; j += kPbwdThreads) s_g[j] = 0.f;
     __syncthreads();
     const bool seen = i < a.P && pbwd_gaussian<ADAM>(a, i, s_co + threadIdx.x * row, s_g + threadIdx.x * row);
     s_seen[threadIdx.x] = seen ? 1 : 0;
@@ -853,13 +857,14 @@ fgs_status run_preprocess_bwd(PbwdArgs& a, cudaStream_t s) {
   a.sh_staged = (a.shs && (a.dsh || a.adam_on) && a.M >= 1 && a.M <= kMaxStagedCoeffs) ? 1 : 0;
   // the fused step keeps dL/dsh only in shared memory
   if (a.adam_on && a.shs && a.D > 0 && !a.sh_staged) return FGS_ERR_BAD_ARG;
-  const int dyn = a.sh_staged ? 2 * 256 * a.M * 3 * (int)sizeof(float) : 0;
+  const int dyn = a.sh_staged ? 2 * kPbwdThreads * a.M * 3 * (int)sizeof(float) : 0;
   const void* kern = a.adam_on ? reinterpret_cast<const void*>(&k_preprocess_bwd<true>)
                                : reinterpret_cast<const void*>(&k_preprocess_bwd<false>);
-  if (dyn) FGS_TRY(allow_dyn_smem(kern, 2 * 256 * kMaxStagedCoeffs * 12));
+  if (dyn) FGS_TRY(allow_dyn_smem(kern, 2 * kPbwdThreads * kMaxStagedCoeffs * 12));
   KernelTimer kt__(FGS_K_PREPROCESS_BWD, s);
-  if (a.adam_on) k_preprocess_bwd<true><<<(a.P + 255) / 256, 256, dyn, s>>>(a);
-  else k_preprocess_bwd<false><<<(a.P + 255) / 256, 256, dyn, s>>>(a);
+  const unsigned blocks = (unsigned)((a.P + kPbwdThreads - 1) / kPbwdThreads);
+  if (a.adam_on) k_preprocess_bwd<true><<<blocks, kPbwdThreads, dyn, s>>>(a);
+  else k_preprocess_bwd<false><<<blocks, kPbwdThreads, dyn, s>>>(a);
   kt__.stop();
   FGS_LAUNCH_CHECK();
   return FGS_OK;
