@@ -251,16 +251,31 @@ __global__ void __launch_bounds__(kScanTiles) k_bucket_fill(int T, const uint32_
     bucket_off[t] = end;
   }
   if (overflow) return;
-  // rounds: one slot request per warp and round
+  // Rounds, 32 at a time: lane j requests the slots of round k0 + j for every
+  // tile of the warp that reaches it (one atomic per warp and round, the 32
+  // in flight together), then each tile writes its entries.  A warp holding a
+  // deep tile (clustered scenes: thousands of buckets) takes ceil(rounds / 32)
+  // steps instead of one dependent atomic per round.
   const uint32_t nr = min(nb, (uint32_t)kRounds);
-  for (uint32_t k = 0;; ++k) {
-    const uint32_t act = __ballot_sync(0xffffffffu, k < nr);
-    if (act == 0) break;
-    const int leader = __ffs(act) - 1;
+  uint32_t wmax = nr;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) wmax = max(wmax, __shfl_xor_sync(0xffffffffu, wmax, o));
+  for (uint32_t k0 = 0; k0 < wmax; k0 += kWarp) {
+    uint32_t my_act = 0;  // tiles of the warp that reach round k0 + lane
+#pragma unroll 4
+    for (int j = 0; j < kWarp; ++j) {
+      const uint32_t act = __ballot_sync(0xffffffffu, k0 + (uint32_t)j < nr);
+      if (lane == j) my_act = act;
+    }
     uint32_t base = 0;
-    if (lane == leader) base = atomicAdd(round_fill + k, (uint32_t)__popc(act));
-    base = __shfl_sync(0xffffffffu, base, leader);
-    if (k < nr) bucket_queue[round_off[k] + base + __popc(act & lanemask_lt())] = make_uint2((uint32_t)t, k);
+    if (my_act) base = atomicAdd(round_fill + k0 + lane, (uint32_t)__popc(my_act));
+#pragma unroll 4
+    for (int j = 0; j < kWarp; ++j) {
+      const uint32_t act = __shfl_sync(0xffffffffu, my_act, j);
+      const uint32_t b = __shfl_sync(0xffffffffu, base, j);
+      if ((act >> lane) & 1u)
+        bucket_queue[round_off[k0 + j] + b + __popc(act & lanemask_lt())] = make_uint2((uint32_t)t, k0 + j);
+    }
   }
   if (t >= T) return;
   const uint32_t tail = round_off[kRounds] + s_base[0] + v[0] - (nb > kRounds ? nb - kRounds : 0u);
