@@ -858,8 +858,8 @@ MUFU_PER_EVAL = {"render_fwd": 1, "render_bwd": 2}
 
 # DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) of the
 # C2 workload, from the ncu captures summarised in profiles/ncu_c2_kernels.md.
-TRAFFIC_PER_LAUNCH = {"render_bwd": 56_158_720, "render_fwd": 43_322_368, "sort_pass": 38_579_456,
-                      "preprocess_bwd": 572_444_928, "preprocess": 200_878_592}
+TRAFFIC_PER_LAUNCH = {"render_bwd": 81_252_608, "render_fwd": 77_669_120, "sort_pass": 38_493_696,
+                      "preprocess_bwd": 511_551_488, "preprocess": 215_542_016}
 
 
 def roofline(res, peaks):
@@ -876,9 +876,10 @@ def roofline(res, peaks):
         "preprocess": P * (56 + 4 * sh_floats) + P * 44 + 12 * K,
         "sort_pass": 24 * K,
         "sort_hist": 8 * K,
-        # composite: records of every pair, plus the folded prefix written once per bucket
-        "render_fwd": 40 * K + 16 * 256 * math.ceil(K / 128),
-        "render_bwd": 40 * K + 16 * 256 * math.ceil(K / 128) + 48 * K,
+        # composite: records of every pair, plus the folded prefix written once per
+        # 64-Gaussian sub-bucket (read once by the backward)
+        "render_fwd": 40 * K + 16 * 256 * math.ceil(K / 64),
+        "render_bwd": 40 * K + 16 * 256 * math.ceil(K / 64) + 48 * K,
         "preprocess_bwd": P * (56 + 4 * sh_floats + 48) + P * (56 + 4 * sh_floats),
         "tile_ranges": 8 * K,
     }
