@@ -787,13 +787,19 @@ def checkpoint_bench(args, dev):
         ev1.record(stream)
         torch.cuda.synchronize(dev)
         _, buckets = rast.status()
+        rg = rast.tile_ranges().to(torch.int64)
+        per_tile = (rg[:, 1] - rg[:, 0]).clamp(min=0)
+        fb_buckets = int(((per_tile + 127) // 128).sum())
+        tiles = int(rg.shape[0])
         out[name] = {"ms_per_step": round(ev0.elapsed_time(ev1) / reps, 3),
                      "peak_hbm_gb": round(torch.cuda.max_memory_allocated(dev) / 1e9, 3),
                      "workspace_gb": round(rast.workspace.numel() / 1e9, 3), "pairs": int(pairs),
-                     "buckets": int(buckets)}
+                     "buckets_128": fb_buckets, "sub_buckets_64": int(buckets),
+                     # prefix samples kept for the backward: 16 B per pixel and sub-bucket, or per tile
+                     "sample_state_gb": round((tiles if rec else int(buckets)) * 256 * 16 / 1e9, 3)}
         del step, rast
-    # FB's sample state for the same frame: 40 bytes per pixel and bucket
-    out["fb_sample_state_gb"] = round(out["store"]["buckets"] * 256 * 40 / 1e9, 3)
+    # FB's sample state for the same frame: 40 bytes per pixel and 128-Gaussian bucket
+    out["fb_sample_state_gb"] = round(out["store"]["buckets_128"] * 256 * 40 / 1e9, 3)
     out["peak_hbm_saved_gb"] = round(out["store"]["peak_hbm_gb"] - out["recompute"]["peak_hbm_gb"], 3)
     del params
     torch.cuda.empty_cache()

@@ -167,6 +167,15 @@ class BatchedRasterizer:
         self.plan(int(pairs * headroom) + (1 << 16))
         return pairs
 
+    def tile_ranges(self) -> torch.Tensor:
+        """Device view (tiles, 2) int32 of the last frame's per-tile [start, end) in the sorted pair
+        list, cameras in order (no copy)."""
+        offs = (C.c_int64 * 10)()
+        _lib.call("fgs_batch_offsets", self.P, self.V, self._cams, C.byref(self._cfg), self.pair_capacity, offs, 10)
+        tiles = sum(((w + self.tune.block_x - 1) // self.tune.block_x) * ((h + self.tune.block_y - 1) // self.tune.block_y)
+                    for h, w in self.sizes)
+        return self.workspace[offs[6]:offs[6] + 8 * tiles].view(torch.int32).view(tiles, 2)
+
     def state(self) -> dict:
         """Host copies of the last frame's records, pairs, sorted lists and ranges (for tests)."""
         offs = (C.c_int64 * 10)()
