@@ -207,7 +207,8 @@ def rast_cam(rast, k):
     return _CAMS[id(rast)][k]
 
 
-TUNES = [TuneConfig(32, 8, 32, 2), TuneConfig(64, 32, 8, 8), TuneConfig(16, 16, 16, 1)]
+TUNES = [TuneConfig(32, 8, 32, 2), TuneConfig(64, 32, 8, 8), TuneConfig(16, 16, 16, 1),
+         TuneConfig(128, 16, 16, 4)]  # FB's bucket: composited as two sub-buckets, stop at the full bucket
 
 
 @pytest.mark.parametrize("tune", TUNES, ids=lambda t: f"b{t.bucket_size}_{t.block_x}x{t.block_y}_p{t.packet}")
