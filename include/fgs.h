@@ -353,12 +353,14 @@ typedef struct {
  * 32*packet tiles are split into sub-tasks of 32*packet tiles, smaller ones
  * are lane-packed by the preprocess warps.  The tile shape and the bucket
  * size change images at the level of the T < 1e-4 stopping rule (which acts
- * per bucket); packet changes only the order in which pairs are emitted.
+ * per bucket; a 128-Gaussian bucket is composited as two 64-Gaussian
+ * sub-buckets with the stop tested after the second, as for fgs_render_fwd);
+ * packet changes only the order in which pairs are emitted.
  * recompute 1: the forward keeps one running (colour, transmittance) prefix
- * per tile instead of one per bucket (4 KB per bucket), and the backward
- * rebuilds each bucket's prefix from it -- bit-identical prefixes, a
- * workspace smaller by about 4 KB per bucket, one extra compositing pass over
- * the needed buckets. */
+ * per tile instead of one per (sub-)bucket (4 KB each), and the backward
+ * rebuilds each one's prefix from it -- bit-identical prefixes, a
+ * workspace smaller by about 4 KB per (sub-)bucket, one extra compositing
+ * pass over the needed buckets. */
 typedef struct {
   int bucket_size;
   int block_x, block_y;
