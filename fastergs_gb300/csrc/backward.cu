@@ -337,31 +337,45 @@ __global__ void __launch_bounds__(kBwdWarps * kWarp, 5) k_render_bwd(const BwdAr
         V10 = f2_fma(nwt2, Lz2, V10);
         const f2x dp2 = f2_mul(nd2, na2);  // dL/dexponent / ln2
         // d exponent / d(centre x) = 2 A1 w, d / d(centre y) = 2 A1 P w + 2 C1 dy
-        const f2x gw2 = f2_mul(A22, w2);
-        const f2x tx2 = f2_mul(dp2, gw2);
-        const f2x ty2 = f2_mul(dp2, f2_fma(gw2, P2, f2_pack(2.f * q.z * dy0, 2.f * q.z * dy1)));
-        V0 = f2_add(V0, tx2);
-        V1 = f2_add(V1, ty2);
-        if constexpr (ABS) {
+        if constexpr (ABS) {  // per-pixel terms: their absolute values are summed too
+          const f2x gw2 = f2_mul(A22, w2);
+          const f2x tx2 = f2_mul(dp2, gw2);
+          const f2x ty2 = f2_mul(dp2, f2_fma(gw2, P2, f2_pack(2.f * q.z * dy0, 2.f * q.z * dy1)));
+          V0 = f2_add(V0, tx2);
+          V1 = f2_add(V1, ty2);
           float tx0, tx1, ty0, ty1;
           f2_unpack(tx2, tx0, tx1);
           f2_unpack(ty2, ty0, ty1);
           v2 += fabsf(tx0) + fabsf(tx1);
           v3 += fabsf(ty0) + fabsf(ty1);
+          V4 = f2_fma(dp2, f2_mul(w2, w2), V4);
+          V5 = f2_fma(f2_mul(dp2, w2), dy2, V5);
+          V7 = f2_fma(f2_mul(dp2, dy2), dy2, V7);
+        } else {
+          // Both mean terms are linear in sum(dp w) and sum(dp dy) (scaled after
+          // the loop), the products the conic moments below need anyway.
+          const f2x u2 = f2_mul(dp2, w2);
+          const f2x t2 = f2_mul(dp2, dy2);
+          V0 = f2_add(V0, u2);
+          V1 = f2_add(V1, t2);
+          V4 = f2_fma(u2, w2, V4);
+          V5 = f2_fma(u2, dy2, V5);
+          V7 = f2_fma(t2, dy2, V7);
         }
-        // Conic-gradient moments in the exponent's own frame (w, dy),
-        // w = dx + P dy.  In pixel coordinates a thin footprint's cross-axis
-        // gradient is a small difference of large sums; here each frame
-        // axis is summed on its own.
-        V4 = f2_fma(dp2, f2_mul(w2, w2), V4);
-        V5 = f2_fma(f2_mul(dp2, w2), dy2, V5);
-        V7 = f2_fma(f2_mul(dp2, dy2), dy2, V7);
+        // (V4, V5, V7: conic-gradient moments in the exponent's own frame
+        // (w, dy), w = dx + P dy.  In pixel coordinates a thin footprint's
+        // cross-axis gradient is a small difference of large sums; here each
+        // frame axis is summed on its own.)
         V11 = f2_add(V11, dp2);
       }
       if (__any_sync(0xffffffffu, any)) {
         float v[12], a0, a1;
         f2_unpack(V0, a0, a1); v[0] = a0 + a1;
         f2_unpack(V1, a0, a1); v[1] = a0 + a1;
+        if constexpr (!ABS) {  // from sum(dp w), sum(dp dy): 2 A1 sum(dp w), P (that) + 2 C1 sum(dp dy)
+          v[0] *= 2.f * q.x;
+          v[1] = fmaf(q.y, v[0], 2.f * q.z * v[1]);
+        }
         v[2] = v2;
         v[3] = v3;
         f2_unpack(V4, a0, a1); v[4] = a0 + a1;
