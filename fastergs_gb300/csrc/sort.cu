@@ -88,10 +88,22 @@ __global__ void __launch_bounds__(kSortThreads) k_histogram(const unsigned long 
   const long long n = pair_count(n_cap, n_dev);
   for (int j = threadIdx.x; j < kMaxPasses * kRadix; j += kSortThreads) (&s_h[0][0])[j] = 0;
   __syncthreads();
-  for (long long k = blockIdx.x * (long long)kSortThreads + threadIdx.x; k < n;
-       k += (long long)gridDim.x * kSortThreads) {
-    const unsigned long long key = keys[k];
-    for (int p = 0; p < passes; ++p) atomicAdd(&s_h[p][(key >> (8 * p)) & 0xff], 1u);
+  // 8 keys per thread and step, loaded before they are counted (memory-level
+  // parallelism with few blocks: every block adds passes x 256 global counts).
+  constexpr int kHistItems = 8;
+  const long long stride = (long long)gridDim.x * kSortThreads * kHistItems;
+  for (long long k0 = blockIdx.x * (long long)kSortThreads * kHistItems + threadIdx.x; k0 < n; k0 += stride) {
+    unsigned long long key[kHistItems];
+#pragma unroll
+    for (int r = 0; r < kHistItems; ++r) {
+      const long long k = k0 + (long long)r * kSortThreads;
+      key[r] = k < n ? __ldg(keys + k) : 0ull;
+    }
+#pragma unroll
+    for (int r = 0; r < kHistItems; ++r) {
+      if (k0 + (long long)r * kSortThreads >= n) break;
+      for (int p = 0; p < passes; ++p) atomicAdd(&s_h[p][(key[r] >> (8 * p)) & 0xff], 1u);
+    }
   }
   __syncthreads();
   for (int j = threadIdx.x; j < passes * kRadix; j += kSortThreads) {
@@ -308,8 +320,8 @@ fgs_status run_sort(int64_t n_cap, const int32_t* n_dev, uint32_t tiles, void* t
   auto* alt_v = reinterpret_cast<uint32_t*>(base + L.alt_vals);
   // hist, counters and the look-back words of every pass start at zero.
   FGS_TRY(cudaMemsetAsync(base, 0, L.alt_keys, s));
-  const int hist_blocks = (int)std::min<int64_t>((n_cap + kSortThreads * 8 - 1) / (kSortThreads * 8),
-                                                 (int64_t)num_sms() * 8);
+  const int hist_blocks = (int)std::max<int64_t>(
+      1, std::min<int64_t>((n_cap + kSortThreads * 8 - 1) / (kSortThreads * 8), (int64_t)num_sms() * 2));
   {
     KernelTimer kt__(FGS_K_SORT_HIST, s);
     k_histogram<<<hist_blocks, kSortThreads, 0, s>>>(reinterpret_cast<const unsigned long long*>(keys_in), n_cap,
