@@ -49,8 +49,8 @@ __global__ void __launch_bounds__(kWarp) k_render_simp(int P, int W, int H, int 
     }
   const int odd = n & 1;
   bool stop = false;
-  for (int base = 0; base < n && !stop; base += kMaxBucket) {
-    const int cnt = min(kMaxBucket, n - base);
+  for (int base = 0; base < n && !stop; base += kSubBucket) {
+    const int cnt = min(kSubBucket, n - base);
     stage_bucket<16>(st, splat, vals + rs + base, cnt, lane, tx0, ty0);
     for (int g = 0; g < cnt; ++g) {
       const int i = base + g;  // position in the tile's list

@@ -121,7 +121,7 @@ __global__ void __launch_bounds__(256) k_live_buckets(uint32_t* bucket_sum, cons
 // ABS: also sum |dL/dmean2D| per Gaussian (dmean2D.zw, for the
 // xyz_gradient_accum_abs statistic); without it those two slots stay zero.
 template <int BX, bool RECOMPUTE, bool ABS>
-__global__ void __launch_bounds__(kBwdWarps * kWarp, 5) k_render_bwd(const BwdArgs a) {
+__global__ void __launch_bounds__(kBwdWarps * kWarp, 6) k_render_bwd(const BwdArgs a) {
   using M = TileMap<BX>;
   constexpr int BY = kTilePixels / BX;
   __shared__ BucketStage s_stage[kBwdWarps];

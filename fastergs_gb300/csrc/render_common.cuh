@@ -14,15 +14,20 @@ constexpr int kMaxBucket = 128;    // largest supported bucket size
 
 // A bucket of bucket_size Gaussians is the merge's stop granularity (FB's
 // BUCKET_SIZE: a pixel stops after the bucket that takes its transmittance
-// below 1e-4).  Buckets larger than kSubBucket are composited as
-// bucket_size / kSubBucket sub-buckets, each with its own prefix sample, and
-// the stop test runs only after a bucket's last sub-bucket, so the outputs
-// keep the bucket's stop semantics while a tile's chain has twice as many
-// links to spread over the GPU.  "Bucket" in the composite kernels, the
-// bookkeeping and the sample state means the sub-bucket.
-constexpr int kSubBucket = 64;
+// below 1e-4).  Buckets larger than kSubBucket are composited as the fewest
+// equal sub-buckets of at most kSubBucket Gaussians (FB's 128: two of 64),
+// each with its own prefix sample, and the stop test runs only after a
+// bucket's last sub-bucket, so the outputs keep the bucket's stop semantics
+// while a tile's chain has more links to spread over the GPU, and a warp
+// stages at most kSubBucket records.
+// "Bucket" in the composite kernels, the bookkeeping and the sample state
+// means the sub-bucket.
+constexpr int kSubBucket = 64;  // largest composited (sub-)bucket: the size of the shared-memory stage
 inline int bucket_split(int bucket_size) {
-  return (bucket_size > kSubBucket && bucket_size % kSubBucket == 0) ? bucket_size / kSubBucket : 1;
+  // fewest equal sub-buckets of at most kSubBucket Gaussians that tile the bucket
+  int s = (bucket_size + kSubBucket - 1) / kSubBucket;
+  while (s < bucket_size && bucket_size % s != 0) ++s;
+  return s < 1 ? 1 : s;
 }
 inline int sub_bucket_size(int bucket_size) { return bucket_size / bucket_split(bucket_size); }
 
@@ -116,10 +121,10 @@ struct TileMap {
 
 // Records of one bucket staged in shared memory, structure-of-arrays.
 struct BucketStage {
-  float4 pos[kMaxBucket];     // floor(x), floor(y), fraction x, fraction y
-  float4 quad[kMaxBucket];    // A1, P, C1, log2 opacity
-  float4 rgb[kMaxBucket];     // r, g, b, Gaussian id bits
-  uint32_t mask[kMaxBucket];  // sub-blocks the Gaussian can reach (bit r * kCols + c)
+  float4 pos[kSubBucket];     // floor(x), floor(y), fraction x, fraction y
+  float4 quad[kSubBucket];    // A1, P, C1, log2 opacity
+  float4 rgb[kSubBucket];     // r, g, b, Gaussian id bits
+  uint32_t mask[kSubBucket];  // sub-blocks the Gaussian can reach (bit r * kCols + c)
 };
 
 // Stage the render fields (floats 0..11) of the n records whose ids start at
