@@ -51,7 +51,7 @@ __global__ void __launch_bounds__(kWarp) k_render_simp(int P, int W, int H, int 
   bool stop = false;
   for (int base = 0; base < n && !stop; base += kSubBucket) {
     const int cnt = min(kSubBucket, n - base);
-    stage_bucket<16>(st, splat, vals + rs + base, cnt, lane, tx0, ty0);
+    stage_bucket<16>(st, splat, load_stage_ids(vals + rs + base, cnt, lane), cnt, lane, tx0, ty0);
     for (int g = 0; g < cnt; ++g) {
       const int i = base + g;  // position in the tile's list
       const uint32_t mask = st.mask[g];

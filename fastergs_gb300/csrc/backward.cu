@@ -178,7 +178,7 @@ __global__ void __launch_bounds__(kBwdWarps * kWarp, 6) k_render_bwd(const BwdAr
                          : (vid >= 4 && vid <= 7) ? -0.5f
                          : (vid >= 8 && vid <= 10) ? -1.0f
                                                    : 1.0f;
-    stage_bucket<BX>(st, a.splat, a.vals + bi.start, bi.n, lane, tx0, ty0);
+    stage_bucket<BX>(st, a.splat, load_stage_ids(a.vals + bi.start, bi.n, lane), bi.n, lane, tx0, ty0);
     float pxc[M::kCols], pyr[M::kRows];
 #pragma unroll
     for (int c = 0; c < M::kCols; ++c) pxc[c] = (float)(tx0 + 8 * c + (lane & 7));

@@ -353,6 +353,7 @@ __global__ void __launch_bounds__(kFwdWarps * kWarp, 7) k_render_fwd(const FwdAr
     uint32_t* stage_word = a.tile_stage + bi.tile;
     uint32_t* alive_words = a.tile_alive + (size_t)bi.tile * kPxPerThread;
 
+    const StageIds sid = load_stage_ids(a.vals + bi.start, bi.n, lane);  // in flight with the reads below
     // Sub-blocks that may still need this bucket: from whatever prefix state
     // the tile has published so far (a superset of the state after bucket k-1;
     // the alive words are read together with the stage and used once it shows
@@ -369,7 +370,7 @@ __global__ void __launch_bounds__(kFwdWarps * kWarp, 7) k_render_fwd(const FwdAr
     }
 
     float T[kPxPerThread], Cr[kPxPerThread], Cg[kPxPerThread], Cb[kPxPerThread];
-    if (spec != 0u) stage_bucket<BX>(st, a.splat, a.vals + bi.start, bi.n, lane, tx0, ty0);
+    if (spec != 0u) stage_bucket<BX>(st, a.splat, sid, bi.n, lane, tx0, ty0);
     {
       float pxc[M::kCols], pyr[M::kRows];
 #pragma unroll

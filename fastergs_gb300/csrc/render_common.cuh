@@ -127,14 +127,32 @@ struct BucketStage {
   uint32_t mask[kSubBucket];  // sub-blocks the Gaussian can reach (bit r * kCols + c)
 };
 
-// Stage the render fields (floats 0..11) of the n records whose ids start at
-// ids, and each Gaussian's sub-block mask for the tile at (tx0, ty0).
+// The record ids of a bucket a lane stages (entries lane, lane + 32), loaded
+// ahead so that their latency overlaps other reads.
+struct StageIds {
+  uint32_t id[kSubBucket / kWarp];
+};
+__device__ __forceinline__ StageIds load_stage_ids(const uint32_t* __restrict__ ids, int n, int lane) {
+  StageIds s;
+#pragma unroll
+  for (int k = 0; k < kSubBucket / kWarp; ++k) {
+    const int j = lane + k * kWarp;
+    s.id[k] = j < n ? ids[j] : 0u;
+  }
+  return s;
+}
+
+// Stage the render fields (floats 0..11) of the n records whose ids are in
+// sid, and each Gaussian's sub-block mask for the tile at (tx0, ty0).
 template <int BX>
-__device__ __forceinline__ void stage_bucket(BucketStage& st, const float* __restrict__ splat,
-                                             const uint32_t* __restrict__ ids, int n, int lane, int tx0, int ty0) {
+__device__ __forceinline__ void stage_bucket(BucketStage& st, const float* __restrict__ splat, const StageIds& sid,
+                                             int n, int lane, int tx0, int ty0) {
   using M = TileMap<BX>;
-  for (int j = lane; j < n; j += kWarp) {
-    const uint32_t id = ids[j];
+#pragma unroll
+  for (int k = 0; k < kSubBucket / kWarp; ++k) {
+    const int j = lane + k * kWarp;
+    if (j >= n) break;
+    const uint32_t id = sid.id[k];
     const float4* r = reinterpret_cast<const float4*>(splat + (size_t)id * 32);
     const float4 a = __ldg(r);        // x, y, r, g
     const float4 b = __ldg(r + 1);    // b, depth, A1, P
