@@ -36,24 +36,41 @@ constexpr int kFwdWarps = 4;
 __global__ void __launch_bounds__(256) k_tile_ranges(const unsigned long long* __restrict__ keys, long long n_cap,
                                                      const int* n_dev, uint32_t num_tiles,
                                                      uint32_t* __restrict__ ranges) {
+  // 4 consecutive keys per thread (two 16-byte loads when aligned), compared
+  // with their predecessors: a tile boundary writes the end of one range and
+  // the start of the next.
+  constexpr int kPer = 4;
   const long long n = n_dev ? min(n_cap, (long long)(unsigned int)*n_dev) : n_cap;
-  const long long i = blockIdx.x * 256ll + threadIdx.x;
-  if (i >= n) return;
-  const uint32_t t = (uint32_t)(keys[i] >> 32);
-  if (t >= num_tiles) {  // not a key of this frame
-    raise_error(kErrCapacity);
-    return;
-  }
-  if (i == 0) {
-    ranges[2 * t] = 0;
+  const long long i0 = (blockIdx.x * 256ll + threadIdx.x) * kPer;
+  if (i0 >= n) return;
+  unsigned long long k[kPer];
+  if (i0 + kPer <= n && ((reinterpret_cast<uintptr_t>(keys) & 15) == 0)) {
+    const ulonglong2 a = __ldg(reinterpret_cast<const ulonglong2*>(keys + i0));
+    const ulonglong2 b = __ldg(reinterpret_cast<const ulonglong2*>(keys + i0) + 1);
+    k[0] = a.x; k[1] = a.y; k[2] = b.x; k[3] = b.y;
   } else {
-    const uint32_t pt = (uint32_t)(keys[i - 1] >> 32);
-    if (pt != t && pt < num_tiles) {
+#pragma unroll
+    for (int r = 0; r < kPer; ++r) k[r] = i0 + r < n ? keys[i0 + r] : 0ull;
+  }
+  uint32_t pt = i0 > 0 ? (uint32_t)(keys[i0 - 1] >> 32) : 0xffffffffu;
+#pragma unroll
+  for (int r = 0; r < kPer; ++r) {
+    const long long i = i0 + r;
+    if (i >= n) break;
+    const uint32_t t = (uint32_t)(k[r] >> 32);
+    if (t >= num_tiles) {  // not a key of this frame
+      raise_error(kErrCapacity);
+      return;
+    }
+    if (i == 0) {
+      ranges[2 * t] = 0;
+    } else if (pt != t && pt < num_tiles) {
       ranges[2 * pt + 1] = (uint32_t)i;
       ranges[2 * t] = (uint32_t)i;
     }
+    if (i == n - 1) ranges[2 * t + 1] = (uint32_t)n;
+    pt = t;
   }
-  if (i == n - 1) ranges[2 * t + 1] = (uint32_t)n;
 }
 
 // Bucket bookkeeping (FB render.cu:418-433 counts buckets per tile, scans them
@@ -290,23 +307,26 @@ __global__ void __launch_bounds__(kTilePixels) k_empty_tiles(const Views views, 
                                                              int* __restrict__ last_contrib,
                                                              float* __restrict__ Ts_final,
                                                              uint32_t* __restrict__ max_contrib) {
-  const int tile = blockIdx.x, p = threadIdx.x;
-  if (ranges[2 * tile + 1] > ranges[2 * tile] && bucket_sum[0] != 0) return;
-  const ViewDesc& cam = views.v[views.of_tile((uint32_t)tile)];
-  const int lt = tile - (int)cam.tile_off, bx = views.bx, by = views.by;
-  const int px = (lt % cam.gx) * bx + p % bx, py = (lt / cam.gx) * by + p / bx;
-  if (p == 0) max_contrib[tile] = 0;
-  if (px >= cam.W || py >= cam.H) return;
-  const size_t HW = (size_t)cam.W * cam.H, pix = (size_t)py * cam.W + px;
-  float* oc = out_color + 3 * (size_t)cam.pix_off;
-  float* pc = pix_color + 3 * (size_t)cam.pix_off;
+  const int p = threadIdx.x;
+  const bool all = bucket_sum[0] == 0;  // the buckets did not fit: every tile gets the empty-list output
+  for (uint32_t tile = blockIdx.x; tile < views.tiles; tile += gridDim.x) {  // block-uniform
+    if (!all && ranges[2 * tile + 1] > ranges[2 * tile]) continue;
+    const ViewDesc& cam = views.v[views.of_tile(tile)];
+    const int lt = (int)tile - (int)cam.tile_off, bx = views.bx, by = views.by;
+    const int px = (lt % cam.gx) * bx + p % bx, py = (lt / cam.gx) * by + p / bx;
+    if (p == 0) max_contrib[tile] = 0;
+    if (px >= cam.W || py >= cam.H) continue;
+    const size_t HW = (size_t)cam.W * cam.H, pix = (size_t)py * cam.W + px;
+    float* oc = out_color + 3 * (size_t)cam.pix_off;
+    float* pc = pix_color + 3 * (size_t)cam.pix_off;
 #pragma unroll
-  for (int ch = 0; ch < 3; ++ch) {
-    oc[ch * HW + pix] = cam.bg[ch];
-    pc[ch * HW + pix] = 0.f;
+    for (int ch = 0; ch < 3; ++ch) {
+      oc[ch * HW + pix] = cam.bg[ch];
+      pc[ch * HW + pix] = 0.f;
+    }
+    last_contrib[cam.pix_off + pix] = 0;
+    Ts_final[cam.pix_off + pix] = 1.f;
   }
-  last_contrib[cam.pix_off + pix] = 0;
-  Ts_final[cam.pix_off + pix] = 1.f;
 }
 
 struct FwdArgs {
@@ -496,7 +516,7 @@ fgs_status run_tile_ranges(int64_t n_cap, const int32_t* n_dev, uint32_t tiles, 
   FGS_TRY(cudaMemsetAsync(ranges, 0, sizeof(uint32_t) * 2 * (size_t)tiles, s));
   if (n_cap > 0) {
     KernelTimer kt__(FGS_K_TILE_RANGES, s);
-    k_tile_ranges<<<(unsigned)((n_cap + 255) / 256), 256, 0, s>>>(
+    k_tile_ranges<<<(unsigned)((n_cap + 1023) / 1024), 256, 0, s>>>(
         reinterpret_cast<const unsigned long long*>(keys_sorted), n_cap, n_dev, tiles, ranges);
     kt__.stop();
     FGS_LAUNCH_CHECK();
@@ -548,8 +568,8 @@ fgs_status run_render_fwd(const Views& views, int64_t n_cap, const int32_t* n_de
   FGS_LAUNCH_CHECK();
   {
     KernelTimer kt__(FGS_K_EMPTY_TILES, s);
-    k_empty_tiles<<<views.tiles, kTilePixels, 0, s>>>(views, ranges, im.bucket_sum, out_color, im.pix_color,
-                                                      last_contributor, Ts_final, im.max_contrib);
+    k_empty_tiles<<<std::min<unsigned>(views.tiles, (unsigned)num_sms() * 8), kTilePixels, 0, s>>>(
+        views, ranges, im.bucket_sum, out_color, im.pix_color, last_contributor, Ts_final, im.max_contrib);
     kt__.stop();
   }
   FGS_LAUNCH_CHECK();
