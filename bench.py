@@ -864,7 +864,7 @@ MUFU_PER_EVAL = {"render_fwd": 1, "render_bwd": 2}
 
 # DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) of the
 # C2 workload, from the ncu captures summarised in profiles/ncu_c2_kernels.md.
-TRAFFIC_PER_LAUNCH = {"render_bwd": 82_011_136, "render_fwd": 77_669_120, "sort_pass": 38_493_696,
+TRAFFIC_PER_LAUNCH = {"render_bwd": 83_665_920, "render_fwd": 77_669_120, "sort_pass": 38_493_696,
                       "preprocess_bwd": 511_551_488, "preprocess": 215_542_016}
 
 
