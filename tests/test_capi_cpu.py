@@ -46,6 +46,10 @@ def test_sizing_helpers(lib):
     assert lib.fgs_max_buckets(1000, 256, 256, 16, 16, 128) == 16 + 256
     assert lib.fgs_max_buckets(1000, 256, 256, 16, 16, 64) == 16 + 256
     assert lib.fgs_max_buckets(1000, 256, 256, 16, 16, 32) == 32 + 256
+    # other sizes: the fewest equal sub-buckets of <= 64 Gaussians that tile the bucket
+    assert lib.fgs_max_buckets(1000, 256, 256, 16, 16, 96) == 21 + 256    # 2 x 48
+    assert lib.fgs_max_buckets(1000, 256, 256, 16, 16, 65) == 77 + 256    # 5 x 13
+    assert lib.fgs_max_buckets(1000, 256, 256, 16, 16, 97) == 1000 + 256  # prime: 97 x 1
     assert lib.fgs_max_buckets(10, 256, 256, 16, 16, 128) == 1 + 10
     ib, sb = C.c_size_t(0), C.c_size_t(0)
     assert lib.fgs_state_bytes(256, 256, 16, 16, 100, C.byref(ib), C.byref(sb)) == 0
