@@ -28,7 +28,11 @@ Also on the line:
   c3          3M clustered Gaussians at 1920x1080, forward only;
   checkpoint  6M clustered Gaussians at 3840x2160: bucket prefixes stored vs
               recomputed in the backward (step time, device memory held);
-  cpu_baseline the FP64 oracle on all host cores on 1/16 of the Gaussians, x16.
+  fb          FB, the reference CUDA backend built for sm_103a (oracle/fb_ref.py),
+              through its own Python API: C2 fwd+bwd and render, C4's 16
+              cameras one after another, C1, the C3 render;
+  cpu_baseline the FP64 oracle on all host cores on the whole C2 workload
+              (3 steps after 1 warm-up).
 Each section has a --no-<section> switch (--no-cpu-baseline, --no-e2e, ...).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
@@ -36,8 +40,8 @@ Each section has a --no-<section> switch (--no-cpu-baseline, --no-e2e, ...).
 N > 1 runs one independent replica per GPU (the path does not shard on one
 view); rank 0 prints one JSON line with the whole-job numbers.
 "--impl reference" times the FP64 CPU restatement of the reference algorithm
-(the reference has no CPU path of its own, and its CUDA build cannot run on
-this box) on all host cores, on a bounded sample of the same workload.
+(the reference has no CPU path of its own) on all host cores, every step one
+full fwd+bwd of the C2 workload (about 2 s on 16 cores).
 """
 from __future__ import annotations
 
@@ -60,7 +64,6 @@ sys.path.insert(0, str(ROOT))
 
 METRIC = "fwd+bwd ms/step & render FPS (1M Gaussians) batched vs plain, same GB300"
 WORKLOAD = "c2: 1M Gaussians, 1297x840, SH degree 3, single view, fwd+bwd"
-CPU_SAMPLE_DIV = 16     # CPU baseline renders 1/16 of the Gaussians at full resolution
 
 
 def parse():
@@ -78,6 +81,7 @@ def parse():
     ap.add_argument("--no-loss", action="store_true")
     ap.add_argument("--no-aux", action="store_true")
     ap.add_argument("--no-c3", action="store_true")
+    ap.add_argument("--no-fb", action="store_true")
     ap.add_argument("--cameras", type=int, default=16)
     ap.add_argument("--tune", choices=["sweep", "default"], default="sweep",
                     help="batched launch config: autotuner sweep (18 configs) or FB's fixed choice")
@@ -163,31 +167,31 @@ class ClockSampler:
 
 # --------------------------------------------------------------------------- CPU baseline (oracle port)
 def cpu_baseline(steps: int, warmup: int, n_gauss: int):
-    """FP64 restatement of the reference on all host cores, on 1/16 of the
-    Gaussians at full resolution; the per-step time is scaled by 16 (pair
-    count and compositing work grow linearly with the Gaussian count)."""
+    """The FP64 restatement of the reference (the oracle) on all host cores,
+    on the whole workload: every step is one full fwd+bwd of the same
+    1297x840 frame of n_gauss Gaussians (scene set-up excluded), median over
+    ``steps`` after ``warmup`` untimed steps.  No scaling or extrapolation."""
     import oracle
     from fastergs_gb300 import scenes
-    P = max(n_gauss // CPU_SAMPLE_DIV, 1)
-    s = scenes.scene_c2(seed=0, P=P)
+    s = scenes.scene_c2(seed=0, P=n_gauss)
     m, sc, rot, op, dc, shs = [np.asarray(a, np.float64) for a in s.activated()]
     dL = scenes.upstream_grad(0, s.camera.height, s.camera.width).astype(np.float64)
     times = []
     for it in range(warmup + steps):
-        t0 = time.perf_counter()
         o = oracle.Oracle().set_scene(m, op, sc, rot, s.camera, dc=dc, shs=shs, sh_degree=s.sh_degree)
+        t0 = time.perf_counter()
         o.preprocess()
         o.emit_sort()
         o.render()
         o.backward(dL)
         dt = time.perf_counter() - t0
+        del o
         if it >= warmup:
             times.append(dt)
-    scale = n_gauss / P
-    return {"value": statistics.median(times) * 1000.0 * scale, "unit": "ms/step", "cores": oracle.num_threads(),
+    return {"value": statistics.median(times) * 1000.0, "unit": "ms/step", "cores": oracle.num_threads(),
             "kind": "port",
-            "sample": f"{P} of {n_gauss} Gaussians (same distribution), full 1297x840 fwd+bwd, "
-                      f"median of {steps} steps x{scale:g}"}
+            "sample": f"the whole workload: {n_gauss} Gaussians, 1297x840, fwd+bwd per step, "
+                      f"median of {steps} steps after {warmup} warm-up"}
 
 
 # --------------------------------------------------------------------------- GPU path
@@ -485,6 +489,9 @@ def gpu_bench(args, rank, local, world):
     c3 = None
     if not args.no_c3 and world == 1:
         c3 = c3_bench(args, dev)
+    fb = None
+    if not args.no_fb and world == 1:
+        fb = fb_bench(args, dev, s, dev_in, K, c3["pairs"] if c3 else None)
     checkpoint = None
     if not args.no_checkpoint and world == 1:
         del dev_in
@@ -494,8 +501,7 @@ def gpu_bench(args, rank, local, world):
     return dict(ms_step=ms_step_job, fwd_ms=fwd_ms, clocks=clocks, ktimes=ktimes, K=K,
                 launches_per_step=launches_per_step, e2e=e2e, P=s.P, W=cam.width, H=cam.height, batched=batched,
                 checkpoint=checkpoint, W_eval=W_eval, fp32_peak=fp32_peak, ex2_peak=ex2_peak, fused_adam=fused_adam,
-                loss=loss,
-                aux=aux, c3=c3)
+                loss=loss, aux=aux, c3=c3, fb=fb)
 
 
 def e2e_bench(args, dev, stream, host, dL_host, dev_in, dL, rast, world):
@@ -745,6 +751,123 @@ def batched_bench(args, dev, s, dev_in, cams, label):
     return out
 
 
+FB_MAX_PAIRS = 1 << 24      # FB's Buffer capacity (FB __init__.py:22); FB writes past it beyond
+
+
+def fb_bench(args, dev, s, dev_in, K_c2, K_c3):
+    """FB, the reference CUDA backend, built for sm_103a from its own sources
+    (oracle/fb_ref.py: one CCCL-3 shim, FB's nvcc flags), timed through its own
+    Python API (GaussianRasterizer + autograd, FB __init__.py:98-187) on the
+    same GPU with the same inputs, steps and CUDA-event timing as this
+    library's plain path: C2 fwd+bwd and render, C1 fwd+bwd, the 16 C4
+    cameras called one after another, and the C3 render.  A workload whose
+    pair count is not safely below FB's 2^24 capacity is skipped (FB writes
+    past its buffer there)."""
+    import torch
+    try:
+        from oracle import fb_ref
+        if not fb_ref.staged():
+            return {"unavailable": "FB sources not staged (oracle/fb_ref.py stage)"}
+        if not fb_ref.built():
+            t0 = time.perf_counter()
+            fb_ref.build()
+            build_s = round(time.perf_counter() - t0, 1)
+        else:
+            build_s = 0.0
+        fb = fb_ref.load()
+    except Exception as e:  # a build failure is reported, not fatal to the bench
+        return {"unavailable": f"FB build/load failed: {str(e).splitlines()[0][:200]}"}
+    from fastergs_gb300 import scenes
+    stream = torch.cuda.current_stream(dev)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    reps = max(3, min(args.steps, 10))
+    t = lambda a: torch.tensor(np.asarray(a, np.float32), device=dev)
+
+    def settings(cam, deg):
+        return fb.GaussianRasterizationSettings(
+            image_height=cam.height, image_width=cam.width, tanfovx=cam.tanfovx, tanfovy=cam.tanfovy,
+            bg=torch.zeros(3, device=dev), scale_modifier=1.0, viewmatrix=t(cam.viewmatrix),
+            projmatrix=t(cam.projmatrix), sh_degree=deg, campos=t(cam.campos), mult=1.0, prefiltered=False,
+            debug=False)
+
+    def step_fn(sets, params, dLs, backward):
+        def fn():
+            for st, dL in zip(sets, dLs):
+                leaves = {k: v.detach().requires_grad_(backward) for k, v in params.items()}
+                img, _ = fb.GaussianRasterizer(st)(means3D=leaves["means"], opacities=leaves["opacities"],
+                                                   dc=leaves["dc"], shs=leaves["shs"], scales=leaves["scales"],
+                                                   rotations=leaves["rotations"])
+                if backward:
+                    torch.autograd.backward(img, grad_tensors=dL)
+        return fn
+
+    def timed(fn):
+        with torch.no_grad() if fn.__name__ == "nograd" else torch.enable_grad():
+            for _ in range(max(args.warmup, 3)):
+                fn()
+            torch.cuda.synchronize(dev)
+            ev0.record(stream)
+            for _ in range(reps):
+                fn()
+            ev1.record(stream)
+            torch.cuda.synchronize(dev)
+        return ev0.elapsed_time(ev1) / reps
+
+    def nograd(fn):
+        def g():
+            with torch.no_grad():
+                fn()
+        g.__name__ = "nograd"
+        return g
+
+    safe = int(0.9 * FB_MAX_PAIRS)
+    out = {"build": "oracle/fb_ref.py: FB's csrc built with nvcc -gencode arch=compute_103a,code=sm_103a -O3, "
+                    "cub::Max -> cuda::maximum<> at render.cu:387", "build_s": build_s,
+           "api": "FB GaussianRasterizer + autograd (its Buffer, host reads and default streams)", "steps": reps}
+    # C2, the headline workload
+    c2 = settings(s.camera, s.sh_degree)
+    dL = [torch.from_numpy(scenes.upstream_grad(0, s.camera.height, s.camera.width)).to(dev)]
+    if K_c2 < safe:
+        out["c2_fwd_bwd_ms"] = round(timed(step_fn([c2], dev_in, dL, True)), 4)
+        out["c2_render_ms"] = round(timed(nograd(step_fn([c2], dev_in, dL, False))), 4)
+        out["c2_render_fps"] = round(1000.0 / out["c2_render_ms"], 1)
+        out["c2_pairs"] = int(fb._RasterizeGaussians.buffer.curr_offset.item())
+    else:
+        out["c2"] = f"skipped: {K_c2} pairs >= 0.9 x 2^24"
+    # C4: the 16 cameras called one after another (FB has no batched path)
+    cams = scenes.cameras_c4(seed=0, n=args.cameras)
+    sets = [settings(c, s.sh_degree) for c in cams]
+    dLs = [torch.from_numpy(scenes.upstream_grad(k, c.height, c.width)).to(dev) for k, c in enumerate(cams)]
+    out["c4_fwd_bwd_ms"] = round(timed(step_fn(sets, dev_in, dLs, True)), 3)
+    out["c4_render_ms"] = round(timed(nograd(step_fn(sets, dev_in, dLs, False))), 3)
+    out["c4_render_fps"] = round(1000.0 * len(cams) / out["c4_render_ms"], 1)
+    del dLs
+    # C1: the oracle-size scene
+    s1 = scenes.scene_c1()
+    m, sc, rot, op, dc, shs = s1.activated()
+    p1 = {k: torch.from_numpy(np.ascontiguousarray(v)).to(dev)
+          for k, v in dict(means=m, scales=sc, rotations=rot, opacities=op, dc=dc, shs=shs).items()}
+    dL1 = [torch.from_numpy(scenes.upstream_grad(0, s1.camera.height, s1.camera.width)).to(dev)]
+    out["c1_fwd_bwd_ms"] = round(timed(step_fn([settings(s1.camera, s1.sh_degree)], p1, dL1, True)), 4)
+    del p1
+    # C3: 3M clustered Gaussians, render only
+    if K_c3 is not None and K_c3 < safe:
+        s3 = scenes.scene_c3(seed=0)
+        m, sc, rot, op, dc, shs = s3.activated()
+        p3 = {k: torch.from_numpy(np.ascontiguousarray(v)).to(dev)
+              for k, v in dict(means=m, scales=sc, rotations=rot, opacities=op, dc=dc, shs=shs).items()}
+        out["c3_render_ms"] = round(timed(nograd(step_fn([settings(s3.camera, s3.sh_degree)], p3, [None],
+                                                         False))), 4)
+        out["c3_render_fps"] = round(1000.0 / out["c3_render_ms"], 1)
+        out["c3_pairs"] = int(fb._RasterizeGaussians.buffer.curr_offset.item())
+        del p3
+    else:
+        out["c3"] = f"skipped: pair count {K_c3} not known to be below 0.9 x 2^24"
+    torch.cuda.synchronize(dev)
+    torch.cuda.empty_cache()
+    return out
+
+
 def checkpoint_bench(args, dev):
     """C5b: 6M Gaussians in 64 Zipf-weighted clusters, 3840x2160, SH degree 3,
     one fwd+bwd step (CUDA graph, batched path with one camera) with every
@@ -957,7 +1080,7 @@ def main():
         barrier(world)
         return
     roof, table = roofline(res, peaks)
-    cb = None if args.no_cpu_baseline else cpu_baseline(1, 0, args.gaussians)
+    cb = None if args.no_cpu_baseline else cpu_baseline(3, 1, args.gaussians)
     ms_job = res["ms_step"] / world
     line = {
         "metric": METRIC, "value": round(ms_job, 4), "unit": "ms/step", "n_gpus": world, "steps": args.steps,
@@ -970,7 +1093,7 @@ def main():
         "e2e": res["e2e"], "gpu_launches": int(round(res["launches_per_step"] * args.steps)),
         "clocks": res["clocks"], "roofline": roof, "kernels": table, "cpu_baseline": cb,
         "batched": res["batched"], "checkpoint": res["checkpoint"], "fused_adam": res["fused_adam"],
-        "loss": res["loss"], "aux": res["aux"], "c3": res["c3"],
+        "loss": res["loss"], "aux": res["aux"], "c3": res["c3"], "fb": res["fb"],
     }
     print(json.dumps(line), flush=True)
     barrier(world)

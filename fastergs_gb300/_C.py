@@ -53,7 +53,10 @@ _COUNTERS: dict = {}
 
 
 def _counters(dev: torch.device) -> torch.Tensor:
-    key = (dev.type, dev.index)
+    """The preprocess's work counters (zeroed and then counted into by every
+    call), one set per (device, stream): calls in flight on different
+    streams of one device each count into their own."""
+    key = (dev.type, dev.index, _stream(dev))
     if key not in _COUNTERS:
         _COUNTERS[key] = torch.zeros(16, dtype=torch.int32, device=dev)
     return _COUNTERS[key]

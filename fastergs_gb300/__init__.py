@@ -15,7 +15,10 @@ Differences that only show where FB would fail:
   * ``Buffer`` is allocated on first use, not at import, so importing the
     package does not need a GPU;
   * ``cov3D_precomp`` raises NotImplementedError (FB accepts it, ignores it
-    and reads the absent scales).
+    and reads the absent scales);
+  * a backward whose forward's pair lists were overwritten by a later
+    forward (the shared ``Buffer`` holds one frame) raises RuntimeError; FB
+    silently differentiates the later frame's lists.
 """
 from __future__ import annotations
 
@@ -27,7 +30,31 @@ import torch.nn as nn
 from . import _C, _lib
 
 __all__ = ["GaussianRasterizationSettings", "GaussianRasterizer", "rasterize_gaussians", "Buffer",
-           "SparseGaussianAdam", "_RasterizeGaussians", "_C"]
+           "SparseGaussianAdam", "_RasterizeGaussians", "_C", "cpu_deep_copy_tuple"]
+
+_EXT = None
+
+
+def _ext():
+    """The compiled extension (``diff_gaussian_rasterization_faster._C``) the drop-in path runs on.
+
+    Its ``ops`` are ``_C.ops`` compiled: the same C ABI calls without the
+    per-call ctypes and Python argument handling.  Missing means unbuilt, and
+    that is an error, not a reason to take another path."""
+    global _EXT
+    if _EXT is None:
+        try:
+            from diff_gaussian_rasterization_faster import _C as ext
+        except ImportError as e:
+            raise ImportError("the compiled extension diff_gaussian_rasterization_faster._C is missing: build it "
+                              "with fastergs_gb300.build.build()") from e
+        _EXT = ext
+    return _EXT
+
+
+def cpu_deep_copy_tuple(input_tuple):
+    """Host copies of the tensors of a tuple, other items as they are (FB __init__.py:16-18)."""
+    return tuple(item.cpu().clone() if isinstance(item, torch.Tensor) else item for item in input_tuple)
 
 
 class Buffer:
@@ -47,6 +74,9 @@ class Buffer:
         self.curr_offset = torch.zeros(1, device=device, dtype=i32)
         self.splat_buffer = torch.zeros([MAX_NUM_RENDERED, 32], device=device, dtype=torch.float32)
         self.device = device
+        # frames binned into this buffer so far; a backward checks that its
+        # forward's frame is still the one the buffer holds
+        self.generation = 0
 
 
 _HOST_COUNTS: dict = {}
@@ -62,8 +92,10 @@ def _host_counts(dev) -> torch.Tensor:
 
 def _bin(buffer, rs, means3D, dc, shs, colors_precomp, opacities, scales, rotations, culling):
     """Preprocess and sort into the shared Buffer (FB __init__.py:96-119): returns (radii, num_rendered)."""
+    buffer.generation = getattr(buffer, "generation", 0) + 1
+    ext = _ext()
     buffer.curr_offset.fill_(0)
-    radii = _C.ops.preprocess(
+    radii = ext.ops.preprocess(
         rs.sh_degree, means3D, colors_precomp, dc, shs, opacities, scales, rotations, rs.scale_modifier,
         rs.image_width, rs.image_height, 16, 16, rs.campos, rs.viewmatrix, rs.projmatrix, rs.tanfovx, rs.tanfovy,
         100.0, 0.01, buffer.gaussian_keys_unsorted, buffer.gaussian_values_unsorted, buffer.gaussian_values_sorted,
@@ -73,8 +105,7 @@ def _bin(buffer, rs, means3D, dc, shs, colors_precomp, opacities, scales, rotati
     # copy-engine queueing behind the caller's own transfers), one synchronisation.
     counts = _host_counts(means3D.device)
     stream = torch.cuda.current_stream(means3D.device)
-    _lib.call("fgs_read_counts", buffer.curr_offset.data_ptr(), _C._counters(means3D.device).data_ptr(),
-              counts.data_ptr(), stream.cuda_stream)
+    ext.read_counts(buffer.curr_offset, counts)
     stream.synchronize()
     num_rendered, num_tasks = int(counts[0]), int(counts[1])
     if num_rendered >= buffer.MAX_NUM_RENDERED or num_tasks > buffer.gaussian_values_sorted.numel() // 2:
@@ -82,9 +113,9 @@ def _bin(buffer, rs, means3D, dc, shs, colors_precomp, opacities, scales, rotati
         if num_rendered >= buffer.MAX_NUM_RENDERED:
             raise RuntimeError("Too many k-v pairs!")
         raise RuntimeError("preprocess overflowed a device queue (too many large Gaussians)")
-    _C.ops.sort_gaussian(num_rendered, rs.image_width, rs.image_height, 16, 16, buffer.list_sorting_space,
-                         buffer.gaussian_keys_unsorted, buffer.gaussian_values_unsorted, buffer.gaussian_keys_sorted,
-                         buffer.gaussian_values_sorted)
+    ext.ops.sort_gaussian(num_rendered, rs.image_width, rs.image_height, 16, 16, buffer.list_sorting_space,
+                          buffer.gaussian_keys_unsorted, buffer.gaussian_values_unsorted,
+                          buffer.gaussian_keys_sorted, buffer.gaussian_values_sorted)
     return radii, num_rendered
 
 
@@ -130,13 +161,14 @@ class _RasterizeGaussians(torch.autograd.Function):
         # every pixel is written by the merge, so no zero-fill is needed
         last_contributor = torch.empty((H, W, 1), device=means3D.device, dtype=torch.int)
         Ts_final = torch.empty((H, W, 1), device=means3D.device, dtype=torch.float)
-        bucket_sum, out_color, img_buffer, smp_buffer = _C.ops.render_16x16(
+        bucket_sum, out_color, img_buffer, smp_buffer = _ext().ops.render_16x16(
             N, num_rendered, W, H, splat_buffer, buffer.gaussian_keys_sorted, buffer.gaussian_values_sorted,
             buffer.ranges, raster_settings.bg, last_contributor, Ts_final, read_bucket_sum=False)
         ctx.raster_settings = raster_settings
         ctx.adam = adam
         ctx.num_rendered = num_rendered
         ctx.buffer = buffer
+        ctx.generation = buffer.generation
         ctx.bucket_sum = bucket_sum
         ctx.save_for_backward(means3D, scales, rotations, dc, shs, opacities, out_color, last_contributor,
                               Ts_final, radii, splat_buffer, img_buffer, smp_buffer, xyz_gradient_accum,
@@ -147,6 +179,9 @@ class _RasterizeGaussians(torch.autograd.Function):
     def backward(ctx, grad_out_color, _):
         rs = ctx.raster_settings
         buffer = ctx.buffer
+        if getattr(buffer, "generation", 0) != ctx.generation:
+            raise RuntimeError("the rasterizer's shared Buffer holds a later frame than this backward's forward: "
+                               "call backward before the next forward (or render_simp / render_depth)")
         zFar, zNear = 100.0, 0.01
         (means3D, scales, rotations, dc, shs, opacities, out_color, last_contributor, Ts_final, radii,
          splat_buffer, img_buffer, smp_buffer, xyz_gradient_accum, xyz_gradient_accum_abs, max_radii,
@@ -163,7 +198,7 @@ class _RasterizeGaussians(torch.autograd.Function):
                 xyz_gradient_accum_abs, max_radii, denom)
             return (None,) * 15
         (grad_mean2D, grad_color, grad_opacity, grad_mean3D, grad_cov3D, grad_dc, grad_shs, grad_scales,
-         grad_rotations) = _C.ops.backward(
+         grad_rotations) = _ext().ops.backward(
             rs.sh_degree, ctx.bucket_sum, means3D, radii, dc, shs, opacities, scales, rotations,
             rs.scale_modifier, rs.image_width, rs.image_height, 16, 16, rs.tanfovx, rs.tanfovy, zFar, zNear,
             rs.campos, rs.viewmatrix, rs.projmatrix, img_buffer, smp_buffer, splat_buffer,
@@ -250,8 +285,9 @@ def _render_simp(self, means3D, opacities, dc=None, shs=None, colors_precomp=Non
     buffer = _RasterizeGaussians.buffer
     with torch.no_grad():
         radii, K = _bin(buffer, rs, means3D, dc, shs, colors_precomp, opacities, scales, rotations, culling)
-        _, w, cnt, mx = _C.ops.render_simp(means3D.shape[0], K, rs.image_width, rs.image_height, buffer.splat_buffer,
-                                           buffer.gaussian_keys_sorted, buffer.gaussian_values_sorted, buffer.ranges)
+        _, w, cnt, mx = _ext().ops.render_simp(means3D.shape[0], K, rs.image_width, rs.image_height,
+                                               buffer.splat_buffer, buffer.gaussian_keys_sorted,
+                                               buffer.gaussian_values_sorted, buffer.ranges)
     return radii, w, cnt, mx
 
 
@@ -268,7 +304,7 @@ def _render_depth(self, means3D, opacities, dc=None, shs=None, colors_precomp=No
     buffer = _RasterizeGaussians.buffer
     with torch.no_grad():
         radii, K = _bin(buffer, rs, means3D, dc, shs, colors_precomp, opacities, scales, rotations, culling)
-        pts, depth, alpha, gidx, disc = _C.ops.render_depth(
+        pts, depth, alpha, gidx, disc = _ext().ops.render_depth(
             means3D.shape[0], K, rs.image_width, rs.image_height, buffer.splat_buffer, buffer.gaussian_keys_sorted,
             buffer.gaussian_values_sorted, buffer.ranges, means3D, scales, rotations, rs.projmatrix, rs.campos)
     return {"out_pts": pts, "rendered_depth": depth, "discriminants": disc, "gidx": gidx, "accum_alpha": alpha,
@@ -385,5 +421,5 @@ class SparseGaussianAdam(torch.optim.Adam):
             state['step'] += 1
             step = state['step']
             M = param.numel() // N
-            _C.ops.adamUpdate(param, param.grad, exp_avg, exp_avg_sq, visibility,
-                              lr * (1 - 0.999 ** step) ** 0.5 / (1 - 0.9 ** step), 0.9, 0.999, eps, N, M)
+            _ext().ops.adamUpdate(param, param.grad, exp_avg, exp_avg_sq, visibility,
+                                  float(lr * (1 - 0.999 ** step) ** 0.5 / (1 - 0.9 ** step)), 0.9, 0.999, eps, N, M)

@@ -18,6 +18,8 @@
 #include <algorithm>
 #include <mutex>
 
+#include <cuda.h>
+
 #include "internal.cuh"
 
 
@@ -380,11 +382,49 @@ constexpr int64_t kNoAllocMaxPairs = FGS_SORT_NOALLOC_MAX_PAIRS;
 constexpr size_t kNoAllocBytes = layout_for(kNoAllocMaxPairs).total;
 static __device__ __align__(256) unsigned char g_sort_scratch[kNoAllocBytes];
 
-// Device address of g_sort_scratch, looked up once per device (the host-side
-// name of a __device__ array is not a device address).
+// Device address of g_sort_scratch, looked up once per device and CUDA
+// context (the host-side name of a __device__ array is not a device address).
+// The cache is keyed on the context's process-unique id: after
+// cudaDeviceReset, or under another context on the same device, the array
+// lives at a new address and is looked up again.  The two driver calls are
+// reached through the runtime's entry-point query, so the library does not
+// link libcuda.
+using CtxGetCurrentFn = CUresult (*)(CUcontext*);
+using CtxGetIdFn = CUresult (*)(CUcontext, unsigned long long*);
+
+// Id of the calling thread's current context, or 0 when there is none or the
+// driver does not provide the query (the caller then looks the address up).
+unsigned long long current_context_id() {
+  static const CtxGetCurrentFn get_current = [] {
+    void* fn = nullptr;
+    cudaDriverEntryPointQueryResult q{};
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &fn, 4000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      fn = nullptr;
+    return reinterpret_cast<CtxGetCurrentFn>(fn);
+  }();
+  static const CtxGetIdFn get_id = [] {
+    void* fn = nullptr;
+    cudaDriverEntryPointQueryResult q{};
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &fn, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      fn = nullptr;
+    return reinterpret_cast<CtxGetIdFn>(fn);
+  }();
+  CUcontext ctx = nullptr;
+  unsigned long long id = 0;
+  if (!get_current || !get_id || get_current(&ctx) != CUDA_SUCCESS || !ctx || get_id(ctx, &id) != CUDA_SUCCESS)
+    return 0;
+  return id;
+}
+
+struct ScratchAddress {
+  unsigned long long context_id = 0;
+  void* ptr = nullptr;
+};
 constexpr int kMaxDevices = 64;
 std::mutex g_scratch_mu;
-void* g_scratch_ptr[kMaxDevices] = {nullptr};
+ScratchAddress g_scratch_addr[kMaxDevices];
 }  // namespace
 }  // namespace fgs
 
@@ -400,13 +440,16 @@ extern "C" fgs_status fgs_sort_noalloc(int64_t num_rendered, int width, int heig
   void* scratch = nullptr;
   {
     std::lock_guard<std::mutex> lk(g_scratch_mu);
-    if (!g_scratch_ptr[dev]) {
+    ScratchAddress& a = g_scratch_addr[dev];
+    const unsigned long long ctx = current_context_id();
+    if (!a.ptr || ctx == 0 || ctx != a.context_id) {
       void* p = nullptr;
       const cudaError_t e = cudaGetSymbolAddress(&p, g_sort_scratch);
       if (e != cudaSuccess || !p) return FGS_ERR_CUDA;
-      g_scratch_ptr[dev] = p;
+      a.ptr = p;
+      a.context_id = current_context_id();  // the lookup makes the runtime's context current
     }
-    scratch = g_scratch_ptr[dev];
+    scratch = a.ptr;
   }
   // fgs_sort zeroes the histogram and look-back words it needs on every call.
   return fgs_sort(num_rendered, width, height, block_x, block_y, scratch, kNoAllocBytes, keys_in, values_in,

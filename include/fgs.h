@@ -118,7 +118,10 @@ fgs_status fgs_sort(int64_t num_rendered, int width, int height, int block_x, in
  * pairs (about 14 MiB, held by every GPU that loads the library until the
  * process exits); larger num_rendered returns FGS_ERR_CAPACITY.  The first
  * call on a device looks up the array's device address, so make that first
- * call before any stream capture.  All calls share the array: calls that
+ * call before any stream capture; the address is cached per CUDA context and
+ * looked up again after cudaDeviceReset or under another context of the same
+ * device (make that first call outside capture too).  All calls share the
+ * array: calls that
  * overlap on the GPU (other streams, other threads) race and must be
  * serialised by the caller.  Calls no allocator.
  */

@@ -14,7 +14,9 @@ cannot run where the fixtures are generated.
 from __future__ import annotations
 
 import ctypes as C
+import hashlib
 import os
+import platform
 import shutil
 import subprocess
 from pathlib import Path
@@ -24,13 +26,18 @@ import numpy as np
 HERE = Path(__file__).resolve().parent
 SRC = HERE / "oracle.cpp"
 LIB = HERE / "liboracle.so"
+STAMP = HERE / "liboracle.so.stamp"
 
 _lib = None
 
 
+def _stamp() -> str:
+    return hashlib.sha256(SRC.read_bytes() + platform.machine().encode()).hexdigest()
+
+
 def build(force: bool = False) -> Path:
-    """g++ -O2 -fopenmp -shared; skipped when the library is newer than the source."""
-    if not force and LIB.exists() and LIB.stat().st_mtime >= SRC.stat().st_mtime:
+    """g++ -O2 -fopenmp -shared; skipped when the stamp (source hash and machine) matches."""
+    if not force and LIB.exists() and STAMP.exists() and STAMP.read_text() == _stamp():
         return LIB
     cxx = os.environ.get("CXX") or shutil.which("g++") or "g++"
     tmp = LIB.with_suffix(".so.tmp")
@@ -39,6 +46,7 @@ def build(force: bool = False) -> Path:
     if r.returncode != 0:
         raise RuntimeError(f"oracle build failed:\n{r.stderr}")
     os.replace(tmp, LIB)
+    STAMP.write_text(_stamp())
     return LIB
 
 

@@ -1,7 +1,7 @@
 """Generates the golden fixtures that pin the CPU oracle against the reference.
 
-Runs the reference's own Python code, imported from a FasterGS checkout
-(default /root/reference, override with FASTERGS_REF), on seeded inputs and
+Runs the reference's own Python code, imported from the FasterGS checkout
+named by the FASTERGS_REF environment variable (required), on seeded inputs and
 stores inputs and outputs in tests/golden/*.npz:
 
   sh_golden.npz       3DGS/utils/sh_utils.py eval_sh, degrees 0..3
@@ -41,11 +41,18 @@ import numpy as np
 import torch
 
 HERE = Path(__file__).resolve().parent
-REF = Path(os.environ.get("FASTERGS_REF", "/root/reference"))
+
+
+def _ref() -> Path:
+    """The FasterGS checkout whose Python code generates the fixtures (FASTERGS_REF, required)."""
+    ref = os.environ.get("FASTERGS_REF")
+    if not ref:
+        raise SystemExit("set FASTERGS_REF to the FasterGS checkout (its 3DGS/ Python code makes the fixtures)")
+    return Path(ref)
 
 
 def _load(rel: str, name: str):
-    spec = importlib.util.spec_from_file_location(name, REF / rel)
+    spec = importlib.util.spec_from_file_location(name, _ref() / rel)
     mod = importlib.util.module_from_spec(spec)
     spec.loader.exec_module(mod)
     return mod
@@ -177,7 +184,7 @@ def make_ply(rng):
     sys.modules["plyfile"] = cap.module
     sys.modules["simple_knn"] = types.ModuleType("simple_knn")
     sys.modules["simple_knn._C"] = types.SimpleNamespace(distCUDA2=None)
-    sys.path.insert(0, str(REF / "3DGS"))
+    sys.path.insert(0, str(_ref() / "3DGS"))
     try:
         gm = _load("3DGS/scene/gaussian_model.py", "ref_gaussian_model")
         proxy = _cpu_torch_proxy()
@@ -214,7 +221,7 @@ def make_ply(rng):
                 out[f"loaded_{k}{deg}"] = t.detach().numpy()
         np.savez_compressed(HERE / "ply_golden.npz", **out)
     finally:
-        sys.path.remove(str(REF / "3DGS"))
+        sys.path.remove(str(_ref() / "3DGS"))
         for k, v in saved.items():
             if v is None:
                 sys.modules.pop(k, None)
@@ -248,8 +255,8 @@ def make_cameras_ts(rng):
 
 
 def main():
-    if not REF.exists():
-        sys.exit(f"reference checkout not found at {REF}")
+    if not _ref().exists():
+        sys.exit(f"reference checkout not found at {_ref()}")
     rng = np.random.default_rng(20240611)
     make_sh(rng)
     make_cov(rng)

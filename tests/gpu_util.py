@@ -18,27 +18,33 @@ def tensors(scene, dev):
 _BUFFERS = {}
 
 
-def buffer(dev, cap=2**21):
-    key = (str(dev), cap)
+def buffer(dev, cap=2**21, buffer_cls=None):
+    cls = Buffer if buffer_cls is None else buffer_cls
+    key = (str(dev), cap, cls)
     if key not in _BUFFERS:
         _BUFFERS.clear()
         torch.cuda.empty_cache()
-        _BUFFERS[key] = Buffer(device=dev, MAX_NUM_RENDERED=cap)
+        _BUFFERS[key] = cls(device=dev, MAX_NUM_RENDERED=cap)
     return _BUFFERS[key]
 
 
 def run_forward(scene, dev, bg=(0.0, 0.0, 0.0), culling=None, colors=None, mult=1.0, smod=1.0, cap=2**21,
-                shs_override="keep"):
+                shs_override="keep", ops=None, buffer_cls=None, T=None):
+    """One forward through ``ops`` (this library's ``_C.ops`` by default, or the reference
+    backend's, which takes the same arguments) in FB's call order (FB ``__init__.py:98-140``).
+    ``T`` overrides the scene's activated parameter tensors."""
+    ours = ops is None
+    ops = _C.ops if ours else ops
     cam = scene.camera
-    T = tensors(scene, dev)
-    buf = buffer(dev, cap)
+    T = tensors(scene, dev) if T is None else T
+    buf = buffer(dev, cap, buffer_cls)
     f = lambda a: torch.tensor(np.asarray(a, np.float32), device=dev)
     empty = torch.tensor([])
     shs = T["shs"] if shs_override == "keep" else shs_override
     cull = empty.bool() if culling is None else torch.tensor(culling, device=dev)
     col = empty if colors is None else f(colors)
     buf.curr_offset.fill_(0)
-    radii = _C.ops.preprocess(scene.sh_degree, T["means"], col, T["dc"] if colors is None else empty,
+    radii = ops.preprocess(scene.sh_degree, T["means"], col, T["dc"] if colors is None else empty,
                               shs if colors is None else empty, T["opacities"], T["scales"], T["rotations"], smod,
                               cam.width, cam.height, 16, 16, f(cam.campos), f(cam.viewmatrix), f(cam.projmatrix),
                               cam.tanfovx, cam.tanfovy, 100.0, 0.01, buf.gaussian_keys_unsorted,
@@ -46,19 +52,19 @@ def run_forward(scene, dev, bg=(0.0, 0.0, 0.0), culling=None, colors=None, mult=
                               buf.splat_buffer, cull)
     K = int(buf.curr_offset.cpu()[0])
     assert K < buf.MAX_NUM_RENDERED
-    assert _C.device_errors(dev) == 0
+    assert not ours or _C.device_errors(dev) == 0
     keys_u = buf.gaussian_keys_unsorted[:K].clone()
     vals_u = buf.gaussian_values_unsorted[:K].clone()
-    _C.ops.sort_gaussian(K, cam.width, cam.height, 16, 16, buf.list_sorting_space, buf.gaussian_keys_unsorted,
+    ops.sort_gaussian(K, cam.width, cam.height, 16, 16, buf.list_sorting_space, buf.gaussian_keys_unsorted,
                          buf.gaussian_values_unsorted, buf.gaussian_keys_sorted, buf.gaussian_values_sorted)
     H, W = cam.height, cam.width
     lc = torch.zeros((H, W, 1), device=dev, dtype=torch.int32)
     Tf = torch.zeros((H, W, 1), device=dev, dtype=torch.float32)
-    bsum, out, img_buf, smp_buf = _C.ops.render_16x16(scene.P, K, W, H, buf.splat_buffer,
+    bsum, out, img_buf, smp_buf = ops.render_16x16(scene.P, K, W, H, buf.splat_buffer,
                                                       buf.gaussian_keys_sorted, buf.gaussian_values_sorted,
                                                       buf.ranges, f(bg), lc, Tf)
     torch.cuda.synchronize()
-    assert _C.device_errors(dev) == 0
+    assert not ours or _C.device_errors(dev) == 0
     P = scene.P
     return dict(
         K=K, bucket_sum=bsum, radii=radii, out_color=out, last_contrib=lc, Ts_final=Tf, img_buf=img_buf,
@@ -66,7 +72,7 @@ def run_forward(scene, dev, bg=(0.0, 0.0, 0.0), culling=None, colors=None, mult=
         keys_sorted=buf.gaussian_keys_sorted[:K].cpu().numpy(), vals_sorted=buf.gaussian_values_sorted[:K].cpu().numpy(),
         ranges=buf.ranges[: ((W + 15) // 16) * ((H + 15) // 16)].cpu().numpy(),
         rec=buf.splat_buffer[:P].cpu().numpy(), T=T, buf=buf, bg=f(bg), culling=cull, colors=col, shs=shs,
-        mult=mult, smod=smod)
+        mult=mult, smod=smod, ops=ops)
 
 
 def run_backward(scene, fw, dL, dev, stats=False):
@@ -78,7 +84,7 @@ def run_backward(scene, fw, dL, dev, stats=False):
     P = scene.P
     accum = [torch.zeros((P, 1), device=dev) for _ in range(4)] if stats else [empty] * 4
     colors = fw["colors"].numel() > 0
-    res = _C.ops.backward(scene.sh_degree, fw["bucket_sum"], T["means"], fw["radii"],
+    res = fw["ops"].backward(scene.sh_degree, fw["bucket_sum"], T["means"], fw["radii"],
                           T["dc"] if not colors else empty, fw["shs"] if not colors else empty, T["opacities"],
                           T["scales"], T["rotations"], fw["smod"], cam.width, cam.height, 16, 16, cam.tanfovx,
                           cam.tanfovy, 100.0, 0.01, f(cam.campos), f(cam.viewmatrix), f(cam.projmatrix),

@@ -61,3 +61,24 @@ def test_scenes_are_seeded_and_shaped():
     m, sc, rot, op, dc, shs = c.activated()
     np.testing.assert_allclose(np.linalg.norm(rot, axis=1), 1, rtol=1e-6)
     assert np.all((op > 0) & (op < 1))
+
+
+def test_reference_import_name_loads_the_compiled_extension():
+    # every backbone's --fastergs path does exactly this import (3DGS/gaussian_renderer/render_faster.py:16)
+    import __graft_entry__
+    __graft_entry__.build()
+    import diff_gaussian_rasterization_faster as drf
+    from diff_gaussian_rasterization_faster import GaussianRasterizationSettings, GaussianRasterizer  # noqa: F401
+    assert drf.GaussianRasterizer is fgs.GaussianRasterizer
+    assert drf._RasterizeGaussians is fgs._RasterizeGaussians
+    assert drf._C.__file__.endswith(".so"), "the _C of the drop-in package is the compiled extension"
+    for op in ("preprocess", "sort_gaussian", "get_sort_buffer_size", "render_16x16", "backward", "adamUpdate",
+               "render_simp", "render_depth"):
+        assert callable(getattr(drf._C.ops, op))
+    assert drf._C.ops.get_sort_buffer_size(1 << 20) == _C.ops.get_sort_buffer_size(1 << 20)
+    t = torch.zeros(4, 1)
+    with pytest.raises(ValueError, match="CUDA"):
+        drf._C.ops.preprocess(0, t, t, t, t, t, t, t, 1.0, 16, 16, 16, 16, t, t, t, 1.0, 1.0, 100.0, 0.01, t, t, t,
+                              t, 1.0, t, t)
+    out = drf.cpu_deep_copy_tuple((t, 3, "x"))
+    assert out[1:] == (3, "x") and out[0] is not t

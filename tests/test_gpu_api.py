@@ -239,3 +239,68 @@ def test_expired_wait_reports_timeout_and_context_survives(cuda_device):
     img, radii = render(s, raw_params(s, cuda_device), cuda_device)
     assert torch.isfinite(img).all() and int((radii > 0).sum()) > 0
     assert _C.device_errors(cuda_device) == 0
+
+
+class _Model:
+    """The attributes a backbone's GaussianModel hands the rasterizer (3DGS/scene/gaussian_model.py:
+    get_xyz, get_opacity = sigmoid, get_scaling = exp, get_rotation = normalize, _features_dc/_rest)."""
+
+    def __init__(self, scene, dev):
+        t = lambda a: torch.nn.Parameter(torch.tensor(np.asarray(a, np.float32), device=dev))
+        self._xyz, self._scaling, self._rotation = t(scene.means), t(scene.log_scales), t(scene.quats)
+        self._opacity, self._features_dc, self._features_rest = t(scene.opacity_logits), t(scene.dc), t(scene.shs)
+        self.active_sh_degree = scene.sh_degree
+
+    get_xyz = property(lambda self: self._xyz)
+    get_opacity = property(lambda self: torch.sigmoid(self._opacity))
+    get_scaling = property(lambda self: torch.exp(self._scaling))
+    get_rotation = property(lambda self: torch.nn.functional.normalize(self._rotation))
+
+
+def test_reference_import_name_runs_the_backbone_call_sequence(cuda_device):
+    # the --fastergs render of 3DGS/gaussian_renderer/render_faster.py:16-66, line for line
+    import math
+    from diff_gaussian_rasterization_faster import GaussianRasterizationSettings as S, GaussianRasterizer as R
+    s = scenes.scene_c2(seed=1, P=20000, width=320, height=208)
+    pc = _Model(s, cuda_device)
+    cam = s.camera
+    t = lambda a: torch.tensor(np.asarray(a, np.float32), device=cuda_device)
+    raster_settings = S(image_height=int(cam.height), image_width=int(cam.width), tanfovx=math.tan(cam.fovx * 0.5),
+                        tanfovy=math.tan(cam.fovy * 0.5), bg=torch.zeros(3, device=cuda_device), scale_modifier=1.0,
+                        viewmatrix=t(cam.viewmatrix), projmatrix=t(cam.projmatrix), sh_degree=pc.active_sh_degree,
+                        mult=1.0, campos=t(cam.campos), prefiltered=False, debug=False)
+    rasterizer = R(raster_settings=raster_settings)
+    dc, shs = pc._features_dc, pc._features_rest
+    rendered_image, radii = rasterizer(means3D=pc.get_xyz, dc=dc, shs=shs, opacities=pc.get_opacity,
+                                       scales=pc.get_scaling, rotations=pc.get_rotation)
+    dL = torch.tensor(scenes.upstream_grad(0, cam.height, cam.width), device=cuda_device)
+    (rendered_image * dL).sum().backward()
+    # the same frame through the ctypes binding of the C ABI (this package's _C.ops)
+    from gpu_util import run_backward, run_forward
+    T = dict(means=pc.get_xyz.detach(), scales=pc.get_scaling.detach().contiguous(),
+             rotations=pc.get_rotation.detach().contiguous(), opacities=pc.get_opacity.detach().contiguous(),
+             dc=dc.detach(), shs=shs.detach())
+    fw = run_forward(s, cuda_device, T=T)
+    assert torch.equal(radii, fw["radii"])
+    assert (rendered_image.detach() - fw["out_color"]).abs().max().item() == 0.0
+    g = run_backward(s, fw, dL.cpu().numpy(), cuda_device)
+    for name, leaf, ref in (("means", pc._xyz, "dmean3D"), ("dc", pc._features_dc, "ddc"),
+                            ("shs", pc._features_rest, "dsh")):
+        a = leaf.grad.cpu().numpy().astype(np.float64).reshape(g[ref].shape)
+        assert np.abs(a - g[ref]).max() <= 1e-6 * max(np.abs(g[ref]).max(), 1e-30), name
+    for leaf in (pc._scaling, pc._rotation, pc._opacity):
+        assert leaf.grad is not None and torch.isfinite(leaf.grad).all()
+
+
+def test_backward_after_a_later_forward_raises(cuda_device):
+    # the shared Buffer holds one frame; FB would silently differentiate the second frame's lists
+    s = scenes.scene_c1(P=2000)
+    p = raw_params(s, cuda_device)
+    img1, _ = render(s, p, cuda_device)
+    with torch.no_grad():
+        render(s, p, cuda_device)
+    with pytest.raises(RuntimeError, match="later frame"):
+        img1.sum().backward()
+    img3, _ = render(s, p, cuda_device)
+    img3.sum().backward()  # forward then backward: fine
+    assert torch.isfinite(p["means"].grad).all()

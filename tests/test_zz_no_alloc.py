@@ -8,6 +8,11 @@ call after call.
 Kept in a file that pytest collects last; it passes alone in a fresh process
 and after the other tests.
 """
+import subprocess
+import sys
+import textwrap
+from pathlib import Path
+
 import numpy as np
 import pytest
 import torch
@@ -62,3 +67,54 @@ def test_sort_noalloc_rejects_more_pairs_than_its_scratch_holds(cuda_device):
     with pytest.raises(_lib.FgsError, match="too small"):
         _lib.call("fgs_sort_noalloc", MAX_PAIRS + 1, 256, 256, 16, 16, 0, 0, 0, 0,
                   torch.cuda.current_stream().cuda_stream)
+
+
+# A process of its own (no torch): sorts through fgs_sort_noalloc, resets the
+# device (which destroys the context and the library's static array with it),
+# and sorts again in the new context.  The second call must find the array's
+# new address instead of reusing the first context's.
+_RESET_CHILD = textwrap.dedent("""
+    import ctypes as C, sys
+    import numpy as np
+    fgs = C.CDLL(sys.argv[1])
+    rt = C.CDLL("libcudart.so.13")
+    vp = C.c_void_p
+    rt.cudaMalloc.argtypes = [C.POINTER(vp), C.c_size_t]
+    rt.cudaMemcpy.argtypes = [vp, vp, C.c_size_t, C.c_int]
+    fgs.fgs_sort_noalloc.argtypes = [C.c_int64, C.c_int, C.c_int, C.c_int, C.c_int, vp, vp, vp, vp, vp]
+    def check(e, what):
+        if e != 0:
+            raise SystemExit(f"{what}: error {e}")
+    def sort_once(seed):
+        rng = np.random.default_rng(seed)
+        K, W, H = 300_001, 1297, 840
+        T = ((W + 15) // 16) * ((H + 15) // 16)
+        keys = (rng.integers(0, T, K, dtype=np.uint64) << np.uint64(32)) | rng.integers(
+            0x3e000000, 0x42000000, K, dtype=np.uint64)
+        vals = rng.permutation(K).astype(np.uint32)
+        bufs = []
+        for n in (8 * K, 4 * K, 8 * K, 4 * K):
+            p = vp()
+            check(rt.cudaMalloc(C.byref(p), n), "cudaMalloc")
+            bufs.append(p)
+        check(rt.cudaMemcpy(bufs[0], keys.ctypes.data, 8 * K, 1), "upload keys")
+        check(rt.cudaMemcpy(bufs[1], vals.ctypes.data, 4 * K, 1), "upload values")
+        check(fgs.fgs_sort_noalloc(K, W, H, 16, 16, bufs[0], bufs[1], bufs[2], bufs[3], None), "fgs_sort_noalloc")
+        check(rt.cudaDeviceSynchronize(), "synchronize")
+        ko, vo = np.empty(K, np.uint64), np.empty(K, np.uint32)
+        check(rt.cudaMemcpy(ko.ctypes.data, bufs[2], 8 * K, 2), "download keys")
+        check(rt.cudaMemcpy(vo.ctypes.data, bufs[3], 4 * K, 2), "download values")
+        order = np.argsort(keys, kind="stable")
+        if not (np.array_equal(ko, keys[order]) and np.array_equal(vo, vals[order])):
+            raise SystemExit(f"seed {seed}: sorted output differs from a stable sort")
+    sort_once(1)
+    check(rt.cudaDeviceReset(), "cudaDeviceReset")
+    sort_once(2)
+    print("ok")
+""")
+
+
+def test_sort_noalloc_after_device_reset(cuda_device):
+    lib = Path(_lib.load()._name)
+    r = subprocess.run([sys.executable, "-c", _RESET_CHILD, str(lib)], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0 and r.stdout.strip().endswith("ok"), r.stdout + r.stderr
