@@ -737,8 +737,9 @@ def batched_bench(args, dev, s, dev_in, cams, label):
         "workload": label, "cameras": V, "resolutions": sorted({f"{c.width}x{c.height}" for c in cams}),
         "pixels": int(sum(c.width * c.height for c in cams)), "pairs": int(pairs),
         "tune": cfg.__dict__.copy(), "tune_sweep_ms": {f"b{r['config']['bucket_size']}_{r['config']['block_x']}x"
-                                                       f"{r['config']['block_y']}_p{r['config']['packet']}":
-                                                       round(r["ms"], 3) for r in table},
+                                                       f"{r['config']['block_y']}_p{r['config']['packet']}"
+                                                       f"_c{r['config']['chain']}": round(r["ms"], 3)
+                                                       for r in table},
         "plain_ms_per_step": round(plain_ms, 3), "batched_ms_per_step": round(batched_ms, 3),
         "speedup_fwd_bwd": round(plain_ms / batched_ms, 3),
         "plain_render_fps": round(1000.0 * V / plain_fwd_ms, 1),
@@ -964,13 +965,17 @@ def ctypes_peak_ex2(dev):
 
 
 def ctypes_peak_fp32(dev):
-    """Measured FP32 FMA throughput (TFLOP/s) of this GPU, via the library's microbenchmark."""
+    """Measured FP32 FMA throughput (TFLOP/s) of this GPU, via the library's microbenchmarks: the
+    larger of scalar fmaf chains and packed fma.rn.f32x2 chains (the form the compositing kernels
+    issue), with both figures."""
     import ctypes
     import torch
     from fastergs_gb300 import _lib
-    out = ctypes.c_double(0.0)
-    _lib.call("fgs_peak_fp32", ctypes.byref(out), torch.cuda.current_stream(dev).cuda_stream)
-    return float(out.value)
+    s = torch.cuda.current_stream(dev).cuda_stream
+    scalar, packed = ctypes.c_double(0.0), ctypes.c_double(0.0)
+    _lib.call("fgs_peak_fp32", ctypes.byref(scalar), s)
+    _lib.call("fgs_peak_fp32x2", ctypes.byref(packed), s)
+    return {"peak": max(scalar.value, packed.value), "ffma": round(scalar.value, 2), "ffma_x2": round(packed.value, 2)}
 
 
 # FP32 FLOPs (FMA = 2) per pixel-Gaussian evaluation in the compositing
@@ -979,14 +984,23 @@ def ctypes_peak_fp32(dev):
 # dL/dalpha and the un-blend (15), mean / conic / colour / opacity terms (25),
 # plus 2 for the |dL/dmean2D| sums when the caller asks for the
 # xyz_gradient_accum_abs statistic (the bench step, like 3DGS and Taming,
-# does not, and the kernel then skips them).
+# does not, and the kernel then skips them).  The backward's 48 counts every
+# FMA as 2; counted as instructions (FMA = 1, as the ~35 FP32 operations per
+# evaluation quoted for FB's pix_backward do) it is 36.
 FLOP_PER_EVAL = {"render_fwd": 17, "render_bwd": 48}
+FLOP_DERIVATION = {
+    "render_fwd": "exponent 5 + exp2/clamp/cut 3 + blend 9 = 17 FLOP (FMA = 2)",
+    "render_bwd": "alpha 8 + dL/dalpha and un-blend 15 + mean/conic/colour/opacity terms 25 = 48 FLOP (FMA = 2; "
+                  "36 FP32 instructions)",
+}
 # MUFU operations per evaluation: the alpha's ex2 (forward); ex2 and the
 # 1 / (1 - alpha) reciprocal (backward).  Against fgs_peak_ex2.
 MUFU_PER_EVAL = {"render_fwd": 1, "render_bwd": 2}
 
 # DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) of the
-# C2 workload, from the ncu captures summarised in profiles/ncu_c2_kernels.md.
+# C2 workload (1M Gaussians, 1297x840, 3,103,742 pairs), from one ncu capture
+# of each kernel; the file gives the command that made it.
+TRAFFIC_SOURCE = "profiles/ncu_c2_kernels.md"
 TRAFFIC_PER_LAUNCH = {"render_bwd": 83_665_920, "render_fwd": 77_669_120, "sort_pass": 38_493_696,
                       "preprocess_bwd": 511_551_488, "preprocess": 215_542_016}
 
@@ -1015,7 +1029,7 @@ def roofline(res, peaks):
     dom = max(steps_ms, key=lambda k: steps_ms[k])
     hbm = peaks.get("hbm_gbs", 6800.0)
     hbm_src = "of measured (MEASURED_PEAKS.json hbm_gbs)" if "hbm_gbs" in peaks else "of fallback 6.8 TB/s"
-    fp32 = res["fp32_peak"]
+    fp32 = res["fp32_peak"]["peak"]
     W = res["W_eval"]
     per_launch_ms = steps_ms[dom] / max(launches[dom], 1)
     traffic = TRAFFIC_PER_LAUNCH.get(dom) if res["P"] == 1_000_000 else None
@@ -1024,17 +1038,22 @@ def roofline(res, peaks):
         achieved = flops / (per_launch_ms * 1e-3) / 1e12
         roof = {"kernel": dom, "bound": "fp32", "achieved": round(achieved, 2), "peak": round(fp32, 2),
                 "unit": "TFLOP/s", "frac": round(achieved / fp32, 4), "traffic": traffic,
-                "peak_source": "of measured (fgs_peak_fp32 FFMA microbenchmark, this run)",
+                "traffic_source": TRAFFIC_SOURCE if traffic else None,
+                "peak_source": "of measured (larger of the fgs_peak_fp32 FFMA and fgs_peak_fp32x2 packed-FFMA "
+                               "microbenchmarks, this run)", "peaks_tflops": res["fp32_peak"],
                 "ms_per_launch": round(per_launch_ms, 4), "evaluations": int(W),
-                "flop_per_evaluation": FLOP_PER_EVAL[dom],
-                "hbm_frac": round(algo[dom] / (per_launch_ms * 1e-3) / 1e9 / hbm, 4),
+                "flop_per_evaluation": FLOP_PER_EVAL[dom], "flop_derivation": FLOP_DERIVATION[dom],
+                # DRAM side from the measured DRAM bytes (the prefix samples the kernel reads stay in L2)
+                "hbm_frac": round(traffic / (per_launch_ms * 1e-3) / 1e9 / hbm, 4) if traffic else None,
+                "algorithmic_bytes": int(algo[dom]),
                 "ex2_peak_gops": round(res["ex2_peak"], 1),
                 "mufu_frac": round(W * MUFU_PER_EVAL[dom] / (per_launch_ms * 1e-3) / 1e9 / res["ex2_peak"], 4)}
     else:
         b = algo.get(dom, 0)
         achieved = b / (per_launch_ms * 1e-3) / 1e9 if per_launch_ms > 0 else 0.0
         roof = {"kernel": dom, "bound": "hbm", "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
-                "frac": round(achieved / hbm, 4), "traffic": traffic, "peak_source": hbm_src,
+                "frac": round(achieved / hbm, 4), "traffic": traffic,
+                "traffic_source": TRAFFIC_SOURCE if traffic else None, "peak_source": hbm_src,
                 "ms_per_launch": round(per_launch_ms, 4), "algorithmic_bytes": int(b)}
     table = {}
     for k in steps_ms:
@@ -1042,7 +1061,8 @@ def roofline(res, peaks):
             pl = steps_ms[k] / launches[k]
             entry = {"ms_per_launch": round(pl, 4), "launches": launches[k]}
             if k in algo and pl > 0:
-                entry["hbm_frac"] = round(algo[k] / (pl * 1e-3) / 1e9 / hbm, 4)
+                b = TRAFFIC_PER_LAUNCH.get(k) if (k in FLOP_PER_EVAL and res["P"] == 1_000_000) else algo[k]
+                entry["hbm_frac"] = round(b / (pl * 1e-3) / 1e9 / hbm, 4) if b else None
             if k in FLOP_PER_EVAL and pl > 0:
                 entry["fp32_frac"] = round(W * FLOP_PER_EVAL[k] / (pl * 1e-3) / 1e12 / fp32, 4)
                 entry["mufu_frac"] = round(W * MUFU_PER_EVAL[k] / (pl * 1e-3) / 1e9 / res["ex2_peak"], 4)

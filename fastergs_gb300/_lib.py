@@ -27,7 +27,8 @@ class Camera(C.Structure):
 
 class TuneConfig(C.Structure):
     """fgs_tune_config: bucket size, tile shape and packet width of a launch."""
-    _fields_ = [("bucket_size", i32), ("block_x", i32), ("block_y", i32), ("packet", i32), ("recompute", i32)]
+    _fields_ = [("bucket_size", i32), ("block_x", i32), ("block_y", i32), ("packet", i32), ("recompute", i32),
+                ("chain", i32)]
 
 
 ADAM_GROUPS = ("xyz", "f_dc", "f_rest", "opacity", "scaling", "rotation")  # FGS_ADAM_* order
@@ -85,6 +86,7 @@ SIGNATURES = {
     "fgs_batch_status": (i32, [i32, i32, camp, tunep, i64, vp, C.POINTER(C.c_int64), C.POINTER(C.c_int64), vp]),
     "fgs_batch_offsets": (i32, [i32, i32, camp, tunep, i64, C.POINTER(C.c_int64), i32]),
     "fgs_peak_fp32": (i32, [C.POINTER(C.c_double), vp]),
+    "fgs_peak_fp32x2": (i32, [C.POINTER(C.c_double), vp]),
     "fgs_peak_ex2": (i32, [C.POINTER(C.c_double), vp]),
     "fgs_kernel_timer": (i32, [i32, i32]),
     "fgs_kernel_timer_read": (i32, [i32, C.POINTER(C.c_double), C.POINTER(C.c_int)]),
@@ -94,7 +96,7 @@ SIGNATURES = {
 KERNELS = {"preprocess": 0, "preprocess_large": 1, "sort_hist": 2, "sort_pass": 3, "tile_ranges": 4,
            "bucket_setup": 5, "render_fwd": 6, "empty_tiles": 7, "render_bwd": 8, "preprocess_bwd": 9,
            "loss": 10, "render_simp": 11, "render_depth": 12, "read_counts": 13,
-           "bwd_list": 14}
+           "bwd_list": 14, "deep_merge": 15}
 
 
 class FgsError(RuntimeError):

@@ -42,9 +42,11 @@ class TuneConfig:
     block_y: int = 16
     packet: int = 4
     recompute: bool = False  # rebuild bucket prefixes in the backward instead of storing them
+    chain: int = 8  # forward fold-chain length per tile, in (sub-)buckets (results identical for any length)
 
     def as_c(self) -> _lib.TuneConfig:
-        return _lib.TuneConfig(self.bucket_size, self.block_x, self.block_y, self.packet, int(self.recompute))
+        return _lib.TuneConfig(self.bucket_size, self.block_x, self.block_y, self.packet, int(self.recompute),
+                               self.chain)
 
 
 class BatchOverflow(RuntimeError):

@@ -67,8 +67,8 @@ __global__ void __launch_bounds__(kWarp) k_render_simp(int P, int W, int H, int 
           for (int cc = 0; cc < M::kCols; ++cc) {
             const int k = r * M::kCols + cc;
             if (!((mask >> k) & 1u) || !((in_img >> k) & 1u)) continue;
-            const float dx = centre_offset(pos.x, pos.z, pxc[cc]), dy = centre_offset(pos.y, pos.w, pyr[r]);
-            const float w = fmaf(q4.y, dy, dx);
+            const float dy = centre_offset(pos.y, pos.w, pyr[r]);
+            const float w = shear_offset(q4.y, pos.y - pyr[r], pos.x - pxc[cc], fmaf(q4.y, pos.w, pos.z));
             const float e = fmaf(q4.x * w, w, fmaf(q4.z * dy, dy, q4.w));
             const float al = fminf(kAlphaMax, ex2_approx(e));
             if (al < kAlphaCut) continue;
@@ -203,8 +203,8 @@ __global__ void __launch_bounds__(kDepthThreads) k_render_depth(
     const int cnt = min(kDepthThreads, re - base);
     for (int g = 0; !done && g < cnt; ++g) {
       const float4 pos = s_pos[g], q4 = s_quad[g];
-      const float dx = centre_offset(pos.x, pos.z, (float)px), dy = centre_offset(pos.y, pos.w, (float)py);
-      const float w = fmaf(q4.y, dy, dx);
+      const float dy = centre_offset(pos.y, pos.w, (float)py);
+      const float w = shear_offset(q4.y, pos.y - (float)py, pos.x - (float)px, fmaf(q4.y, pos.w, pos.z));
       const float e = fmaf(q4.x * w, w, fmaf(q4.z * dy, dy, q4.w));
       const float al = fminf(kAlphaMax, ex2_approx(e));
       if (al < kAlphaCut) continue;

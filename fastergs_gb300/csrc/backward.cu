@@ -290,9 +290,11 @@ __global__ void __launch_bounds__(kBwdWarps * kWarp, 6) k_render_bwd(const BwdAr
       const float4 c = st.rgb[g];
       const f2x A12 = f2_pack(q.x, q.x), A22 = f2_pack(2.f * q.x, 2.f * q.x), P2 = f2_pack(q.y, q.y);
       const f2x nr2 = f2_pack(-c.x, -c.x), ng2 = f2_pack(-c.y, -c.y), nb2 = f2_pack(-c.z, -c.z);
-      float dx[M::kCols];
+      const float wfrac = fmaf(q.y, pos.w, pos.z);  // P fy + fx (shear_offset)
+      const f2x wf2 = f2_pack(wfrac, wfrac);
+      float ix[M::kCols];
 #pragma unroll
-      for (int cc = 0; cc < M::kCols; ++cc) dx[cc] = centre_offset(pos.x, pos.z, pxc[cc]);
+      for (int cc = 0; cc < M::kCols; ++cc) ix[cc] = pos.x - pxc[cc];  // exact
       // Packed accumulators (the two halves are summed after the pixel loop):
       // mean x, y; conic moments w^2, w dy, dy^2; -colour; opacity.
       const f2x z2 = f2_pack(0.f, 0.f);
@@ -304,12 +306,13 @@ __global__ void __launch_bounds__(kBwdWarps * kWarp, 6) k_render_bwd(const BwdAr
         const int k0 = 2 * j, k1 = 2 * j + 1;
         if (((mask >> k0) & 3u) == 0u) continue;
         const int r0 = k0 / M::kCols, c0 = k0 % M::kCols, r1 = k1 / M::kCols, c1 = k1 % M::kCols;
-        const float dy0 = centre_offset(pos.y, pos.w, pyr[r0]);
-        const float dy1 = r1 == r0 ? dy0 : centre_offset(pos.y, pos.w, pyr[r1]);
+        const float iy0 = pos.y - pyr[r0], iy1 = r1 == r0 ? iy0 : pos.y - pyr[r1];  // exact
+        const float dy0 = iy0 + pos.w;
+        const float dy1 = r1 == r0 ? dy0 : iy1 + pos.w;
         const float f0 = fmaf(q.z * dy0, dy0, q.w);
         const float f1 = r1 == r0 ? f0 : fmaf(q.z * dy1, dy1, q.w);
         const f2x dy2 = f2_pack(dy0, dy1);
-        const f2x w2 = f2_fma(P2, dy2, f2_pack(dx[c0], dx[c1]));
+        const f2x w2 = f2_add(f2_fma(P2, f2_pack(iy0, iy1), f2_pack(ix[c0], ix[c1])), wf2);  // as the forward
         const f2x e2 = f2_fma(f2_mul(A12, w2), w2, f2_pack(f0, f1));
         float e0, e1;
         f2_unpack(e2, e0, e1);

@@ -74,7 +74,7 @@ BatchLayout plan(int P, int V, const int* W, const int* H, int bx, int by, int64
 bool config_ok(const fgs_tune_config* c) {
   return c && c->bucket_size >= 1 && c->bucket_size <= kMaxBucket && tile_shape_ok(c->block_x, c->block_y) &&
          (c->packet == 1 || c->packet == 2 || c->packet == 4 || c->packet == 8) &&
-         (c->recompute == 0 || c->recompute == 1);
+         (c->recompute == 0 || c->recompute == 1) && c->chain >= 0 && c->chain <= kRounds;
 }
 
 bool cameras_ok(int V, const fgs_camera* cams) {
@@ -174,7 +174,7 @@ extern "C" fgs_status fgs_render_batched_fwd(int P, int D, int M, const float* m
                         reinterpret_cast<uint64_t*>(ws + L.keys_s), reinterpret_cast<uint32_t*>(ws + L.vals_s),
                         reinterpret_cast<uint32_t*>(ws + L.ranges), out_color,
                         reinterpret_cast<int32_t*>(ws + L.last_contrib), reinterpret_cast<float*>(ws + L.ts_final),
-                        im, sm, L.buckets, cfg->recompute != 0, s);
+                        im, sm, L.buckets, cfg->recompute != 0, s, cfg->chain > 0 ? cfg->chain : kChainBuckets);
 }
 
 extern "C" fgs_status fgs_render_batched_bwd(int P, int D, int M, const float* means3D, const float* dc,

@@ -32,7 +32,7 @@ struct PreArgs {
 // Preprocess + large-Gaussian emission for every view (grid.y = view).
 fgs_status run_preprocess(PreArgs& a, cudaStream_t s);
 
-// Stable radix sort of n pairs on 32 + ceil(log2 tiles) key bits.  n = n_cap,
+// Stable radix sort of n pairs on 31 depth + ceil(log2 tiles) tile bits.  n = n_cap,
 // or min(n_cap, *n_dev) when n_dev is given (grids are sized for n_cap).
 fgs_status run_sort(int64_t n_cap, const int32_t* n_dev, uint32_t tiles, void* temp, size_t temp_bytes,
                     const uint64_t* keys_in, const uint32_t* values_in, uint64_t* keys_out, uint32_t* values_out,

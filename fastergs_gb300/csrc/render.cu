@@ -347,6 +347,7 @@ struct FwdArgs {
   uint32_t* max_contrib;
   int bs;      // Gaussians per (sub-)bucket
   int split;   // sub-buckets per bucket of the stop granularity
+  int chain;   // the tile's fold chain covers its first `chain` buckets (store mode)
 };
 
 template <int BX, bool RECOMPUTE>
@@ -400,6 +401,23 @@ __global__ void __launch_bounds__(kFwdWarps * kWarp, 7) k_render_fwd(const FwdAr
       composite_bucket<BX>(st, bi.n, spec, pxc, pyr, T, Cr, Cg, Cb);
     }
     __syncwarp();
+
+    if (!RECOMPUTE && bi.local >= a.chain) {
+      // Past the tile's chain: keep this bucket's own (C, T) for the
+      // sub-blocks that may still need it; k_deep_merge folds it in.
+      if (spec != 0u) {
+        float4* agg = a.samples + (size_t)b * kTilePixels;
+#pragma unroll
+        for (int r = 0; r < M::kRows; ++r)
+#pragma unroll
+          for (int cc = 0; cc < M::kCols; ++cc) {
+            const int k = r * M::kCols + cc;
+            if ((spec >> k) & 1u) __stcg(agg + M::pix(r, cc, lane), make_float4(Cr[k], Cg[k], Cb[k], T[k]));
+          }
+      }
+      q = q_next;
+      continue;
+    }
 
     // Fold into the tile's prefix (FB's merge, render.cu:285-391, per pixel
     // and in bucket order): C += T_prefix * C_b, T_prefix *= T_b; a pixel
@@ -490,6 +508,83 @@ __global__ void __launch_bounds__(kFwdWarps * kWarp, 7) k_render_fwd(const FwdAr
   }
 }
 
+// The buckets of deep tiles past their chain (local index >= FwdArgs::chain),
+// folded pixel-parallel once the composite kernel is done: FB's mergeResults
+// (render.cu:285-391) for those buckets.  One thread per pixel walks the
+// tile's remaining buckets in order from the chain's prefix, C += T C_b,
+// T *= T_b, overwriting each bucket's own (C_b, T_b) with the prefix after it
+// (what the backward reads), and stops after the bucket of the stop
+// granularity that takes T below 1e-4, or at the tile's last bucket, where it
+// writes its outputs.  Loads run kMergeAhead buckets ahead of the fold.
+constexpr int kMergeAhead = 4;
+
+template <int BX>
+__global__ void __launch_bounds__(kTilePixels) k_deep_merge(const FwdArgs a) {
+  using M = TileMap<BX>;
+  constexpr int BY = kTilePixels / BX;
+  __shared__ uint32_t s_max;
+  if (a.bucket_sum[0] == 0) return;  // the buckets did not fit: k_empty_tiles writes every tile
+  const int p = threadIdx.x, x = p % BX, y = p / BX;
+  const int k = (y / 4) * M::kCols + x / 8;  // the pixel's sub-block slot and lane in the composite kernels
+  const int owner = (y % 4) * 8 + (x % 8);
+  for (uint32_t tile = blockIdx.x; tile < a.views.tiles; tile += gridDim.x) {  // block-uniform
+    const int first = tile ? (int)a.bucket_off[tile - 1] : 0;
+    const int nb = (int)a.bucket_off[tile] - first;
+    if (nb <= a.chain || a.tile_stage[tile] == kStageDead) continue;  // the chain wrote every output
+    const ViewDesc& cam = a.views.v[a.views.of_tile(tile)];
+    const int lt = (int)tile - (int)cam.tile_off;
+    const int px = (lt % cam.gx) * BX + x, py = (lt / cam.gx) * BY + y;
+    const int ntile = (int)(a.ranges[2 * tile + 1] - a.ranges[2 * tile]);
+    if (p == 0) s_max = 0u;
+    __syncthreads();
+    uint32_t contrib = 0u;
+    if ((a.tile_alive[(size_t)tile * kPxPerThread + k] >> owner) & 1u) {  // still compositing after the chain
+      float4* slot = a.samples + (size_t)first * kTilePixels + p;
+      float4 pre = __ldcg(slot + (size_t)(a.chain - 1) * kTilePixels);
+      float4 ahead[kMergeAhead];
+#pragma unroll
+      for (int j = 0; j < kMergeAhead; ++j)
+        ahead[j] = a.chain + j < nb ? __ldcg(slot + (size_t)(a.chain + j) * kTilePixels)
+                                    : make_float4(0.f, 0.f, 0.f, 1.f);
+      for (int l0 = a.chain; l0 < nb && contrib == 0u; l0 += kMergeAhead) {
+        float4 cur[kMergeAhead];
+#pragma unroll
+        for (int j = 0; j < kMergeAhead; ++j) {
+          cur[j] = ahead[j];
+          const int ln = l0 + kMergeAhead + j;
+          ahead[j] = ln < nb ? __ldcg(slot + (size_t)ln * kTilePixels) : make_float4(0.f, 0.f, 0.f, 1.f);
+        }
+#pragma unroll
+        for (int j = 0; j < kMergeAhead; ++j) {
+          const int l = l0 + j;
+          if (l >= nb || contrib != 0u) break;
+          const float4 c = cur[j];
+          pre = make_float4(fmaf(pre.w, c.x, pre.x), fmaf(pre.w, c.y, pre.y), fmaf(pre.w, c.z, pre.z), pre.w * c.w);
+          __stcg(slot + (size_t)l * kTilePixels, pre);
+          if (((l + 1) % a.split == 0 && pre.w < kTMin) || l == nb - 1) {
+            contrib = (uint32_t)min(ntile, (l + 1) * a.bs);
+            const size_t HW = (size_t)cam.W * cam.H, pix = (size_t)py * cam.W + px;
+            float* oc = a.out_color + 3 * (size_t)cam.pix_off;
+            float* pc = a.pix_color + 3 * (size_t)cam.pix_off;
+            oc[pix] = pre.x + pre.w * cam.bg[0];
+            oc[HW + pix] = pre.y + pre.w * cam.bg[1];
+            oc[2 * HW + pix] = pre.z + pre.w * cam.bg[2];
+            pc[pix] = pre.x;
+            pc[HW + pix] = pre.y;
+            pc[2 * HW + pix] = pre.z;
+            a.last_contrib[cam.pix_off + pix] = (int)contrib;
+            a.Ts_final[cam.pix_off + pix] = pre.w;
+          }
+        }
+      }
+    }
+    if (contrib) atomicMax(&s_max, contrib);
+    __syncthreads();
+    if (p == 0) a.max_contrib[tile] = s_max;
+    __syncthreads();
+  }
+}
+
 // Self-check of the bounded waits: one warp waits, as a bucket of the chain
 // does, for a stage that nothing publishes; the wait gives up after
 // kSpinLimit polls, raises the timeout bit and the warp returns.
@@ -528,7 +623,8 @@ fgs_status run_render_fwd(const Views& views, int64_t n_cap, const int32_t* n_de
                           const float* splat, const uint64_t* keys_sorted, const uint32_t* values_sorted,
                           uint32_t* ranges, float* out_color, int32_t* last_contributor, float* Ts_final,
                           const ImageState& im, const SampleState& sm, int64_t max_buckets, bool recompute,
-                          cudaStream_t s) {
+                          cudaStream_t s, int chain) {
+  if (chain < 1) return FGS_ERR_BAD_ARG;
   fgs_status st = run_tile_ranges(n_cap, n_dev, views.tiles, keys_sorted, ranges, s);
   if (st != FGS_OK) return st;
   const int split = bucket_split(bucket_size), sub = sub_bucket_size(bucket_size);
@@ -547,7 +643,7 @@ fgs_status run_render_fwd(const Views& views, int64_t n_cap, const int32_t* n_de
   FGS_LAUNCH_CHECK();
   FwdArgs fa{views, splat, values_sorted, ranges, sm.bucket_queue, im.bucket_off, im.bucket_sum,
              sm.samples, im.tile_stage, im.tile_alive, out_color, im.pix_color, last_contributor, Ts_final,
-             im.max_contrib, sub, split};
+             im.max_contrib, sub, split, chain};
   {
     KernelTimer kt__(FGS_K_RENDER_FWD, s);
     const int nt = kFwdWarps * kWarp;
@@ -566,6 +662,15 @@ fgs_status run_render_fwd(const Views& views, int64_t n_cap, const int32_t* n_de
     kt__.stop();
   }
   FGS_LAUNCH_CHECK();
+  if (!recompute) {
+    KernelTimer kt__(FGS_K_DEEP_MERGE, s);
+    const unsigned grid = std::min<unsigned>(views.tiles, (unsigned)num_sms() * 8);
+    if (views.bx == 8) k_deep_merge<8><<<grid, kTilePixels, 0, s>>>(fa);
+    else if (views.bx == 16) k_deep_merge<16><<<grid, kTilePixels, 0, s>>>(fa);
+    else k_deep_merge<32><<<grid, kTilePixels, 0, s>>>(fa);
+    kt__.stop();
+    FGS_LAUNCH_CHECK();
+  }
   {
     KernelTimer kt__(FGS_K_EMPTY_TILES, s);
     k_empty_tiles<<<std::min<unsigned>(views.tiles, (unsigned)num_sms() * 8), kTilePixels, 0, s>>>(

@@ -201,6 +201,16 @@ __device__ __forceinline__ float centre_offset(float whole, float frac, float pi
   return (whole - pixel) + frac;
 }
 
+// The exponent's sheared offset w = dx + P dy from the exact integer offsets
+// ix = X - px, iy = Y - py and the Gaussian's constant wfrac = P fy + fx:
+// one rounding at the size of w itself.  Summing dx and P dy as rounded
+// values lost ~1e-4 px for a far-away elongated footprint (dx and P dy near
+// -1100 and +1100 px, w near 2), which moved alpha by 1e-4 relative and
+// could flip its 1/255 cut; here w is good to ~1e-7 px.
+__device__ __forceinline__ float shear_offset(float P, float iy, float ix, float wfrac) {
+  return fmaf(P, iy, ix) + wfrac;
+}
+
 // Composites a staged bucket front to back from T = 1, C = 0 for this lane's
 // 8 pixels, restricted to the sub-blocks in `live` (FB renderBucket,
 // render.cu:285-391): alpha = min(0.99, o 2^e), dropped below 1/255.
@@ -233,20 +243,23 @@ __device__ __forceinline__ void composite_bucket(const BucketStage& st, int n, u
       const float4 c = st.rgb[g];
       const f2x A2 = f2_pack(q4.x, q4.x), P2 = f2_pack(q4.y, q4.y);
       const f2x nr2 = f2_pack(-c.x, -c.x), ng2 = f2_pack(-c.y, -c.y), nb2 = f2_pack(-c.z, -c.z);
-      float dx[M::kCols];
+      const float wfrac = fmaf(q4.y, pos.w, pos.z);  // P fy + fx (shear_offset)
+      const f2x wf2 = f2_pack(wfrac, wfrac);
+      float ix[M::kCols];
 #pragma unroll
-      for (int cc = 0; cc < M::kCols; ++cc) dx[cc] = centre_offset(pos.x, pos.z, pxc[cc]);
+      for (int cc = 0; cc < M::kCols; ++cc) ix[cc] = pos.x - pxc[cc];  // exact
 #pragma unroll
       for (int j = 0; j < kPairs; ++j) {
         const int k0 = 2 * j, k1 = 2 * j + 1;  // pixel slots k = r * kCols + cc
         if (((mask >> k0) & 3u) == 0u) continue;
         const int r0 = k0 / M::kCols, c0 = k0 % M::kCols, r1 = k1 / M::kCols, c1 = k1 % M::kCols;
-        const float dy0 = centre_offset(pos.y, pos.w, pyr[r0]);
-        const float dy1 = r1 == r0 ? dy0 : centre_offset(pos.y, pos.w, pyr[r1]);
+        const float iy0 = pos.y - pyr[r0], iy1 = r1 == r0 ? iy0 : pos.y - pyr[r1];  // exact
+        const float dy0 = iy0 + pos.w;
+        const float dy1 = r1 == r0 ? dy0 : iy1 + pos.w;
         const float f0 = fmaf(q4.z * dy0, dy0, q4.w);  // log2 o + C1 dy^2
         const float f1 = r1 == r0 ? f0 : fmaf(q4.z * dy1, dy1, q4.w);
-        // alpha = o * exp(-q/2) = 2^(log2 o + A1 (dx + P dy)^2 + C1 dy^2)
-        const f2x w2 = f2_fma(P2, f2_pack(dy0, dy1), f2_pack(dx[c0], dx[c1]));
+        // alpha = o * exp(-q/2) = 2^(log2 o + A1 (dx + P dy)^2 + C1 dy^2), w = dx + P dy (shear_offset)
+        const f2x w2 = f2_add(f2_fma(P2, f2_pack(iy0, iy1), f2_pack(ix[c0], ix[c1])), wf2);
         const f2x e2 = f2_fma(f2_mul(A2, w2), w2, f2_pack(f0, f1));
         float e0, e1;
         f2_unpack(e2, e0, e1);
@@ -275,6 +288,19 @@ __device__ __forceinline__ void composite_bucket(const BucketStage& st, int n, u
 // tile_stage value of a tile whose pixels have all stopped: it satisfies every
 // wait, and the buckets that read it do nothing.
 constexpr uint32_t kStageDead = 0xffffffffu;
+
+// Length of a tile's fold chain in the forward (store mode).  The chain folds
+// a tile's first kChainBuckets (sub-)buckets one after another, which lets
+// every later bucket skip the sub-blocks whose pixels have stopped; each
+// link costs a few dependent L2 round trips.  A deep tile (hundreds of
+// buckets in a dense cluster) would make that chain the frame's critical
+// path, so its later buckets composite without waiting, store their own
+// (C, T) from T = 1 in their sample slot, and k_deep_merge folds them into
+// the prefix pixel-parallel once the composite kernel is done (FB's merge,
+// for those buckets only).  Both orders compute the same operations on the
+// same values: the results are bit-identical.  kChainBuckets is the default
+// length; the batched path takes it from its launch configuration.
+constexpr int kChainBuckets = 8;
 
 // Waits until a tile's first `stage` buckets are folded into its prefix.
 // Lane 0 polls (bounded); the bucket it waits for was handed out earlier and
@@ -365,7 +391,7 @@ fgs_status run_render_fwd(const Views& views, int64_t n_cap, const int32_t* n_de
                           const float* splat, const uint64_t* keys_sorted, const uint32_t* values_sorted,
                           uint32_t* ranges, float* out_color, int32_t* last_contributor, float* Ts_final,
                           const ImageState& im, const SampleState& sm, int64_t max_buckets, bool recompute,
-                          cudaStream_t s);
+                          cudaStream_t s, int chain = kChainBuckets);
 // Backward composite into grad_record (records x FGS_GRAD_STRIDE, zeroed here).
 // In recompute mode every needed bucket's prefix is rebuilt from the tile's
 // running prefix, in bucket order per tile.

@@ -11,8 +11,13 @@
 //     stable), publishes its per-digit counts, sorts the tile locally, obtains
 //     the exclusive prefix of all earlier tiles by a decoupled look-back, and
 //     scatters so that global writes form contiguous runs per digit;
-//   * only the key bits that can differ are sorted: 32 depth bits plus
-//     ceil(log2(tiles)) tile bits, i.e. 5-6 passes for 256..32768 tiles.
+//   * only the key bits that can differ are sorted: 31 depth bits (a depth is
+//     a positive float, so bit 31 of a key is zero) plus ceil(log2(tiles))
+//     tile bits.  The first pass packs each key to (tile << 31) | depth bits
+//     and the last one unpacks it, so 17 tile bits (the 16 views of a batched
+//     frame) still fit six 8-bit passes; 4-6 passes for 1..131072 tiles.  A
+//     key with bit 31 set is not a (tile, depth) key: the histogram raises the
+//     capacity bit of the error word for it.
 // Every look-back wait is bounded (kSpinLimit polls); on expiry the kernel
 // records kErrTimeout in the error word and continues, so it never hangs.
 #include <algorithm>
@@ -57,6 +62,14 @@ constexpr SortLayout layout_for(int64_t n) {
   L.alt_vals = off;  off = up(off + sizeof(uint32_t) * (size_t)n);
   L.total = off;
   return L;
+}
+
+// (tile << 32) | depth bits  <->  (tile << 31) | depth bits.
+__device__ __forceinline__ unsigned long long pack_key(unsigned long long k) {
+  return ((k >> 32) << 31) | (k & 0x7fffffffull);
+}
+__device__ __forceinline__ unsigned long long unpack_key(unsigned long long c) {
+  return ((c >> 31) << 32) | (c & 0x7fffffffull);
 }
 
 // All pass histograms in one read of the keys; the last block to finish turns
@@ -104,7 +117,9 @@ __global__ void __launch_bounds__(kSortThreads) k_histogram(const unsigned long 
 #pragma unroll
     for (int r = 0; r < kHistItems; ++r) {
       if (k0 + (long long)r * kSortThreads >= n) break;
-      for (int p = 0; p < passes; ++p) atomicAdd(&s_h[p][(key[r] >> (8 * p)) & 0xff], 1u);
+      if (key[r] & 0x80000000ull) raise_error(kErrCapacity);
+      const unsigned long long c = pack_key(key[r]);
+      for (int p = 0; p < passes; ++p) atomicAdd(&s_h[p][(c >> (8 * p)) & 0xff], 1u);
     }
   }
   __syncthreads();
@@ -153,7 +168,8 @@ __global__ void __launch_bounds__(kSortThreads) k_histogram(const unsigned long 
 __global__ void __launch_bounds__(kSortThreads, 2) k_onesweep(
     const unsigned long long* __restrict__ keys_in, const uint32_t* __restrict__ vals_in,
     unsigned long long* __restrict__ keys_out, uint32_t* __restrict__ vals_out, long long n_cap, const int* n_dev,
-    int shift, const uint32_t* __restrict__ digit_base, uint32_t* lookback, uint32_t* tile_counter) {
+    int shift, bool first, bool last, const uint32_t* __restrict__ digit_base, uint32_t* lookback,
+    uint32_t* tile_counter) {
   extern __shared__ __align__(16) unsigned char s_dyn[];  // kSortDynSmem bytes
   unsigned long long* s_keys = reinterpret_cast<unsigned long long*>(s_dyn);
   uint32_t* s_vals = reinterpret_cast<uint32_t*>(s_dyn + sizeof(unsigned long long) * kSortTile);
@@ -182,7 +198,7 @@ __global__ void __launch_bounds__(kSortThreads, 2) k_onesweep(
   for (int r = 0; r < kSortItems; ++r) {
     const long long idx = tile_base + warp * (kWarp * kSortItems) + r * kWarp + lane;
     if (idx < n) {
-      k[r] = keys_in[idx];
+      k[r] = first ? pack_key(keys_in[idx]) : keys_in[idx];
       v[r] = vals_in[idx];
     } else {
       k[r] = ~0ull;  // digit 255, ranked after every real key of the tile
@@ -286,7 +302,7 @@ __global__ void __launch_bounds__(kSortThreads, 2) k_onesweep(
     const unsigned long long kk = s_keys[j];
     const uint32_t pos = s_dst[(uint32_t)(kk >> shift) & 0xff] + (uint32_t)j;
     if ((long long)pos < n) {
-      keys_out[pos] = kk;
+      keys_out[pos] = last ? unpack_key(kk) : kk;
       vals_out[pos] = s_vals[j];
     } else {
       raise_error(kErrTimeout);  // only reachable after an expired look-back
@@ -312,7 +328,7 @@ fgs_status run_sort(int64_t n_cap, const int32_t* n_dev, uint32_t tiles, void* t
   if (((uintptr_t)temp & 255) || ((uintptr_t)keys_in & 7) || ((uintptr_t)keys_out & 7)) return FGS_ERR_BAD_ARG;
   const SortLayout L = layout_for(n_cap);
   if (temp_bytes < L.total) return FGS_ERR_CAPACITY;
-  const int bits = 32 + tile_bits(tiles);
+  const int bits = 31 + tile_bits(tiles);
   const int passes = (bits + 7) / 8;
   char* base = static_cast<char*>(temp);
   uint32_t* hist = reinterpret_cast<uint32_t*>(base + L.hist);
@@ -342,7 +358,7 @@ fgs_status run_sort(int64_t n_cap, const int32_t* n_dev, uint32_t tiles, void* t
     {
       KernelTimer kt__(FGS_K_SORT_PASS, s);
       k_onesweep<<<(unsigned)L.tiles, kSortThreads, kSortDynSmem, s>>>(src_k, src_v, dk, dv, n_cap, n_dev, 8 * p,
-                                                                      hist + p * kRadix,
+                                                                      p == 0, p == passes - 1, hist + p * kRadix,
                                                                       lookback + (size_t)p * L.tiles * kRadix,
                                                                       counters + p);
       kt__.stop();

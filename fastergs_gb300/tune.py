@@ -5,7 +5,9 @@ FB fixes bucket size 128, 16x16 tiles and 128-tile sub-tasks at compile time
 the scene (footprint spread, Gaussians per tile) and the camera set, so the
 batched path picks them per workload: every candidate ``TuneConfig`` is
 planned, captured as a CUDA graph of one step (forward, or forward +
-backward) and timed by replaying it; the fastest wins.  Results are cached
+backward) and timed by replaying it; the fastest wins.  The search sweeps
+bucket x tile x packet, then the forward's fold-chain length (``chain``,
+which leaves the results bit-identical) for the winner.  Results are cached
 per (Gaussian-count range, camera resolutions, SH degree, step kind) in
 memory and, when ``cache_path`` (or ``FGS_TUNE_CACHE``) names a file, on
 disk as JSON.
@@ -28,6 +30,7 @@ from .batched import BatchedRasterizer, CapturedStep, TuneConfig
 BUCKETS = (16, 32, 64)
 TILES = ((16, 16), (8, 32))
 PACKETS = (2, 4, 8)
+CHAINS = (2, 4, 8, 16, 32)
 
 _MEMO: dict = {}
 
@@ -112,12 +115,19 @@ def autotune(settings, params: dict, sh_degree: int = 3, candidates: Iterable[Tu
             return cfg, []
     table = []
     t0 = time.time()
-    for cfg in (list(candidates) if candidates is not None else search_space()):
-        ms, pairs = time_config(settings, params, sh_degree, cfg, backward, reps, warmup)
-        table.append(dict(config=dataclasses.asdict(cfg), ms=ms, pairs=pairs))
-        if verbose:
-            print(f"  {cfg}: {ms:.3f} ms  ({pairs} pairs)")
-        torch.cuda.empty_cache()
+
+    def sweep(cands):
+        for cfg in cands:
+            ms, pairs = time_config(settings, params, sh_degree, cfg, backward, reps, warmup)
+            table.append(dict(config=dataclasses.asdict(cfg), ms=ms, pairs=pairs))
+            if verbose:
+                print(f"  {cfg}: {ms:.3f} ms  ({pairs} pairs)")
+            torch.cuda.empty_cache()
+
+    sweep(list(candidates) if candidates is not None else search_space())
+    if candidates is None:  # second stage: the fold-chain length of the winner
+        lead = TuneConfig(**min(table, key=lambda r: r["ms"])["config"])
+        sweep([dataclasses.replace(lead, chain=c) for c in CHAINS if c != lead.chain])
     best = min(table, key=lambda r: r["ms"])
     cfg = TuneConfig(**best["config"])
     _MEMO[key] = cfg

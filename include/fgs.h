@@ -99,8 +99,12 @@ fgs_status fgs_preprocess(
 size_t fgs_sort_temp_bytes(int64_t num_rendered);
 
 /*
- * Stable ascending LSD radix sort of (key, value) pairs on the low
- * 32 + ceil(log2(tiles)) key bits, tiles = ceil(W/bx)*ceil(H/by).
+ * Stable ascending LSD radix sort of (key, value) pairs on the key bits
+ * that can differ: 31 depth bits and ceil(log2(tiles)) tile bits,
+ * tiles = ceil(W/bx)*ceil(H/by).  Keys are (tile << 32) | the bits of a
+ * positive float depth, so bit 31 is zero (FB's keys, whose depths exceed
+ * the 0.2 near cut); a key with bit 31 set raises the capacity bit of the
+ * device error word.
  * Replaces faster::sort_gaussian (FB csrc/ops.h:87-92, sort.cu:28-44), which
  * calls cub::DeviceRadixSort::SortPairs.  Inputs are not modified.
  */
@@ -359,6 +363,11 @@ typedef struct {
  * per bucket; a 128-Gaussian bucket is composited as two 64-Gaussian
  * sub-buckets with the stop tested after the second, as for fgs_render_fwd);
  * packet changes only the order in which pairs are emitted.
+ * chain 1..4096 (0: 8): the length of each tile's fold chain in the forward
+ * composite, in composited (sub-)buckets; a tile's later buckets composite
+ * without waiting and are folded pixel-parallel afterwards.  Results are
+ * bit-identical for every length; it only moves time between the chain's
+ * serial links and the speculative compositing of deep tiles.
  * recompute 1: the forward keeps one running (colour, transmittance) prefix
  * per tile instead of one per (sub-)bucket (4 KB each), and the backward
  * rebuilds each one's prefix from it -- bit-identical prefixes, a
@@ -369,6 +378,7 @@ typedef struct {
   int block_x, block_y;
   int packet;
   int recompute;
+  int chain;
 } fgs_tune_config;
 
 /* Workspace bytes (256-byte aligned base required) of a batched frame. */
@@ -457,13 +467,14 @@ fgs_status fgs_batch_offsets(int P, int num_views, const fgs_camera* cams, const
  * regions since the last read (FGS_K_BUCKET_SETUP times its three kernels as
  * one region; FGS_K_READ_COUNTS is the one-thread store of the pair and task
  * counts that fgs_read_counts launches; FGS_K_BWD_LIST builds the backward's
- * list of buckets that some pixel reaches).  No
+ * list of buckets that some pixel reaches; FGS_K_DEEP_MERGE folds the buckets
+ * of deep tiles past their chain).  No
  * counterpart in FB (its DEBUG_TIME macros are unused, ops.h:10-14). */
 enum {
   FGS_K_PREPROCESS = 0, FGS_K_PREPROCESS_LARGE = 1, FGS_K_SORT_HIST = 2, FGS_K_SORT_PASS = 3,
   FGS_K_TILE_RANGES = 4, FGS_K_BUCKET_SETUP = 5, FGS_K_RENDER_FWD = 6, FGS_K_EMPTY_TILES = 7,
   FGS_K_RENDER_BWD = 8, FGS_K_PREPROCESS_BWD = 9, FGS_K_LOSS = 10, FGS_K_SIMP = 11, FGS_K_DEPTH = 12,
-  FGS_K_READ_COUNTS = 13, FGS_K_BWD_LIST = 14, FGS_K_COUNT = 15
+  FGS_K_READ_COUNTS = 13, FGS_K_BWD_LIST = 14, FGS_K_DEEP_MERGE = 15, FGS_K_COUNT = 16
 };
 fgs_status fgs_kernel_timer(int kernel_id, int enable);
 fgs_status fgs_kernel_timer_read(int kernel_id, double* total_ms, int* launches);
@@ -472,6 +483,9 @@ fgs_status fgs_kernel_timer_read(int kernel_id, double* total_ms, int* launches)
  * thread on every SM; synchronises the stream): the ceiling for the
  * compositing kernels, which are bound by FP32 issue, not by HBM. */
 fgs_status fgs_peak_fp32(double* tflops, void* stream);
+/* The same with packed fma.rn.f32x2 (two FMAs per instruction, 4 FLOP), the
+ * form the compositing kernels issue their pixel pairs in. */
+fgs_status fgs_peak_fp32x2(double* tflops, void* stream);
 /* MUFU ex2.approx throughput in Gop/s (8 independent chains per thread on
  * every SM; synchronises the stream): one ex2 per pixel-Gaussian evaluation
  * in both compositing kernels. */

@@ -127,3 +127,58 @@ def replay_oracle(scene, fw, bg=(0.0, 0.0, 0.0), eps_alpha=1e-5, eps_T=1e-5, **k
     o.set_lists(fw["vals_sorted"], fw["ranges"])
     o.render(bg=bg, eps_alpha=eps_alpha, eps_T=eps_T)
     return o
+
+
+GRAD_KEYS = ["dmean2D", "dopacity", "dcolor", "dmean3D", "ddc", "dsh", "dscale", "drot"]
+# Per-entry floor of the gradient check, as a fraction of the tensor's largest
+# value: entries are sums over many pixels whose terms can cancel to a small
+# value, and the rounding of those terms stays behind.  dL/drot of a thin
+# footprint (condition number in the thousands) is a small difference of
+# large products: its entries are held to the per-tensor bound alone (on the
+# full-size C2 frame the worst needs 1.3e-5 of the largest value, summed over
+# three C4 views 7e-5).
+ELEM_FLOOR = {"drot": 1e-4}
+ELEM_FLOOR_DEFAULT = 5e-6
+
+
+def check_gradients(g, r, keys=GRAD_KEYS, tol=1e-4, per_entry=True):
+    """Per tensor max |g - r| <= tol max |r|, and (per_entry) every entry |g - r| <= tol |r| + floor max |r|.
+    The floor is relative to the tensor's largest value, which only sets a scale when the frame has
+    many pixels: tests of frames of a few pixels check the per-tensor bound alone."""
+    bad = {}
+    for k in keys:
+        a = np.asarray(g[k], np.float64).reshape(len(g[k]), -1)
+        b = np.asarray(r[k], np.float64).reshape(len(r[k]), -1)
+        if k == "dmean2D":  # [:, 2:] are the |dL/dmean2D| sums, compared where a test asks for them
+            a, b = a[:, :2], b[:, :2]
+        mx = float(np.abs(b).max())
+        if mx == 0.0:
+            if not np.all(a == 0.0):
+                bad[k] = "non-zero where the oracle is zero"
+            continue
+        e = np.abs(a - b)
+        msg = []
+        if e.max() > tol * mx:
+            msg.append(f"norm-relative {e.max() / mx:.2e}")
+        over = e > tol * np.abs(b) + ELEM_FLOOR.get(k, ELEM_FLOOR_DEFAULT) * mx
+        if per_entry and over.any():
+            i = np.flatnonzero(over.ravel())[:3]
+            msg.append(f"{int(over.sum())} entries above the per-entry bound (device {a.ravel()[i]}, "
+                       f"oracle {b.ravel()[i]}, max {mx:.3e})")
+        if msg:
+            bad[k] = ", ".join(msg)
+    assert not bad, bad
+
+
+def ambiguous_tiles_mask(o, im, width):
+    """(H, W) bool: the oracle's flagged pixels plus every pixel of a tile whose list holds a pair
+    whose tile test is within rounding distance of its threshold."""
+    pr = o.pairs()
+    mask = im["ambiguous"].copy()
+    gx = (width + 15) // 16
+    rg = pr["ranges"]
+    for t in range(rg.shape[0]):
+        if pr["ambiguous"][rg[t, 0]:rg[t, 1]].any():
+            ty, tx = divmod(t, gx)
+            mask[ty * 16:(ty + 1) * 16, tx * 16:(tx + 1) * 16] = True
+    return mask

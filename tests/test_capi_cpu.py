@@ -100,7 +100,8 @@ def test_batch_workspace_sizing_and_validation():
     st, b16 = _ws(100_000, sizes, _lib.TuneConfig(16, 8, 32, 2, 0), 1 << 22)
     assert st == 0 and b16 > big  # eight times the buckets
     for cfg in (_lib.TuneConfig(0, 16, 16, 4, 0), _lib.TuneConfig(129, 16, 16, 4, 0),
-                _lib.TuneConfig(64, 8, 16, 4, 0), _lib.TuneConfig(64, 16, 16, 3, 0), _lib.TuneConfig(64, 16, 16, 4, 2)):
+                _lib.TuneConfig(64, 8, 16, 4, 0), _lib.TuneConfig(64, 16, 16, 3, 0), _lib.TuneConfig(64, 16, 16, 4, 2),
+                _lib.TuneConfig(64, 16, 16, 4, 0, -1)):
         assert _ws(1000, sizes, cfg, 1 << 20)[0] == 1  # FGS_ERR_BAD_ARG
     assert _ws(1000, [], fb, 1 << 20)[0] == 1
     assert _ws(1000, [(64, 64)] * 33, fb, 1 << 20)[0] == 1

@@ -1,48 +1,43 @@
 """GPU parity of the backward path against the FP64 oracle.
 
 Tolerance: every gradient tensor within 1e-4 relative, measured as
-max |device - oracle| <= 1e-4 * max |oracle| per tensor.  Upstream gradients
-are zeroed at pixels the oracle flags as ambiguous (a discrete decision within
+max |device - oracle| <= 1e-4 * max |oracle| per tensor, and every entry
+within 1e-4 of itself plus a floor of 5e-6 of the tensor's largest value
+(dL/drot: the per-tensor bound alone; gpu_util.check_gradients).  Upstream gradients are
+zeroed at pixels the oracle flags as ambiguous (a discrete decision within
 rounding distance of its threshold), in both the device and the oracle run,
-so a flipped decision cannot leak into the comparison.
+so a flipped decision cannot leak into the comparison; against the fully
+independent FP64 pipeline also on the tiles whose lists hold a pair whose
+tile test is within rounding distance (a pair one side keeps and the other
+drops changes every pixel of the tile).
 """
 import numpy as np
 import pytest
 import torch
 
 from fastergs_gb300 import scenes
-from gpu_util import oracle_scene, replay_oracle, run_backward, run_forward
+from gpu_util import ambiguous_tiles_mask, check_gradients, oracle_scene, replay_oracle, run_backward, run_forward
 
 pytestmark = pytest.mark.gpu
 
 KEYS = ["dmean2D", "dopacity", "dcolor", "dmean3D", "ddc", "dsh", "dscale", "drot"]
 
 
-def _rel_err(a, b):
-    a = np.asarray(a, np.float64).reshape(a.shape[0], -1)
-    b = np.asarray(b, np.float64).reshape(b.shape[0], -1)
-    scale = np.abs(b).max()
-    return 0.0 if scale == 0 else float(np.abs(a - b).max() / scale)
-
-
-def _compare(gpu, orc, keys=KEYS, tol=1e-4):
-    errs = {}
-    for k in keys:
-        g = gpu[k]
-        r = orc[k]
-        if k == "dopacity":
-            g, r = g.reshape(-1), r.reshape(-1)
-        errs[k] = _rel_err(g, r)
-    bad = {k: v for k, v in errs.items() if not v <= tol}
-    assert not bad, f"relative errors above {tol}: {bad} (all: {errs})"
-    return errs
+def _compare(gpu, orc, keys=KEYS, tol=1e-4, per_entry=True):
+    check_gradients(gpu, orc, keys=keys, tol=tol, per_entry=per_entry)
 
 
 def small_c2(seed=0, P=20000, W=320, H=208):
     return scenes.scene_c2(seed=seed, P=P, width=W, height=H)
 
 
-SCENES = {"c1": lambda: scenes.scene_c1(), "c5a": lambda: scenes.scene_c5a(), "c2_small": lambda: small_c2()}
+def deep_tiles():
+    from test_gpu_forward import deep_tiles as scene
+    return scene()
+
+
+SCENES = {"c1": lambda: scenes.scene_c1(), "c5a": lambda: scenes.scene_c5a(), "c2_small": lambda: small_c2(),
+          "deep": deep_tiles}
 
 
 @pytest.mark.parametrize("name", list(SCENES))
@@ -55,18 +50,19 @@ def test_backward_matches_oracle_replay(cuda_device, name):
     dL[:, amb] = 0.0
     g = run_backward(s, fw, dL, cuda_device)
     r = o.backward(dL.astype(np.float64))
-    conic_gpu = g["dmean2D"]  # noqa: F841 (kept for debugging)
     _compare(g, r)
 
 
-@pytest.mark.parametrize("name", ["c1", "c5a"])
+@pytest.mark.parametrize("name", ["c1", "c5a", "c2_small"])
 def test_backward_end_to_end_vs_fp64_oracle(cuda_device, name):
     s = SCENES[name]()
     fw = run_forward(s, cuda_device)
     o = oracle_scene(s).preprocess()
     o.emit_sort(eps_pair=1e-4)
     o.render(eps_alpha=1e-4, eps_T=1e-4)
-    amb = o.image()["ambiguous"] | replay_oracle(s, fw).image()["ambiguous"]
+    im = o.image()
+    amb = ambiguous_tiles_mask(o, im, s.camera.width) | replay_oracle(s, fw).image()["ambiguous"]
+    assert amb.mean() < 0.2
     dL = scenes.upstream_grad(2, s.camera.height, s.camera.width)
     dL[:, amb] = 0.0
     o2 = oracle_scene(s).preprocess()
@@ -74,7 +70,7 @@ def test_backward_end_to_end_vs_fp64_oracle(cuda_device, name):
     o2.render()
     r = o2.backward(dL.astype(np.float64))
     g = run_backward(s, fw, dL, cuda_device)
-    _compare(g, r, tol=1e-3)
+    _compare(g, r)
 
 
 def test_densification_statistics(cuda_device):
@@ -126,7 +122,7 @@ def test_backward_huge_gaussians_and_odd_image_sizes(cuda_device, WH):
     dL[:, amb] = 0.0
     g = run_backward(s, fw, dL, cuda_device, stats=True)
     r = o.backward(dL.astype(np.float64))
-    _compare(g, r)
+    _compare(g, r, per_entry=WH[0] * WH[1] >= 1000)
     # a Gaussian that no pixel saw has exactly zero gradients
     unseen = ~np.isin(np.arange(s.P), fw["vals_sorted"])
     for k in ("dmean3D", "dopacity", "ddc", "dscale", "drot"):

@@ -208,10 +208,12 @@ def rast_cam(rast, k):
 
 
 TUNES = [TuneConfig(32, 8, 32, 2), TuneConfig(64, 32, 8, 8), TuneConfig(16, 16, 16, 1),
-         TuneConfig(128, 16, 16, 4)]  # FB's bucket: composited as two sub-buckets, stop at the full bucket
+         TuneConfig(128, 16, 16, 4),  # FB's bucket: composited as two sub-buckets, stop at the full bucket
+         # short fold chains: most tiles' later buckets go through the pixel-parallel merge
+         TuneConfig(16, 16, 16, 4, chain=1), TuneConfig(32, 8, 32, 2, chain=2)]
 
 
-@pytest.mark.parametrize("tune", TUNES, ids=lambda t: f"b{t.bucket_size}_{t.block_x}x{t.block_y}_p{t.packet}")
+@pytest.mark.parametrize("tune", TUNES, ids=lambda t: f"b{t.bucket_size}_{t.block_x}x{t.block_y}_p{t.packet}_c{t.chain}")
 def test_tuned_configs_match_oracle_replay(setup, tune):
     s, T, cams, sets = setup
     rast, _ = _batched(T, sets, tune=tune)
@@ -323,7 +325,8 @@ def test_autograd_batched_matches_direct_backward(setup):
         assert _rel(leaves[kp].grad.cpu().numpy(), g[kb].cpu().numpy()) <= 1e-5, kp
 
 
-@pytest.mark.parametrize("tune", TUNES[:2], ids=lambda t: f"b{t.bucket_size}_{t.block_x}x{t.block_y}_p{t.packet}")
+@pytest.mark.parametrize("tune", TUNES[:2] + TUNES[-1:],
+                         ids=lambda t: f"b{t.bucket_size}_{t.block_x}x{t.block_y}_p{t.packet}_c{t.chain}")
 def test_tuned_backward_matches_oracle_replay(setup, tune):
     """Gradients summed over cameras against the oracle's per-camera replay
     backward (dL zeroed at ambiguous pixels), 1e-4 relative."""

@@ -1,0 +1,108 @@
+"""This library's CUDA path against the golden vectors the reference CUDA
+backend (FB) produced on a GB300 (tests/golden/fb_*.npz, made by
+tests/golden/make_fb_golden.py): the same seeded scenes and upstream gradient
+through this library's ``_C.ops`` (the C ABI), compared with FB's own outputs.
+
+Tolerances are the ones tests/test_fb_golden_cpu.py holds the FP64 oracle to
+against FB (FB runs in FP32 with approximate transcendental functions):
+radii and every unflagged tile's sorted id list bit-exact, bucket count equal,
+last_contributor bit-exact and image / Ts_final within 1e-5 (with FB's
+documented FP32 outliers on c2_small), gradients within 1e-4 of each
+tensor's largest value per Gaussian, plus FB's kappa^2 term on the
+covariance path.  On those ill-conditioned footprints this library is
+checked to be closer to FP64 than FB.
+"""
+import numpy as np
+import pytest
+
+from fastergs_gb300 import scenes
+from gpu_util import run_backward, run_forward
+from test_fb_golden_cpu import COV_PATH, GRADS, KAPPA_COEF, SCENES, kappa_of, load, oracle_run
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module", params=list(SCENES))
+def case(request, cuda_device):
+    name = request.param
+    g = load(name)
+    s, o, rec, pr, im = oracle_run(name)
+    fw = run_forward(s, cuda_device)
+    dL = scenes.upstream_grad(0, s.camera.height, s.camera.width)
+    dL[:, g["dL_mask"]] = 0.0
+    dev = run_backward(s, fw, dL, cuda_device, stats=True)
+    ref = o.backward(dL.astype(np.float64))
+    return name, g, s, rec, pr, fw, dev, ref
+
+
+def test_forward_matches_fb(case):
+    name, g, s, rec, pr, fw, dev, ref = case
+    amb = rec["ambiguous"]
+    np.testing.assert_array_equal(fw["radii"].cpu().numpy()[~amb], g["radii"][~amb])
+    assert fw["bucket_sum"] == int(g["bucket_sum"])
+    rg_d, rg_fb, rg_o = fw["ranges"], g["ranges"], pr["ranges"]
+    for t in range(rg_o.shape[0]):
+        if pr["ambiguous"][rg_o[t, 0]:rg_o[t, 1]].any():
+            continue
+        np.testing.assert_array_equal(fw["vals_sorted"][rg_d[t, 0]:rg_d[t, 1]],
+                                      g["vals_sorted"][rg_fb[t, 0]:rg_fb[t, 1]], err_msg=f"tile {t}")
+    ok = ~g["dL_mask"]
+    lc = fw["last_contrib"].cpu().numpy()[..., 0]
+    np.testing.assert_array_equal(lc[ok], g["last_contributor"][ok])
+    img = fw["out_color"].cpu().numpy()
+    tf = fw["Ts_final"].cpu().numpy()[..., 0]
+    for err in (np.abs(img - g["out_color"]).max(0)[ok], np.abs(tf - g["Ts_final"])[ok]):
+        if name in ("c1", "c5a"):
+            assert err.max() <= 1e-5, err.max()
+        assert (err <= 1e-5).mean() >= 0.995, (err > 1e-5).sum()
+        assert (err <= 3e-5).mean() >= 0.9999, (err > 3e-5).sum()
+        assert err.max() <= 2e-3, err.max()
+
+
+def test_gradients_match_fb(case):
+    name, g, s, rec, pr, fw, dev, ref = case
+    kappa = kappa_of(rec)
+    for k in GRADS:
+        fb = g[k].astype(np.float64)
+        d = dev[k][: fb.shape[0]].reshape(fb.shape)
+        fb, d = fb.reshape(fb.shape[0], -1), d.reshape(d.shape[0], -1)
+        if k == "dmean2D":
+            fb, d = fb[:, :2], d[:, :2]
+        mx = np.abs(fb).max()
+        if mx == 0.0:
+            assert np.all(d == 0.0), k
+            continue
+        row = np.abs(fb - d).max(1) / mx
+        bound = 1e-4 + (KAPPA_COEF * kappa[: fb.shape[0]] ** 2 if k in COV_PATH else 0.0)
+        worst = int(np.argmax(row - bound))
+        assert np.all(row <= bound), (k, worst, row[worst], kappa[worst])
+    for i, k in enumerate(("xyz_gradient_accum", "xyz_gradient_accum_abs", "max_radii", "denom")):
+        a, b = dev["stats"][i], g[k].astype(np.float64)
+        if k in ("max_radii", "denom"):
+            amb = rec["ambiguous"]
+            np.testing.assert_array_equal(a[~amb], b[~amb])
+        else:
+            assert np.abs(a - b).max() <= 1e-4 * max(np.abs(b).max(), 1e-30), k
+
+
+def test_ill_conditioned_footprints_closer_to_fp64_than_fb(cuda_device):
+    """c2_small holds footprints with kappa up to ~5000.  Where FB's FP32
+    covariance backward cancels (kappa > 1000), this library's gradients stay
+    within 1e-4 of FP64 while FB's do not."""
+    g = load("c2_small")
+    s, o, rec, pr, im = oracle_run("c2_small")
+    kappa = kappa_of(rec)
+    thin = kappa > 1000.0
+    assert thin.sum() >= 5
+    fw = run_forward(s, cuda_device)
+    dL = scenes.upstream_grad(0, s.camera.height, s.camera.width)
+    dL[:, g["dL_mask"]] = 0.0
+    dev = run_backward(s, fw, dL, cuda_device)
+    ref = o.backward(dL.astype(np.float64))
+    for k in ("dscale", "drot"):
+        r = ref[k].reshape(ref[k].shape[0], -1)
+        mx = np.abs(r).max()
+        e_dev = np.abs(dev[k].reshape(r.shape) - r)[thin].max() / mx
+        e_fb = np.abs(g[k].astype(np.float64).reshape(r.shape) - r)[thin].max() / mx
+        assert e_dev <= 1e-4, (k, e_dev)
+        assert e_dev < 0.1 * e_fb, (k, e_dev, e_fb)
