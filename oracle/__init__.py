@@ -4,12 +4,12 @@ Only tests/, ``__graft_entry__.smoke()`` and the CPU-baseline leg of
 ``bench.py`` import this package, and only as the checker or the timed CPU
 baseline.  The product (``fastergs_gb300``) never calls it.
 
-Parity status: pinned against the reference's own Python code for SH
-evaluation, scale/rotation covariance and camera matrices (fixtures under
-tests/golden/); the rasterizer core is a restatement of the reference CUDA
-source (see oracle.cpp for the file:line map) and is otherwise unpinned,
-because the reference ships no tests or golden vectors and its CUDA build
-cannot run where the fixtures are generated.
+Parity status: pinned.  SH evaluation, scale/rotation covariance and camera
+matrices against the reference's own Python code (fixtures under
+tests/golden/); the rasterizer core, a restatement of the reference CUDA
+source (oracle.cpp holds the file:line map), against the outputs of the
+reference CUDA backend built for sm_103a and run on a GB300
+(tests/golden/fb_*.npz, made by tests/golden/make_fb_golden.py).
 """
 from __future__ import annotations
 
@@ -67,6 +67,8 @@ def load():
             "orc_set_lists": (None, [vp, i64, vp, vp]),
             "orc_render": (None, [vp, vp, i32, f64, f64]),
             "orc_num_pairs": (i64, [vp]),
+            "orc_num_candidates": (i64, [vp]),
+            "orc_get_candidates": (None, [vp, vp, vp]),
             "orc_num_buckets": (i64, [vp]),
             "orc_get_preprocess": (None, [vp, vp, vp, vp, vp, vp]),
             "orc_get_pairs": (None, [vp, vp, vp, vp, vp]),
@@ -159,13 +161,24 @@ class Oracle:
         return int(self.lib.orc_emit_sort(self.h, float(eps_pair)))
 
     def pairs(self):
+        """Sorted (key, id) lists with their ambiguity flags and tile ranges, plus the candidate-only
+        pairs (``cand_keys`` / ``cand_ids``: the FP64 tile test rejects them, an FP32 evaluation of
+        the same test may accept them; they are not in the lists) and ``flagged_tiles``, the tiles
+        holding a flagged or candidate pair."""
         K = int(self.lib.orc_num_pairs(self.h))
         keys = np.empty(K, np.uint64)
         ids = np.empty(K, np.int32)
         amb = np.empty(K, np.uint8)
         ranges = np.empty((self.gx * self.gy, 2), np.int32)
         self.lib.orc_get_pairs(self.h, _p(keys), _p(ids), _p(amb), _p(ranges))
-        return dict(keys=keys, ids=ids, ambiguous=amb.astype(bool), ranges=ranges)
+        Kc = int(self.lib.orc_num_candidates(self.h))
+        ckeys = np.empty(Kc, np.uint64)
+        cids = np.empty(Kc, np.int32)
+        self.lib.orc_get_candidates(self.h, _p(ckeys), _p(cids))
+        amb = amb.astype(bool)
+        flagged = np.union1d(keys[amb] >> np.uint64(32), ckeys >> np.uint64(32)).astype(np.int64)
+        return dict(keys=keys, ids=ids, ambiguous=amb, ranges=ranges, cand_keys=ckeys, cand_ids=cids,
+                    flagged_tiles=flagged)
 
     def set_lists(self, ids, ranges):
         ids = np.ascontiguousarray(ids, dtype=np.int32)

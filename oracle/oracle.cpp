@@ -6,12 +6,15 @@
 // linked only by tests/, by __graft_entry__.smoke() and by the CPU-baseline leg
 // of bench.py; the product never calls it.
 //
-// Parity status: the reference ships no tests, golden vectors or CPU code for
-// this path, and its CUDA build cannot run in the container that generated the
-// fixtures.  The pieces of the reference that are plain Python (SH evaluation,
-// scale/rotation covariance, camera matrices) are pinned by fixtures under
-// tests/golden/; the rasterizer core (tile test, compositing, backward) is
-// restated from the reference source and is otherwise unpinned.
+// Parity status: pinned.  The reference ships no tests, golden vectors or CPU
+// code for this path.  The pieces of the reference that are plain Python (SH
+// evaluation, scale/rotation covariance, camera matrices) are pinned by
+// fixtures under tests/golden/ made from that Python code; the rasterizer core
+// (tile test, key emission, sort order, tile ranges, compositing and merge,
+// backward, densification statistics) is pinned by tests/golden/fb_*.npz, the
+// outputs of the reference CUDA backend itself, built for sm_103a from its own
+// sources (oracle/fb_ref.py) and run on a GB300 on three seeded scenes
+// (tests/golden/make_fb_golden.py, tests/test_fb_golden_cpu.py).
 //
 // Reference map (paths relative to the FasterGS repository):
 //   FB/csrc/cuda_rasterizer/preprocess.cu:79-117   2D covariance (EWA)
@@ -151,6 +154,10 @@ struct Scene {
   std::vector<int> ids;
   std::vector<uint8_t> pair_amb;
   std::vector<int> ranges;
+  // pairs the FP64 test rejects but an FP32 evaluation may accept (kept out of
+  // the lists; tests count them as flagged)
+  std::vector<uint64_t> cand_keys;
+  std::vector<int> cand_ids;
   // composite
   int bucket_size = 128;
   std::vector<int> tile_boff;     // T+1 bucket offsets
@@ -309,6 +316,52 @@ bool tile_hit(double x0, double x1, double y0, double y1, double cx, double cy, 
   return chord_hits(cn[0], -2.0 * cn[1] * dy, cn[2] * dy * dy - w, cx, x0, x1);
 }
 
+// FP32 decidability of the same test.  The device evaluates tile_hit in FP32 on
+// the record's f32 values; here each comparison is made in FP64 together with a
+// first-order bound on the FP32 evaluation error of its sides (unit roundoff
+// 2^-24 per operation, propagated through dx, B, C, the discriminant and the
+// segment ends, times a safety factor of 4).  A comparison inside its bound can
+// resolve either way on the device, so the result is three-valued and a pair
+// whose test stays undecided is ambiguous.  Thin footprints need this: the
+// discriminant 4 dx^2 (b^2 - a c) + 4 c w cancels with the footprint's
+// anisotropy, and a nudge of the centre or the power does not always bracket
+// the FP32 outcome.
+enum Tri : uint8_t { kNo = 0, kYes = 1, kMaybe = 2 };
+Tri tri_and(Tri a, Tri b) { return (a == kNo || b == kNo) ? kNo : (a == kYes && b == kYes) ? kYes : kMaybe; }
+Tri tri_or(Tri a, Tri b) { return (a == kYes || b == kYes) ? kYes : (a == kNo && b == kNo) ? kNo : kMaybe; }
+Tri tri_pos(double v, double err) { return v > err ? kYes : (v < -err ? kNo : kMaybe); }
+// chord_hits on A u^2 + B u + C with B = -2 b e, C = q e^2 - w, e = centre - edge.
+Tri chord_tri(double A, double b, double q, double e, double w, double d, double l, double r) {
+  const double u = 1.0 / 16777216.0, K = 4.0;
+  const double err_e = u * std::fabs(e);
+  const double B = -2.0 * b * e, C = q * e * e - w;
+  const double err_B = u * std::fabs(B) + 2.0 * std::fabs(b) * err_e;
+  const double err_C = 3.0 * u * (std::fabs(q) * e * e + std::fabs(w)) + 2.0 * std::fabs(q * e) * err_e;
+  const double disc = B * B - 4.0 * A * C;
+  const double err_disc = 2.0 * u * (B * B + 4.0 * std::fabs(A * C) + std::fabs(disc)) + 2.0 * std::fabs(B) * err_B +
+                          4.0 * std::fabs(A) * err_C;
+  auto seg = [&](double end, Tri& sign_ok, Tri& inside, bool lower) {
+    const double t = (end - d) * (2.0 * A) + B;
+    const double err_t = 3.0 * u * (std::fabs((end - d) * 2.0 * A) + std::fabs(B) + std::fabs(t)) + err_B;
+    sign_ok = tri_pos(lower ? -t : t, K * err_t);   // t <= 0 (lower end) or t >= 0 (upper end)
+    const double g = disc - t * t;                   // t^2 <= disc
+    inside = tri_pos(g, K * (err_disc + u * t * t + 2.0 * std::fabs(t) * err_t));
+  };
+  Tri s1, i1, s2, i2;
+  seg(l, s1, i1, true);
+  seg(r, s2, i2, false);
+  return tri_and(tri_pos(disc, K * err_disc), tri_and(tri_or(s1, i1), tri_or(s2, i2)));
+}
+Tri tile_hit_fp32(double x0, double x1, double y0, double y1, double cx, double cy, const double* cn, double power) {
+  if (cx >= x0 && cx <= x1 && cy >= y0 && cy <= y1) return kYes;
+  const double w = 2.0 * power;
+  const double dx = cx - ((cx * 2.0 < x0 + x1) ? x0 : x1);
+  const Tri first = chord_tri(cn[2], cn[1], cn[0], dx, w, cy, y0, y1);
+  if (first == kYes) return kYes;
+  const double dy = cy - ((cy * 2.0 < y0 + y1) ? y0 : y1);
+  return tri_or(first, chord_tri(cn[0], cn[1], cn[2], dy, w, cx, x0, x1));
+}
+
 struct Pair { uint64_t key; double depth; int id; uint8_t amb; };
 
 // Enumerate every (tile, Gaussian) pair FB emits: all tiles of the rectangle
@@ -334,7 +387,7 @@ void emit_and_sort(Scene& s, double eps_pair) {
         const double sh = 1e-3 * std::max(1.0, eps_pair / 1e-5);
         const bool hi = tile_hit(px0, px1, py0, py1, cx + sx * sh, cy + sy * sh, r + F_CONIC, power * (1 + eps_pair));
         const bool lo = tile_hit(px0, px1, py0, py1, cx - sx * sh, cy - sy * sh, r + F_CONIC, power * (1 - eps_pair));
-        const bool amb = hi != lo;
+        const bool amb = hi != lo || tile_hit_fp32(px0, px1, py0, py1, cx, cy, r + F_CONIC, power) == kMaybe;
         if (hit || amb) {
           Pair p;
           p.key = ((uint64_t)(uint32_t)(ty * c.gx + tx) << 32) | float_bits(depth_f);
@@ -361,8 +414,11 @@ void emit_and_sort(Scene& s, double eps_pair) {
 // candidate-only pairs are dropped from the list the compositor sees.
 void build_ranges_from_pairs(Scene& s) {
   std::vector<uint64_t> k2; std::vector<int> i2; std::vector<uint8_t> a2;
-  for (size_t k = 0; k < s.keys.size(); ++k)
+  s.cand_keys.clear(); s.cand_ids.clear();
+  for (size_t k = 0; k < s.keys.size(); ++k) {
     if (!(s.pair_amb[k] & 2)) { k2.push_back(s.keys[k]); i2.push_back(s.ids[k]); a2.push_back(s.pair_amb[k]); }
+    else { s.cand_keys.push_back(s.keys[k]); s.cand_ids.push_back(s.ids[k]); }
+  }
   s.keys.swap(k2); s.ids.swap(i2); s.pair_amb.swap(a2);
   s.ranges.assign(2 * (size_t)s.T(), 0);
   for (size_t k = 0; k < s.keys.size(); ++k) {
@@ -925,6 +981,12 @@ void orc_render(void* h, const double* bg, int bucket_size, double eps_alpha, do
 }
 
 int64_t orc_num_pairs(void* h) { return (int64_t)static_cast<Scene*>(h)->keys.size(); }
+int64_t orc_num_candidates(void* h) { return (int64_t)static_cast<Scene*>(h)->cand_keys.size(); }
+void orc_get_candidates(void* h, uint64_t* keys, int* ids) {
+  Scene& s = *static_cast<Scene*>(h);
+  if (keys) std::memcpy(keys, s.cand_keys.data(), s.cand_keys.size() * 8);
+  if (ids) std::memcpy(ids, s.cand_ids.data(), s.cand_ids.size() * 4);
+}
 int64_t orc_num_buckets(void* h) {
   Scene& s = *static_cast<Scene*>(h);
   return s.tile_boff.empty() ? 0 : s.tile_boff.back();

@@ -176,9 +176,7 @@ def ambiguous_tiles_mask(o, im, width):
     pr = o.pairs()
     mask = im["ambiguous"].copy()
     gx = (width + 15) // 16
-    rg = pr["ranges"]
-    for t in range(rg.shape[0]):
-        if pr["ambiguous"][rg[t, 0]:rg[t, 1]].any():
-            ty, tx = divmod(t, gx)
-            mask[ty * 16:(ty + 1) * 16, tx * 16:(tx + 1) * 16] = True
+    for t in pr["flagged_tiles"].tolist():
+        ty, tx = divmod(t, gx)
+        mask[ty * 16:(ty + 1) * 16, tx * 16:(tx + 1) * 16] = True
     return mask

@@ -91,9 +91,10 @@ def test_pairs_sort_and_ranges_match_fb(case):
     rg_fb, rg_o = g["ranges"], pr["ranges"]
     assert rg_fb.shape == rg_o.shape
     flagged = 0
+    flagged_tiles = set(pr["flagged_tiles"].tolist())
     for t in range(rg_o.shape[0]):
         ids_o = pr["ids"][rg_o[t, 0]:rg_o[t, 1]]
-        if pr["ambiguous"][rg_o[t, 0]:rg_o[t, 1]].any():
+        if t in flagged_tiles:
             flagged += 1
             continue
         np.testing.assert_array_equal(g["vals_sorted"][rg_fb[t, 0]:rg_fb[t, 1]], ids_o, err_msg=f"tile {t}")

@@ -41,8 +41,9 @@ def test_forward_matches_fb(case):
     np.testing.assert_array_equal(fw["radii"].cpu().numpy()[~amb], g["radii"][~amb])
     assert fw["bucket_sum"] == int(g["bucket_sum"])
     rg_d, rg_fb, rg_o = fw["ranges"], g["ranges"], pr["ranges"]
+    flagged_tiles = set(pr["flagged_tiles"].tolist())
     for t in range(rg_o.shape[0]):
-        if pr["ambiguous"][rg_o[t, 0]:rg_o[t, 1]].any():
+        if t in flagged_tiles:
             continue
         np.testing.assert_array_equal(fw["vals_sorted"][rg_d[t, 0]:rg_d[t, 1]],
                                       g["vals_sorted"][rg_fb[t, 0]:rg_fb[t, 1]], err_msg=f"tile {t}")

@@ -94,6 +94,7 @@ def test_emitted_pairs_match_oracle_replay(cuda_device, name):
     otile = (pr["keys"] >> np.uint64(32)).astype(np.int64)
     orc = set(zip(otile.tolist(), pr["ids"].tolist()))
     amb = set(zip(otile[pr["ambiguous"]].tolist(), pr["ids"][pr["ambiguous"]].tolist()))
+    amb |= set(zip((pr["cand_keys"] >> np.uint64(32)).astype(np.int64).tolist(), pr["cand_ids"].tolist()))
     assert len(amb) <= 0.01 * len(orc), len(amb)  # the flagged pairs are few
     assert (gpu ^ orc) <= amb, f"{len(gpu - orc)} extra / {len(orc - gpu)} missing pairs"
     # depth bits of every key are the record's depth
@@ -287,6 +288,8 @@ def test_huge_gaussians_and_odd_image_sizes(cuda_device, WH):
     otile = (pr["keys"] >> np.uint64(32)).astype(np.int64)
     orc = set(zip(otile.tolist(), pr["ids"].tolist()))
     amb = set(zip(otile[pr["ambiguous"]].tolist(), pr["ids"][pr["ambiguous"]].tolist()))
+    amb |= set(zip((pr["cand_keys"] >> np.uint64(32)).astype(np.int64).tolist(), pr["cand_ids"].tolist()))
+    assert len(amb) <= 0.01 * max(len(orc), 100), len(amb)  # the flagged pairs are few
     assert (gpu ^ orc) <= amb, f"{len(gpu - orc)} extra / {len(orc - gpu)} missing pairs"
     o2 = oracle_scene(s).preprocess()
     r = o2.records()

@@ -14,8 +14,10 @@ Checks and tolerances:
   * sort: the sorted pairs are a stable sort of the emitted pairs, bit for bit;
     tile ranges bit-exact;
   * pair sets: equal to the oracle's tile test on the device's records except
-    pairs the oracle flags as within 1e-4 relative of the test's threshold
-    (at most 0.1% of the pairs; the test is a discriminant, which cancels);
+    pairs the oracle flags: a nudge of 1e-4 relative in the power or of 0.01 px
+    of the centre changes the outcome, or a comparison of the test lies within
+    its FP32 rounding bound (the discriminant cancels for thin footprints);
+    flagged pairs, including the ones the FP64 test rejects, at most 0.5%;
   * images: max-abs 1e-5 on pixels the oracle does not flag as ambiguous (an
     alpha within 1e-5 relative of 1/255, or a bucket-end transmittance within
     1e-5 relative of 1e-4); at most 1% of the pixels may be flagged;
@@ -61,9 +63,9 @@ def check_forward(s, fw, bg=(0.0, 0.0, 0.0)):
     assert np.unique(gpu).size == gpu.size, "duplicate pairs emitted"
     orc = code(pr["keys"] >> np.uint64(32), pr["ids"].astype(np.uint64))
     diff = np.setxor1d(gpu, orc)
-    amb = orc[pr["ambiguous"]]
+    amb = np.union1d(orc[pr["ambiguous"]], code(pr["cand_keys"] >> np.uint64(32), pr["cand_ids"].astype(np.uint64)))
     assert np.isin(diff, amb).all(), f"{int((~np.isin(diff, amb)).sum())} pairs differ outside the flagged ones"
-    assert amb.size <= 1e-3 * max(orc.size, 1), amb.size
+    assert amb.size <= 5e-3 * max(orc.size, 1), amb.size
     # image
     o = replay_oracle(s, fw, bg=bg)
     im = o.image()
@@ -94,9 +96,10 @@ def test_c2_full_forward_and_backward(cuda_device):
 
 def test_c3_full_forward(cuda_device):
     s = scenes.scene_c3(seed=0)
-    fw = run_forward(s, cuda_device, cap=1 << 22)
+    bg = (0.1, 0.2, 0.3)
+    fw = run_forward(s, cuda_device, bg=bg, cap=1 << 22)
     assert fw["K"] > 1_000_000
-    check_forward(s, fw, bg=(0.1, 0.2, 0.3))
+    check_forward(s, fw, bg=bg)
 
 
 def _batched_replay(s, rast, state, k, cam, tune, bg):
