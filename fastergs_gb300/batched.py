@@ -169,6 +169,13 @@ class BatchedRasterizer:
         self.plan(int(pairs * headroom) + (1 << 16))
         return pairs
 
+    def pair_count_word(self) -> torch.Tensor:
+        """Device view (1,) int32 of the workspace word that holds the last frame's pair count (the
+        pairs the frame needed, also when they exceeded the capacity)."""
+        offs = (C.c_int64 * 10)()
+        _lib.call("fgs_batch_offsets", self.P, self.V, self._cams, C.byref(self._cfg), self.pair_capacity, offs, 10)
+        return self.workspace[offs[0]:offs[0] + 4].view(torch.int32)
+
     def tile_ranges(self) -> torch.Tensor:
         """Device view (tiles, 2) int32 of the last frame's per-tile [start, end) in the sorted pair
         list, cameras in order (no copy)."""
@@ -352,6 +359,14 @@ class CapturedStep:
     step fused; ``params`` may then be None.  Each ``replay()`` advances the
     optimiser's step counts and writes the new step sizes into the graph's
     step-size table first.  Re-capture after densification (new tensors).
+
+    Overflow: the graph keeps the largest pair count of its replays on the
+    device and copies it to pinned host memory at the end of every replay, so
+    no replay synchronises.  ``replay()`` raises ``BatchOverflow`` when an
+    earlier replay that has completed needed more pairs than the workspace
+    holds (its extra pairs were dropped, nothing was written past a buffer);
+    ``check()`` waits for the last replay and raises the same way.  Recover
+    with ``rast.fit(...)`` and a new CapturedStep.
     """
 
     def __init__(self, rast: BatchedRasterizer, params: dict | None, dL_dpixels: torch.Tensor, sh_degree: int = 0,
@@ -368,6 +383,10 @@ class CapturedStep:
             self.params = params
         shs = self.params.get("shs")
         self.grads = rast.alloc_grads(shs.size(1) if shs is not None and shs.numel() else 0) if adam is None else {}
+        self._pairs_word = rast.pair_count_word()
+        self._pairs_max = torch.zeros(1, dtype=torch.int32, device=rast.device)
+        self._pairs_host = torch.zeros(1, dtype=torch.int32).pin_memory()
+        self._capacity = rast.pair_capacity
         # Warm up on a side stream (first-call runtime setup must not be captured);
         # the warm-up never steps the optimiser.
         side = torch.cuda.Stream(device=rast.device)
@@ -424,6 +443,9 @@ class CapturedStep:
             self._activations()
         self.rast.forward(p["means3D"], p["opacities"], p.get("dc"), p.get("shs"), p.get("colors_precomp"),
                           p["scales"], p["rotations"], p.get("culling"), self.sh_degree)
+        if not warmup:  # sticky largest pair count, read by the host without a synchronisation
+            torch.maximum(self._pairs_max, self._pairs_word, out=self._pairs_max)
+            self._pairs_host.copy_(self._pairs_max, non_blocking=True)
         if not self.with_backward:
             return
         st = self.stats
@@ -439,7 +461,18 @@ class CapturedStep:
                                     p["rotations"], self.sh_degree, self._fused, st.get("xyz_gradient_accum"),
                                     st.get("xyz_gradient_accum_abs"), st.get("max_radii"), st.get("denom"))
 
+    def _raise_if_overflowed(self) -> None:
+        pairs = int(self._pairs_host[0])
+        if pairs > self._capacity:
+            raise BatchOverflow(pairs, self._capacity)
+
+    def check(self) -> None:
+        """Wait for the last replay; raise BatchOverflow if any replay so far overflowed."""
+        torch.cuda.current_stream(self.rast.device).synchronize()
+        self._raise_if_overflowed()
+
     def replay(self):
+        self._raise_if_overflowed()
         if self.adam is not None:
             fused, _, lrs = self.adam._fused_args(self.rast.P, self.rast.device, lr_device=self._lr)
             for g in range(6):

@@ -304,6 +304,30 @@ def test_overflow_is_reported_not_written(setup):
     assert _C.device_errors(dev) == 0
 
 
+def test_captured_step_reports_overflow_without_synchronising(setup):
+    s, T, cams, sets = setup
+    dev = T["means"].device
+    rast = BatchedRasterizer(sets, s.P, pair_capacity=1000)
+    params = {"means3D": T["means"], "opacities": T["opacities"], "dc": T["dc"], "shs": T["shs"],
+              "scales": T["scales"], "rotations": T["rotations"]}
+    dL = torch.zeros(rast.out_color.numel(), device=dev)
+    step = CapturedStep(rast, params, dL, sh_degree=3, with_backward=False)
+    step.replay()  # nothing has completed yet that could report
+    with pytest.raises(BatchOverflow) as ei:
+        step.check()
+    assert ei.value.pairs > 1000 and ei.value.capacity == 1000
+    with pytest.raises(BatchOverflow):  # the next replay raises before it launches
+        step.replay()
+    assert _C.device_errors(dev) != 0  # capacity bit latched by the kernels, cleared by the read
+    # a fitted workspace replays without a report
+    rast.fit(T["means"], T["opacities"], T["dc"], T["shs"], None, T["scales"], T["rotations"], None, 3)
+    step = CapturedStep(rast, params, dL, sh_degree=3, with_backward=False)
+    step.replay()
+    step.replay()
+    step.check()
+    assert _C.device_errors(dev) == 0
+
+
 def test_autograd_batched_matches_direct_backward(setup):
     s, T, cams, sets = setup
     dev = T["means"].device
