@@ -702,6 +702,16 @@ def batched_bench(args, dev, s, dev_in, cams, label):
     plain_ms = timed(plain_step, reps)
     with torch.no_grad():
         plain_fwd_ms = timed(lambda: plain_step(False), reps)
+    # per-kernel device time of the 16 plain calls (the same kernels, one view each)
+    _lib.kernel_timers(True)
+    _lib.read_kernel_timers()
+    for _ in range(reps):
+        plain_step()
+    torch.cuda.synchronize()
+    kt_plain = _lib.read_kernel_timers()
+    _lib.kernel_timers(False)
+    plain_kernels = {k: {"ms_per_step": round(v[0] / reps, 4), "launches_per_step": v[1] / reps}
+                     for k, v in kt_plain.items() if v[1]}
 
     params = {"means3D": dev_in["means"], "opacities": dev_in["opacities"], "dc": dev_in["dc"],
               "shs": dev_in["shs"], "scales": dev_in["scales"], "rotations": dev_in["rotations"]}
@@ -746,6 +756,11 @@ def batched_bench(args, dev, s, dev_in, cams, label):
         "batched_render_fps": round(1000.0 * V / batched_fwd_ms, 1),
         "speedup_render": round(plain_fwd_ms / batched_fwd_ms, 3),
         "batched_kernels": kernels,
+        "plain_kernels": plain_kernels,
+        # kernel time per step of each path: the plain path's step is kernels plus host work, the
+        # captured batched step is kernels only
+        "plain_kernel_ms_per_step": round(sum(v["ms_per_step"] for v in plain_kernels.values()), 3),
+        "batched_kernel_ms_per_step": round(sum(v["ms_per_step"] for v in kernels.values()), 3),
     }
     del step, fwd, rast
     torch.cuda.empty_cache()

@@ -40,7 +40,7 @@ class TuneConfig:
     bucket_size: int = 128
     block_x: int = 16
     block_y: int = 16
-    packet: int = 4
+    packet: int = 1  # small-footprint candidate tiles per lane and step of the preprocess (FB: 1)
     recompute: bool = False  # rebuild bucket prefixes in the backward instead of storing them
     chain: int = 8  # forward fold-chain length per tile, in (sub-)buckets (results identical for any length)
 

@@ -160,7 +160,8 @@ extern "C" fgs_status fgs_render_batched_fwd(int P, int D, int M, const float* m
     a.curr = reinterpret_cast<unsigned int*>(curr);
     a.counters = reinterpret_cast<int*>(ws + L.counters);
     a.radii = radii;
-    a.large_tiles = kWarp * cfg->packet;
+    a.large_tiles = kLargeTiles;
+    a.packet = cfg->packet;
     const fgs_status st = run_preprocess(a, s);
     if (st != FGS_OK) return st;
   }

@@ -37,6 +37,10 @@ constexpr int kWarp = 32;
 // Gaussians whose tile rect reaches this many tiles take the split path
 // (FB rasterizer_imp.h:40-41: large_threshold / large_split_tile_count).
 constexpr int kLargeTiles = 128;
+// Candidate tiles of small footprints each lane tests per step of the
+// preprocess's flattened candidate list in the plain entry points (the
+// autotuner's packet for the batched ones).
+constexpr int kPacket = 1;
 
 constexpr float kLn2 = 0.69314718055994531f;
 constexpr float kLog2e = 1.44269504088896341f;

@@ -27,6 +27,7 @@ struct PreArgs {
   int* radii;            // V * P
   int large_tiles;       // footprints of >= large_tiles tiles are split into sub-tasks of that many tiles
                          // (a multiple of 32; FB: 128)
+  int packet;            // small footprints: consecutive candidate tiles each lane tests per step (1, 2, 4, 8)
 };
 
 // Preprocess + large-Gaussian emission for every view (grid.y = view).

@@ -300,7 +300,9 @@ __global__ void __launch_bounds__(kPreThreads, 4) k_preprocess(const PreArgs a) 
   }
 
   // Small footprints: flatten the warp's (Gaussian, tile) candidates and test
-  // 32 at a time (the lane packing of FB preprocess.cu:536-696).
+  // 32 x packet at a time, packet consecutive candidates per lane (the lane
+  // packing of FB preprocess.cu:536-696, which tests one per lane): a lane
+  // finds the owner of its first candidate and walks on from there.
   const int cnt = small ? area : 0;
   int incl = cnt;
 #pragma unroll
@@ -317,27 +319,35 @@ __global__ void __launch_bounds__(kPreThreads, 4) k_preprocess(const PreArgs a) 
 
   WarpStage st{s_key[warp], s_val[warp], 0};
   const int warp_first = chunk * kPreThreads + warp * kWarp;
-  for (int base = 0; base < total; base += kWarp) {
-    const int c = base + lane;
-    bool hit = false;
-    unsigned long long key = 0;
-    uint32_t gid = 0;
-    if (c < total) {
-      // Owner = last lane whose candidate start is <= c (steps sum to 31, so
-      // lo + step never leaves the warp).
-      int lo = 0;
+  const int pk = a.packet;
+  for (int base = 0; base < total; base += kWarp * pk) {
+    const int c0 = base + lane * pk;
+    // Owner = last lane whose candidate start is <= c (steps sum to 31, so
+    // lo + step never leaves the warp); lanes with no candidates share the
+    // start of the next lane and are passed over.
+    int lo = 0;
+    if (c0 < total) {
 #pragma unroll
       for (int step = 16; step > 0; step >>= 1)
-        if (s_geo[warp][lo + step].w <= c) lo += step;
-      const int4 g = s_geo[warp][lo];
-      const int local = c - g.w;
-      const int ty = local / g.z, tx = local - ty * g.z;
-      const int x = g.x + tx, y = g.y + ty;
-      hit = tile_hit(x * bx, y * by, bx, by, s_xy[warp][lo], s_cp[warp][lo]);
-      key = ((unsigned long long)(cam.tile_off + (uint32_t)(y * cam.gx + x)) << 32) | s_depth[warp][lo];
-      gid = (uint32_t)(rbase + warp_first + lo);
+        if (s_geo[warp][lo + step].w <= c0) lo += step;
     }
-    stage_push(st, a, lane, hit, key, gid);
+    for (int j = 0; j < pk; ++j) {  // warp-uniform trip count
+      const int c = c0 + j;
+      bool hit = false;
+      unsigned long long key = 0;
+      uint32_t gid = 0;
+      if (c < total) {
+        while (lo < kWarp - 1 && s_geo[warp][lo + 1].w <= c) ++lo;
+        const int4 g = s_geo[warp][lo];
+        const int local = c - g.w;
+        const int ty = local / g.z, tx = local - ty * g.z;
+        const int x = g.x + tx, y = g.y + ty;
+        hit = tile_hit(x * bx, y * by, bx, by, s_xy[warp][lo], s_cp[warp][lo]);
+        key = ((unsigned long long)(cam.tile_off + (uint32_t)(y * cam.gx + x)) << 32) | s_depth[warp][lo];
+        gid = (uint32_t)(rbase + warp_first + lo);
+      }
+      stage_push(st, a, lane, hit, key, gid);
+    }
   }
   stage_flush(st, a, lane);
 }
@@ -441,5 +451,6 @@ extern "C" fgs_status fgs_preprocess(
   a.cap = pair_capacity; a.tasks = task_scratch; a.task_cap = task_scratch_words / 2;
   a.curr = reinterpret_cast<unsigned int*>(curr_offset); a.counters = counters; a.radii = radii;
   a.large_tiles = kLargeTiles;
+  a.packet = kPacket;
   return run_preprocess(a, (cudaStream_t)stream);
 }

@@ -1,6 +1,6 @@
 """Autotuner for the batched rasterizer's launch configuration.
 
-FB fixes bucket size 128, 16x16 tiles and 128-tile sub-tasks at compile time
+FB fixes bucket size 128, 16x16 tiles and one candidate tile per lane at compile time
 (rasterizer_imp.h:24, :40-41; __init__.py:109).  Their best values depend on
 the scene (footprint spread, Gaussians per tile) and the camera set, so the
 batched path picks them per workload: every candidate ``TuneConfig`` is
@@ -29,14 +29,14 @@ from .batched import BatchedRasterizer, CapturedStep, TuneConfig
 
 BUCKETS = (16, 32, 64)
 TILES = ((16, 16), (8, 32))
-PACKETS = (2, 4, 8)
+PACKETS = (1, 2, 4, 8)
 CHAINS = (2, 4, 8, 16, 32)
 
 _MEMO: dict = {}
 
 
 def search_space(buckets=BUCKETS, tiles=TILES, packets=PACKETS, include_default: bool = True) -> list[TuneConfig]:
-    """bucket x tile x packet, plus FB's fixed choice (bucket 128, 16x16, packet 4)."""
+    """bucket x tile x packet, plus FB's fixed choice (bucket 128, 16x16, packet 1)."""
     space = [TuneConfig(b, bx, by, p) for b, (bx, by), p in itertools.product(buckets, tiles, packets)]
     if include_default and TuneConfig() not in space:
         space.append(TuneConfig())

@@ -356,13 +356,15 @@ typedef struct {
 
 /* Launch configuration picked by the autotuner; FB's fixed choice is
  * {128, 16, 16, 4, 0}.  bucket_size 1..128 Gaussians per bucket; tile 16x16,
- * 8x32 or 32x8 pixels; packet 1, 2, 4 or 8: footprints of at least
- * 32*packet tiles are split into sub-tasks of 32*packet tiles, smaller ones
- * are lane-packed by the preprocess warps.  The tile shape and the bucket
- * size change images at the level of the T < 1e-4 stopping rule (which acts
- * per bucket; a 128-Gaussian bucket is composited as two 64-Gaussian
- * sub-buckets with the stop tested after the second, as for fgs_render_fwd);
- * packet changes only the order in which pairs are emitted.
+ * 8x32 or 32x8 pixels; packet 1, 2, 4 or 8: the small-footprint packing
+ * width of the preprocess, i.e. how many consecutive candidate tiles of the
+ * warp's flattened list each lane tests per step (FB packs one per lane;
+ * footprints of 128 tiles or more are split into 128-tile sub-tasks as FB
+ * does).  The tile shape and the bucket size change images at the level of
+ * the T < 1e-4 stopping rule (which acts per bucket; a 128-Gaussian bucket is
+ * composited as two 64-Gaussian sub-buckets with the stop tested after the
+ * second, as for fgs_render_fwd); packet changes only the order in which
+ * pairs are emitted (the sort keeps equal keys in that order).
  * chain 1..4096 (0: 8): the length of each tile's fold chain in the forward
  * composite, in composited (sub-)buckets; a tile's later buckets composite
  * without waiting and are folded pixel-parallel afterwards.  Results are

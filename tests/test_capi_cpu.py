@@ -112,12 +112,12 @@ def test_tuner_search_space_and_cache_key():
     from fastergs_gb300 import tune
     from fastergs_gb300.batched import TuneConfig
     space = tune.search_space(include_default=False)
-    assert len(space) == 18 and len(set(space)) == 18
-    assert TuneConfig() in tune.search_space() and len(tune.search_space()) == 19
+    assert len(space) == 24 and len(set(space)) == 24
+    assert TuneConfig() in tune.search_space() and len(tune.search_space()) == 25
     assert {c.bucket_size for c in space} == {16, 32, 64}
     assert {(c.block_x, c.block_y) for c in space} == {(16, 16), (8, 32)}
-    assert {c.packet for c in space} == {2, 4, 8}
-    assert TuneConfig() == TuneConfig(128, 16, 16, 4, False)  # FB's fixed choice
+    assert {c.packet for c in space} == {1, 2, 4, 8}
+    assert TuneConfig() == TuneConfig(128, 16, 16, 1, False)  # FB's fixed choice
     k1 = tune.cache_key(1_000_000, [(840, 1297), (360, 640)], 3, True)
     assert k1 == tune.cache_key(600_000, [(840, 1297), (360, 640)], 3, True)  # same power-of-two range
     assert k1 != tune.cache_key(1_000_000, [(840, 1297), (360, 640)], 3, False)
