@@ -423,12 +423,30 @@ __device__ __forceinline__ float adam_lr(const fgs_adam_fused& ad, int g) {
 // One Gaussian: co / gsh are its SH row and its dL/dsh row (shared memory
 // when staged, else global); gsh starts at zero and is accumulated over views.
 // Returns whether some view saw the Gaussian (radius > 0).
-template <bool ADAM>
-__device__ __forceinline__ bool pbwd_gaussian(const PbwdArgs& a, int i, const float* co, float* gsh) {
-  bool seen = false;
-  float m3[3] = {0.f, 0.f, 0.f}, gc[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f}, gs[3] = {0.f, 0.f, 0.f};
-  float gq[4] = {0.f, 0.f, 0.f, 0.f}, gdc[3] = {0.f, 0.f, 0.f};
-  float4 gco_sum = make_float4(0.f, 0.f, 0.f, 0.f);
+// Per-Gaussian sums carried from the geometry part of the backward to its SH
+// part and outputs.
+struct PbwdAcc {
+  float m3[3], gc[6], gs[3], gdc[3];
+  float dR[3][3];  // dL/dR of the raw quaternion's rotation, summed over views
+  float4 gco_sum;
+  bool seen;
+};
+
+// The backward of one Gaussian over every view, in two parts that can run on
+// either side of a block barrier: GEOM (covariance, projection, densification
+// statistics; zeroes acc first) and SHFIN (SH, then the rotation and the
+// outputs or the fused Adam step).  The staged kernel runs the geometry while
+// its SH rows are still being copied into shared memory.
+template <bool ADAM, bool GEOM, bool SHFIN>
+__device__ __forceinline__ bool pbwd_part(const PbwdArgs& a, int i, const float* co, float* gsh, PbwdAcc& acc) {
+  if constexpr (GEOM) acc = PbwdAcc{};
+  bool& seen = acc.seen;
+  float(&m3)[3] = acc.m3;
+  float(&gc)[6] = acc.gc;
+  float(&gs)[3] = acc.gs;
+  float(&gdc)[3] = acc.gdc;
+  float4& gco_sum = acc.gco_sum;
+  float gq[4] = {0.f, 0.f, 0.f, 0.f};
   const float3 p = make_float3(a.means[3 * (size_t)i], a.means[3 * (size_t)i + 1], a.means[3 * (size_t)i + 2]);
   // --- rotation of the raw quaternion (FB backward.cu:407-430)
   const float4 q = reinterpret_cast<const float4*>(a.rots)[i];
@@ -437,11 +455,7 @@ __device__ __forceinline__ bool pbwd_gaussian(const PbwdArgs& a, int i, const fl
   R[0][0] = 1.f - 2.f * (qy * qy + qz * qz); R[0][1] = 2.f * (qx * qy - qr * qz); R[0][2] = 2.f * (qx * qz + qr * qy);
   R[1][0] = 2.f * (qx * qy + qr * qz); R[1][1] = 1.f - 2.f * (qx * qx + qz * qz); R[1][2] = 2.f * (qy * qz - qr * qx);
   R[2][0] = 2.f * (qx * qz - qr * qy); R[2][1] = 2.f * (qy * qz + qr * qx); R[2][2] = 1.f - 2.f * (qx * qx + qy * qy);
-  float dR[3][3];  // dL/dR of the raw quaternion's rotation, summed over views
-#pragma unroll
-  for (int r = 0; r < 3; ++r)
-#pragma unroll
-    for (int c = 0; c < 3; ++c) dR[r][c] = 0.f;
+  float(&dR)[3][3] = acc.dR;
 
   for (int vi = 0; vi < a.views.V; ++vi) {
     const ViewDesc& cam = a.views.v[vi];
@@ -449,6 +463,7 @@ __device__ __forceinline__ bool pbwd_gaussian(const PbwdArgs& a, int i, const fl
     const float4* gr = reinterpret_cast<const float4*>(a.grad + rid * FGS_GRAD_STRIDE);
     const float4 gm2 = gr[0], gcn = gr[1], gco = gr[2];
     const int radius = a.radii[rid];
+    if constexpr (GEOM) {
     // gcn: -1/2 x the conic-gradient moments sum dp w^2, dp w dy, dp dy^2 in
     // the (w = dx + P dy, dy) frame of the record's exponent.  In pixel
     // coordinates dL/dconic (off-diagonal halved, as FB stores it) is
@@ -541,8 +556,11 @@ __device__ __forceinline__ bool pbwd_gaussian(const PbwdArgs& a, int i, const fl
       const float jy = Pm[4 * k + 1] * mw - Pm[4 * k + 3] * hp.y * mw * mw;
       m3[k] += jx * gm2.x + jy * gm2.y;
     }
+    } else {  // SH part only: the views that saw the Gaussian
+      if (!(radius > 0)) continue;
+    }
     // --- SH (FB backward.cu:121-245), only when SH coefficients were given
-    if (a.shs) {
+    if (SHFIN && a.shs) {
       const float* rec = a.splat + rid * 32;
       const float3 drgb = make_float3(gco.x * (1.f - rec[F_CLAMP]), gco.y * (1.f - rec[F_CLAMP + 1]),
                                       gco.z * (1.f - rec[F_CLAMP + 2]));
@@ -594,13 +612,14 @@ __device__ __forceinline__ bool pbwd_gaussian(const PbwdArgs& a, int i, const fl
       m3[2] += (dd.z * n2 - vz * vd) * inv3;
     }
     // --- densification statistics (FB backward.cu:892-918), once per view
-    if (a.accum) {
+    if (GEOM && a.accum) {
       if (a.denom) a.denom[i] += 1.f;
       if (a.max_radii) a.max_radii[i] = fmaxf(a.max_radii[i], (float)radius);
       a.accum[i] += sqrt_approx(gm2.x * gm2.x + gm2.y * gm2.y);
       if (a.accum_abs) a.accum_abs[i] += sqrt_approx(gm2.z * gm2.z + gm2.w * gm2.w);
     }
   }
+  if constexpr (!SHFIN) return seen;
   // --- rotation (FB backward.cu:460-482): dL/dq from dL/dR of the raw quaternion
   gq[0] = 2.f * qz * (dR[1][0] - dR[0][1]) + 2.f * qy * (dR[0][2] - dR[2][0]) + 2.f * qx * (dR[2][1] - dR[1][2]);
   gq[1] = 2.f * qy * (dR[0][1] + dR[1][0]) + 2.f * qz * (dR[0][2] + dR[2][0]) + 2.f * qr * (dR[2][1] - dR[1][2]) -
@@ -688,6 +707,12 @@ __device__ __forceinline__ bool pbwd_gaussian(const PbwdArgs& a, int i, const fl
   a.dscale[3 * (size_t)i] = gs[0]; a.dscale[3 * (size_t)i + 1] = gs[1]; a.dscale[3 * (size_t)i + 2] = gs[2];
   reinterpret_cast<float4*>(a.drot)[i] = make_float4(gq[0], gq[1], gq[2], gq[3]);
   return seen;
+}
+
+template <bool ADAM>
+__device__ __forceinline__ bool pbwd_gaussian(const PbwdArgs& a, int i, const float* co, float* gsh) {
+  PbwdAcc acc;
+  return pbwd_part<ADAM, true, true>(a, i, co, gsh, acc);
 }
 
 // f_rest rows of one block of Gaussians, [first, first + n), row floats each,
@@ -783,10 +808,25 @@ __global__ void __launch_bounds__(kPbwdThreads, kPbwdBlocks) k_preprocess_bwd(co
   if (a.sh_staged) {
     float* s_co = s_pb;
     float* s_g = s_pb + kPbwdThreads * row;
-    block_copy_to_smem(s_co, a.shs, (size_t)first * row, n * row);
-    for (int j = threadIdx.x; j < n * row; j += kPbwdThreads) s_g[j] = 0.f;
-    __syncthreads();
-    const bool seen = i < a.P && pbwd_gaussian<ADAM>(a, i, s_co + threadIdx.x * row, s_g + threadIdx.x * row);
+    bool seen;
+    if (a.views.V == 1) {
+      // one view: the SH rows arrive while the geometry part runs (with many
+      // views the geometry alone outlasts the copy, and a second walk over
+      // the views would cost more than the overlap gains)
+      block_copy_to_smem_async(s_co, a.shs, (size_t)first * row, n * row);
+      for (int j = threadIdx.x; j < n * row; j += kPbwdThreads) s_g[j] = 0.f;
+      PbwdAcc acc;
+      const bool active = i < a.P;
+      if (active) pbwd_part<ADAM, true, false>(a, i, nullptr, nullptr, acc);
+      cp_async_wait_all();
+      __syncthreads();
+      seen = active && pbwd_part<ADAM, false, true>(a, i, s_co + threadIdx.x * row, s_g + threadIdx.x * row, acc);
+    } else {
+      block_copy_to_smem(s_co, a.shs, (size_t)first * row, n * row);
+      for (int j = threadIdx.x; j < n * row; j += kPbwdThreads) s_g[j] = 0.f;
+      __syncthreads();
+      seen = i < a.P && pbwd_gaussian<ADAM>(a, i, s_co + threadIdx.x * row, s_g + threadIdx.x * row);
+    }
     s_seen[threadIdx.x] = seen ? 1 : 0;
     __syncthreads();
     if constexpr (!ADAM) {

@@ -185,6 +185,26 @@ __device__ __forceinline__ void st_release_u32(uint32_t* p, uint32_t v) {
 // memory (16-byte aligned dst), with 16-byte loads when the source allows:
 // turns per-thread strided reads of a Gaussian's coefficient row (180 bytes
 // apart at SH degree 3) into coalesced ones.  No barrier; the caller syncs.
+// Asynchronous form (cp.async, 16 bytes at a time, L2 only): issues the copy
+// and returns; the caller does other work, then cp.async.wait_group 0 and a
+// block barrier before reading dst.  An unaligned source or tail is copied
+// synchronously.
+__device__ __forceinline__ void block_copy_to_smem_async(float* dst, const float* src, size_t first, int n) {
+  const float* s = src + first;
+  int done = 0;
+  if ((reinterpret_cast<uintptr_t>(s) & 15) == 0 && (reinterpret_cast<uintptr_t>(dst) & 15) == 0) {
+    const int n4 = n >> 2;
+    for (int j = threadIdx.x; j < n4; j += blockDim.x) {
+      const uint32_t d = static_cast<uint32_t>(__cvta_generic_to_shared(dst + 4 * j));
+      asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(d), "l"(s + 4 * j) : "memory");
+    }
+    asm volatile("cp.async.commit_group;" ::: "memory");
+    done = 4 * n4;
+  }
+  for (int j = done + threadIdx.x; j < n; j += blockDim.x) dst[j] = __ldg(s + j);
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
+
 __device__ __forceinline__ void block_copy_to_smem(float* dst, const float* src, size_t first, int n) {
   const float* s = src + first;
   if ((reinterpret_cast<uintptr_t>(s) & 15) == 0) {
