@@ -320,6 +320,30 @@ __global__ void __launch_bounds__(kPreThreads, 4) k_preprocess(const PreArgs a) 
   WarpStage st{s_key[warp], s_val[warp], 0};
   const int warp_first = chunk * kPreThreads + warp * kWarp;
   const int pk = a.packet;
+  if (pk == 1) {  // one candidate per lane (FB's packing): no owner walk
+    for (int base = 0; base < total; base += kWarp) {
+      const int c = base + lane;
+      bool hit = false;
+      unsigned long long key = 0;
+      uint32_t gid = 0;
+      if (c < total) {
+        int lo = 0;
+#pragma unroll
+        for (int step = 16; step > 0; step >>= 1)
+          if (s_geo[warp][lo + step].w <= c) lo += step;
+        const int4 g = s_geo[warp][lo];
+        const int local = c - g.w;
+        const int ty = local / g.z, tx = local - ty * g.z;
+        const int x = g.x + tx, y = g.y + ty;
+        hit = tile_hit(x * bx, y * by, bx, by, s_xy[warp][lo], s_cp[warp][lo]);
+        key = ((unsigned long long)(cam.tile_off + (uint32_t)(y * cam.gx + x)) << 32) | s_depth[warp][lo];
+        gid = (uint32_t)(rbase + warp_first + lo);
+      }
+      stage_push(st, a, lane, hit, key, gid);
+    }
+    stage_flush(st, a, lane);
+    return;
+  }
   for (int base = 0; base < total; base += kWarp * pk) {
     const int c0 = base + lane * pk;
     // Owner = last lane whose candidate start is <= c (steps sum to 31, so
