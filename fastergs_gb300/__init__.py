@@ -102,20 +102,19 @@ def _bin(buffer, rs, means3D, dc, shs, colors_precomp, opacities, scales, rotati
         buffer.curr_offset, rs.mult, buffer.splat_buffer, culling)
     # One host read per frame (FB's K read): the pair count and the
     # large-footprint task count, stored into pinned memory by a kernel (no
-    # copy-engine queueing behind the caller's own transfers), one synchronisation.
+    # copy-engine queueing behind the caller's own transfers), one
+    # synchronisation, and the sort (FB's sort_gaussian) launched from the same
+    # C++ call when the pairs fit, so the GPU waits on no Python in between.
     counts = _host_counts(means3D.device)
-    stream = torch.cuda.current_stream(means3D.device)
-    ext.read_counts(buffer.curr_offset, counts)
-    stream.synchronize()
-    num_rendered, num_tasks = int(counts[0]), int(counts[1])
+    num_rendered, num_tasks = ext.count_and_sort(
+        buffer.curr_offset, counts, buffer.MAX_NUM_RENDERED, buffer.gaussian_values_sorted.numel(), rs.image_width,
+        rs.image_height, 16, 16, buffer.list_sorting_space, buffer.gaussian_keys_unsorted,
+        buffer.gaussian_values_unsorted, buffer.gaussian_keys_sorted, buffer.gaussian_values_sorted)
     if num_rendered >= buffer.MAX_NUM_RENDERED or num_tasks > buffer.gaussian_values_sorted.numel() // 2:
         _C.device_errors(means3D.device)  # clears the capacity bit the skipped writes latched
         if num_rendered >= buffer.MAX_NUM_RENDERED:
             raise RuntimeError("Too many k-v pairs!")
         raise RuntimeError("preprocess overflowed a device queue (too many large Gaussians)")
-    ext.ops.sort_gaussian(num_rendered, rs.image_width, rs.image_height, 16, 16, buffer.list_sorting_space,
-                          buffer.gaussian_keys_unsorted, buffer.gaussian_values_unsorted,
-                          buffer.gaussian_keys_sorted, buffer.gaussian_values_sorted)
     return radii, num_rendered
 
 

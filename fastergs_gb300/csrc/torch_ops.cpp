@@ -142,6 +142,31 @@ void read_counts(const Tensor& curr_offset, Tensor& host_counts) {
         "fgs_read_counts");
 }
 
+void sort_gaussian(int64_t num_rendered, int width, int height, int block_x, int block_y, Tensor& sorting_space,
+                   const Tensor& keys_unsorted, const Tensor& values_unsorted, Tensor& keys_sorted,
+                   Tensor& values_sorted);
+
+// The drop-in forward's host read and sort in one call: the pair and task
+// counts stored into pinned memory, one stream synchronisation, and -- when
+// the pairs fit max_pairs and the tasks fit task_words / 2 -- the sort
+// launched at once, so no Python runs between the synchronisation and the
+// first sort kernel.  Returns (pairs, tasks); the caller raises on overflow.
+std::tuple<int64_t, int64_t> count_and_sort(const Tensor& curr_offset, Tensor& host_counts, int64_t max_pairs,
+                                            int64_t task_words, int width, int height, int block_x, int block_y,
+                                            Tensor& sorting_space, const Tensor& keys_unsorted,
+                                            const Tensor& values_unsorted, Tensor& keys_sorted,
+                                            Tensor& values_sorted) {
+  read_counts(curr_offset, host_counts);
+  const at::Device dev = cuda_device_of(curr_offset);
+  if (cudaStreamSynchronize(stream_of(dev)) != cudaSuccess) throw std::runtime_error("count_and_sort: sync failed");
+  const int32_t* hc = static_cast<const int32_t*>(host_counts.data_ptr());
+  const int64_t pairs = hc[0], tasks = hc[1];
+  if (pairs < max_pairs && tasks <= task_words / 2)
+    sort_gaussian(pairs, width, height, block_x, block_y, sorting_space, keys_unsorted, values_unsorted, keys_sorted,
+                  values_sorted);
+  return {pairs, tasks};
+}
+
 // FB pybind.cpp:78-93: stable sort of the first num_rendered pairs.
 void sort_gaussian(int64_t num_rendered, int width, int height, int block_x, int block_y, Tensor& sorting_space,
                    const Tensor& keys_unsorted, const Tensor& values_unsorted, Tensor& keys_sorted,
@@ -356,5 +381,6 @@ PYBIND11_MODULE(TORCH_EXTENSION_NAME, m) {
           py::arg("minimal") = false);
   ops.def("adamUpdate", &adamUpdate, "masked Adam step");
   m.def("read_counts", &read_counts, "pair and task counts of the last preprocess into pinned host memory");
+  m.def("count_and_sort", &count_and_sort, "read_counts, one synchronisation and the sort when the pairs fit");
   m.def("version", [] { return std::string(fgs_version()); });
 }
