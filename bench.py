@@ -1016,8 +1016,8 @@ MUFU_PER_EVAL = {"render_fwd": 1, "render_bwd": 2}
 # C2 workload (1M Gaussians, 1297x840, 3,103,742 pairs), from one ncu capture
 # of each kernel; the file gives the command that made it.
 TRAFFIC_SOURCE = "profiles/ncu_c2_kernels.md"
-TRAFFIC_PER_LAUNCH = {"render_bwd": 83_665_920, "render_fwd": 77_669_120, "sort_pass": 38_493_696,
-                      "preprocess_bwd": 511_551_488, "preprocess": 215_542_016}
+TRAFFIC_PER_LAUNCH = {"render_bwd": 82_207_488, "render_fwd": 90_761_728, "sort_pass": 38_357_760,
+                      "preprocess_bwd": 509_822_976, "preprocess": 215_812_096}
 
 
 def roofline(res, peaks):
