@@ -100,6 +100,8 @@ __global__ void __launch_bounds__(256) k_live_buckets(uint32_t* bucket_sum, cons
                                                       const uint32_t* __restrict__ ranges,
                                                       const uint32_t* __restrict__ max_contrib, int bs,
                                                       uint4* __restrict__ live) {
+  pdl_wait();  // the preceding kernel of the stream is done
+  pdl_trigger();
   const int q = blockIdx.x * 256 + threadIdx.x, lane = threadIdx.x & 31;
   const int B = (int)bucket_sum[0];
   bool keep = false;
@@ -122,6 +124,8 @@ __global__ void __launch_bounds__(256) k_live_buckets(uint32_t* bucket_sum, cons
 // xyz_gradient_accum_abs statistic); without it those two slots stay zero.
 template <int BX, bool RECOMPUTE, bool ABS>
 __global__ void __launch_bounds__(kBwdWarps * kWarp, 6) k_render_bwd(const BwdArgs a) {
+  pdl_wait();  // the preceding kernel of the stream is done
+  pdl_trigger();
   using M = TileMap<BX>;
   constexpr int BY = kTilePixels / BX;
   __shared__ BucketStage s_stage[kBwdWarps];
@@ -800,6 +804,8 @@ __device__ __forceinline__ void adam_rest_rows(const PbwdArgs& a, int first, int
 // ADAM: the sparse Adam step fused in place of the gradient outputs.
 template <bool ADAM>
 __global__ void __launch_bounds__(kPbwdThreads, kPbwdBlocks) k_preprocess_bwd(const PbwdArgs a) {
+  pdl_wait();  // the preceding kernel of the stream is done
+  pdl_trigger();
   // sh_staged: [kPbwdThreads x M x 3] SH rows, then as many dL/dsh accumulators
   extern __shared__ __align__(16) float s_pb[];
   __shared__ uint8_t s_seen[kPbwdThreads];
@@ -875,7 +881,7 @@ fgs_status run_render_bwd(const Views& views, int64_t records, int bucket_size, 
   if (!recompute) {
     KernelTimer kt__(FGS_K_BWD_LIST, s);
     const unsigned blocks = (unsigned)((std::max<int64_t>(sm.max_buckets, 1) + 255) / 256);
-    k_live_buckets<<<blocks, 256, 0, s>>>(im.bucket_sum, sm.bucket_queue, im.bucket_off, ranges, im.max_contrib,
+    (void)launch_pdl(k_live_buckets, dim3(blocks), dim3(256), 0, s, im.bucket_sum, sm.bucket_queue, im.bucket_off, ranges, im.max_contrib,
                                           sub, sm.live);
     kt__.stop();
     FGS_LAUNCH_CHECK();
@@ -887,7 +893,7 @@ fgs_status run_render_bwd(const Views& views, int64_t records, int bucket_size, 
     KernelTimer kt__(FGS_K_RENDER_BWD, s);
     const int nt = kBwdWarps * kWarp;
     auto launch = [&](auto kernel) {
-      kernel<<<num_sms() * resident_blocks(kernel, nt, 0), nt, 0, s>>>(a);
+      (void)launch_pdl(kernel, dim3(num_sms() * resident_blocks(kernel, nt, 0)), dim3(nt), 0, s, a);
     };
     auto by_tile = [&](auto rc, auto ab) {
       constexpr bool R = decltype(rc)::value, A = decltype(ab)::value;
@@ -920,8 +926,8 @@ fgs_status run_preprocess_bwd(PbwdArgs& a, cudaStream_t s) {
   if (dyn) FGS_TRY(allow_dyn_smem(kern, 2 * kPbwdThreads * kMaxStagedCoeffs * 12));
   KernelTimer kt__(FGS_K_PREPROCESS_BWD, s);
   const unsigned blocks = (unsigned)((a.P + kPbwdThreads - 1) / kPbwdThreads);
-  if (a.adam_on) k_preprocess_bwd<true><<<blocks, kPbwdThreads, dyn, s>>>(a);
-  else k_preprocess_bwd<false><<<blocks, kPbwdThreads, dyn, s>>>(a);
+  if (a.adam_on) (void)launch_pdl(k_preprocess_bwd<true>, dim3(blocks), dim3(kPbwdThreads), dyn, s, a);
+  else (void)launch_pdl(k_preprocess_bwd<false>, dim3(blocks), dim3(kPbwdThreads), dyn, s, a);
   kt__.stop();
   FGS_LAUNCH_CHECK();
   return FGS_OK;

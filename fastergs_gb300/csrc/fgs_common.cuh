@@ -3,6 +3,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <utility>
+
 #include "../../include/fgs.h"
 
 namespace fgs {
@@ -152,6 +154,32 @@ __device__ __forceinline__ f2x f2_sub(f2x a, f2x b) {
   f2x d;
   asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
   return d;
+}
+
+// Programmatic dependent launch (sm_90+).  Kernels of the path start with
+// pdl_wait(), which returns once the preceding kernel in the stream has
+// completed and its writes are visible (immediately for a kernel launched
+// without the attribute), then pdl_trigger(), which lets the next kernel's
+// launch begin while this one's blocks run.  launch_pdl() launches with the
+// attribute, so a kernel's launch and prologue overlap its predecessor's last
+// wave instead of following its completion.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
+template <typename... KArgs, typename... Args>
+inline cudaError_t launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s,
+                              Args&&... args) {
+  cudaLaunchConfig_t cfg{};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
 }
 
 __device__ __forceinline__ uint32_t lanemask_lt() {

@@ -120,6 +120,8 @@ __device__ __forceinline__ float3 sh_colour(int D, float x, float y, float z, co
 }
 
 __global__ void __launch_bounds__(kPreThreads, 4) k_preprocess(const PreArgs a) {
+  pdl_wait();  // the preceding kernel of the stream is done
+  pdl_trigger();
   __shared__ float2 s_xy[kPreWarps][kWarp];
   __shared__ float4 s_cp[kPreWarps][kWarp];    // conic a, b, c, power
   __shared__ int4 s_geo[kPreWarps][kWarp];     // rect min x, min y, width, candidate start
@@ -380,6 +382,8 @@ __global__ void __launch_bounds__(kPreThreads, 4) k_preprocess(const PreArgs a) 
 // persistent grid (FB preprocess.cu:749-895 uses a work-stealing cursor and a
 // host read of the task count; here the count stays on the device).
 __global__ void __launch_bounds__(kPreThreads) k_preprocess_large(const PreArgs a) {
+  pdl_wait();  // the preceding kernel of the stream is done
+  pdl_trigger();
   __shared__ unsigned long long s_key[kPreWarps][kStage];
   __shared__ uint32_t s_val[kPreWarps][kStage];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -428,13 +432,13 @@ fgs_status run_preprocess(PreArgs& a, cudaStream_t s) {
   {
     KernelTimer kt__(FGS_K_PREPROCESS, s);
     const unsigned blocks = (unsigned)((a.P + kPreThreads - 1) / kPreThreads) * (unsigned)a.views.V;
-    k_preprocess<<<blocks, kPreThreads, 0, s>>>(a);
+    (void)launch_pdl(k_preprocess, dim3(blocks), dim3(kPreThreads), 0, s, a);
     kt__.stop();
   }
   FGS_LAUNCH_CHECK();
   {
     KernelTimer kt__(FGS_K_PREPROCESS_LARGE, s);
-    k_preprocess_large<<<num_sms() * 4, kPreThreads, 0, s>>>(a);
+    (void)launch_pdl(k_preprocess_large, dim3(num_sms() * 4), dim3(kPreThreads), 0, s, a);
     kt__.stop();
   }
   FGS_LAUNCH_CHECK();

@@ -36,6 +36,8 @@ constexpr int kFwdWarps = 4;
 __global__ void __launch_bounds__(256) k_tile_ranges(const unsigned long long* __restrict__ keys, long long n_cap,
                                                      const int* n_dev, uint32_t num_tiles,
                                                      uint32_t* __restrict__ ranges) {
+  pdl_wait();  // the preceding kernel of the stream is done
+  pdl_trigger();
   // 4 consecutive keys per thread (two 16-byte loads when aligned), compared
   // with their predecessors: a tile boundary writes the end of one range and
   // the start of the next.
@@ -134,6 +136,8 @@ __global__ void __launch_bounds__(kScanTiles) k_bucket_count(int T, const uint32
                                                              uint32_t* __restrict__ block_sums,
                                                              uint32_t* __restrict__ round_hist,
                                                              uint32_t* __restrict__ bucket_sum) {
+  pdl_wait();  // the preceding kernel of the stream is done
+  pdl_trigger();
   __shared__ uint32_t s_warp[kScanTiles / 32][kScanValues];
   const int t = blockIdx.x * kScanTiles + threadIdx.x;
   const uint32_t nb = t < T ? tile_buckets(ranges, t, bs) : 0u;
@@ -158,6 +162,8 @@ __global__ void __launch_bounds__(kScanTiles) k_bucket_count(int T, const uint32
 __global__ void __launch_bounds__(1024) k_round_offsets(const uint32_t* __restrict__ round_hist,
                                                         uint32_t* __restrict__ round_off,
                                                         uint32_t* __restrict__ round_fill) {
+  pdl_wait();  // the preceding kernel of the stream is done
+  pdl_trigger();
   constexpr int kPer = kRounds / 1024;
   __shared__ uint32_t s_warp[32];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -226,6 +232,8 @@ __global__ void __launch_bounds__(kScanTiles) k_bucket_fill(int T, const uint32_
                                                             uint32_t* __restrict__ bucket_off,
                                                             uint2* __restrict__ bucket_queue,
                                                             uint32_t* __restrict__ tile_stage, uint32_t* bucket_sum) {
+  pdl_wait();  // the preceding kernel of the stream is done
+  pdl_trigger();
   __shared__ uint32_t s_warp[kScanTiles / 32][kScanValues];
   __shared__ uint32_t s_base[kScanValues], s_total[kScanValues];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -307,6 +315,8 @@ __global__ void __launch_bounds__(kTilePixels) k_empty_tiles(const Views views, 
                                                              int* __restrict__ last_contrib,
                                                              float* __restrict__ Ts_final,
                                                              uint32_t* __restrict__ max_contrib) {
+  pdl_wait();  // the preceding kernel of the stream is done
+  pdl_trigger();
   const int p = threadIdx.x;
   const bool all = bucket_sum[0] == 0;  // the buckets did not fit: every tile gets the empty-list output
   for (uint32_t tile = blockIdx.x; tile < views.tiles; tile += gridDim.x) {  // block-uniform
@@ -352,6 +362,8 @@ struct FwdArgs {
 
 template <int BX, bool RECOMPUTE>
 __global__ void __launch_bounds__(kFwdWarps * kWarp, 7) k_render_fwd(const FwdArgs a) {
+  pdl_wait();  // the preceding kernel of the stream is done
+  pdl_trigger();
   using M = TileMap<BX>;
   constexpr int BY = kTilePixels / BX;
   __shared__ BucketStage s_stage[kFwdWarps];
@@ -520,6 +532,8 @@ constexpr int kMergeAhead = 4;
 
 template <int BX>
 __global__ void __launch_bounds__(kTilePixels) k_deep_merge(const FwdArgs a) {
+  pdl_wait();  // the preceding kernel of the stream is done
+  pdl_trigger();
   using M = TileMap<BX>;
   constexpr int BY = kTilePixels / BX;
   __shared__ uint32_t s_max;
@@ -611,7 +625,7 @@ fgs_status run_tile_ranges(int64_t n_cap, const int32_t* n_dev, uint32_t tiles, 
   FGS_TRY(cudaMemsetAsync(ranges, 0, sizeof(uint32_t) * 2 * (size_t)tiles, s));
   if (n_cap > 0) {
     KernelTimer kt__(FGS_K_TILE_RANGES, s);
-    k_tile_ranges<<<(unsigned)((n_cap + 1023) / 1024), 256, 0, s>>>(
+    (void)launch_pdl(k_tile_ranges, dim3((unsigned)((n_cap + 1023) / 1024)), dim3(256), 0, s, 
         reinterpret_cast<const unsigned long long*>(keys_sorted), n_cap, n_dev, tiles, ranges);
     kt__.stop();
     FGS_LAUNCH_CHECK();
@@ -632,10 +646,10 @@ fgs_status run_render_fwd(const Views& views, int64_t n_cap, const int32_t* n_de
     KernelTimer kt__(FGS_K_BUCKET_SETUP, s, 3);
     const unsigned nblk = (views.tiles + kScanTiles - 1) / kScanTiles;
     FGS_TRY(cudaMemsetAsync(im.round_hist, 0, sizeof(uint32_t) * (kRounds + 1), s));
-    k_bucket_count<<<nblk, kScanTiles, 0, s>>>((int)views.tiles, ranges, sub, im.block_sums, im.round_hist,
+    (void)launch_pdl(k_bucket_count, dim3(nblk), dim3(kScanTiles), 0, s, (int)views.tiles, ranges, sub, im.block_sums, im.round_hist,
                                                im.bucket_sum);
-    k_round_offsets<<<1, 1024, 0, s>>>(im.round_hist, im.round_off, im.round_fill);
-    k_bucket_fill<<<nblk, kScanTiles, 0, s>>>((int)views.tiles, ranges, sub, split, max_buckets, im.block_sums,
+    (void)launch_pdl(k_round_offsets, dim3(1), dim3(1024), 0, s, im.round_hist, im.round_off, im.round_fill);
+    (void)launch_pdl(k_bucket_fill, dim3(nblk), dim3(kScanTiles), 0, s, (int)views.tiles, ranges, sub, split, max_buckets, im.block_sums,
                                               im.round_off, im.round_fill, im.bucket_off, sm.bucket_queue,
                                               im.tile_stage, im.bucket_sum);
     kt__.stop();
@@ -648,7 +662,7 @@ fgs_status run_render_fwd(const Views& views, int64_t n_cap, const int32_t* n_de
     KernelTimer kt__(FGS_K_RENDER_FWD, s);
     const int nt = kFwdWarps * kWarp;
     auto launch = [&](auto kernel) {
-      kernel<<<num_sms() * resident_blocks(kernel, nt, 0), nt, 0, s>>>(fa);
+      (void)launch_pdl(kernel, dim3(num_sms() * resident_blocks(kernel, nt, 0)), dim3(nt), 0, s, fa);
     };
     if (recompute) {  // samples hold one running prefix per tile
       if (views.bx == 8) launch(k_render_fwd<8, true>);
@@ -665,15 +679,15 @@ fgs_status run_render_fwd(const Views& views, int64_t n_cap, const int32_t* n_de
   if (!recompute) {
     KernelTimer kt__(FGS_K_DEEP_MERGE, s);
     const unsigned grid = std::min<unsigned>(views.tiles, (unsigned)num_sms() * 8);
-    if (views.bx == 8) k_deep_merge<8><<<grid, kTilePixels, 0, s>>>(fa);
-    else if (views.bx == 16) k_deep_merge<16><<<grid, kTilePixels, 0, s>>>(fa);
-    else k_deep_merge<32><<<grid, kTilePixels, 0, s>>>(fa);
+    if (views.bx == 8) (void)launch_pdl(k_deep_merge<8>, dim3(grid), dim3(kTilePixels), 0, s, fa);
+    else if (views.bx == 16) (void)launch_pdl(k_deep_merge<16>, dim3(grid), dim3(kTilePixels), 0, s, fa);
+    else (void)launch_pdl(k_deep_merge<32>, dim3(grid), dim3(kTilePixels), 0, s, fa);
     kt__.stop();
     FGS_LAUNCH_CHECK();
   }
   {
     KernelTimer kt__(FGS_K_EMPTY_TILES, s);
-    k_empty_tiles<<<std::min<unsigned>(views.tiles, (unsigned)num_sms() * 8), kTilePixels, 0, s>>>(
+    (void)launch_pdl(k_empty_tiles, dim3(std::min<unsigned>(views.tiles, (unsigned)num_sms() * 8)), dim3(kTilePixels), 0, s, 
         views, ranges, im.bucket_sum, out_color, im.pix_color, last_contributor, Ts_final, im.max_contrib);
     kt__.stop();
   }

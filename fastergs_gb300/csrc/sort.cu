@@ -98,6 +98,8 @@ __device__ __forceinline__ long long pair_count(long long n_cap, const int* n_de
 __global__ void __launch_bounds__(kSortThreads) k_histogram(const unsigned long long* keys, long long n_cap,
                                                             const int* n_dev, int passes, uint32_t* hist,
                                                             uint32_t* done) {
+  pdl_wait();  // the preceding kernel of the stream is done
+  pdl_trigger();
   __shared__ uint32_t s_h[kMaxPasses][kRadix];
   __shared__ bool s_last;
   const long long n = pair_count(n_cap, n_dev);
@@ -170,6 +172,8 @@ __global__ void __launch_bounds__(kSortThreads, 2) k_onesweep(
     unsigned long long* __restrict__ keys_out, uint32_t* __restrict__ vals_out, long long n_cap, const int* n_dev,
     int shift, bool first, bool last, const uint32_t* __restrict__ digit_base, uint32_t* lookback,
     uint32_t* tile_counter) {
+  pdl_wait();  // the preceding kernel of the stream is done
+  pdl_trigger();
   extern __shared__ __align__(16) unsigned char s_dyn[];  // kSortDynSmem bytes
   unsigned long long* s_keys = reinterpret_cast<unsigned long long*>(s_dyn);
   uint32_t* s_vals = reinterpret_cast<uint32_t*>(s_dyn + sizeof(unsigned long long) * kSortTile);
@@ -342,7 +346,7 @@ fgs_status run_sort(int64_t n_cap, const int32_t* n_dev, uint32_t tiles, void* t
       1, std::min<int64_t>((n_cap + kSortThreads * 8 - 1) / (kSortThreads * 8), (int64_t)num_sms() * 2));
   {
     KernelTimer kt__(FGS_K_SORT_HIST, s);
-    k_histogram<<<hist_blocks, kSortThreads, 0, s>>>(reinterpret_cast<const unsigned long long*>(keys_in), n_cap,
+    (void)launch_pdl(k_histogram, dim3(hist_blocks), dim3(kSortThreads), 0, s, reinterpret_cast<const unsigned long long*>(keys_in), n_cap,
                                                      n_dev, passes, hist, counters + kMaxPasses);
     kt__.stop();
   }
@@ -357,7 +361,7 @@ fgs_status run_sort(int64_t n_cap, const int32_t* n_dev, uint32_t tiles, void* t
     uint32_t* dv = to_out ? values_out : alt_v;
     {
       KernelTimer kt__(FGS_K_SORT_PASS, s);
-      k_onesweep<<<(unsigned)L.tiles, kSortThreads, kSortDynSmem, s>>>(src_k, src_v, dk, dv, n_cap, n_dev, 8 * p,
+      (void)launch_pdl(k_onesweep, dim3((unsigned)L.tiles), dim3(kSortThreads), kSortDynSmem, s, src_k, src_v, dk, dv, n_cap, n_dev, 8 * p,
                                                                       p == 0, p == passes - 1, hist + p * kRadix,
                                                                       lookback + (size_t)p * L.tiles * kRadix,
                                                                       counters + p);
