@@ -96,7 +96,7 @@ SIGNATURES = {
 KERNELS = {"preprocess": 0, "preprocess_large": 1, "sort_hist": 2, "sort_pass": 3, "tile_ranges": 4,
            "bucket_setup": 5, "render_fwd": 6, "empty_tiles": 7, "render_bwd": 8, "preprocess_bwd": 9,
            "loss": 10, "render_simp": 11, "render_depth": 12, "read_counts": 13,
-           "bwd_list": 14, "deep_merge": 15}
+           "bwd_list": 14, "deep_merge": 15, "zero": 16}
 
 
 class FgsError(RuntimeError):

@@ -1,5 +1,6 @@
 // Library-wide C entry points: status strings, device error word, SM count
 // cache, and the masked Adam step.
+#include <algorithm>
 #include <map>
 #include <mutex>
 #include <utility>
@@ -8,6 +9,35 @@
 #include "fgs_common.cuh"
 
 namespace fgs {
+
+namespace {
+// Zero fill as a kernel of the launch chain (a memset node would break the
+// programmatic dependent launches around it): the 16-byte-aligned middle with
+// vector stores, the ragged head and tail byte by byte.
+__global__ void __launch_bounds__(256) k_zero(unsigned char* p, size_t head, size_t n16, size_t tail) {
+  pdl_wait();
+  pdl_trigger();
+  const size_t t = blockIdx.x * 256ull + threadIdx.x, stride = (size_t)gridDim.x * 256;
+  uint4* mid = reinterpret_cast<uint4*>(p + head);
+  for (size_t i = t; i < n16; i += stride) mid[i] = make_uint4(0u, 0u, 0u, 0u);
+  if (t < head) p[t] = 0;
+  if (t < tail) p[head + 16 * n16 + t] = 0;
+}
+}  // namespace
+
+fgs_status zero_async(void* ptr, size_t bytes, cudaStream_t s) {
+  if (bytes == 0) return FGS_OK;
+  KernelTimer kt__(FGS_K_ZERO, s);
+  unsigned char* p = static_cast<unsigned char*>(ptr);
+  const size_t head = std::min<size_t>(bytes, (16 - (reinterpret_cast<uintptr_t>(p) & 15)) & 15);
+  const size_t n16 = (bytes - head) / 16, tail = bytes - head - 16 * n16;
+  const size_t want = (n16 + 1023) / 1024;  // about four 16-byte stores per thread
+  const unsigned blocks = (unsigned)std::max<size_t>(1, std::min<size_t>(want, (size_t)num_sms() * 8));
+  (void)launch_pdl(k_zero, dim3(blocks), dim3(256), 0, s, p, head, n16, tail);
+  kt__.stop();
+  FGS_LAUNCH_CHECK();
+  return FGS_OK;
+}
 
 cudaError_t allow_dyn_smem(const void* kernel, int bytes) {
   static std::mutex mu;

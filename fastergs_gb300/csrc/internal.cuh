@@ -80,6 +80,10 @@ struct PbwdArgs {
 bool adam_args_ok(const fgs_adam_fused* ad, const float* shs, const float* opacities);
 
 fgs_status run_preprocess_bwd(PbwdArgs& a, cudaStream_t s);
+// cudaMemsetAsync(ptr, 0, bytes) as a kernel launched with programmatic
+// dependent launch, so the chain of the path's kernels is not broken.
+fgs_status zero_async(void* ptr, size_t bytes, cudaStream_t s);
+
 fgs_status run_tile_ranges(int64_t n_cap, const int32_t* n_dev, uint32_t tiles, const uint64_t* keys_sorted,
                            uint32_t* ranges, cudaStream_t s);
 

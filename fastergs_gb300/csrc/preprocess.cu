@@ -428,7 +428,10 @@ namespace fgs {
 // Launches preprocess + large-Gaussian emission for every view of a.views
 // (grid.y = view).  Shared by the plain and the batched entry points.
 fgs_status run_preprocess(PreArgs& a, cudaStream_t s) {
-  FGS_TRY(cudaMemsetAsync(a.counters, 0, FGS_COUNTER_WORDS * sizeof(int32_t), s));
+  {
+    const fgs_status z = zero_async(a.counters, FGS_COUNTER_WORDS * sizeof(int32_t), s);
+    if (z != FGS_OK) return z;
+  }
   {
     KernelTimer kt__(FGS_K_PREPROCESS, s);
     const unsigned blocks = (unsigned)((a.P + kPreThreads - 1) / kPreThreads) * (unsigned)a.views.V;

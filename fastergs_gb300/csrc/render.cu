@@ -622,7 +622,10 @@ extern "C" fgs_status fgs_selftest_wait(uint32_t* flag, void* stream) {
 namespace fgs {
 fgs_status run_tile_ranges(int64_t n_cap, const int32_t* n_dev, uint32_t tiles, const uint64_t* keys_sorted,
                            uint32_t* ranges, cudaStream_t s) {
-  FGS_TRY(cudaMemsetAsync(ranges, 0, sizeof(uint32_t) * 2 * (size_t)tiles, s));
+  {
+    const fgs_status z = zero_async(ranges, sizeof(uint32_t) * 2 * (size_t)tiles, s);
+    if (z != FGS_OK) return z;
+  }
   if (n_cap > 0) {
     KernelTimer kt__(FGS_K_TILE_RANGES, s);
     (void)launch_pdl(k_tile_ranges, dim3((unsigned)((n_cap + 1023) / 1024)), dim3(256), 0, s, 
@@ -643,9 +646,10 @@ fgs_status run_render_fwd(const Views& views, int64_t n_cap, const int32_t* n_de
   if (st != FGS_OK) return st;
   const int split = bucket_split(bucket_size), sub = sub_bucket_size(bucket_size);
   {
+    const fgs_status z = zero_async(im.round_hist, sizeof(uint32_t) * (kRounds + 1), s);
+    if (z != FGS_OK) return z;
     KernelTimer kt__(FGS_K_BUCKET_SETUP, s, 3);
     const unsigned nblk = (views.tiles + kScanTiles - 1) / kScanTiles;
-    FGS_TRY(cudaMemsetAsync(im.round_hist, 0, sizeof(uint32_t) * (kRounds + 1), s));
     (void)launch_pdl(k_bucket_count, dim3(nblk), dim3(kScanTiles), 0, s, (int)views.tiles, ranges, sub, im.block_sums, im.round_hist,
                                                im.bucket_sum);
     (void)launch_pdl(k_round_offsets, dim3(1), dim3(1024), 0, s, im.round_hist, im.round_off, im.round_fill);

@@ -341,7 +341,10 @@ fgs_status run_sort(int64_t n_cap, const int32_t* n_dev, uint32_t tiles, void* t
   auto* alt_k = reinterpret_cast<unsigned long long*>(base + L.alt_keys);
   auto* alt_v = reinterpret_cast<uint32_t*>(base + L.alt_vals);
   // hist, counters and the look-back words of every pass start at zero.
-  FGS_TRY(cudaMemsetAsync(base, 0, L.alt_keys, s));
+  {
+    const fgs_status z = zero_async(base, L.alt_keys, s);
+    if (z != FGS_OK) return z;
+  }
   const int hist_blocks = (int)std::max<int64_t>(
       1, std::min<int64_t>((n_cap + kSortThreads * 8 - 1) / (kSortThreads * 8), (int64_t)num_sms() * 2));
   {

@@ -470,13 +470,15 @@ fgs_status fgs_batch_offsets(int P, int num_views, const fgs_camera* cams, const
  * one region; FGS_K_READ_COUNTS is the one-thread store of the pair and task
  * counts that fgs_read_counts launches; FGS_K_BWD_LIST builds the backward's
  * list of buckets that some pixel reaches; FGS_K_DEEP_MERGE folds the buckets
- * of deep tiles past their chain).  No
+ * of deep tiles past their chain; FGS_K_ZERO is the zero fill of counters,
+ * tile ranges, sort look-back words and gradient records, a kernel so that
+ * the programmatic dependent launches of the path stay chained).  No
  * counterpart in FB (its DEBUG_TIME macros are unused, ops.h:10-14). */
 enum {
   FGS_K_PREPROCESS = 0, FGS_K_PREPROCESS_LARGE = 1, FGS_K_SORT_HIST = 2, FGS_K_SORT_PASS = 3,
   FGS_K_TILE_RANGES = 4, FGS_K_BUCKET_SETUP = 5, FGS_K_RENDER_FWD = 6, FGS_K_EMPTY_TILES = 7,
   FGS_K_RENDER_BWD = 8, FGS_K_PREPROCESS_BWD = 9, FGS_K_LOSS = 10, FGS_K_SIMP = 11, FGS_K_DEPTH = 12,
-  FGS_K_READ_COUNTS = 13, FGS_K_BWD_LIST = 14, FGS_K_DEEP_MERGE = 15, FGS_K_COUNT = 16
+  FGS_K_READ_COUNTS = 13, FGS_K_BWD_LIST = 14, FGS_K_DEEP_MERGE = 15, FGS_K_ZERO = 16, FGS_K_COUNT = 17
 };
 fgs_status fgs_kernel_timer(int kernel_id, int enable);
 fgs_status fgs_kernel_timer_read(int kernel_id, double* total_ms, int* launches);
