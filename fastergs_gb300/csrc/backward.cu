@@ -887,8 +887,8 @@ fgs_status run_render_bwd(const Views& views, int64_t records, int bucket_size, 
   if (!recompute) {
     KernelTimer kt__(FGS_K_BWD_LIST, s);
     const unsigned blocks = (unsigned)((std::max<int64_t>(sm.max_buckets, 1) + 255) / 256);
-    (void)launch_pdl(k_live_buckets, dim3(blocks), dim3(256), 0, s, im.bucket_sum, sm.bucket_queue, im.bucket_off, ranges, im.max_contrib,
-                                          sub, sm.live);
+    (void)launch_pdl(k_live_buckets, dim3(blocks), dim3(256), 0, s, im.bucket_sum, sm.bucket_queue, im.bucket_off,
+                     ranges, im.max_contrib, sub, sm.live);
     kt__.stop();
     FGS_LAUNCH_CHECK();
   }

@@ -650,12 +650,12 @@ fgs_status run_render_fwd(const Views& views, int64_t n_cap, const int32_t* n_de
     if (z != FGS_OK) return z;
     KernelTimer kt__(FGS_K_BUCKET_SETUP, s, 3);
     const unsigned nblk = (views.tiles + kScanTiles - 1) / kScanTiles;
-    (void)launch_pdl(k_bucket_count, dim3(nblk), dim3(kScanTiles), 0, s, (int)views.tiles, ranges, sub, im.block_sums, im.round_hist,
-                                               im.bucket_sum);
+    (void)launch_pdl(k_bucket_count, dim3(nblk), dim3(kScanTiles), 0, s, (int)views.tiles, ranges, sub,
+                     im.block_sums, im.round_hist, im.bucket_sum);
     (void)launch_pdl(k_round_offsets, dim3(1), dim3(1024), 0, s, im.round_hist, im.round_off, im.round_fill);
-    (void)launch_pdl(k_bucket_fill, dim3(nblk), dim3(kScanTiles), 0, s, (int)views.tiles, ranges, sub, split, max_buckets, im.block_sums,
-                                              im.round_off, im.round_fill, im.bucket_off, sm.bucket_queue,
-                                              im.tile_stage, im.bucket_sum);
+    (void)launch_pdl(k_bucket_fill, dim3(nblk), dim3(kScanTiles), 0, s, (int)views.tiles, ranges, sub, split,
+                     max_buckets, im.block_sums, im.round_off, im.round_fill, im.bucket_off, sm.bucket_queue,
+                     im.tile_stage, im.bucket_sum);
     kt__.stop();
   }
   FGS_LAUNCH_CHECK();
@@ -691,8 +691,9 @@ fgs_status run_render_fwd(const Views& views, int64_t n_cap, const int32_t* n_de
   }
   {
     KernelTimer kt__(FGS_K_EMPTY_TILES, s);
-    (void)launch_pdl(k_empty_tiles, dim3(std::min<unsigned>(views.tiles, (unsigned)num_sms() * 8)), dim3(kTilePixels), 0, s, 
-        views, ranges, im.bucket_sum, out_color, im.pix_color, last_contributor, Ts_final, im.max_contrib);
+    (void)launch_pdl(k_empty_tiles, dim3(std::min<unsigned>(views.tiles, (unsigned)num_sms() * 8)), dim3(kTilePixels),
+                     0, s, views, ranges, im.bucket_sum, out_color, im.pix_color, last_contributor, Ts_final,
+                     im.max_contrib);
     kt__.stop();
   }
   FGS_LAUNCH_CHECK();

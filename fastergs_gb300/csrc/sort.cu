@@ -349,8 +349,9 @@ fgs_status run_sort(int64_t n_cap, const int32_t* n_dev, uint32_t tiles, void* t
       1, std::min<int64_t>((n_cap + kSortThreads * 8 - 1) / (kSortThreads * 8), (int64_t)num_sms() * 2));
   {
     KernelTimer kt__(FGS_K_SORT_HIST, s);
-    (void)launch_pdl(k_histogram, dim3(hist_blocks), dim3(kSortThreads), 0, s, reinterpret_cast<const unsigned long long*>(keys_in), n_cap,
-                                                     n_dev, passes, hist, counters + kMaxPasses);
+    (void)launch_pdl(k_histogram, dim3(hist_blocks), dim3(kSortThreads), 0, s,
+                     reinterpret_cast<const unsigned long long*>(keys_in), n_cap, n_dev, passes, hist,
+                     counters + kMaxPasses);
     kt__.stop();
   }
   FGS_LAUNCH_CHECK();
@@ -364,10 +365,9 @@ fgs_status run_sort(int64_t n_cap, const int32_t* n_dev, uint32_t tiles, void* t
     uint32_t* dv = to_out ? values_out : alt_v;
     {
       KernelTimer kt__(FGS_K_SORT_PASS, s);
-      (void)launch_pdl(k_onesweep, dim3((unsigned)L.tiles), dim3(kSortThreads), kSortDynSmem, s, src_k, src_v, dk, dv, n_cap, n_dev, 8 * p,
-                                                                      p == 0, p == passes - 1, hist + p * kRadix,
-                                                                      lookback + (size_t)p * L.tiles * kRadix,
-                                                                      counters + p);
+      (void)launch_pdl(k_onesweep, dim3((unsigned)L.tiles), dim3(kSortThreads), kSortDynSmem, s, src_k, src_v, dk,
+                       dv, n_cap, n_dev, 8 * p, p == 0, p == passes - 1, hist + p * kRadix,
+                       lookback + (size_t)p * L.tiles * kRadix, counters + p);
       kt__.stop();
     }
     FGS_LAUNCH_CHECK();
