@@ -157,7 +157,10 @@ class BatchedRasterizer:
 
     def fit(self, means3D, opacities, dc=None, shs=None, colors_precomp=None, scales=None, rotations=None,
             culling=None, sh_degree=0, headroom: float = 1.25) -> int:
-        """Render once, then re-plan the workspace for the pairs seen times headroom.  Returns the pairs."""
+        """Render once, then re-plan the workspace for the pairs seen times headroom.  Returns the pairs.
+
+        The re-planned workspace is rendered into once more, so that after fit() the frame state
+        (sorted lists, ranges, per-pixel state for backward(), state()) belongs to these inputs."""
         for _ in range(3):
             self.forward(means3D, opacities, dc, shs, colors_precomp, scales, rotations, culling, sh_degree)
             pairs, _ = self.status(raise_on_overflow=False)
@@ -167,6 +170,7 @@ class BatchedRasterizer:
         from . import _C
         _C.device_errors(self.device)  # clear a capacity flag left by an undersized attempt
         self.plan(int(pairs * headroom) + (1 << 16))
+        self.forward(means3D, opacities, dc, shs, colors_precomp, scales, rotations, culling, sh_degree)
         return pairs
 
     def pair_count_word(self) -> torch.Tensor:

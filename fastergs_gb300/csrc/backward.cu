@@ -436,14 +436,48 @@ struct PbwdAcc {
   bool seen;
 };
 
+// A Gaussian that no view saw (radius 0 everywhere) has no pairs, so its
+// gradient records were zeroed and never added to: every gradient is zero,
+// as FB leaves it (its backward returns early for radius 0).  Its outputs are
+// written as zeros without reading its parameters or records.
+template <bool ADAM, bool GEOM, bool SHFIN>
+__device__ __forceinline__ bool pbwd_unseen(const PbwdArgs& a, int i) {
+  const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
+  if constexpr (GEOM) {
+    for (int vi = 0; vi < a.views.V; ++vi) {
+      const size_t rid = (size_t)vi * a.P + i;
+      if (a.dmean2D) reinterpret_cast<float4*>(a.dmean2D)[rid] = z4;
+      if (a.dconic) reinterpret_cast<float4*>(a.dconic)[rid] = z4;
+    }
+  }
+  if constexpr (SHFIN && !ADAM) {  // the fused Adam step leaves unseen rows alone
+    if (a.dcolor) {
+      a.dcolor[3 * (size_t)i] = 0.f; a.dcolor[3 * (size_t)i + 1] = 0.f; a.dcolor[3 * (size_t)i + 2] = 0.f;
+    }
+    a.dopac[i] = 0.f;
+    a.dmean3D[3 * (size_t)i] = 0.f; a.dmean3D[3 * (size_t)i + 1] = 0.f; a.dmean3D[3 * (size_t)i + 2] = 0.f;
+    if (a.dcov3D) {
+#pragma unroll
+      for (int k = 0; k < 6; ++k) a.dcov3D[6 * (size_t)i + k] = 0.f;
+    }
+    a.ddc[3 * (size_t)i] = 0.f; a.ddc[3 * (size_t)i + 1] = 0.f; a.ddc[3 * (size_t)i + 2] = 0.f;
+    a.dscale[3 * (size_t)i] = 0.f; a.dscale[3 * (size_t)i + 1] = 0.f; a.dscale[3 * (size_t)i + 2] = 0.f;
+    reinterpret_cast<float4*>(a.drot)[i] = z4;
+  }
+  return false;
+}
+
 // The backward of one Gaussian over every view, in two parts that can run on
 // either side of a block barrier: GEOM (covariance, projection, densification
 // statistics; zeroes acc first) and SHFIN (SH, then the rotation and the
 // outputs or the fused Adam step).  The staged kernel runs the geometry while
-// its SH rows are still being copied into shared memory.
+// its SH rows are still being copied into shared memory.  vis: some view saw
+// the Gaussian (else pbwd_unseen).
 template <bool ADAM, bool GEOM, bool SHFIN>
-__device__ __forceinline__ bool pbwd_part(const PbwdArgs& a, int i, const float* co, float* gsh, PbwdAcc& acc) {
+__device__ __forceinline__ bool pbwd_part(const PbwdArgs& a, int i, bool vis, const float* co, float* gsh,
+                                          PbwdAcc& acc) {
   if constexpr (GEOM) acc = PbwdAcc{};
+  if (!vis) return pbwd_unseen<ADAM, GEOM, SHFIN>(a, i);
   bool& seen = acc.seen;
   float(&m3)[3] = acc.m3;
   float(&gc)[6] = acc.gc;
@@ -714,9 +748,16 @@ __device__ __forceinline__ bool pbwd_part(const PbwdArgs& a, int i, const float*
 }
 
 template <bool ADAM>
-__device__ __forceinline__ bool pbwd_gaussian(const PbwdArgs& a, int i, const float* co, float* gsh) {
+__device__ __forceinline__ bool pbwd_gaussian(const PbwdArgs& a, int i, bool vis, const float* co, float* gsh) {
   PbwdAcc acc;
-  return pbwd_part<ADAM, true, true>(a, i, co, gsh, acc);
+  return pbwd_part<ADAM, true, true>(a, i, vis, co, gsh, acc);
+}
+
+// Whether some view saw Gaussian i (radius > 0).
+__device__ __forceinline__ bool pbwd_visible(const PbwdArgs& a, int i) {
+  bool vis = false;
+  for (int vi = 0; vi < a.views.V && !vis; ++vi) vis = a.radii[(size_t)vi * a.P + i] > 0;
+  return vis;
 }
 
 // f_rest rows of one block of Gaussians, [first, first + n), row floats each,
@@ -814,24 +855,30 @@ __global__ void __launch_bounds__(kPbwdThreads, kPbwdBlocks) k_preprocess_bwd(co
   if (a.sh_staged) {
     float* s_co = s_pb;
     float* s_g = s_pb + kPbwdThreads * row;
+    // Only the SH rows of Gaussians some view saw are read (at 1M Gaussians
+    // in one view, about a third): copy those alone.
+    const bool vis = i < a.P && pbwd_visible(a, i);
+    s_seen[threadIdx.x] = vis ? 1 : 0;
+    __syncthreads();
     bool seen;
     if (a.views.V == 1) {
       // one view: the SH rows arrive while the geometry part runs (with many
       // views the geometry alone outlasts the copy, and a second walk over
       // the views would cost more than the overlap gains)
-      block_copy_to_smem_async(s_co, a.shs, (size_t)first * row, n * row);
+      block_copy_rows_to_smem_async(s_co, a.shs, (size_t)first * row, n, row, s_seen);
       for (int j = threadIdx.x; j < n * row; j += kPbwdThreads) s_g[j] = 0.f;
       PbwdAcc acc;
       const bool active = i < a.P;
-      if (active) pbwd_part<ADAM, true, false>(a, i, nullptr, nullptr, acc);
+      if (active) pbwd_part<ADAM, true, false>(a, i, vis, nullptr, nullptr, acc);
       cp_async_wait_all();
       __syncthreads();
-      seen = active && pbwd_part<ADAM, false, true>(a, i, s_co + threadIdx.x * row, s_g + threadIdx.x * row, acc);
+      seen = active && pbwd_part<ADAM, false, true>(a, i, vis, s_co + threadIdx.x * row, s_g + threadIdx.x * row,
+                                                    acc);
     } else {
-      block_copy_to_smem(s_co, a.shs, (size_t)first * row, n * row);
+      block_copy_rows_to_smem(s_co, a.shs, (size_t)first * row, n, row, s_seen);
       for (int j = threadIdx.x; j < n * row; j += kPbwdThreads) s_g[j] = 0.f;
       __syncthreads();
-      seen = i < a.P && pbwd_gaussian<ADAM>(a, i, s_co + threadIdx.x * row, s_g + threadIdx.x * row);
+      seen = i < a.P && pbwd_gaussian<ADAM>(a, i, vis, s_co + threadIdx.x * row, s_g + threadIdx.x * row);
     }
     s_seen[threadIdx.x] = seen ? 1 : 0;
     __syncthreads();
@@ -846,7 +893,7 @@ __global__ void __launch_bounds__(kPbwdThreads, kPbwdBlocks) k_preprocess_bwd(co
   float* gsh = a.dsh ? a.dsh + (size_t)i * row : nullptr;
   if (gsh)
     for (int k = 0; k < row; ++k) gsh[k] = 0.f;
-  pbwd_gaussian<ADAM>(a, i, a.shs ? a.shs + (size_t)i * row : nullptr, gsh);
+  pbwd_gaussian<ADAM>(a, i, pbwd_visible(a, i), a.shs ? a.shs + (size_t)i * row : nullptr, gsh);
 }
 
 __global__ void __launch_bounds__(256) k_densify(int P, const int* radii, const float4* dm2, float* accum,

@@ -209,40 +209,59 @@ __device__ __forceinline__ void st_release_u32(uint32_t* p, uint32_t v) {
   asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 
-// Block-cooperative copy of n floats starting at src + first into shared
-// memory (16-byte aligned dst), with 16-byte loads when the source allows:
+// Row of float j of a block's span of rows `row` floats wide, in FP32:
+// floor((j + 1/2) / row), equal to j / row for j < 256 row and 3 <= row <= 48
+// (tests/test_capi_cpu.py checks every row and j).
+__device__ __forceinline__ int row_of(int j, float inv_row) { return (int)(((float)j + 0.5f) * inv_row); }
+
+// Block-cooperative copy into shared memory (16-byte aligned dst) of the rows
+// of `nrows` consecutive rows, `row` floats each, that start at src + first
+// and whose keep flag is set, with 16-byte loads when the source allows:
 // turns per-thread strided reads of a Gaussian's coefficient row (180 bytes
-// apart at SH degree 3) into coalesced ones.  No barrier; the caller syncs.
+// apart at SH degree 3) into coalesced ones, and skips the rows that are not
+// needed (the floats of a skipped row are left as they were; a 16-byte piece
+// shared with a kept row is copied).  No barrier; the caller syncs.
 // Asynchronous form (cp.async, 16 bytes at a time, L2 only): issues the copy
 // and returns; the caller does other work, then cp.async.wait_group 0 and a
 // block barrier before reading dst.  An unaligned source or tail is copied
 // synchronously.
-__device__ __forceinline__ void block_copy_to_smem_async(float* dst, const float* src, size_t first, int n) {
+__device__ __forceinline__ void block_copy_rows_to_smem_async(float* dst, const float* src, size_t first,
+                                                              int nrows, int row, const uint8_t* keep) {
   const float* s = src + first;
+  const int n = nrows * row;
+  const float inv_row = 1.f / (float)row;
   int done = 0;
   if ((reinterpret_cast<uintptr_t>(s) & 15) == 0 && (reinterpret_cast<uintptr_t>(dst) & 15) == 0) {
     const int n4 = n >> 2;
     for (int j = threadIdx.x; j < n4; j += blockDim.x) {
+      if (!(keep[row_of(4 * j, inv_row)] | keep[row_of(4 * j + 3, inv_row)])) continue;
       const uint32_t d = static_cast<uint32_t>(__cvta_generic_to_shared(dst + 4 * j));
       asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(d), "l"(s + 4 * j) : "memory");
     }
     asm volatile("cp.async.commit_group;" ::: "memory");
     done = 4 * n4;
   }
-  for (int j = done + threadIdx.x; j < n; j += blockDim.x) dst[j] = __ldg(s + j);
+  for (int j = done + threadIdx.x; j < n; j += blockDim.x)
+    if (keep[row_of(j, inv_row)]) dst[j] = __ldg(s + j);
 }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
 
-__device__ __forceinline__ void block_copy_to_smem(float* dst, const float* src, size_t first, int n) {
+// Synchronous form of block_copy_rows_to_smem_async.
+__device__ __forceinline__ void block_copy_rows_to_smem(float* dst, const float* src, size_t first, int nrows,
+                                                        int row, const uint8_t* keep) {
   const float* s = src + first;
+  const int n = nrows * row;
+  const float inv_row = 1.f / (float)row;
+  int done = 0;
   if ((reinterpret_cast<uintptr_t>(s) & 15) == 0) {
     const int n4 = n >> 2;
     for (int j = threadIdx.x; j < n4; j += blockDim.x)
-      reinterpret_cast<float4*>(dst)[j] = __ldg(reinterpret_cast<const float4*>(s) + j);
-    for (int j = 4 * n4 + threadIdx.x; j < n; j += blockDim.x) dst[j] = __ldg(s + j);
-  } else {
-    for (int j = threadIdx.x; j < n; j += blockDim.x) dst[j] = __ldg(s + j);
+      if (keep[row_of(4 * j, inv_row)] | keep[row_of(4 * j + 3, inv_row)])
+        reinterpret_cast<float4*>(dst)[j] = __ldg(reinterpret_cast<const float4*>(s) + j);
+    done = 4 * n4;
   }
+  for (int j = done + threadIdx.x; j < n; j += blockDim.x)
+    if (keep[row_of(j, inv_row)]) dst[j] = __ldg(s + j);
 }
 // The reverse: n floats from shared memory to dst + first.
 __device__ __forceinline__ void block_copy_from_smem(float* dst, size_t first, const float* src, int n) {
