@@ -209,9 +209,11 @@ __device__ __forceinline__ void st_release_u32(uint32_t* p, uint32_t v) {
   asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 
-// Row of float j of a block's span of rows `row` floats wide, in FP32:
-// floor((j + 1/2) / row), equal to j / row for j < 256 row and 3 <= row <= 48
-// (tests/test_capi_cpu.py checks every row and j).
+// Row of element j of a span of rows `row` elements wide, in FP32 from the
+// correctly rounded inv_row = 1 / row: floor((j + 1/2) inv_row), equal to
+// j / row for j < 256 row with 3 <= row <= 48 (SH rows) and for j < 256 with
+// 1 <= row <= 255 (tile rectangles); tests/test_capi_cpu.py checks every row
+// and j of both ranges.
 __device__ __forceinline__ int row_of(int j, float inv_row) { return (int)(((float)j + 0.5f) * inv_row); }
 
 // Block-cooperative copy into shared memory (16-byte aligned dst) of the rows

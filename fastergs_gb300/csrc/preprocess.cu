@@ -125,6 +125,7 @@ __global__ void __launch_bounds__(kPreThreads, 4) k_preprocess(const PreArgs a) 
   __shared__ float2 s_xy[kPreWarps][kWarp];
   __shared__ float4 s_cp[kPreWarps][kWarp];    // conic a, b, c, power
   __shared__ int4 s_geo[kPreWarps][kWarp];     // rect min x, min y, width, candidate start
+  __shared__ float s_inv_w[kPreWarps][kWarp];  // 1 / rect width
   __shared__ uint32_t s_depth[kPreWarps][kWarp];
   __shared__ unsigned long long s_key[kPreWarps][kStage];
   __shared__ uint32_t s_val[kPreWarps][kStage];
@@ -220,13 +221,16 @@ __global__ void __launch_bounds__(kPreThreads, 4) k_preprocess(const PreArgs a) 
       const float ca = sc2.a, cb = sc2.b, cc = sc2.c, det = sc2.det;
       const float det_inv = 1.0f / det;
       const float3 conic = f3(cc * det_inv, -cb * det_inv, ca * det_inv);
-      // Reported radius (FB preprocess.cu:480-485; the 3.33 bound is a double there).
+      // Reported radius (FB preprocess.cu:480-485).  FB compares with the
+      // double 3.33 and stores the result in a float, so the extent, the
+      // product and its ceiling are all FP32 (for o <= 1 the square root is
+      // at most sqrt(2 ln 255) = 3.329, below the bound).
       const float mid = 0.5f * (ca + cc);
-      const double extent = fmin(3.33, (double)sqrtf(2.0f * logf(o * 255.0f)));
+      const float extent = fminf(3.33f, sqrtf(2.0f * logf(o * 255.0f)));
       // mid^2 - det written as ((a - c)/2)^2 + b^2, which does not cancel
       const float hd = 0.5f * (ca - cc);
       const float lambda = mid + sqrtf(fmaxf(0.01f, hd * hd + cb * cb));
-      radius = (float)ceil(extent * (double)sqrtf(lambda));
+      radius = ceilf(extent * sqrtf(lambda));
       // Tile rectangle of the 1/256 level set (FB preprocess.cu:488-497).
       const float log2o = lg2_approx(o);
       const float power = (kLn2 * 8.0f + kLn2 * log2o) * cam.mult;
@@ -301,7 +305,9 @@ __global__ void __launch_bounds__(kPreThreads, 4) k_preprocess(const PreArgs a) 
     }
   }
 
-  // Small footprints: flatten the warp's (Gaussian, tile) candidates and test
+  // Small footprints (area < LT <= 256 tiles, so the row of candidate `local`
+  // is row_of(local, 1 / width), exact for local < 256 width): flatten the
+  // warp's (Gaussian, tile) candidates and test
   // 32 x packet at a time, packet consecutive candidates per lane (the lane
   // packing of FB preprocess.cu:536-696, which tests one per lane): a lane
   // finds the owner of its first candidate and walks on from there.
@@ -316,6 +322,7 @@ __global__ void __launch_bounds__(kPreThreads, 4) k_preprocess(const PreArgs a) 
   s_xy[warp][lane] = xy;
   s_cp[warp][lane] = cp;
   s_geo[warp][lane] = make_int4(rmin.x, rmin.y, tw, incl - cnt);
+  s_inv_w[warp][lane] = tw > 0 ? 1.0f / (float)tw : 0.f;
   s_depth[warp][lane] = __float_as_uint(depth);
   __syncwarp();
 
@@ -335,7 +342,7 @@ __global__ void __launch_bounds__(kPreThreads, 4) k_preprocess(const PreArgs a) 
           if (s_geo[warp][lo + step].w <= c) lo += step;
         const int4 g = s_geo[warp][lo];
         const int local = c - g.w;
-        const int ty = local / g.z, tx = local - ty * g.z;
+        const int ty = row_of(local, s_inv_w[warp][lo]), tx = local - ty * g.z;
         const int x = g.x + tx, y = g.y + ty;
         hit = tile_hit(x * bx, y * by, bx, by, s_xy[warp][lo], s_cp[warp][lo]);
         key = ((unsigned long long)(cam.tile_off + (uint32_t)(y * cam.gx + x)) << 32) | s_depth[warp][lo];
@@ -366,7 +373,7 @@ __global__ void __launch_bounds__(kPreThreads, 4) k_preprocess(const PreArgs a) 
         while (lo < kWarp - 1 && s_geo[warp][lo + 1].w <= c) ++lo;
         const int4 g = s_geo[warp][lo];
         const int local = c - g.w;
-        const int ty = local / g.z, tx = local - ty * g.z;
+        const int ty = row_of(local, s_inv_w[warp][lo]), tx = local - ty * g.z;
         const int x = g.x + tx, y = g.y + ty;
         hit = tile_hit(x * bx, y * by, bx, by, s_xy[warp][lo], s_cp[warp][lo]);
         key = ((unsigned long long)(cam.tile_off + (uint32_t)(y * cam.gx + x)) << 32) | s_depth[warp][lo];

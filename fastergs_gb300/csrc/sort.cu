@@ -40,7 +40,11 @@ constexpr int kMaxPasses = 8;
 constexpr uint32_t kFlagAgg = 1u << 30;
 constexpr uint32_t kFlagInc = 2u << 30;
 constexpr uint32_t kValueMask = (1u << 30) - 1;
-constexpr int kLookWindow = 32;  // predecessor words read per look-back round
+// Predecessor words read per look-back round.  The nearest few predecessors
+// usually hold an inclusive prefix already, so a narrow window wins: per C2
+// pass (3.1M keys) 38.5 us at 32 words, 36.3 at 16, 35.4 at 8 and 4, 35.9 at
+// 2; a 47M-key batched sort 2.47 / 2.32 / 2.24 / 2.22 / 2.28 ms.
+constexpr int kLookWindow = 4;
 constexpr int kSortDynSmem = (int)((sizeof(unsigned long long) + sizeof(uint32_t)) * kSortTile);
 
 struct SortLayout {

@@ -186,6 +186,18 @@ def test_fused_adam_row_index_in_fp32_is_exact():
             assert np.array_equal(got, (j + off) // row), row
 
 
+def test_rect_row_index_in_fp32_is_exact():
+    """The preprocess finds the tile row of candidate `local` of a small Gaussian's rectangle
+    (area < 128 tiles, width w) as floor((local + 1/2) * fl(1 / w)) in FP32: equal to integer
+    division for every width up to 255 and every local < 256."""
+    import numpy as np
+    j = np.arange(256, dtype=np.int64)
+    for w in range(1, 256):
+        inv = np.float32(1) / np.float32(w)
+        got = ((j.astype(np.float32) + np.float32(0.5)) * inv).astype(np.int64)
+        assert np.array_equal(got, j // w), w
+
+
 def _declarations():
     """{name: (return type, [parameter declarations])} of every function include/fgs.h declares."""
     text = re.sub(r"/\*.*?\*/", "", HEADER.read_text(), flags=re.S)
