@@ -918,14 +918,11 @@ fgs_status run_render_bwd(const Views& views, int64_t records, int bucket_size, 
                           const int32_t* last_contributor, const ImageState& im, const SampleState& sm,
                           const float* dL_dpixels, float* grad_record, bool recompute, bool abs_grad,
                           cudaStream_t s) {
+  // the gradient records, and the backward work cursor and live-list count
+  // (words 3 and 5 of the image-state header): reset on every call, one launch
   {
-    const fgs_status z = zero_async(grad_record, sizeof(float) * FGS_GRAD_STRIDE * (size_t)records, s);
-    if (z != FGS_OK) return z;
-  }
-  // backward work cursor and live-list count (words 3 and 5 of the
-  // image-state header); reset on every call
-  {
-    const fgs_status z = zero_async(im.bucket_sum + 3, 3 * sizeof(uint32_t), s);
+    const fgs_status z = zero_async(grad_record, sizeof(float) * FGS_GRAD_STRIDE * (size_t)records, s,
+                                    im.bucket_sum + 3, 3 * sizeof(uint32_t));
     if (z != FGS_OK) return z;
   }
   // recompute mode rebuilds every tile's prefix from the start

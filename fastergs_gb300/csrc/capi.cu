@@ -12,28 +12,43 @@ namespace fgs {
 
 namespace {
 // Zero fill as a kernel of the launch chain (a memset node would break the
-// programmatic dependent launches around it): the 16-byte-aligned middle with
-// vector stores, the ragged head and tail byte by byte.
-__global__ void __launch_bounds__(256) k_zero(unsigned char* p, size_t head, size_t n16, size_t tail) {
+// programmatic dependent launches around it), of up to two byte ranges in one
+// launch: the 16-byte-aligned middle with vector stores, the ragged head and
+// tail byte by byte.
+struct ZeroRange {
+  unsigned char* p;
+  size_t head, n16, tail;
+};
+ZeroRange zero_range(void* ptr, size_t bytes) {
+  ZeroRange r{static_cast<unsigned char*>(ptr), 0, 0, 0};
+  if (!ptr || bytes == 0) return r;
+  r.head = std::min<size_t>(bytes, (16 - (reinterpret_cast<uintptr_t>(ptr) & 15)) & 15);
+  r.n16 = (bytes - r.head) / 16;
+  r.tail = bytes - r.head - 16 * r.n16;
+  return r;
+}
+__device__ __forceinline__ void zero_fill(const ZeroRange& r, size_t t, size_t stride) {
+  uint4* mid = reinterpret_cast<uint4*>(r.p + r.head);
+  for (size_t i = t; i < r.n16; i += stride) mid[i] = make_uint4(0u, 0u, 0u, 0u);
+  if (t < r.head) r.p[t] = 0;
+  if (t < r.tail) r.p[r.head + 16 * r.n16 + t] = 0;
+}
+__global__ void __launch_bounds__(256) k_zero(ZeroRange r0, ZeroRange r1) {
   pdl_wait();
   pdl_trigger();
   const size_t t = blockIdx.x * 256ull + threadIdx.x, stride = (size_t)gridDim.x * 256;
-  uint4* mid = reinterpret_cast<uint4*>(p + head);
-  for (size_t i = t; i < n16; i += stride) mid[i] = make_uint4(0u, 0u, 0u, 0u);
-  if (t < head) p[t] = 0;
-  if (t < tail) p[head + 16 * n16 + t] = 0;
+  zero_fill(r0, t, stride);
+  zero_fill(r1, t, stride);
 }
 }  // namespace
 
-fgs_status zero_async(void* ptr, size_t bytes, cudaStream_t s) {
-  if (bytes == 0) return FGS_OK;
+fgs_status zero_async(void* ptr, size_t bytes, cudaStream_t s, void* ptr2, size_t bytes2) {
+  const ZeroRange r0 = zero_range(ptr, bytes), r1 = zero_range(ptr2, bytes2);
+  if (r0.head + r0.n16 + r0.tail + r1.head + r1.n16 + r1.tail == 0) return FGS_OK;
   KernelTimer kt__(FGS_K_ZERO, s);
-  unsigned char* p = static_cast<unsigned char*>(ptr);
-  const size_t head = std::min<size_t>(bytes, (16 - (reinterpret_cast<uintptr_t>(p) & 15)) & 15);
-  const size_t n16 = (bytes - head) / 16, tail = bytes - head - 16 * n16;
-  const size_t want = (n16 + 1023) / 1024;  // about four 16-byte stores per thread
+  const size_t want = (r0.n16 + r1.n16 + 1023) / 1024;  // about four 16-byte stores per thread
   const unsigned blocks = (unsigned)std::max<size_t>(1, std::min<size_t>(want, (size_t)num_sms() * 8));
-  (void)launch_pdl(k_zero, dim3(blocks), dim3(256), 0, s, p, head, n16, tail);
+  (void)launch_pdl(k_zero, dim3(blocks), dim3(256), 0, s, r0, r1);
   kt__.stop();
   FGS_LAUNCH_CHECK();
   return FGS_OK;

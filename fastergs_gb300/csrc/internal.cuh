@@ -81,10 +81,13 @@ bool adam_args_ok(const fgs_adam_fused* ad, const float* shs, const float* opaci
 
 fgs_status run_preprocess_bwd(PbwdArgs& a, cudaStream_t s);
 // cudaMemsetAsync(ptr, 0, bytes) as a kernel launched with programmatic
-// dependent launch, so the chain of the path's kernels is not broken.
-fgs_status zero_async(void* ptr, size_t bytes, cudaStream_t s);
+// dependent launch, so the chain of the path's kernels is not broken; a
+// second range (ptr2, bytes2) is zeroed by the same launch.
+fgs_status zero_async(void* ptr, size_t bytes, cudaStream_t s, void* ptr2 = nullptr, size_t bytes2 = 0);
 
+// Tile ranges of the sorted keys; (zero_also, zero_bytes) is zeroed by the
+// same launch that clears the ranges.
 fgs_status run_tile_ranges(int64_t n_cap, const int32_t* n_dev, uint32_t tiles, const uint64_t* keys_sorted,
-                           uint32_t* ranges, cudaStream_t s);
+                           uint32_t* ranges, cudaStream_t s, void* zero_also = nullptr, size_t zero_bytes = 0);
 
 }  // namespace fgs

@@ -621,9 +621,9 @@ extern "C" fgs_status fgs_selftest_wait(uint32_t* flag, void* stream) {
 
 namespace fgs {
 fgs_status run_tile_ranges(int64_t n_cap, const int32_t* n_dev, uint32_t tiles, const uint64_t* keys_sorted,
-                           uint32_t* ranges, cudaStream_t s) {
+                           uint32_t* ranges, cudaStream_t s, void* zero_also, size_t zero_bytes) {
   {
-    const fgs_status z = zero_async(ranges, sizeof(uint32_t) * 2 * (size_t)tiles, s);
+    const fgs_status z = zero_async(ranges, sizeof(uint32_t) * 2 * (size_t)tiles, s, zero_also, zero_bytes);
     if (z != FGS_OK) return z;
   }
   if (n_cap > 0) {
@@ -642,12 +642,12 @@ fgs_status run_render_fwd(const Views& views, int64_t n_cap, const int32_t* n_de
                           const ImageState& im, const SampleState& sm, int64_t max_buckets, bool recompute,
                           cudaStream_t s, int chain) {
   if (chain < 1) return FGS_ERR_BAD_ARG;
-  fgs_status st = run_tile_ranges(n_cap, n_dev, views.tiles, keys_sorted, ranges, s);
+  // the ranges and the round histogram of the bucket setup are cleared by one launch
+  fgs_status st = run_tile_ranges(n_cap, n_dev, views.tiles, keys_sorted, ranges, s, im.round_hist,
+                                  sizeof(uint32_t) * (kRounds + 1));
   if (st != FGS_OK) return st;
   const int split = bucket_split(bucket_size), sub = sub_bucket_size(bucket_size);
   {
-    const fgs_status z = zero_async(im.round_hist, sizeof(uint32_t) * (kRounds + 1), s);
-    if (z != FGS_OK) return z;
     KernelTimer kt__(FGS_K_BUCKET_SETUP, s, 3);
     const unsigned nblk = (views.tiles + kScanTiles - 1) / kScanTiles;
     (void)launch_pdl(k_bucket_count, dim3(nblk), dim3(kScanTiles), 0, s, (int)views.tiles, ranges, sub,
