@@ -420,7 +420,7 @@ def gpu_bench(args, rank, local, world):
         step(dev_in)
     torch.cuda.synchronize()
     K = int(slot._buf.curr_offset.item())
-    W_eval = needed_evaluations(s, settings, dev_in, slot._buf, dev)
+    W_eval, visible = needed_evaluations(s, settings, dev_in, slot._buf, dev)
     fp32_peak = ctypes_peak_fp32(dev)
     ex2_peak = ctypes_peak_ex2(dev)
 
@@ -498,7 +498,7 @@ def gpu_bench(args, rank, local, world):
         fgs._RasterizeGaussians.__dict__["buffer"]._buf = None  # the drop-in path's shared buffers
         torch.cuda.empty_cache()
         checkpoint = checkpoint_bench(args, dev)
-    return dict(ms_step=ms_step_job, fwd_ms=fwd_ms, clocks=clocks, ktimes=ktimes, K=K,
+    return dict(ms_step=ms_step_job, fwd_ms=fwd_ms, clocks=clocks, ktimes=ktimes, K=K, visible=visible,
                 launches_per_step=launches_per_step, e2e=e2e, P=s.P, W=cam.width, H=cam.height, batched=batched,
                 checkpoint=checkpoint, W_eval=W_eval, fp32_peak=fp32_peak, ex2_peak=ex2_peak, fused_adam=fused_adam,
                 loss=loss, aux=aux, c3=c3, fb=fb)
@@ -948,13 +948,15 @@ def checkpoint_bench(args, dev):
 def needed_evaluations(scene, settings, dev_in, buf, dev):
     """Pixel-Gaussian evaluations FB's merge uses: the sum over pixels of the
     last contributor count (every Gaussian of every bucket up to the one
-    after which the pixel stops).  This is the composite's algorithmic work."""
+    after which the pixel stops).  This is the composite's algorithmic work.
+    Also returns the number of Gaussians the view sees (radius > 0), which
+    sets the preprocess kernels' algorithmic bytes."""
     import torch
     from fastergs_gb300 import _C
     cam = scene.camera
     buf.curr_offset.fill_(0)
     e = torch.empty(0, device=dev)
-    _C.ops.preprocess(scene.sh_degree, dev_in["means"], e, dev_in["dc"], dev_in["shs"], dev_in["opacities"],
+    radii = _C.ops.preprocess(scene.sh_degree, dev_in["means"], e, dev_in["dc"], dev_in["shs"], dev_in["opacities"],
                       dev_in["scales"], dev_in["rotations"], 1.0, cam.width, cam.height, 16, 16, settings.campos,
                       settings.viewmatrix, settings.projmatrix, cam.tanfovx, cam.tanfovy, 100.0, 0.01,
                       buf.gaussian_keys_unsorted, buf.gaussian_values_unsorted, buf.gaussian_values_sorted,
@@ -966,7 +968,7 @@ def needed_evaluations(scene, settings, dev_in, buf, dev):
     tf = torch.empty((cam.height, cam.width, 1), dtype=torch.float32, device=dev)
     _C.ops.render_16x16(scene.P, K, cam.width, cam.height, buf.splat_buffer, buf.gaussian_keys_sorted,
                         buf.gaussian_values_sorted, buf.ranges, settings.bg, lc, tf)
-    return int(lc.to(torch.int64).sum().item())
+    return int(lc.to(torch.int64).sum().item()), int((radii > 0).sum().item())
 
 
 def ctypes_peak_ex2(dev):
@@ -1016,8 +1018,8 @@ MUFU_PER_EVAL = {"render_fwd": 1, "render_bwd": 2}
 # C2 workload (1M Gaussians, 1297x840, 3,103,742 pairs), from one ncu capture
 # of each kernel; the file gives the command that made it.
 TRAFFIC_SOURCE = "profiles/ncu_c2_kernels.md"
-TRAFFIC_PER_LAUNCH = {"render_bwd": 82_207_488, "render_fwd": 90_761_728, "sort_pass": 38_357_760,
-                      "preprocess_bwd": 509_822_976, "preprocess": 215_812_096}
+TRAFFIC_PER_LAUNCH = {"render_bwd": 83_665_408, "render_fwd": 89_218_560, "sort_pass": 38_302_976,
+                      "preprocess_bwd": 404_708_096, "preprocess": 215_154_944}
 
 
 def roofline(res, peaks):
@@ -1025,20 +1027,25 @@ def roofline(res, peaks):
     The compositing kernels are bound by FP32 issue: their roofline is
     achieved FP32 TFLOP/s (needed evaluations x FLOPs per evaluation / time)
     against the FFMA peak measured in this run; the rest are bound by HBM."""
-    P, K = res["P"], res["K"]
+    P, K, Pv = res["P"], res["K"], res["visible"]
     steps_ms = {k: v[0] for k, v in res["ktimes"].items()}
     launches = {k: v[1] for k, v in res["ktimes"].items()}
     sh_floats = 45
-    # algorithmic bytes per launch
+    # algorithmic bytes per launch (Pv: Gaussians the view sees)
     algo = {
-        "preprocess": P * (56 + 4 * sh_floats) + P * 44 + 12 * K,
+        # every Gaussian: means, opacity, scales, rotation read, radius written;
+        # seen ones: dc and SH read, the 128-byte record written; 12 B per pair
+        "preprocess": P * (12 + 4 + 12 + 16 + 4) + Pv * (12 + 4 * sh_floats + 128) + 12 * K,
         "sort_pass": 24 * K,
         "sort_hist": 8 * K,
         # composite: records of every pair, plus the folded prefix written once per
         # 64-Gaussian sub-bucket (read once by the backward)
         "render_fwd": 40 * K + 16 * 256 * math.ceil(K / 64),
         "render_bwd": 40 * K + 16 * 256 * math.ceil(K / 64) + 48 * K,
-        "preprocess_bwd": P * (56 + 4 * sh_floats + 48) + P * (56 + 4 * sh_floats),
+        # every Gaussian: radius read, the autograd outputs written (opacity, mean,
+        # dc, SH, scale, rotation); seen ones: means, scales, rotation, SH, the
+        # gradient record and 16 B of the splat record read
+        "preprocess_bwd": P * (4 + 4 + 12 + 12 + 4 * sh_floats + 12 + 16) + Pv * (12 + 12 + 16 + 4 * sh_floats + 48 + 16),
         "tile_ranges": 8 * K,
     }
     dom = max(steps_ms, key=lambda k: steps_ms[k])
