@@ -753,10 +753,12 @@ __device__ __forceinline__ bool pbwd_gaussian(const PbwdArgs& a, int i, bool vis
   return pbwd_part<ADAM, true, true>(a, i, vis, co, gsh, acc);
 }
 
-// Whether some view saw Gaussian i (radius > 0).
+// Whether some view saw Gaussian i (radius > 0).  The views' radii are read
+// as independent loads (no early exit), so many views cost one latency.
 __device__ __forceinline__ bool pbwd_visible(const PbwdArgs& a, int i) {
   bool vis = false;
-  for (int vi = 0; vi < a.views.V && !vis; ++vi) vis = a.radii[(size_t)vi * a.P + i] > 0;
+#pragma unroll 4
+  for (int vi = 0; vi < a.views.V; ++vi) vis |= a.radii[(size_t)vi * a.P + i] > 0;
   return vis;
 }
 
@@ -855,16 +857,17 @@ __global__ void __launch_bounds__(kPbwdThreads, kPbwdBlocks) k_preprocess_bwd(co
   if (a.sh_staged) {
     float* s_co = s_pb;
     float* s_g = s_pb + kPbwdThreads * row;
-    // Only the SH rows of Gaussians some view saw are read (at 1M Gaussians
-    // in one view, about a third): copy those alone.
     const bool vis = i < a.P && pbwd_visible(a, i);
-    s_seen[threadIdx.x] = vis ? 1 : 0;
-    __syncthreads();
     bool seen;
     if (a.views.V == 1) {
-      // one view: the SH rows arrive while the geometry part runs (with many
-      // views the geometry alone outlasts the copy, and a second walk over
-      // the views would cost more than the overlap gains)
+      // one view: only the SH rows of Gaussians it saw are read (at 1M
+      // Gaussians in one 1297x840 view, about a third), so only those are
+      // copied, and they arrive while the geometry part runs (with many
+      // views the geometry alone outlasts the copy, a second walk over the
+      // views would cost more than the overlap gains, and nearly every row
+      // is seen by some view)
+      s_seen[threadIdx.x] = vis ? 1 : 0;
+      __syncthreads();
       block_copy_rows_to_smem_async(s_co, a.shs, (size_t)first * row, n, row, s_seen);
       for (int j = threadIdx.x; j < n * row; j += kPbwdThreads) s_g[j] = 0.f;
       PbwdAcc acc;
@@ -875,7 +878,7 @@ __global__ void __launch_bounds__(kPbwdThreads, kPbwdBlocks) k_preprocess_bwd(co
       seen = active && pbwd_part<ADAM, false, true>(a, i, vis, s_co + threadIdx.x * row, s_g + threadIdx.x * row,
                                                     acc);
     } else {
-      block_copy_rows_to_smem(s_co, a.shs, (size_t)first * row, n, row, s_seen);
+      block_copy_rows_to_smem(s_co, a.shs, (size_t)first * row, n, row, nullptr);
       for (int j = threadIdx.x; j < n * row; j += kPbwdThreads) s_g[j] = 0.f;
       __syncthreads();
       seen = i < a.P && pbwd_gaussian<ADAM>(a, i, vis, s_co + threadIdx.x * row, s_g + threadIdx.x * row);

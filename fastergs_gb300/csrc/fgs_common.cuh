@@ -248,7 +248,7 @@ __device__ __forceinline__ void block_copy_rows_to_smem_async(float* dst, const 
 }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
 
-// Synchronous form of block_copy_rows_to_smem_async.
+// Synchronous form of block_copy_rows_to_smem_async; keep == nullptr copies every row.
 __device__ __forceinline__ void block_copy_rows_to_smem(float* dst, const float* src, size_t first, int nrows,
                                                         int row, const uint8_t* keep) {
   const float* s = src + first;
@@ -258,12 +258,12 @@ __device__ __forceinline__ void block_copy_rows_to_smem(float* dst, const float*
   if ((reinterpret_cast<uintptr_t>(s) & 15) == 0) {
     const int n4 = n >> 2;
     for (int j = threadIdx.x; j < n4; j += blockDim.x)
-      if (keep[row_of(4 * j, inv_row)] | keep[row_of(4 * j + 3, inv_row)])
+      if (!keep || (keep[row_of(4 * j, inv_row)] | keep[row_of(4 * j + 3, inv_row)]))
         reinterpret_cast<float4*>(dst)[j] = __ldg(reinterpret_cast<const float4*>(s) + j);
     done = 4 * n4;
   }
   for (int j = done + threadIdx.x; j < n; j += blockDim.x)
-    if (keep[row_of(j, inv_row)]) dst[j] = __ldg(s + j);
+    if (!keep || keep[row_of(j, inv_row)]) dst[j] = __ldg(s + j);
 }
 // The reverse: n floats from shared memory to dst + first.
 __device__ __forceinline__ void block_copy_from_smem(float* dst, size_t first, const float* src, int n) {
