@@ -305,10 +305,8 @@ __global__ void __launch_bounds__(kBwdWarps * kWarp, 6) k_render_bwd(const BwdAr
       f2x V0 = z2, V1 = z2, V4 = z2, V5 = z2, V7 = z2, V8 = z2, V9 = z2, V10 = z2, V11 = z2;
       float v2 = 0.f, v3 = 0.f;
       bool any = false;
-#pragma unroll
-      for (int j = 0; j < kPairs; ++j) {
+      auto pair_step = [&](const int j) {
         const int k0 = 2 * j, k1 = 2 * j + 1;
-        if (((mask >> k0) & 3u) == 0u) continue;
         const int r0 = k0 / M::kCols, c0 = k0 % M::kCols, r1 = k1 / M::kCols, c1 = k1 % M::kCols;
         const float iy0 = pos.y - pyr[r0], iy1 = r1 == r0 ? iy0 : pos.y - pyr[r1];  // exact
         const float dy0 = iy0 + pos.w;
@@ -374,6 +372,17 @@ __global__ void __launch_bounds__(kBwdWarps * kWarp, 6) k_render_bwd(const BwdAr
         // cross-axis gradient is a small difference of large sums; here each
         // frame axis is summed on its own.)
         V11 = f2_add(V11, dp2);
+      };
+      // Every pixel pair has a sub-block the Gaussian reaches (the common case
+      // for large footprints): the four pair chains run without per-pair
+      // branches, so they interleave; otherwise pairs without one are skipped.
+      if (((mask | (mask >> 1)) & 0x55u) == 0x55u) {
+#pragma unroll
+        for (int j = 0; j < kPairs; ++j) pair_step(j);
+      } else {
+#pragma unroll
+        for (int j = 0; j < kPairs; ++j)
+          if (((mask >> (2 * j)) & 3u) != 0u) pair_step(j);
       }
       if (__any_sync(0xffffffffu, any)) {
         float v[12], a0, a1;

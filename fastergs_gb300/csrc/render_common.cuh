@@ -248,10 +248,8 @@ __device__ __forceinline__ void composite_bucket(const BucketStage& st, int n, u
       float ix[M::kCols];
 #pragma unroll
       for (int cc = 0; cc < M::kCols; ++cc) ix[cc] = pos.x - pxc[cc];  // exact
-#pragma unroll
-      for (int j = 0; j < kPairs; ++j) {
+      auto pair_step = [&](const int j) {
         const int k0 = 2 * j, k1 = 2 * j + 1;  // pixel slots k = r * kCols + cc
-        if (((mask >> k0) & 3u) == 0u) continue;
         const int r0 = k0 / M::kCols, c0 = k0 % M::kCols, r1 = k1 / M::kCols, c1 = k1 % M::kCols;
         const float iy0 = pos.y - pyr[r0], iy1 = r1 == r0 ? iy0 : pos.y - pyr[r1];  // exact
         const float dy0 = iy0 + pos.w;
@@ -273,6 +271,17 @@ __device__ __forceinline__ void composite_bucket(const BucketStage& st, int n, u
         G2[j] = f2_fma(ng2, nwt2, G2[j]);
         B2[j] = f2_fma(nb2, nwt2, B2[j]);
         T2[j] = f2_fma(na2, T2[j], T2[j]);    // T (1 - alpha), rounded once
+      };
+      // Every pixel pair has a sub-block the Gaussian reaches (the common case
+      // for large footprints): the four pair chains run without per-pair
+      // branches, so they interleave; otherwise pairs without one are skipped.
+      if (((mask | (mask >> 1)) & 0x55u) == 0x55u) {
+#pragma unroll
+        for (int j = 0; j < kPairs; ++j) pair_step(j);
+      } else {
+#pragma unroll
+        for (int j = 0; j < kPairs; ++j)
+          if (((mask >> (2 * j)) & 3u) != 0u) pair_step(j);
       }
     }
   }
