@@ -305,7 +305,7 @@ __global__ void __launch_bounds__(kBwdWarps * kWarp, 6) k_render_bwd(const BwdAr
       f2x V0 = z2, V1 = z2, V4 = z2, V5 = z2, V7 = z2, V8 = z2, V9 = z2, V10 = z2, V11 = z2;
       float v2 = 0.f, v3 = 0.f;
       bool any = false;
-      auto pair_step = [&](const int j) {
+      auto pair_step = [&](const int j, auto track) {
         const int k0 = 2 * j, k1 = 2 * j + 1;
         const int r0 = k0 / M::kCols, c0 = k0 % M::kCols, r1 = k1 / M::kCols, c1 = k1 % M::kCols;
         const float iy0 = pos.y - pyr[r0], iy1 = r1 == r0 ? iy0 : pos.y - pyr[r1];  // exact
@@ -323,7 +323,7 @@ __global__ void __launch_bounds__(kBwdWarps * kWarp, 6) k_render_bwd(const BwdAr
         float n0 = fmaxf(-kAlphaMax, -ex2_approx(e0)), n1 = fmaxf(-kAlphaMax, -ex2_approx(e1));
         n0 = n0 > -kAlphaCut ? 0.f : n0;
         n1 = n1 > -kAlphaCut ? 0.f : n1;
-        any |= (n0 != 0.f) | (n1 != 0.f);
+        if constexpr (decltype(track)::value) any |= (n0 != 0.f) | (n1 != 0.f);
         const f2x na2 = f2_pack(n0, n1);
         const float4 la = lk[(2 * j) * kWarp + lane], lb = lk[(2 * j + 1) * kWarp + lane];
         const f2x Lx2 = f2_pack(la.x, la.y), Ly2 = f2_pack(la.z, la.w), Lz2 = f2_pack(lb.x, lb.y),
@@ -378,11 +378,14 @@ __global__ void __launch_bounds__(kBwdWarps * kWarp, 6) k_render_bwd(const BwdAr
       // branches, so they interleave; otherwise pairs without one are skipped.
       if (((mask | (mask >> 1)) & 0x55u) == 0x55u) {
 #pragma unroll
-        for (int j = 0; j < kPairs; ++j) pair_step(j);
+        for (int j = 0; j < kPairs; ++j) pair_step(j, std::false_type{});
+        // no per-pixel contribution test here: a lane whose alphas were all cut
+        // holds exact zeros, so the reduction below then only adds zeros
+        any = true;
       } else {
 #pragma unroll
         for (int j = 0; j < kPairs; ++j)
-          if (((mask >> (2 * j)) & 3u) != 0u) pair_step(j);
+          if (((mask >> (2 * j)) & 3u) != 0u) pair_step(j, std::true_type{});
       }
       if (__any_sync(0xffffffffu, any)) {
         float v[12], a0, a1;
