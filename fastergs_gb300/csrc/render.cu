@@ -32,6 +32,12 @@ namespace fgs {
 namespace {
 
 constexpr int kFwdWarps = 4;
+// Blocks per SM of the composite kernel: 6 (85 registers, no spills) for
+// frames of up to kFwdFewTiles tiles, 7 (72 registers, a few spills) above.
+// A 1297x840 frame (4346 tiles, ~12 buckets per warp): 0.178 -> 0.169 ms with
+// 6; the 16-camera C4 frame (58k tiles, ~180 buckets per warp): 1.87 ms with
+// 7, 1.93 with 6.
+constexpr uint32_t kFwdFewTiles = 16384;
 
 __global__ void __launch_bounds__(256) k_tile_ranges(const unsigned long long* __restrict__ keys, long long n_cap,
                                                      const int* n_dev, uint32_t num_tiles,
@@ -360,8 +366,8 @@ struct FwdArgs {
   int chain;   // the tile's fold chain covers its first `chain` buckets (store mode)
 };
 
-template <int BX, bool RECOMPUTE>
-__global__ void __launch_bounds__(kFwdWarps * kWarp, 7) k_render_fwd(const FwdArgs a) {
+template <int BX, bool RECOMPUTE, int MIN_BLOCKS>
+__global__ void __launch_bounds__(kFwdWarps * kWarp, MIN_BLOCKS) k_render_fwd(const FwdArgs a) {
   pdl_wait();  // the preceding kernel of the stream is done
   pdl_trigger();
   using M = TileMap<BX>;
@@ -668,14 +674,22 @@ fgs_status run_render_fwd(const Views& views, int64_t n_cap, const int32_t* n_de
     auto launch = [&](auto kernel) {
       (void)launch_pdl(kernel, dim3(num_sms() * resident_blocks(kernel, nt, 0)), dim3(nt), 0, s, fa);
     };
-    if (recompute) {  // samples hold one running prefix per tile
-      if (views.bx == 8) launch(k_render_fwd<8, true>);
-      else if (views.bx == 16) launch(k_render_fwd<16, true>);
-      else launch(k_render_fwd<32, true>);
+    auto by_tile = [&](auto rc, auto mb) {
+      constexpr bool R = decltype(rc)::value;
+      constexpr int B = decltype(mb)::value;
+      if (views.bx == 8) launch(k_render_fwd<8, R, B>);
+      else if (views.bx == 16) launch(k_render_fwd<16, R, B>);
+      else launch(k_render_fwd<32, R, B>);
+    };
+    using Few = std::integral_constant<int, 6>;
+    using Many = std::integral_constant<int, 7>;
+    // recompute mode: the samples hold one running prefix per tile
+    if (recompute) {
+      if (views.tiles <= kFwdFewTiles) by_tile(std::true_type{}, Few{});
+      else by_tile(std::true_type{}, Many{});
     } else {
-      if (views.bx == 8) launch(k_render_fwd<8, false>);
-      else if (views.bx == 16) launch(k_render_fwd<16, false>);
-      else launch(k_render_fwd<32, false>);
+      if (views.tiles <= kFwdFewTiles) by_tile(std::false_type{}, Few{});
+      else by_tile(std::false_type{}, Many{});
     }
     kt__.stop();
   }
