@@ -1018,8 +1018,8 @@ MUFU_PER_EVAL = {"render_fwd": 1, "render_bwd": 2}
 # C2 workload (1M Gaussians, 1297x840, 3,103,742 pairs), from one ncu capture
 # of each kernel; the file gives the command that made it.
 TRAFFIC_SOURCE = "profiles/ncu_c2_kernels.md"
-TRAFFIC_PER_LAUNCH = {"render_bwd": 83_665_408, "render_fwd": 89_218_560, "sort_pass": 38_302_976,
-                      "preprocess_bwd": 404_708_096, "preprocess": 215_154_944}
+TRAFFIC_PER_LAUNCH = {"render_bwd": 82_264_576, "render_fwd": 74_994_432, "sort_pass": 38_371_669,
+                      "preprocess_bwd": 404_383_488, "preprocess": 215_580_928}
 
 
 def roofline(res, peaks):

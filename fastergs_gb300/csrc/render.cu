@@ -32,8 +32,8 @@ namespace fgs {
 namespace {
 
 constexpr int kFwdWarps = 4;
-// Blocks per SM of the composite kernel: 6 (85 registers, no spills) for
-// frames of up to kFwdFewTiles tiles, 7 (72 registers, a few spills) above.
+// Blocks per SM of the composite kernel: 6 (80 registers, 16 B of spills)
+// for frames of up to kFwdFewTiles tiles, 7 (72 registers, 72 B of spills) above.
 // A 1297x840 frame (4346 tiles, ~12 buckets per warp): 0.178 -> 0.169 ms with
 // 6; the 16-camera C4 frame (58k tiles, ~180 buckets per warp): 1.87 ms with
 // 7, 1.93 with 6.
