@@ -3,7 +3,7 @@
 // Restates FB csrc/cuda_rasterizer/preprocess.cu (projection, EWA covariance,
 // SH colour, tile rectangle, ellipse/tile test, lane-packed emission of small
 // Gaussians, 128-tile sub-tasks for large ones) with a GB300 layout:
-//   * one CTA of 8 warps handles 256 consecutive Gaussians, one per thread;
+//   * one CTA of 4 warps handles 128 consecutive Gaussians, one per thread;
 //   * the warp's small Gaussians are flattened into one candidate list
 //     (exclusive scan of rect areas) and 32 candidates are tested per step, so
 //     every lane does useful work whatever the footprint mix;
@@ -16,7 +16,9 @@
 namespace fgs {
 namespace {
 
-constexpr int kPreThreads = 256;
+// Gaussians per preprocess block: 128 at 8 blocks per SM (64 registers);
+// 256 at 4 per SM ran 0.117 ms at C2 against 0.113, 3 per SM 0.126.
+constexpr int kPreThreads = 128;
 constexpr int kPreWarps = kPreThreads / kWarp;
 constexpr int kStage = 128;  // staged pairs per warp before a flush
 
@@ -119,7 +121,7 @@ __device__ __forceinline__ float3 sh_colour(int D, float x, float y, float z, co
   return f3(fmaxf(r.x, 0.0f), fmaxf(r.y, 0.0f), fmaxf(r.z, 0.0f));
 }
 
-__global__ void __launch_bounds__(kPreThreads, 4) k_preprocess(const PreArgs a) {
+__global__ void __launch_bounds__(kPreThreads, 8) k_preprocess(const PreArgs a) {
   pdl_wait();  // the preceding kernel of the stream is done
   pdl_trigger();
   __shared__ float2 s_xy[kPreWarps][kWarp];
@@ -131,7 +133,7 @@ __global__ void __launch_bounds__(kPreThreads, 4) k_preprocess(const PreArgs a) 
   __shared__ uint32_t s_val[kPreWarps][kStage];
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  // Block b covers Gaussians [(b / V) * 256, +256) of view b % V: the views of
+  // Block b covers Gaussians [(b / V) * kPreThreads, +kPreThreads) of view b % V: the views of
   // one Gaussian chunk run back to back, so its parameters come from L2 after
   // the first view instead of being re-read from HBM per view.
   const int vi = (int)(blockIdx.x % (unsigned)a.views.V);
@@ -448,7 +450,7 @@ fgs_status run_preprocess(PreArgs& a, cudaStream_t s) {
   FGS_LAUNCH_CHECK();
   {
     KernelTimer kt__(FGS_K_PREPROCESS_LARGE, s);
-    (void)launch_pdl(k_preprocess_large, dim3(num_sms() * 4), dim3(kPreThreads), 0, s, a);
+    (void)launch_pdl(k_preprocess_large, dim3(num_sms() * (1024 / kPreThreads)), dim3(kPreThreads), 0, s, a);
     kt__.stop();
   }
   FGS_LAUNCH_CHECK();
