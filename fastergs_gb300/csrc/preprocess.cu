@@ -3,7 +3,7 @@
 // Restates FB csrc/cuda_rasterizer/preprocess.cu (projection, EWA covariance,
 // SH colour, tile rectangle, ellipse/tile test, lane-packed emission of small
 // Gaussians, 128-tile sub-tasks for large ones) with a GB300 layout:
-//   * one CTA of 4 warps handles 128 consecutive Gaussians, one per thread;
+//   * one CTA of 2 warps handles 64 consecutive Gaussians, one per thread;
 //   * the warp's small Gaussians are flattened into one candidate list
 //     (exclusive scan of rect areas) and 32 candidates are tested per step, so
 //     every lane does useful work whatever the footprint mix;
@@ -16,9 +16,10 @@
 namespace fgs {
 namespace {
 
-// Gaussians per preprocess block: 128 at 8 blocks per SM (64 registers);
-// 256 at 4 per SM ran 0.117 ms at C2 against 0.113, 3 per SM 0.126.
-constexpr int kPreThreads = 128;
+// Gaussians per preprocess block: 64 at 16 blocks per SM (64 registers, 32
+// warps per SM); at 1M Gaussians in a 1297x840 view 0.109 ms, against 0.111
+// with 128 at 8 per SM, 0.117 with 256 at 4 and 0.126 with 256 at 3.
+constexpr int kPreThreads = 64;
 constexpr int kPreWarps = kPreThreads / kWarp;
 constexpr int kStage = 128;  // staged pairs per warp before a flush
 
@@ -121,7 +122,7 @@ __device__ __forceinline__ float3 sh_colour(int D, float x, float y, float z, co
   return f3(fmaxf(r.x, 0.0f), fmaxf(r.y, 0.0f), fmaxf(r.z, 0.0f));
 }
 
-__global__ void __launch_bounds__(kPreThreads, 8) k_preprocess(const PreArgs a) {
+__global__ void __launch_bounds__(kPreThreads, 16) k_preprocess(const PreArgs a) {
   pdl_wait();  // the preceding kernel of the stream is done
   pdl_trigger();
   __shared__ float2 s_xy[kPreWarps][kWarp];
