@@ -353,8 +353,10 @@ fgs_status run_sort(int64_t n_cap, const int32_t* n_dev, uint32_t tiles, void* t
     const fgs_status z = zero_async(base, L.alt_keys, s);
     if (z != FGS_OK) return z;
   }
+  // histogram blocks: up to 3 per SM (a 47M-key batched histogram 0.119 ms
+  // at 2 per SM, 0.115 at 3)
   const int hist_blocks = (int)std::max<int64_t>(
-      1, std::min<int64_t>((n_cap + kSortThreads * 8 - 1) / (kSortThreads * 8), (int64_t)num_sms() * 2));
+      1, std::min<int64_t>((n_cap + kSortThreads * 8 - 1) / (kSortThreads * 8), (int64_t)num_sms() * 3));
   {
     KernelTimer kt__(FGS_K_SORT_HIST, s);
     (void)launch_pdl(k_histogram, dim3(hist_blocks), dim3(kSortThreads), 0, s,
